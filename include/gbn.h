@@ -1,0 +1,196 @@
+/*
+ * gbn.h - C ABI of the GB300 tTV-NESTA library (libgbnesta.so).
+ *
+ * This is the drop-in boundary for OpenCLIPER's compressed-sensing hot path:
+ * the NESTA solver with temporal total variation over multicoil Cartesian
+ * k-space (src/processes/nesta/NestaUp.cpp) and the operator processes it is
+ * built from.  The reference exposes these as C++ Process classes with
+ * init()/launch() on XData/KData/SensitivityMapsData objects; the C++ facade in
+ * include/OpenCLIPER/ keeps that API and forwards to the functions below.
+ *
+ * Conventions
+ *  - Complex data are interleaved complex64 (re, im float pairs), passed as
+ *    float* whose element count is 2x the number of complex values.
+ *  - Layouts are the reference's (Data.cpp:1305-1343, width fastest):
+ *      XData              [F][H][W]
+ *      KData              [F][C][H][W]
+ *      SensitivityMaps    [C][H][W]
+ *      pixel mask (uint8) [F][H][W], 0 = not sampled (SamplingMasksData PIXELMASK)
+ *      row mask (uint32)  [F][H], 0/1 per phase-encode line (ROWMASK)
+ *  - W (columns, readout) must be a multiple of 8 (Data.cpp:1360-1372).  FFT
+ *    lengths W and H must be 7-smooth and in [8, 512] (clFFT radices 2,3,5,7).
+ *  - Pointers named d_* are device pointers on the context's device; every
+ *    call is asynchronous on the context stream unless documented otherwise.
+ *  - Every function returns GBN_OK (0) or a negative GBN_ERR_* code;
+ *    gbn_last_error_string() describes the last failure of the calling thread.
+ *    The reference throws CLError/std::invalid_argument (Utils.hpp:67-83); the
+ *    C++ facade turns these codes back into exceptions.
+ *  - A context is used by one host thread at a time, like the reference's
+ *    CLapp with its single in-order queue (src/Process.cpp:53-56).
+ */
+#ifndef GBN_H
+#define GBN_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define GBN_API __attribute__((visibility("default")))
+#else
+#define GBN_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define GBN_VERSION 1
+
+enum {
+  GBN_OK = 0,
+  GBN_ERR_INVALID = -1,     /* bad argument (reference: std::invalid_argument) */
+  GBN_ERR_UNSUPPORTED = -2, /* size/shape outside what this build implements */
+  GBN_ERR_CUDA = -3,        /* CUDA runtime failure (reference: CLError) */
+  GBN_ERR_NOMEM = -4        /* device allocation failed */
+};
+
+/* TemporalTV::Direction (include/OpenCLIPER/processes/nesta/TemporalTV.hpp:47) */
+enum { GBN_TTV_ADJOINT = 0, GBN_TTV_FORWARD = 1 };
+/* FFT::Direction = clfftDirection (include/OpenCLIPER/processes/FFT.hpp:74-79) */
+enum { GBN_FFT_FORWARD = -1, GBN_FFT_BACKWARD = 1 };
+/* ComplexElementProd::ConjugateSensMap_t (ComplexElementProd.hpp:48-56) */
+enum { GBN_NOT_CONJUGATE = 0, GBN_CONJUGATE = 1 };
+
+typedef struct gbn_ctx gbn_ctx;
+typedef struct gbn_problem gbn_problem;
+
+/* ------------------------------------------------------------------------ */
+/* Runtime: replaces CLapp (src/CLapp.cpp:188-575: platform/device/context/  */
+/* queue) and the device-buffer registry (CLapp::addData, CLapp.cpp:1735).   */
+/* ------------------------------------------------------------------------ */
+GBN_API const char* gbn_last_error_string(void);
+GBN_API int gbn_version(void);
+/* number of supported FFT lengths written to out (up to cap); returns count */
+GBN_API int gbn_supported_lengths(int* out, int cap);
+
+/* CLapp::create (CLapp.hpp:239-240): bind device `device`, create a stream. */
+GBN_API int gbn_ctx_create(int device, gbn_ctx** out);
+GBN_API int gbn_ctx_destroy(gbn_ctx* ctx);
+/* the cudaStream_t every call of this context is issued on */
+GBN_API int gbn_ctx_get_stream(gbn_ctx* ctx, void** stream);
+/* issue on a caller-owned cudaStream_t instead (NULL restores the own stream) */
+GBN_API int gbn_ctx_set_stream(gbn_ctx* ctx, void* stream);
+/* CLapp::getCommandQueue().finish() */
+GBN_API int gbn_ctx_sync(gbn_ctx* ctx);
+/* State of the drand48 generator used by the power-method restart
+ * (NestaUp.cpp:369-385).  A new context starts like a fresh process
+ * (glibc's default state, as if seed48 were never called). */
+GBN_API int gbn_ctx_seed48(gbn_ctx* ctx, const unsigned short seed16v[3]);
+GBN_API int gbn_ctx_get_rand48(gbn_ctx* ctx, unsigned short state16v[3]);
+/* tuning knobs: "k1_coils_per_block", "k2_ctas_per_sm" */
+GBN_API int gbn_ctx_set_tuning(gbn_ctx* ctx, const char* key, int value);
+
+/* Device memory (DeviceDataProperties::createEmptyDeviceBuffers,
+ * DeviceDataProperties.cpp:156-230; host2Device/device2Host 383-398). */
+GBN_API int gbn_alloc(gbn_ctx* ctx, size_t bytes, void** d_ptr);
+GBN_API int gbn_free(gbn_ctx* ctx, void* d_ptr);
+GBN_API int gbn_upload(gbn_ctx* ctx, void* d_dst, const void* h_src, size_t bytes);
+GBN_API int gbn_download(gbn_ctx* ctx, void* h_dst, const void* d_src, size_t bytes);
+GBN_API int gbn_memset(gbn_ctx* ctx, void* d_dst, int value, size_t bytes);
+/* page-locked host buffers for fast transfers */
+GBN_API int gbn_host_alloc(size_t bytes, void** h_ptr);
+GBN_API int gbn_host_free(void* h_ptr);
+
+/* ------------------------------------------------------------------------ */
+/* Operators (one entry per Process on the NESTA path).                     */
+/* ------------------------------------------------------------------------ */
+/* TemporalTV (TemporalTV.cpp:49-86; temporalTV.cl:49-107).
+ * FORWARD: out[f] = in[f] - in[(f-1) mod F]
+ * ADJOINT: out[f] = in[(f+1) mod F] - in[f]   (= -D^T, as the reference) */
+GBN_API int gbn_op_ttv(gbn_ctx* ctx, int direction, const float* d_in, float* d_out, int W, int H, int F);
+/* VectorNormalization (VectorNormalization.cpp:56-87; vectorNormalization.cl:42-56):
+ * out = in / max(mu, |in|), n complex elements; in place allowed. */
+GBN_API int gbn_op_normalize(gbn_ctx* ctx, const float* d_in, float* d_out, size_t n, float mu);
+/* ComplexElementProd (ComplexElementProd.cpp:64-131; complexElementProd.cl:42-76):
+ * out[f][c] = in[f] * S[c] (in_has_coils = 0, XData input) or in[f][c] * S[c]
+ * (in_has_coils = 1, KData input), S conjugated when conjugate = 1. */
+GBN_API int gbn_op_sensmul(gbn_ctx* ctx, int conjugate, const float* d_in, int in_has_coils, const float* d_S, float* d_out,
+                   int W, int H, int F, int C);
+/* XImageSum (XImageSum.cpp:79-96; xImageSum.cl:42-61): out[f] = sum_c in[f][c] */
+GBN_API int gbn_op_coilsum(gbn_ctx* ctx, const float* d_in, float* d_out, int W, int H, int F, int C);
+/* ApplyMask (ApplyMask.cpp:21-51; applyMask.cl:5-40): data[f][c][p] = 0 where mask[f][p] == 0 */
+GBN_API int gbn_op_mask(gbn_ctx* ctx, float* d_data, const uint8_t* d_mask, int W, int H, int F, int C);
+/* SamplingMasksData::rowmask2pixelmask (SamplingMasksData.cpp:389-441): rows
+ * with value 1 become 255, value 0 becomes 0; any other value is an error
+ * (reported through the return code after a device round trip). */
+GBN_API int gbn_op_rowmask_to_pixelmask(gbn_ctx* ctx, const uint32_t* d_rowmask, uint8_t* d_pixmask, int W, int H, int F);
+/* ComplexAbs (complexAbs.cl:43-70): out = (|in|, 0); ComplexAbsPow2
+ * (complexAbsPow2.cl:43-71): out = (|in|^2, 0).  n complex elements. */
+GBN_API int gbn_op_abs(gbn_ctx* ctx, const float* d_in, float* d_out, size_t n);
+GBN_API int gbn_op_abs2(gbn_ctx* ctx, const float* d_in, float* d_out, size_t n);
+/* FFT process, dim = -1 (FFT.cpp:116-201, 456-542): 2-D C2C over (W, H) of
+ * `batch` images stored back to back; FORWARD unscaled, BACKWARD scaled 1/(W*H);
+ * no fftshift.  In place allowed. */
+GBN_API int gbn_op_fft2(gbn_ctx* ctx, int direction, const float* d_in, float* d_out, int W, int H, int batch);
+/* NestaUp::operatorA plus the 1/sqrt(N) post-scale (NestaUp.cpp:162-190, 712-718):
+ * k[f][c] = mask[f] * FFT2(S[c] * x[f]) / sqrt(W*H) */
+GBN_API int gbn_op_encode(gbn_ctx* ctx, const float* d_x, const float* d_S, const uint8_t* d_mask, float* d_k, int W, int H,
+                  int F, int C);
+/* NestaUp::operatorAt with the sqrt(N) pre-scale (NestaUp.cpp:117-151, 749-753):
+ * x[f] = sum_c conj(S[c]) * IFFT2(sqrt(W*H) * k[f][c])   (no mask) */
+GBN_API int gbn_op_encode_adjoint(gbn_ctx* ctx, const float* d_k, const float* d_S, float* d_x, int W, int H, int F, int C);
+
+/* SimpleMRIRecon (src/processes/examples/SimpleMRIRecon.cpp:58-101):
+ * x[f] = sum_c conj(S[c]) * IFFT2(y[f][c]).  The input is not modified. */
+GBN_API int gbn_simple_recon(gbn_ctx* ctx, const float* d_y, const float* d_S, float* d_x, int W, int H, int F, int C);
+
+/* ------------------------------------------------------------------------ */
+/* NESTA (NestaUp::launch, NestaUp.cpp:442-910)                              */
+/* ------------------------------------------------------------------------ */
+/* NestaUp::LaunchParameters (NestaUp.hpp:67-83) without argsMC/showProgress
+ * (motion compensation and display are not part of this library). */
+typedef struct gbn_nesta_params {
+  float lambda_i;
+  float mu_f;
+  float La;
+  unsigned int maxIntIter;
+  float tolVar;
+  int verbose;
+  unsigned int maxIter;
+  unsigned int stoptest;
+  unsigned int miniter;
+} gbn_nesta_params;
+
+typedef struct gbn_nesta_stats {
+  float normU;        /* myNormest result (NestaUp.cpp:291-439) */
+  float maxX, maxUX;  /* max|x0|, max|U x0| (NestaUp.cpp:521-568) */
+  float lambda, muf, mu0;
+  float mu_final;
+  float tolVar_final; /* the reference writes this back into LaunchParameters::tolVar */
+  float fx_final;     /* objective of the last inner iteration */
+  float qp_final;
+  int inner_iters;    /* inner iterations executed, all outer loops */
+  int normest_iters;
+  int kept_rows;      /* k-space rows carried by the solver (sampled or nonzero) */
+} gbn_nesta_stats;
+
+/* Binds the caller's device buffers (not copied, not modified):
+ * y = KData [F][C][H][W], S = [C][H][W], mask = pixel mask [F][H][W].
+ * Allocates the solver workspace. */
+GBN_API int gbn_problem_create(gbn_ctx* ctx, int W, int H, int F, int C, const float* d_y, const float* d_S,
+                       const uint8_t* d_mask, gbn_problem** out);
+GBN_API int gbn_problem_destroy(gbn_problem* p);
+/* One reconstruction into d_x ([F][H][W], the reference's output XData).
+ * Runs asynchronously; when stats != NULL the call waits for completion and
+ * fills *stats. */
+GBN_API int gbn_nesta_run(gbn_ctx* ctx, gbn_problem* p, const gbn_nesta_params* params, float* d_x, gbn_nesta_stats* stats);
+/* End-to-end form with host buffers: uploads y, S and the pixel mask, runs,
+ * downloads x, and returns when x is on the host. */
+GBN_API int gbn_nesta_run_host(gbn_ctx* ctx, int W, int H, int F, int C, const float* h_y, const float* h_S,
+                       const uint8_t* h_mask, const gbn_nesta_params* params, float* h_x, gbn_nesta_stats* stats);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GBN_H */

@@ -1,0 +1,247 @@
+"""Device context and device arrays over the C ABI (numpy on the host side)."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _abi
+from ._abi import NestaParams, NestaStats, call
+
+
+class DeviceArray:
+    """A device allocation owned by a Context, with a numpy-like shape/dtype."""
+
+    def __init__(self, ctx: "Context", shape, dtype, ptr: int | None = None):
+        self.ctx = ctx
+        self.shape = tuple(int(s) for s in shape)
+        self.dtype = np.dtype(dtype)
+        self.nbytes = int(np.prod(self.shape, dtype=np.int64)) * self.dtype.itemsize
+        if ptr is None:
+            p = C.c_void_p()
+            call("gbn_alloc", ctx.handle, self.nbytes, C.byref(p))
+            ptr = p.value
+            self._owned = True
+        else:
+            self._owned = False
+        self.ptr = int(ptr)
+
+    @property
+    def size(self) -> int:
+        return int(np.prod(self.shape, dtype=np.int64))
+
+    def get(self) -> np.ndarray:
+        out = np.empty(self.shape, self.dtype)
+        call("gbn_download", self.ctx.handle, out.ctypes.data, self.ptr, self.nbytes)
+        return out
+
+    def set(self, arr: np.ndarray) -> "DeviceArray":
+        a = np.ascontiguousarray(arr, dtype=self.dtype)
+        if a.nbytes != self.nbytes:
+            raise ValueError(f"size mismatch: {a.nbytes} bytes into {self.nbytes}")
+        call("gbn_upload", self.ctx.handle, self.ptr, a.ctypes.data, self.nbytes)
+        self.ctx.sync()  # the host array may go away after return
+        return self
+
+    def zero(self) -> "DeviceArray":
+        call("gbn_memset", self.ctx.handle, self.ptr, 0, self.nbytes)
+        return self
+
+    def free(self) -> None:
+        if self._owned and self.ptr and self.ctx.handle:
+            call("gbn_free", self.ctx.handle, self.ptr)
+        self.ptr = 0
+
+    def __del__(self):
+        try:
+            self.free()
+        except Exception:
+            pass
+
+
+class Context:
+    """One device and one stream (the reference's CLapp, src/CLapp.cpp:188-575)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        call("gbn_ctx_create", int(device), C.byref(h))
+        self.handle = h.value
+        self.device = device
+
+    def close(self) -> None:
+        if self.handle:
+            call("gbn_ctx_destroy", self.handle)
+            self.handle = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    # memory -----------------------------------------------------------
+    def empty(self, shape, dtype) -> DeviceArray:
+        return DeviceArray(self, shape, dtype)
+
+    def zeros(self, shape, dtype) -> DeviceArray:
+        return DeviceArray(self, shape, dtype).zero()
+
+    def to_device(self, arr: np.ndarray) -> DeviceArray:
+        a = np.ascontiguousarray(arr)
+        d = DeviceArray(self, a.shape, a.dtype)
+        return d.set(a)
+
+    def sync(self) -> None:
+        call("gbn_ctx_sync", self.handle)
+
+    @property
+    def stream(self) -> int:
+        s = C.c_void_p()
+        call("gbn_ctx_get_stream", self.handle, C.byref(s))
+        return s.value or 0
+
+    def set_stream(self, stream: int | None) -> None:
+        call("gbn_ctx_set_stream", self.handle, stream)
+
+    def seed48(self, seed16v) -> None:
+        arr = (C.c_ushort * 3)(*seed16v)
+        call("gbn_ctx_seed48", self.handle, arr)
+
+    def rand48(self) -> tuple[int, int, int]:
+        arr = (C.c_ushort * 3)()
+        call("gbn_ctx_get_rand48", self.handle, arr)
+        return tuple(arr)
+
+    def set_tuning(self, key: str, value: int) -> None:
+        call("gbn_ctx_set_tuning", self.handle, key.encode(), int(value))
+
+
+def supported_lengths() -> list[int]:
+    buf = (C.c_int * 64)()
+    n = _abi.lib().gbn_supported_lengths(buf, 64)
+    return list(buf[:n])
+
+
+def _ck(a: DeviceArray, dtype) -> int:
+    if a.dtype != np.dtype(dtype):
+        raise TypeError(f"expected {np.dtype(dtype)}, got {a.dtype}")
+    return a.ptr
+
+
+# operator entry points on device arrays --------------------------------------
+def op_ttv(ctx: Context, direction: int, x: DeviceArray, out: DeviceArray) -> None:
+    F, H, W = x.shape
+    call("gbn_op_ttv", ctx.handle, direction, _ck(x, np.complex64), _ck(out, np.complex64), W, H, F)
+
+
+def op_normalize(ctx: Context, x: DeviceArray, out: DeviceArray, mu: float) -> None:
+    call("gbn_op_normalize", ctx.handle, _ck(x, np.complex64), _ck(out, np.complex64), x.size, float(mu))
+
+
+def op_sensmul(ctx: Context, conjugate: bool, x: DeviceArray, S: DeviceArray, out: DeviceArray) -> None:
+    F, Cc, H, W = out.shape
+    in_coils = 1 if len(x.shape) == 4 else 0
+    call("gbn_op_sensmul", ctx.handle, int(bool(conjugate)), _ck(x, np.complex64), in_coils,
+         _ck(S, np.complex64), _ck(out, np.complex64), W, H, F, Cc)
+
+
+def op_coilsum(ctx: Context, k: DeviceArray, out: DeviceArray) -> None:
+    F, Cc, H, W = k.shape
+    call("gbn_op_coilsum", ctx.handle, _ck(k, np.complex64), _ck(out, np.complex64), W, H, F, Cc)
+
+
+def op_mask(ctx: Context, k: DeviceArray, mask: DeviceArray) -> None:
+    F, Cc, H, W = k.shape
+    call("gbn_op_mask", ctx.handle, _ck(k, np.complex64), _ck(mask, np.uint8), W, H, F, Cc)
+
+
+def op_rowmask_to_pixelmask(ctx: Context, rowmask: DeviceArray, pixmask: DeviceArray) -> None:
+    F, H, W = pixmask.shape
+    call("gbn_op_rowmask_to_pixelmask", ctx.handle, _ck(rowmask, np.uint32), _ck(pixmask, np.uint8), W, H, F)
+
+
+def op_abs(ctx: Context, x: DeviceArray, out: DeviceArray, squared: bool = False) -> None:
+    call("gbn_op_abs2" if squared else "gbn_op_abs", ctx.handle, _ck(x, np.complex64),
+         _ck(out, np.complex64), x.size)
+
+
+def op_fft2(ctx: Context, direction: int, x: DeviceArray, out: DeviceArray) -> None:
+    H, W = x.shape[-2:]
+    batch = x.size // (H * W)
+    call("gbn_op_fft2", ctx.handle, direction, _ck(x, np.complex64), _ck(out, np.complex64), W, H, batch)
+
+
+def op_encode(ctx: Context, x: DeviceArray, S: DeviceArray, mask: DeviceArray, out: DeviceArray) -> None:
+    F, Cc, H, W = out.shape
+    call("gbn_op_encode", ctx.handle, _ck(x, np.complex64), _ck(S, np.complex64), _ck(mask, np.uint8),
+         _ck(out, np.complex64), W, H, F, Cc)
+
+
+def op_encode_adjoint(ctx: Context, k: DeviceArray, S: DeviceArray, out: DeviceArray) -> None:
+    F, Cc, H, W = k.shape
+    call("gbn_op_encode_adjoint", ctx.handle, _ck(k, np.complex64), _ck(S, np.complex64),
+         _ck(out, np.complex64), W, H, F, Cc)
+
+
+def simple_recon(ctx: Context, y: DeviceArray, S: DeviceArray, out: DeviceArray) -> None:
+    F, Cc, H, W = y.shape
+    call("gbn_simple_recon", ctx.handle, _ck(y, np.complex64), _ck(S, np.complex64),
+         _ck(out, np.complex64), W, H, F, Cc)
+
+
+class Problem:
+    """Solver workspace bound to device-resident y, S and pixel mask."""
+
+    def __init__(self, ctx: Context, y: DeviceArray, S: DeviceArray, mask: DeviceArray):
+        F, Cc, H, W = y.shape
+        h = C.c_void_p()
+        call("gbn_problem_create", ctx.handle, W, H, F, Cc, _ck(y, np.complex64), _ck(S, np.complex64),
+             _ck(mask, np.uint8), C.byref(h))
+        self.handle = h.value
+        self.ctx, self.shape = ctx, (F, Cc, H, W)
+        self._keep = (y, S, mask)
+
+    def run(self, params: NestaParams, out: DeviceArray, stats: bool = True) -> dict | None:
+        st = NestaStats() if stats else None
+        call("gbn_nesta_run", self.ctx.handle, self.handle, C.byref(params), _ck(out, np.complex64),
+             C.byref(st) if st is not None else None)
+        return st.as_dict() if st is not None else None
+
+    def close(self) -> None:
+        if self.handle:
+            call("gbn_problem_destroy", self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def nesta_params(lambda_i=1e-2, mu_f=3e-4, La=1.0, maxIntIter=4, tolVar=3e-4, verbose=1, maxIter=100,
+                 stoptest=1, miniter=7) -> NestaParams:
+    """NestaUp::LaunchParameters (NestaUp.hpp:67-83); defaults are tests/MRIRecon.cpp:105-114."""
+    return NestaParams(float(lambda_i), float(mu_f), float(La), int(maxIntIter), float(tolVar), int(verbose),
+                       int(maxIter), int(stoptest), int(miniter))
+
+
+def nesta_run_host(ctx: Context, y: np.ndarray, S: np.ndarray, mask: np.ndarray, params: NestaParams,
+                   out: np.ndarray | None = None) -> tuple[np.ndarray, dict]:
+    """End-to-end reconstruction from host arrays (uploads, runs, downloads)."""
+    F, Cc, H, W = y.shape
+    y = np.ascontiguousarray(y, np.complex64)
+    S = np.ascontiguousarray(S, np.complex64)
+    mask = np.ascontiguousarray(mask, np.uint8)
+    if out is None:
+        out = np.empty((F, H, W), np.complex64)
+    st = NestaStats()
+    call("gbn_nesta_run_host", ctx.handle, W, H, F, Cc, y.ctypes.data, S.ctypes.data, mask.ctypes.data,
+         C.byref(params), out.ctypes.data, C.byref(st))
+    return out, st.as_dict()

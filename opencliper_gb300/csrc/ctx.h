@@ -1,0 +1,75 @@
+// Library-private definitions of the context and problem objects behind the
+// C ABI (include/gbn.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <map>
+#include <string>
+
+#include "gbn.h"
+#include "registry.h"
+#include "types.h"
+
+struct gbn_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  bool own_stream = true;
+  int nsm = 0;
+  std::map<int, float2*> tw;          // device twiddle tables, one per supported length
+  float2* tw_block = nullptr;         // single allocation holding all tables
+  uint64_t rand48 = 0x1234ABCD330EULL;  // drand48 state (glibc default before any seeding)
+  void* scratch = nullptr;            // grow-only scratch for per-operator entry points
+  size_t scratch_bytes = 0;
+  int k1_coils_per_block = 2;         // tuning: coils per CTA in the forward column pass
+  int k2_ctas_per_sm = 4;             // tuning: persistent CTAs per SM in the row pass
+};
+
+struct gbn_problem {
+  gbn_ctx* ctx = nullptr;
+  int W = 0, H = 0, F = 0, C = 0;
+  const float2* y = nullptr;          // caller's KData, not owned
+  const float2* S = nullptr;          // caller's sensitivity maps, not owned
+  const uint8_t* mask = nullptr;      // caller's pixel mask, not owned
+  // owned workspace
+  int* flags = nullptr;               // [F*H]
+  int* full_fh = nullptr;             // [F*H]
+  int* rowmap = nullptr;              // [F*H]
+  int* rowoff = nullptr;              // [F+1]
+  int* rows_h = nullptr;              // [F*H]
+  int* rows_f = nullptr;              // [F*H]
+  int* row_full = nullptr;            // [F*H]
+  float2* T = nullptr;                // [F*H*C*W] worst case
+  float2* xk0 = nullptr;
+  float2* xk1 = nullptr;
+  float2* wacc = nullptr;
+  gbn::NestaDevState* st = nullptr;
+  float* fmean = nullptr;
+  int fmean_cap = 0;
+  double* part_tv = nullptr;
+  int part_tv_cap = 0;
+  double* part_r = nullptr;
+  int part_r_cap = 0;
+  double* part_ne = nullptr;          // power-method partial sums
+  int part_ne_cap = 0;
+};
+
+namespace gbn {
+
+// error helpers (capi.cu)
+int set_error(int code, const std::string& msg);
+int cuda_status(cudaError_t e, const char* what);
+
+// twiddle table for length L (nullptr when unsupported)
+const float2* ctx_twiddles(gbn_ctx* ctx, int L);
+// grow-only scratch of at least `bytes`
+int ctx_scratch(gbn_ctx* ctx, size_t bytes, void** out);
+
+// drand48 arithmetic on 48-bit states (POSIX: X' = (0x5DEECE66D X + 0xB) mod 2^48)
+struct Lcg48 {
+  uint64_t a, c;  // X -> a*X + c (mod 2^48)
+};
+Lcg48 lcg48_jump(uint64_t k);
+uint64_t lcg48_apply(const Lcg48& j, uint64_t x);
+
+}  // namespace gbn

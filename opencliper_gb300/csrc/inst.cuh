@@ -1,0 +1,52 @@
+// Host launchers for the templated kernels of one transform length.
+#pragma once
+
+#include "nesta_kernels.cuh"
+#include "registry.h"
+
+namespace gbn {
+
+template <int L>
+struct Launchers {
+  static void fwd_cols(const FusedArgs& a, int it, int cpb, dim3 grid, cudaStream_t s) {
+    k_fwd_cols<L><<<grid, kColNT, 0, s>>>(a, it, cpb);
+  }
+  static void rows(const FusedArgs& a, int it, bool resid, int grid, cudaStream_t s) {
+    if (resid)
+      k_rows<L, true><<<grid, kRowNT, 0, s>>>(a, it);
+    else
+      k_rows<L, false><<<grid, kRowNT, 0, s>>>(a, it);
+  }
+  static void inv_cols(const FusedArgs& a, int it, bool update, dim3 grid, cudaStream_t s) {
+    if (update)
+      k_inv_cols<L, true><<<grid, kColNT, 0, s>>>(a, it);
+    else
+      k_inv_cols<L, false><<<grid, kColNT, 0, s>>>(a, it);
+  }
+  static void fft_rows(const float2* in, float2* out, int nrows, int inv, float scale, const float2* tw, int grid,
+                       cudaStream_t s) {
+    k_fft_rows_dense<L><<<grid, kRowNT, 0, s>>>(in, out, nrows, inv, scale, tw);
+  }
+  static void fft_cols(const float2* in, float2* out, int W, int nimg, int inv, float scale, const float2* tw,
+                       cudaStream_t s) {
+    k_fft_cols_dense<L><<<dim3(W / kWB, nimg), kColNT, 0, s>>>(in, out, W, inv, scale, tw);
+  }
+  static SizeKernels entry() {
+    static_assert(fft_size_ok(L), "unsupported transform length");
+    return SizeKernels{L, &fwd_cols, &rows, &inv_cols, &fft_rows, &fft_cols, RowCfg<L>::RPC};
+  }
+};
+
+}  // namespace gbn
+
+// Defines gbn::register_sizes_<TAG>(SizeKernels* out) returning the count.
+#define GBN_SIZE_TU(TAG, ...)                                              \
+  namespace gbn {                                                          \
+  int register_sizes_##TAG(SizeKernels* out) {                             \
+    const SizeKernels e[] = {__VA_ARGS__};                                 \
+    const int n = int(sizeof(e) / sizeof(e[0]));                           \
+    for (int i = 0; i < n; ++i) out[i] = e[i];                             \
+    return n;                                                              \
+  }                                                                        \
+  }
+#define GBN_L(L) gbn::Launchers<L>::entry()

@@ -1,0 +1,592 @@
+// tTV-NESTA solver: launch sequence of NestaUp::launch
+// (src/processes/nesta/NestaUp.cpp:442-910) on one CUDA stream with all scalar
+// bookkeeping kept on the device, plus the non-templated kernels (kept-row
+// analysis, initial maxima, power-method norm estimate, scalar setup).
+#include <algorithm>
+#include <climits>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "ctx.h"
+#include "nesta_kernels.cuh"
+
+namespace gbn {
+
+constexpr int kNeIters = 100;  // myNormest maxiter (NestaUp.cpp:294)
+constexpr int kNeNT = 256;
+
+// ---------------------------------------------------------------------------
+// drand48 jump-ahead (host and device)
+// ---------------------------------------------------------------------------
+constexpr uint64_t kMask48 = (1ULL << 48) - 1;
+constexpr uint64_t kRandA = 0x5DEECE66DULL, kRandC = 0xBULL;
+
+__host__ __device__ inline Lcg48 lcg_compose(Lcg48 first, Lcg48 second) {
+  // x -> second(first(x)) = sa*(fa*x + fc) + sc
+  return Lcg48{(second.a * first.a) & kMask48, (second.a * first.c + second.c) & kMask48};
+}
+__host__ __device__ inline Lcg48 lcg_jump_k(uint64_t k) {
+  Lcg48 r{1, 0}, b{kRandA, kRandC};
+  while (k) {
+    if (k & 1) r = lcg_compose(r, b);
+    b = lcg_compose(b, b);
+    k >>= 1;
+  }
+  return r;
+}
+Lcg48 lcg48_jump(uint64_t k) { return lcg_jump_k(k); }
+uint64_t lcg48_apply(const Lcg48& j, uint64_t x) { return (j.a * x + j.c) & kMask48; }
+
+// ---------------------------------------------------------------------------
+// Kept k-space rows: a row (f, h) is carried by the solver when its mask row
+// has any sampled pixel or any coil holds a nonzero datum there.  Rows that are
+// neither contribute exactly zero to E^H(Ex - y) and to ||Ex - y||^2.
+// grid = (H, F)
+// ---------------------------------------------------------------------------
+__global__ void k_rowflags(const float2* __restrict__ y, const uint8_t* __restrict__ mask, int W, int H, int F, int C,
+                           int* __restrict__ flags, int* __restrict__ full) {
+  const int h = blockIdx.x, f = blockIdx.y, t = threadIdx.x;
+  const uint8_t* m = mask + (size_t(f) * H + h) * W;
+  int any = 0, all = 1;
+  for (int w = t; w < W; w += blockDim.x) {
+    const int nz = m[w] != 0;
+    any |= nz;
+    all &= nz;
+  }
+  any = __syncthreads_or(any);
+  all = __syncthreads_and(all);
+  if (!any) {
+    for (int c = 0; c < C && !any; ++c) {
+      const float4* yr = reinterpret_cast<const float4*>(y + ((size_t(f) * C + c) * H + h) * W);
+      int nz = 0;
+      for (int i = t; i < W / 2; i += blockDim.x) {
+        const float4 v = yr[i];
+        nz |= (v.x != 0.f) | (v.y != 0.f) | (v.z != 0.f) | (v.w != 0.f);
+      }
+      any = __syncthreads_or(nz);
+    }
+  }
+  if (t == 0) {
+    flags[f * H + h] = any;
+    full[f * H + h] = all;
+  }
+}
+
+// one CTA of 512 threads (H <= 512): per-frame prefix numbering of kept rows
+__global__ void __launch_bounds__(512) k_rowscan(const int* __restrict__ flags, const int* __restrict__ full, int H,
+                                                 int F, int* __restrict__ rowmap, int* __restrict__ rowoff,
+                                                 int* __restrict__ rows_h, int* __restrict__ rows_f,
+                                                 int* __restrict__ row_full) {
+  __shared__ int wsum[16];
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  int base = 0;
+  for (int f = 0; f < F; ++f) {
+    const int fl = (t < H) ? flags[f * H + t] : 0;
+    const unsigned bal = __ballot_sync(0xffffffffu, fl);
+    const int pre = __popc(bal & ((1u << lane) - 1u));
+    if (lane == 0) wsum[wid] = __popc(bal);
+    __syncthreads();
+    int woff = 0, tot = 0;
+    for (int i = 0; i < 16; ++i) {
+      if (i < wid) woff += wsum[i];
+      tot += wsum[i];
+    }
+    if (t < H) {
+      const int j = fl ? woff + pre : -1;
+      rowmap[f * H + t] = j;
+      if (fl) {
+        rows_h[base + j] = t;
+        rows_f[base + j] = f;
+        row_full[base + j] = full[f * H + t];
+      }
+    }
+    if (t == 0) rowoff[f] = base;
+    base += tot;
+    __syncthreads();
+  }
+  if (t == 0) rowoff[F] = base;
+}
+
+// every row kept, in natural order (SimpleMRIRecon: fully sampled data)
+__global__ void k_rows_identity(int H, int F, int* __restrict__ rowmap, int* __restrict__ rowoff,
+                                int* __restrict__ rows_h, int* __restrict__ rows_f, int* __restrict__ row_full) {
+  const int n = H * F;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    rowmap[i] = i % H;
+    rows_h[i] = i % H;
+    rows_f[i] = i / H;
+    row_full[i] = 1;
+  }
+  for (int f = blockIdx.x * blockDim.x + threadIdx.x; f <= F; f += gridDim.x * blockDim.x) rowoff[f] = f * H;
+}
+
+// ---------------------------------------------------------------------------
+// State initialisation from the launch parameters (one thread).
+// ---------------------------------------------------------------------------
+__global__ void k_state_init(NestaDevState* st, gbn_nesta_params p) {
+  NestaDevState s;
+  memset(&s, 0, sizeof(s));
+  s.lambda_i = p.lambda_i;
+  s.mu_f = p.mu_f;
+  s.La = p.La;
+  s.tolVar_in = p.tolVar;
+  s.maxIntIter = int(p.maxIntIter);
+  s.maxIter = int(p.maxIter);
+  s.stoptest = int(p.stoptest);
+  s.miniter = int(p.miniter);
+  s.last_iter = -1;
+  *st = s;
+}
+
+// ---------------------------------------------------------------------------
+// max|x0| and max|U x0| (NestaUp.cpp:521-568: ComplexAbs + host loop).  Values
+// are non-negative, so float order equals unsigned order of their bits.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) k_maxima(const float2* __restrict__ x, int N, int F, NestaDevState* st) {
+  __shared__ float s1[8], s2[8];
+  const size_t total = size_t(N) * F;
+  float m1 = 0.f, m2 = 0.f;
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < total; i += size_t(gridDim.x) * blockDim.x) {
+    const int f = int(i / N);
+    const size_t p = i - size_t(f) * N;
+    const float2 a = x[i];
+    const float2 b = x[size_t((f + F - 1) % F) * N + p];
+    const float2 d = csub(a, b);
+    m1 = fmaxf(m1, sqrtf(a.x * a.x + a.y * a.y));
+    m2 = fmaxf(m2, sqrtf(d.x * d.x + d.y * d.y));
+  }
+  m1 = warp_max(m1);
+  m2 = warp_max(m2);
+  if ((threadIdx.x & 31) == 0) {
+    s1[threadIdx.x >> 5] = m1;
+    s2[threadIdx.x >> 5] = m2;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    for (int i = 1; i < 8; ++i) {
+      m1 = fmaxf(m1, s1[i]);
+      m2 = fmaxf(m2, s2[i]);
+    }
+    atomicMax(&st->maxX_bits, __float_as_uint(m1));
+    atomicMax(&st->maxUX_bits, __float_as_uint(m2));
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Power method for ||U|| (myNormest, NestaUp.cpp:291-439).
+//
+// The start vector is all ones, so U x = 0 exactly and the reference always
+// restarts from r = (drand48(), 0) drawn in [frame][row][col] order
+// (NestaUp.cpp:369-385).  From there e_1 = ||r|| and, for m >= 1,
+// e_{m+1} = ||D b_m|| / ||b_m|| with b_1 = D^T r and b_{m+1} = D^T D b_m
+// (the reference's per-iteration normalisations and the sign of its adjoint
+// kernel cancel in these ratios).  D acts along frames only, so every pixel's
+// frame vector evolves independently: one thread per pixel runs all 99 steps
+// in registers (scaled by 1/4 per step, exact in binary floating point, to
+// stay in range) and per-step sums of ||b_m||^2 and ||D b_m||^2 are reduced
+// per block; k_normest_final replays the reference's stopping rule on them.
+// part layout: [block][m][2], m in [0, kNeIters), m = 0 holds ||r||^2.
+// ---------------------------------------------------------------------------
+template <int FMAX>
+__global__ void __launch_bounds__(kNeNT) k_normest_pixels(int N, int F, unsigned long long x0,
+                                                          unsigned long long jumpN_a, unsigned long long jumpN_c,
+                                                          double* __restrict__ part) {
+  __shared__ float sw[kNeNT / 32][kNeIters][2];
+  const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
+  const int p = blockIdx.x * kNeNT + t;
+  const bool act = p < N;
+  float b[FMAX], d[FMAX];
+  {
+    // element (f, p) is draw number f*N + p + 1 after the state x0
+    const Lcg48 jp = lcg_jump_k(uint64_t(act ? p : 0) + 1);
+    uint64_t X = (jp.a * x0 + jp.c) & kMask48;
+#pragma unroll
+    for (int f = 0; f < FMAX; ++f) {
+      if (f < F && act) {
+        d[f] = __double2float_rn(double(X) * 0x1p-48);
+        X = (jumpN_a * X + jumpN_c) & kMask48;
+      } else {
+        d[f] = 0.f;
+      }
+    }
+  }
+  float s0 = 0.f;
+#pragma unroll
+  for (int f = 0; f < FMAX; ++f) s0 = fmaf(d[f], d[f], s0);
+  // b_1 = D^T r: (D^T v)_f = v_f - v_{f+1 mod F}
+#pragma unroll
+  for (int f = 0; f < FMAX; ++f) {
+    const float nx = (f + 1 < FMAX && f + 1 < F) ? d[(f + 1) % FMAX] : d[0];
+    b[f] = (f < F) ? d[f] - nx : 0.f;
+  }
+  float r0 = s0;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) r0 += __shfl_down_sync(0xffffffffu, r0, o);
+  if (lane == 0) {
+    sw[wid][0][0] = r0;
+    sw[wid][0][1] = 0.f;
+  }
+  for (int m = 1; m < kNeIters; ++m) {
+    float last = b[0];
+#pragma unroll
+    for (int f = 1; f < FMAX; ++f)
+      if (f == F - 1) last = b[f];
+    float sb = 0.f, sd = 0.f;
+#pragma unroll
+    for (int f = 0; f < FMAX; ++f) {
+      const float pv = (f == 0) ? last : b[(f + FMAX - 1) % FMAX];
+      d[f] = (f < F) ? b[f] - pv : 0.f;
+      sb = fmaf(b[f], b[f], sb);
+      sd = fmaf(d[f], d[f], sd);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      sb += __shfl_down_sync(0xffffffffu, sb, o);
+      sd += __shfl_down_sync(0xffffffffu, sd, o);
+    }
+    if (lane == 0) {
+      sw[wid][m][0] = sb;
+      sw[wid][m][1] = sd;
+    }
+#pragma unroll
+    for (int f = 0; f < FMAX; ++f) {
+      const float nx = (f + 1 < FMAX && f + 1 < F) ? d[(f + 1) % FMAX] : d[0];
+      b[f] = (f < F) ? (d[f] - nx) * 0.25f : 0.f;
+    }
+  }
+  __syncthreads();
+  for (int i = t; i < kNeIters * 2; i += kNeNT) {
+    double s = 0.0;
+    for (int w = 0; w < kNeNT / 32; ++w) s += double(sw[w][i >> 1][i & 1]);
+    part[size_t(blockIdx.x) * kNeIters * 2 + i] = s;
+  }
+}
+
+__global__ void __launch_bounds__(256) k_normest_final(const double* __restrict__ part, int nblk, int N, int F,
+                                                       NestaDevState* st) {
+  __shared__ double tot[kNeIters * 2];
+  for (int i = threadIdx.x; i < kNeIters * 2; i += blockDim.x) {
+    double s = 0.0;
+    for (int b = 0; b < nblk; ++b) s += part[size_t(b) * kNeIters * 2 + i];
+    tot[i] = s;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const float n = float(unsigned(N) * unsigned(F));
+    const float tol = 1e-3f;
+    float e = sqrtf(n);  // ||ones||
+    float e0 = 0.f;
+    int cnt = 0;
+    while (fabsf(e - e0) > tol * e && cnt < kNeIters) {
+      e0 = e;
+      if (cnt == 0)
+        e = float(sqrt(tot[0]));
+      else
+        e = float(sqrt(tot[2 * cnt + 1] / tot[2 * cnt]));
+      ++cnt;
+    }
+    st->normU = e;
+    st->normest_iters = cnt;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Derived constants (NestaUp.cpp:570-583), one thread.
+// ---------------------------------------------------------------------------
+__global__ void k_setup(NestaDevState* st) {
+  NestaDevState& s = *st;
+  s.maxX = __uint_as_float(s.maxX_bits);
+  s.maxUX = __uint_as_float(s.maxUX_bits);
+  s.lambda = s.lambda_i * s.maxX;
+  s.muf = s.mu_f * s.maxX;
+  s.mu0 = float(0.9 * double(s.maxUX));
+  const float muL = s.lambda / s.La;
+  if (muL > s.mu0) s.mu0 = muL;
+  s.gamma = float(pow(double(s.muf / s.mu0), 1.0 / double(unsigned(s.maxIntIter))));
+  s.mu = s.mu0;
+  s.gammat = float(pow(double(s.tolVar_in) / 0.1, 1.0 / double(unsigned(s.maxIntIter))));
+  s.tolVar = 0.1f;
+}
+
+// Start of an outer (continuation) loop (NestaUp.cpp:604-648):
+// mu and tolVar updates, Lmu, w = 0, x_k = x_ref.
+__global__ void k_outer_begin(NestaDevState* st, float* fmean, const float2* __restrict__ xref,
+                              float2* __restrict__ xk0, float2* __restrict__ wacc, size_t n) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    NestaDevState& s = *st;
+    s.nl += 1;
+    s.mu = s.mu * s.gamma;
+    s.tolVar = s.tolVar * s.gammat;
+    s.Ak = 0.0f;
+    float Lmu = s.normU / s.mu;
+    if (s.miniter > 0) fmean[s.miniter - 1] = float(LONG_MAX);
+    Lmu = s.lambda * Lmu + s.La;
+    s.Lmu = Lmu;
+    s.Lmu1 = 1.0f / Lmu;
+    s.qpDone = 0;
+    s.last_iter = s.maxIter - 1;
+  }
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+    xk0[i] = xref[i];
+    wacc[i] = make_float2(0.f, 0.f);
+  }
+}
+
+// End of an outer loop: x_ref = x_k (NestaUp.cpp:889).
+__global__ void k_outer_end(const NestaDevState* st, const float2* __restrict__ xk0, const float2* __restrict__ xk1,
+                            float2* __restrict__ xref, size_t n) {
+  const float2* src = ((st->last_iter + 1) & 1) ? xk1 : xk0;
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
+    xref[i] = src[i];
+}
+
+// ---------------------------------------------------------------------------
+// Host side
+// ---------------------------------------------------------------------------
+namespace {
+
+template <typename T>
+int grow(T*& p, int& cap, int need) {
+  if (need <= cap) return GBN_OK;
+  if (p) cudaFree(p);
+  p = nullptr;
+  cap = 0;
+  if (cudaMalloc(&p, sizeof(T) * size_t(need)) != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(GBN_ERR_NOMEM, "workspace allocation failed");
+  }
+  cap = need;
+  return GBN_OK;
+}
+
+int normest_fmax(int F) { return F <= 8 ? 8 : F <= 16 ? 16 : F <= 32 ? 32 : F <= 64 ? 64 : 0; }
+
+void launch_normest(int fmax, int nblk, cudaStream_t s, int N, int F, uint64_t x0, const Lcg48& jN, double* part) {
+  switch (fmax) {
+    case 8: k_normest_pixels<8><<<nblk, kNeNT, 0, s>>>(N, F, x0, jN.a, jN.c, part); break;
+    case 16: k_normest_pixels<16><<<nblk, kNeNT, 0, s>>>(N, F, x0, jN.a, jN.c, part); break;
+    case 32: k_normest_pixels<32><<<nblk, kNeNT, 0, s>>>(N, F, x0, jN.a, jN.c, part); break;
+    default: k_normest_pixels<64><<<nblk, kNeNT, 0, s>>>(N, F, x0, jN.a, jN.c, part); break;
+  }
+}
+
+}  // namespace
+
+int problem_alloc(gbn_problem* P) {
+  const size_t FH = size_t(P->F) * P->H;
+  const size_t X = size_t(P->F) * P->H * P->W;
+  const size_t K = X * P->C;
+  cudaError_t e = cudaSuccess;
+  auto A = [&](void** p, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMalloc(p, bytes);
+  };
+  A((void**)&P->flags, FH * sizeof(int));
+  A((void**)&P->full_fh, FH * sizeof(int));
+  A((void**)&P->rowmap, FH * sizeof(int));
+  A((void**)&P->rowoff, (P->F + 1) * sizeof(int));
+  A((void**)&P->rows_h, FH * sizeof(int));
+  A((void**)&P->rows_f, FH * sizeof(int));
+  A((void**)&P->row_full, FH * sizeof(int));
+  A((void**)&P->T, K * sizeof(float2));
+  A((void**)&P->xk0, X * sizeof(float2));
+  A((void**)&P->xk1, X * sizeof(float2));
+  A((void**)&P->wacc, X * sizeof(float2));
+  A((void**)&P->st, sizeof(NestaDevState));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_error(GBN_ERR_NOMEM, std::string("problem workspace allocation failed: ") + cudaGetErrorString(e));
+  }
+  return GBN_OK;
+}
+
+void problem_free(gbn_problem* P) {
+  void* ptrs[] = {P->flags, P->full_fh, P->rowmap, P->rowoff, P->rows_h, P->rows_f, P->row_full, P->T,
+                  P->xk0,   P->xk1,     P->wacc,   P->st,     P->fmean,  P->part_tv, P->part_r, P->part_ne};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+}
+
+// Kept-row analysis for the current contents of y and mask (device only).
+void launch_row_analysis(gbn_problem* P, cudaStream_t s) {
+  k_rowflags<<<dim3(P->H, P->F), 128, 0, s>>>(P->y, P->mask, P->W, P->H, P->F, P->C, P->flags, P->full_fh);
+  k_rowscan<<<1, 512, 0, s>>>(P->flags, P->full_fh, P->H, P->F, P->rowmap, P->rowoff, P->rows_h, P->rows_f,
+                              P->row_full);
+}
+
+FusedArgs make_args(gbn_problem* P, float2* xref) {
+  gbn_ctx* ctx = P->ctx;
+  FusedArgs a;
+  memset(&a, 0, sizeof(a));
+  a.W = P->W;
+  a.H = P->H;
+  a.F = P->F;
+  a.C = P->C;
+  a.N = P->W * P->H;
+  a.y = P->y;
+  a.S = P->S;
+  a.mask = P->mask;
+  a.rowmap = P->rowmap;
+  a.rowoff = P->rowoff;
+  a.rows_h = P->rows_h;
+  a.rows_f = P->rows_f;
+  a.row_full = P->row_full;
+  a.T = P->T;
+  a.xk0 = P->xk0;
+  a.xk1 = P->xk1;
+  a.xref = xref;
+  a.wacc = P->wacc;
+  a.st = P->st;
+  a.fmean = P->fmean;
+  a.part_tv = P->part_tv;
+  a.part_r = P->part_r;
+  a.twH = ctx_twiddles(ctx, P->H);
+  a.twW = ctx_twiddles(ctx, P->W);
+  const unsigned N = unsigned(P->W) * unsigned(P->H);
+  a.s_fwd = float(1.0 / std::sqrt(double(N)));               // NestaUp.cpp:712: 1/(sqrt(cols*rows*slices))
+  a.s_adj = std::sqrt(float(N)) * (1.0f / float(N));        // NestaUp.cpp:749 sqrt(float(N)) times clFFT 1/N
+  return a;
+}
+
+int validate_problem_dims(int W, int H, int F, int C) {
+  if (W <= 0 || H <= 0 || F <= 0 || C <= 0) return set_error(GBN_ERR_INVALID, "dimensions must be positive");
+  if (W % 8 != 0) return set_error(GBN_ERR_INVALID, "NDArray dimension 0 (width) is not multiple of 8");
+  if (!find_size(W) || !find_size(H))
+    return set_error(GBN_ERR_UNSUPPORTED,
+                     "FFT lengths must be 7-smooth multiples of 8 in [8, 512] (got W=" + std::to_string(W) +
+                         ", H=" + std::to_string(H) + ")");
+  return GBN_OK;
+}
+
+int nesta_run(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, float2* x_out, gbn_nesta_stats* stats) {
+  if (!ctx || !P || !prm || !x_out) return set_error(GBN_ERR_INVALID, "null argument");
+  if (P->F < 2) return set_error(GBN_ERR_INVALID, "temporal TV needs at least 2 frames (F=1 makes ||U|| undefined)");
+  if (prm->stoptest == 1 && prm->miniter == 0) return set_error(GBN_ERR_INVALID, "miniter must be >= 1 when stoptest == 1");
+  const int fmax = normest_fmax(P->F);
+  if (!fmax) return set_error(GBN_ERR_UNSUPPORTED, "more than 64 frames is not supported");
+  const SizeKernels* kh = find_size(P->H);
+  const SizeKernels* kw = find_size(P->W);
+  if (!kh || !kw) return set_error(GBN_ERR_UNSUPPORTED, "unsupported FFT length");
+  const int W = P->W, H = P->H, F = P->F, C = P->C, N = W * H;
+  cudaStream_t s = ctx->stream;
+
+  const int cpb = std::max(1, std::min(ctx->k1_coils_per_block, C));
+  const dim3 g1(W / kWB, (C + cpb - 1) / cpb, F);
+  const int nblk_k1 = int(g1.x * g1.y * g1.z);
+  const long long rows_max = (long long)F * H * C;
+  const int g2 = int(std::max<long long>(1, std::min<long long>((rows_max + kw->rows_per_cta - 1) / kw->rows_per_cta,
+                                                                 (long long)ctx->nsm * ctx->k2_ctas_per_sm)));
+  const dim3 g3(W / kWB, F);
+  const int nblk_ne = (N + kNeNT - 1) / kNeNT;
+  int rc;
+  if ((rc = grow(P->fmean, P->fmean_cap, std::max<int>(1, int(prm->miniter)))) != GBN_OK) return rc;
+  if ((rc = grow(P->part_tv, P->part_tv_cap, 2 * nblk_k1)) != GBN_OK) return rc;
+  if ((rc = grow(P->part_r, P->part_r_cap, g2)) != GBN_OK) return rc;
+  if ((rc = grow(P->part_ne, P->part_ne_cap, nblk_ne * kNeIters * 2)) != GBN_OK) return rc;
+
+  FusedArgs a = make_args(P, x_out);
+  a.nblk_k1 = nblk_k1;
+  const size_t X = size_t(N) * F;
+  const int gx = int(std::min<size_t>((X + 255) / 256, size_t(ctx->nsm) * 8));
+
+  k_state_init<<<1, 1, 0, s>>>(P->st, *prm);
+  launch_row_analysis(P, s);
+  // x0 = E^H y (NestaUp.cpp:465-486)
+  kw->rows(a, 0, false, g2, s);
+  kh->inv_cols(a, 0, false, g3, s);
+  // maxima, norm estimate, constants (NestaUp.cpp:521-583)
+  k_maxima<<<gx, 256, 0, s>>>(x_out, N, F, P->st);
+  const Lcg48 jN = lcg_jump_k(uint64_t(N));
+  launch_normest(fmax, nblk_ne, s, N, F, ctx->rand48, jN, P->part_ne);
+  ctx->rand48 = lcg48_apply(lcg_jump_k(uint64_t(N) * uint64_t(F)), ctx->rand48);
+  k_normest_final<<<1, 256, 0, s>>>(P->part_ne, nblk_ne, N, F, P->st);
+  k_setup<<<1, 1, 0, s>>>(P->st);
+
+  for (unsigned nl = 1; nl <= prm->maxIntIter; ++nl) {
+    k_outer_begin<<<gx, 256, 0, s>>>(P->st, P->fmean, x_out, P->xk0, P->wacc, X);
+    for (unsigned it = 0; it < prm->maxIter; ++it) {
+      kh->fwd_cols(a, int(it), cpb, g1, s);
+      kw->rows(a, int(it), true, g2, s);
+      kh->inv_cols(a, int(it), true, g3, s);
+    }
+    k_outer_end<<<gx, 256, 0, s>>>(P->st, P->xk0, P->xk1, x_out, X);
+  }
+  cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_status(e, "nesta launch");
+  if (stats) {
+    NestaDevState h;
+    int G = 0;
+    if ((e = cudaMemcpyAsync(&h, P->st, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+      return cuda_status(e, "stats copy");
+    if ((e = cudaMemcpyAsync(&G, P->rowoff + F, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+      return cuda_status(e, "stats copy");
+    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e, "nesta run");
+    stats->normU = h.normU;
+    stats->maxX = h.maxX;
+    stats->maxUX = h.maxUX;
+    stats->lambda = h.lambda;
+    stats->muf = h.muf;
+    stats->mu0 = h.mu0;
+    stats->mu_final = h.mu;
+    stats->tolVar_final = h.tolVar;
+    stats->fx_final = h.fx;
+    stats->qp_final = h.qp;
+    stats->inner_iters = h.iters_total;
+    stats->normest_iters = h.normest_iters;
+    stats->kept_rows = G;
+  }
+  return GBN_OK;
+}
+
+// SimpleMRIRecon: x = sum_c conj(S_c) ifft2(y_c) through the adjoint row and
+// column passes with every row kept.
+int simple_recon(gbn_ctx* ctx, const float2* y, const float2* S, float2* x, int W, int H, int F, int C) {
+  const SizeKernels* kh = find_size(H);
+  const SizeKernels* kw = find_size(W);
+  if (!kh || !kw) return set_error(GBN_ERR_UNSUPPORTED, "unsupported FFT length");
+  const size_t FH = size_t(F) * H, K = FH * C * W;
+  // scratch: T [F*H][C][W] + rowmap/rowoff/rows_h/rows_f
+  const size_t bytes = K * sizeof(float2) + (3 * FH + F + 1 + FH) * sizeof(int) + 256;
+  void* scr = nullptr;
+  int rc = ctx_scratch(ctx, bytes, &scr);
+  if (rc != GBN_OK) return rc;
+  float2* T = reinterpret_cast<float2*>(scr);
+  int* ip = reinterpret_cast<int*>(T + K);
+  int* rowmap = ip;
+  int* rows_h = rowmap + FH;
+  int* rows_f = rows_h + FH;
+  int* row_full = rows_f + FH;
+  int* rowoff = row_full + FH;
+  cudaStream_t s = ctx->stream;
+  k_rows_identity<<<int(std::min<size_t>((FH + 255) / 256, 1024)), 256, 0, s>>>(H, F, rowmap, rowoff, rows_h, rows_f,
+                                                                                row_full);
+  FusedArgs a;
+  memset(&a, 0, sizeof(a));
+  a.W = W;
+  a.H = H;
+  a.F = F;
+  a.C = C;
+  a.N = W * H;
+  a.y = y;
+  a.S = S;
+  a.rowmap = rowmap;
+  a.rowoff = rowoff;
+  a.rows_h = rows_h;
+  a.rows_f = rows_f;
+  a.row_full = row_full;
+  a.T = T;
+  a.xref = x;
+  a.twH = ctx_twiddles(ctx, H);
+  a.twW = ctx_twiddles(ctx, W);
+  a.s_adj = 1.0f / float(W * H);  // clFFT BACKWARD scale
+  const long long rows = (long long)FH * C;
+  const int g2 = int(std::max<long long>(
+      1, std::min<long long>((rows + kw->rows_per_cta - 1) / kw->rows_per_cta, (long long)ctx->nsm * ctx->k2_ctas_per_sm)));
+  kw->rows(a, 0, false, g2, s);
+  kh->inv_cols(a, 0, false, dim3(W / kWB, F), s);
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_status(e, "simple recon launch");
+  return GBN_OK;
+}
+
+}  // namespace gbn

@@ -1,0 +1,68 @@
+// Structures shared by host and device code of the tTV-NESTA solver.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gbn {
+
+// Scalar state of one NESTA reconstruction, kept in device memory so that the
+// whole solve runs without host round trips.  Field meanings follow the local
+// variables of NestaUp::launch (src/processes/nesta/NestaUp.cpp:442-910).
+struct NestaDevState {
+  // launch parameters (NestaUp::LaunchParameters, NestaUp.hpp:67-83)
+  float lambda_i, mu_f, La, tolVar_in;
+  int maxIntIter, maxIter, stoptest, miniter;
+
+  // initial maxima (NestaUp.cpp:521-568), as float bit patterns for atomicMax
+  unsigned int maxX_bits, maxUX_bits;
+
+  // derived constants (NestaUp.cpp:572-583)
+  float maxX, maxUX, lambda, muf, mu0, normU, gamma, gammat;
+  int normest_iters;
+
+  // per outer (continuation) loop (NestaUp.cpp:604-648)
+  float mu, tolVar, Lmu, Lmu1, Ak;
+  int nl;
+
+  // per inner iteration (NestaUp.cpp:651-880)
+  int last_iter;  // index of the last inner iteration that runs in this outer loop
+  int qpDone;
+  float qp, fx, apk, tauk;
+  float normUk, fxdot, l2term;
+  unsigned int ticket;
+
+  // statistics
+  int iters_total;
+  int status;
+};
+
+// Arguments of the fused per-iteration kernels (passed by value).
+struct FusedArgs {
+  int W, H, F, C, N;
+  const float2* y;        // KData [F][C][H][W], zero-copy
+  const float2* S;        // SensitivityMaps [C][H][W]
+  const uint8_t* mask;    // pixel mask [F][H][W] (0 = not sampled)
+  // kept k-space rows (rows with any sampled pixel or any nonzero datum)
+  const int* rowmap;      // [F][H] -> index j within the frame, or -1
+  const int* rowoff;      // [F+1] prefix count of kept rows; G = rowoff[F]
+  const int* rows_h;      // [G] row (phase-encode line) of kept row g
+  const int* rows_f;      // [G] frame of kept row g
+  const int* row_full;    // [G] 1 when the pixel mask row is entirely sampled
+  float2* T;              // intermediates [G][C][W]
+  float2* xk0;            // x_k ping
+  float2* xk1;            // x_k pong
+  float2* xref;           // x_ref == output XData [F][H][W]
+  float2* wacc;           // Nesterov weighted gradient sum w_k
+  NestaDevState* st;
+  float* fmean;           // [miniter] rolling objective buffer
+  double* part_tv;        // [nblk_k1][2] partial sums of ||u||^2 and Re<u,d>
+  double* part_r;         // [nblk_k2] partial sums of ||E x - y||^2
+  const float2* twH;      // twiddles w_H^j (forward sign), j in [0,H)
+  const float2* twW;      // twiddles w_W^j
+  float s_fwd;            // 1/sqrt(N) as the reference computes it (double -> float)
+  float s_adj;            // sqrt(N)/N: the reference's sqrt(N) pre-scale times clFFT's 1/N
+  int nblk_k1;            // number of blocks of the forward column kernel
+};
+
+}  // namespace gbn
