@@ -1,0 +1,367 @@
+#!/usr/bin/env python3
+"""Benchmark: tTV-NESTA reconstructions per second on GB300.
+
+Workload (one step = one complete reconstruction, NestaUp::launch end to end:
+kept-row analysis, x0 = E^H y, maxima, power-method norm estimate, 100 NESTA
+iterations): 256 x 256 image series with 20 frames and 12 coils, Cartesian
+phase-encode undersampling R = 8, mu_f = 1e-3, lambda_i = 0.01, 100 fixed
+iterations, plain FP32 (complex64).  Inputs are seeded synthetic data with the
+workload's shapes (no dataset is available offline).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Multi-GPU: one process per GPU (torchrun); every rank runs independent
+replicas of the workload (the path shards only across reconstructions), no
+data-path collective; value = all ranks' reconstructions / max rank time.
+
+`--impl reference` times the reference algorithm's CPU implementation on the
+host cores: the reference's OpenCL library cannot be built here, so this is
+the FP32 CPU restatement of NestaUp::launch (oracle port).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "tTV-NESTA recons/s at NRMSE≤1e-3 vs FP64: mixed+batched vs plain FP32, GB300"
+UNIT = "recons/s"
+WL = dict(W=256, H=256, F=20, C=12, R=8, seed=0)
+NESTA = dict(lambda_i=0.01, mu_f=1e-3, La=1.0, maxIntIter=1, maxIter=100, stoptest=0, miniter=7, tolVar=3e-4)
+L2_FLUSH_BYTES = 256 << 20
+
+
+def workload_config(extra: dict | None = None) -> dict:
+    cfg = {"workload": "tTV-NESTA cine CS, 256x256 x 20 frames, 12 coils, R=8, 100 iterations, plain FP32",
+           **{k: WL[k] for k in ("W", "H", "F", "C", "R")}, "iterations": NESTA["maxIter"],
+           "mu_f": NESTA["mu_f"], "lambda_i": NESTA["lambda_i"],
+           "l2": "flushed between timed steps (256 MiB device write)", "parallelism": "replicas"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+DATA_DESC = ("synthetic: seeded 10-ellipse cine phantom x smooth phase, Gaussian coil maps, "
+             "variable-density row masks, noise 1e-3")
+
+
+# ---------------------------------------------------------------------------
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Host-side barrier and max-reduction over ranks (gloo); no GPU collective."""
+
+    def __init__(self):
+        self.ws, self.rank, self.local = dist_env()
+        self.pg = None
+        if self.ws > 1:
+            import torch.distributed as td
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            td.init_process_group("gloo", rank=self.rank, world_size=self.ws)
+            self.td = td
+
+    def barrier(self):
+        if self.ws > 1:
+            self.td.barrier()
+
+    def max(self, v: float) -> float:
+        if self.ws == 1:
+            return v
+        import torch
+        t = torch.tensor([v], dtype=torch.float64)
+        self.td.all_reduce(t, op=self.td.ReduceOp.MAX)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.td.destroy_process_group()
+
+
+class ClockSampler:
+    """nvidia-smi SM clock / throttle-reason samples during the timed region."""
+
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, local_rank: int):
+        vis = os.environ.get("CUDA_VISIBLE_DEVICES")
+        idx = vis.split(",")[local_rank] if vis else str(local_rank)
+        self.lines: list[str] = []
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--id={idx}", f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except (OSError, ValueError):
+            self.p = None
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self) -> dict:
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.t.join(timeout=2)
+        sm, mx, pw, reasons = [], [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+                pw.append(float(f[2]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower().startswith("active"):
+                    reasons.add(n)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "power_w_max": max(pw) if pw else None, "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def measured_peak_hbm() -> tuple[float, str]:
+    p = ROOT / "MEASURED_PEAKS.json"
+    try:
+        return float(json.loads(p.read_text())["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def algorithmic_bytes(kind: str, G: int) -> int:
+    """Compulsory DRAM bytes of one launch of a fused kernel (complex64 = 8 B)."""
+    W, H, F, C = WL["W"], WL["H"], WL["F"], WL["C"]
+    N = W * H
+    X, Sb, T = 8 * N * F, 8 * N * C, 8 * G * C * W
+    if kind == "fwd_cols":   # x_k, S in; kept rows of DFT_H(S x) out
+        return X + Sb + T
+    if kind == "rows":       # T in, kept rows of y and mask in, T out
+        return T + T + G * W + T
+    if kind == "inv_cols":   # T, S, x_k, x_ref, w in; x_{k+1}, w out
+        return T + Sb + 3 * X + 2 * X
+    raise KeyError(kind)
+
+
+def ncu_traffic(kind: str) -> float | None:
+    """DRAM bytes per launch from the committed ncu summary, when present."""
+    p = ROOT / "profiles" / "dram_traffic.json"
+    try:
+        d = json.loads(p.read_text())
+        return float(d[kind]["bytes_per_launch"])
+    except (OSError, KeyError, ValueError):
+        return None
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args, dist: Dist) -> dict | None:
+    import torch
+
+    import opencliper_gb300 as g
+    from opencliper_gb300 import synth
+
+    torch.cuda.set_device(dist.local)
+    stream = torch.cuda.current_stream()
+    prob_h = synth.make_problem(WL["W"], WL["H"], WL["F"], WL["C"], WL["R"], seed=WL["seed"] + dist.rank)
+    ctx = g.Context(dist.local)
+    ctx.set_stream(stream.cuda_stream)
+    y, S, m = ctx.to_device(prob_h.y), ctx.to_device(prob_h.S), ctx.to_device(prob_h.mask)
+    x = ctx.empty((WL["F"], WL["H"], WL["W"]), np.complex64)
+    prob = g.Problem(ctx, y, S, m)
+    prm = g.nesta_params(**NESTA)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device="cuda")
+
+    st = prob.run(prm, x, stats=True)  # first run: stats (kept rows) and warm-up
+    for _ in range(max(0, args.warmup - 1)):
+        prob.run(prm, x, stats=False)
+    torch.cuda.synchronize()
+
+    # ---- device-resident throughput -------------------------------------
+    K = args.steps
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    dist.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dist.local)
+    n0 = ctx.launch_count()
+    wall0 = time.perf_counter()
+    for k in range(K):
+        flush.fill_(k & 0xFF)
+        ev[k][0].record(stream)
+        prob.run(prm, x, stats=False)
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - wall0
+    clk = clocks.stop()
+    dist.barrier()
+    launches = ctx.launch_count() - n0
+    t_ms = sum(a.elapsed_time(b) for a, b in ev)
+    t_max = dist.max(t_ms)
+
+    # ---- end to end through the C ABI with pinned host buffers ------------
+    import ctypes as C
+
+    from opencliper_gb300._abi import call
+    hy = torch.from_numpy(prob_h.y.view(np.float32)).pin_memory()
+    hS = torch.from_numpy(prob_h.S.view(np.float32)).pin_memory()
+    hm = torch.from_numpy(prob_h.mask).pin_memory()
+    hx = torch.empty(x.nbytes // 4, dtype=torch.float32).pin_memory()
+    bi = hy.numel() * 4 + hS.numel() * 4 + hm.numel()
+    bo = x.nbytes
+
+    def e2e_step():
+        call("gbn_upload", ctx.handle, y.ptr, hy.data_ptr(), y.nbytes)
+        call("gbn_upload", ctx.handle, S.ptr, hS.data_ptr(), S.nbytes)
+        call("gbn_upload", ctx.handle, m.ptr, hm.data_ptr(), m.nbytes)
+        prob.run(prm, x, stats=False)
+        call("gbn_download_async", ctx.handle, C.c_void_p(hx.data_ptr()), x.ptr, x.nbytes)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    dist.barrier()
+    torch.cuda.synchronize()
+    for k in range(K):
+        flush.fill_(k & 0xFF)
+        ev2[k][0].record(stream)
+        e2e_step()
+        ev2[k][1].record(stream)
+    torch.cuda.synchronize()
+    dist.barrier()
+    t2_max = dist.max(sum(a.elapsed_time(b) for a, b in ev2))
+
+    # ---- live per-kernel durations for the roofline ----------------------
+    ctx.profile(True)
+    ctx.profile_reset()
+    for _ in range(2):
+        flush.fill_(1)
+        prob.run(prm, x, stats=False)
+    prof = ctx.profile_read()
+    ctx.profile(False)
+    G = int(st["kept_rows"])
+    fused = {k: prof[k] for k in ("fwd_cols", "rows", "inv_cols")}
+    dom = max(fused, key=lambda k: fused[k][1])
+    n_dom, ms_dom = fused[dom]
+    avg_s = ms_dom / 1e3 / max(n_dom, 1)
+    alg = algorithmic_bytes(dom, G)
+    peak, peak_src = measured_peak_hbm()
+    achieved = alg / avg_s / 1e9
+    traffic = ncu_traffic(dom)
+    total_prof = sum(v[1] for v in prof.values())
+    roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+            "frac": round(achieved / peak, 4), "peak_source": f"{peak_src} hbm_gbs",
+            "traffic": traffic, "algorithmic_bytes_per_launch": alg, "avg_launch_us": round(avg_s * 1e6, 2),
+            "share_of_step": round(ms_dom / max(total_prof, 1e-9), 3),
+            "groups_us_per_launch": {k: round(v[1] * 1e3 / max(v[0], 1), 2) for k, v in prof.items()}}
+
+    ctx.set_stream(None)
+    prob.close()
+    for a in (y, S, m, x):
+        a.free()
+    ctx.close()
+    n = dist.ws
+    out = {"metric": METRIC, "value": round(n * K / (t_max / 1e3), 3), "unit": UNIT, "n_gpus": n, "steps": K,
+           "warmup": args.warmup, "ms_per_step": round(t_max / K, 4), "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "c64", "data": DATA_DESC,
+           "config": workload_config({"kept_rows": G}),
+           "e2e": {"value": round(n * K / (t2_max / 1e3), 3), "unit": UNIT, "h2d_bytes_per_step": int(bi),
+                   "d2h_bytes_per_step": int(bo)},
+           "gpu_launches": int(launches), "roofline": roof, "clocks": clk,
+           "wall_s_timed_region": round(wall, 3)}
+    return out
+
+
+def cpu_port_sample(iters: int = 3) -> dict:
+    """FP32 CPU restatement timed on a bounded sample: setup plus `iters` inner
+    iterations of one reconstruction, extrapolated to the full 100."""
+    from opencliper_gb300 import synth
+    from oracle import nesta_ref as R
+    p = synth.make_problem(WL["W"], WL["H"], WL["F"], WL["C"], WL["R"], seed=WL["seed"])
+    prm = R.NestaParams(**{**NESTA, "maxIter": iters})
+    tm: dict = {}
+    t0 = time.perf_counter()
+    R.nesta(p.y, p.S, p.mask, prm, "f32", timings=tm)
+    wall = time.perf_counter() - t0
+    per_iter = float(np.mean(tm["iters"]))
+    est = tm["setup"] + NESTA["maxIter"] * per_iter
+    return {"value": round(1.0 / est, 6), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+            "sample": f"FP32 numpy/scipy restatement (scipy.fft workers={os.cpu_count()}): setup "
+                      f"{tm['setup']:.2f} s + {iters} inner iterations ({per_iter:.3f} s each) of one "
+                      f"reconstruction of this workload, extrapolated to {NESTA['maxIter']} iterations",
+            "est_seconds_per_recon": round(est, 3), "sample_wall_s": round(wall, 2)}
+
+
+def run_reference(args, dist: Dist) -> dict | None:
+    if dist.rank != 0:
+        return None
+    samples = []
+    for k in range(args.warmup + args.steps):
+        s = cpu_port_sample(iters=2)
+        if k >= args.warmup:
+            samples.append(s["est_seconds_per_recon"])
+    est = float(np.mean(samples))
+    v = round(1.0 / est, 6)
+    return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": dist.ws,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(est * 1e3, 2),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": DATA_DESC,
+            "config": workload_config(),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                             "sample": "per step: FP32 numpy/scipy restatement of NestaUp::launch, setup + 2 "
+                                       "inner iterations of one reconstruction, extrapolated to 100 iterations "
+                                       "(the reference's OpenCL build is unavailable: no OpenCL ICD, clFFT, "
+                                       "CLBlast)"},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU restatement timing")
+    args = ap.parse_args(argv)
+    if args.warmup < 3:
+        args.warmup = 3
+    dist = Dist()
+    try:
+        if args.impl == "reference":
+            out = run_reference(args, dist)
+        else:
+            out = run_ours(args, dist)
+            if out is not None and dist.rank == 0 and dist.ws == 1:
+                out["cpu_baseline"] = (cpu_port_sample() if not args.no_cpu_baseline else
+                                       {"value": None, "unit": UNIT, "cores": 0, "kind": "port",
+                                        "sample": "skipped (--no-cpu-baseline)"})
+    finally:
+        dist.close()
+    if out is not None and dist.rank == 0:
+        print(json.dumps(out), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

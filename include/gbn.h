@@ -89,6 +89,25 @@ GBN_API int gbn_ctx_seed48(gbn_ctx* ctx, const unsigned short seed16v[3]);
 GBN_API int gbn_ctx_get_rand48(gbn_ctx* ctx, unsigned short state16v[3]);
 /* tuning knobs: "k1_coils_per_block", "k2_ctas_per_sm" */
 GBN_API int gbn_ctx_set_tuning(gbn_ctx* ctx, const char* key, int value);
+/* number of kernels this context has launched so far */
+GBN_API int gbn_ctx_launch_count(gbn_ctx* ctx, unsigned long long* count);
+
+/* Kernel-group timing with CUDA events on the context stream, the analogue of
+ * ProfileParameters{enable} and ProcessCore::getKernelGroupExecutionTimes
+ * (ProcessCore.hpp:71-84, ProcessCore.cpp:270-300).  While enabled, every
+ * launch of a group is bracketed by two events; gbn_ctx_profile_read waits for
+ * the stream and returns the launches and summed milliseconds of one group. */
+enum {
+  GBN_PROF_FWD_COLS = 0, /* forward column pass (S x -> kept rows)        */
+  GBN_PROF_ROWS = 1,     /* row pass (residual and its row transform)     */
+  GBN_PROF_INV_COLS = 2, /* adjoint column pass + tTV gradient + update   */
+  GBN_PROF_SETUP = 3,    /* x0, maxima, norm estimate, row analysis       */
+  GBN_PROF_OUTER = 4,    /* continuation-loop begin/end copies            */
+  GBN_PROF_KINDS = 5
+};
+GBN_API int gbn_ctx_profile(gbn_ctx* ctx, int enable);
+GBN_API int gbn_ctx_profile_read(gbn_ctx* ctx, int kind, unsigned long long* launches, double* total_ms);
+GBN_API int gbn_ctx_profile_reset(gbn_ctx* ctx);
 
 /* Device memory (DeviceDataProperties::createEmptyDeviceBuffers,
  * DeviceDataProperties.cpp:156-230; host2Device/device2Host 383-398). */
@@ -96,6 +115,8 @@ GBN_API int gbn_alloc(gbn_ctx* ctx, size_t bytes, void** d_ptr);
 GBN_API int gbn_free(gbn_ctx* ctx, void* d_ptr);
 GBN_API int gbn_upload(gbn_ctx* ctx, void* d_dst, const void* h_src, size_t bytes);
 GBN_API int gbn_download(gbn_ctx* ctx, void* h_dst, const void* d_src, size_t bytes);
+/* like gbn_download but returns without waiting (h_dst should be page-locked) */
+GBN_API int gbn_download_async(gbn_ctx* ctx, void* h_dst, const void* d_src, size_t bytes);
 GBN_API int gbn_memset(gbn_ctx* ctx, void* d_dst, int value, size_t bytes);
 /* page-locked host buffers for fast transfers */
 GBN_API int gbn_host_alloc(size_t bytes, void** h_ptr);

@@ -24,6 +24,8 @@ GBN_FFT_BACKWARD = 1
 GBN_NOT_CONJUGATE = 0
 GBN_CONJUGATE = 1
 
+PROFILE_KINDS = {"fwd_cols": 0, "rows": 1, "inv_cols": 2, "setup": 3, "outer": 4}
+
 
 class GbnError(RuntimeError):
     def __init__(self, code: int, msg: str):
@@ -66,10 +68,15 @@ SIGNATURES: dict[str, list] = {
     "gbn_ctx_seed48": [_vp, C.POINTER(C.c_ushort)],
     "gbn_ctx_get_rand48": [_vp, C.POINTER(C.c_ushort)],
     "gbn_ctx_set_tuning": [_vp, C.c_char_p, _i],
+    "gbn_ctx_launch_count": [_vp, C.POINTER(C.c_ulonglong)],
+    "gbn_ctx_profile": [_vp, _i],
+    "gbn_ctx_profile_read": [_vp, _i, C.POINTER(C.c_ulonglong), C.POINTER(C.c_double)],
+    "gbn_ctx_profile_reset": [_vp],
     "gbn_alloc": [_vp, _sz, C.POINTER(_vp)],
     "gbn_free": [_vp, _vp],
     "gbn_upload": [_vp, _vp, _vp, _sz],
     "gbn_download": [_vp, _vp, _vp, _sz],
+    "gbn_download_async": [_vp, _vp, _vp, _sz],
     "gbn_memset": [_vp, _vp, _i, _sz],
     "gbn_host_alloc": [_sz, C.POINTER(_vp)],
     "gbn_host_free": [_vp],

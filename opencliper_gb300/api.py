@@ -121,6 +121,26 @@ class Context:
     def set_tuning(self, key: str, value: int) -> None:
         call("gbn_ctx_set_tuning", self.handle, key.encode(), int(value))
 
+    def launch_count(self) -> int:
+        n = C.c_ulonglong()
+        call("gbn_ctx_launch_count", self.handle, C.byref(n))
+        return int(n.value)
+
+    def profile(self, enable: bool) -> None:
+        call("gbn_ctx_profile", self.handle, int(bool(enable)))
+
+    def profile_reset(self) -> None:
+        call("gbn_ctx_profile_reset", self.handle)
+
+    def profile_read(self) -> dict[str, tuple[int, float]]:
+        """{group: (launches, total ms)} of the event-profiled kernel groups."""
+        out = {}
+        for name, kind in _abi.PROFILE_KINDS.items():
+            n, ms = C.c_ulonglong(), C.c_double()
+            call("gbn_ctx_profile_read", self.handle, kind, C.byref(n), C.byref(ms))
+            out[name] = (int(n.value), float(ms.value))
+        return out
+
 
 def supported_lengths() -> list[int]:
     buf = (C.c_int * 64)()

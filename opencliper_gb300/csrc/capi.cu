@@ -100,6 +100,49 @@ const float2* ctx_twiddles(gbn_ctx* ctx, int L) {
   return it == ctx->tw.end() ? nullptr : it->second;
 }
 
+namespace {
+cudaEvent_t prof_event(gbn_ctx* ctx) {
+  cudaEvent_t ev = nullptr;
+  if (!ctx->prof_pool.empty()) {
+    ev = ctx->prof_pool.back();
+    ctx->prof_pool.pop_back();
+  } else if (cudaEventCreate(&ev) != cudaSuccess) {
+    cudaGetLastError();
+    ev = nullptr;
+  }
+  return ev;
+}
+}  // namespace
+
+void prof_begin(gbn_ctx* ctx, int, cudaEvent_t* ev) {
+  *ev = prof_event(ctx);
+  if (*ev) cudaEventRecord(*ev, ctx->stream);
+}
+
+void prof_end(gbn_ctx* ctx, int kind, cudaEvent_t start) {
+  cudaEvent_t stop = prof_event(ctx);
+  if (!start || !stop) return;
+  cudaEventRecord(stop, ctx->stream);
+  ctx->prof_pending.push_back({kind, start, stop});
+}
+
+int prof_collect(gbn_ctx* ctx) {
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e != cudaSuccess) return cuda_status(e, "profile collect");
+  for (auto& p : ctx->prof_pending) {
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, p.start, p.stop) == cudaSuccess && p.kind >= 0 && p.kind < 8) {
+      ctx->prof_ms[p.kind] += ms;
+      ctx->prof_count[p.kind] += 1;
+    }
+    ctx->prof_pool.push_back(p.start);
+    ctx->prof_pool.push_back(p.stop);
+  }
+  ctx->prof_pending.clear();
+  cudaGetLastError();
+  return GBN_OK;
+}
+
 int ctx_scratch(gbn_ctx* ctx, size_t bytes, void** out) {
   if (bytes > ctx->scratch_bytes) {
     if (ctx->scratch) {
@@ -142,19 +185,25 @@ int gbn_ctx_create(int device, gbn_ctx** out) {
     delete ctx;
     return cuda_status(e, "context setup");
   }
-  // twiddle tables w_L^j = (cos, -sin)(2 pi j / L) for every supported length
+  // two-pass twiddle tables for every supported length L = A*B:
+  // [k1*B + s] = w_L^(s*k1) (k1 < A, s < B) and [L + k1'*A + s'] = w_L^(s'*k1')
+  // (k1' < B, s' < A), w_L^j = (cos, -sin)(2 pi j / L)
   int lens[64];
   const int nl = supported_sizes(lens, 64);
   size_t total = 0;
-  for (int i = 0; i < nl; ++i) total += size_t(lens[i]);
+  for (int i = 0; i < nl; ++i) total += 2 * size_t(lens[i]);
   std::vector<float2> h(total);
   size_t off = 0;
   std::vector<size_t> offs(nl);
+  auto w = [](long long j, long long L) { return make_float2(float(cx_cos2pi(j, L)), -float(cx_sin2pi(j, L))); };
   for (int i = 0; i < nl; ++i) {
+    const int L = lens[i], A = split_a(L), B = split_b(L);
     offs[i] = off;
-    for (int j = 0; j < lens[i]; ++j)
-      h[off + j] = make_float2(float(cx_cos2pi(j, lens[i])), -float(cx_sin2pi(j, lens[i])));
-    off += size_t(lens[i]);
+    for (int k1 = 0; k1 < A; ++k1)
+      for (int s = 0; s < B; ++s) h[off + size_t(k1) * B + s] = w((long long)s * k1, L);
+    for (int k1 = 0; k1 < B; ++k1)
+      for (int s = 0; s < A; ++s) h[off + L + size_t(k1) * A + s] = w((long long)s * k1, L);
+    off += 2 * size_t(L);
   }
   if ((e = cudaMalloc(&ctx->tw_block, total * sizeof(float2))) != cudaSuccess ||
       (e = cudaMemcpy(ctx->tw_block, h.data(), total * sizeof(float2), cudaMemcpyHostToDevice)) != cudaSuccess) {
@@ -171,6 +220,11 @@ int gbn_ctx_destroy(gbn_ctx* ctx) {
   CHECK_CTX(ctx);
   cudaStreamSynchronize(ctx->stream);
   free_host_cache(ctx);
+  for (auto& p : ctx->prof_pending) {
+    cudaEventDestroy(p.start);
+    cudaEventDestroy(p.stop);
+  }
+  for (cudaEvent_t ev : ctx->prof_pool) cudaEventDestroy(ev);
   if (ctx->scratch) cudaFree(ctx->scratch);
   if (ctx->tw_block) cudaFree(ctx->tw_block);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -236,6 +290,44 @@ int gbn_ctx_set_tuning(gbn_ctx* ctx, const char* key, int value) {
   return GBN_OK;
 }
 
+int gbn_ctx_launch_count(gbn_ctx* ctx, unsigned long long* count) {
+  CHECK_CTX(ctx);
+  if (!count) return set_error(GBN_ERR_INVALID, "null output pointer");
+  *count = ctx->launches;
+  return GBN_OK;
+}
+
+int gbn_ctx_profile(gbn_ctx* ctx, int enable) {
+  CHECK_CTX(ctx);
+  if (!enable && ctx->profile) {
+    int rc = prof_collect(ctx);
+    if (rc) return rc;
+  }
+  ctx->profile = enable != 0;
+  return GBN_OK;
+}
+
+int gbn_ctx_profile_read(gbn_ctx* ctx, int kind, unsigned long long* launches, double* total_ms) {
+  CHECK_CTX(ctx);
+  if (kind < 0 || kind >= GBN_PROF_KINDS) return set_error(GBN_ERR_INVALID, "unknown profile kind");
+  int rc = prof_collect(ctx);
+  if (rc) return rc;
+  if (launches) *launches = ctx->prof_count[kind];
+  if (total_ms) *total_ms = ctx->prof_ms[kind];
+  return GBN_OK;
+}
+
+int gbn_ctx_profile_reset(gbn_ctx* ctx) {
+  CHECK_CTX(ctx);
+  int rc = prof_collect(ctx);
+  if (rc) return rc;
+  for (int i = 0; i < 8; ++i) {
+    ctx->prof_ms[i] = 0.0;
+    ctx->prof_count[i] = 0;
+  }
+  return GBN_OK;
+}
+
 int gbn_alloc(gbn_ctx* ctx, size_t bytes, void** d_ptr) {
   CHECK_CTX(ctx);
   if (!d_ptr) return set_error(GBN_ERR_INVALID, "null output pointer");
@@ -261,6 +353,12 @@ int gbn_download(gbn_ctx* ctx, void* h_dst, const void* d_src, size_t bytes) {
   cudaError_t e = cudaMemcpyAsync(h_dst, d_src, bytes, cudaMemcpyDeviceToHost, ctx->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
   return cuda_status(e, "download");
+}
+
+int gbn_download_async(gbn_ctx* ctx, void* h_dst, const void* d_src, size_t bytes) {
+  CHECK_CTX(ctx);
+  if ((!h_dst || !d_src) && bytes) return set_error(GBN_ERR_INVALID, "null buffer");
+  return cuda_status(cudaMemcpyAsync(h_dst, d_src, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download");
 }
 
 int gbn_memset(gbn_ctx* ctx, void* d_dst, int value, size_t bytes) {

@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <map>
 #include <string>
+#include <vector>
 
 #include "gbn.h"
 #include "registry.h"
@@ -23,6 +24,17 @@ struct gbn_ctx {
   size_t scratch_bytes = 0;
   int k1_coils_per_block = 2;         // tuning: coils per CTA in the forward column pass
   int k2_ctas_per_sm = 4;             // tuning: persistent CTAs per SM in the row pass
+  unsigned long long launches = 0;    // kernels launched by this context
+  // event profiling of kernel groups (reference: ProcessCore::getKernelGroupExecutionTimes)
+  bool profile = false;
+  struct ProfEntry {
+    int kind;
+    cudaEvent_t start, stop;
+  };
+  std::vector<ProfEntry> prof_pending;
+  std::vector<cudaEvent_t> prof_pool;
+  double prof_ms[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  unsigned long long prof_count[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
 struct gbn_problem {
@@ -52,6 +64,8 @@ struct gbn_problem {
   int part_r_cap = 0;
   double* part_ne = nullptr;          // power-method partial sums
   int part_ne_cap = 0;
+  float* ne_b = nullptr;              // power-method frame vectors between chunks [F][N]
+  int ne_b_cap = 0;
 };
 
 namespace gbn {
@@ -64,6 +78,11 @@ int cuda_status(cudaError_t e, const char* what);
 const float2* ctx_twiddles(gbn_ctx* ctx, int L);
 // grow-only scratch of at least `bytes`
 int ctx_scratch(gbn_ctx* ctx, size_t bytes, void** out);
+
+// event-profiling helpers: bracket one launch of kernel group `kind`
+void prof_begin(gbn_ctx* ctx, int kind, cudaEvent_t* ev);
+void prof_end(gbn_ctx* ctx, int kind, cudaEvent_t ev);
+int prof_collect(gbn_ctx* ctx);
 
 // drand48 arithmetic on 48-bit states (POSIX: X' = (0x5DEECE66D X + 0xB) mod 2^48)
 struct Lcg48 {

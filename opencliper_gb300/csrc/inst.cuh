@@ -6,22 +6,41 @@
 
 namespace gbn {
 
+// opt a kernel into more than 48 KB of dynamic shared memory (once)
+template <typename K>
+inline void allow_smem(K kernel, int bytes, bool& done) {
+  if (!done) {
+    cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+    done = true;
+  }
+}
+
 template <int L>
 struct Launchers {
   static void fwd_cols(const FusedArgs& a, int it, int cpb, dim3 grid, cudaStream_t s) {
-    k_fwd_cols<L><<<grid, kColNT, 0, s>>>(a, it, cpb);
+    static bool ok = false;
+    allow_smem(k_fwd_cols<L>, FwdColsSmem<L>::BYTES, ok);
+    k_fwd_cols<L><<<grid, kColNT, FwdColsSmem<L>::BYTES, s>>>(a, it, cpb);
   }
   static void rows(const FusedArgs& a, int it, bool resid, int grid, cudaStream_t s) {
-    if (resid)
-      k_rows<L, true><<<grid, kRowNT, 0, s>>>(a, it);
-    else
-      k_rows<L, false><<<grid, kRowNT, 0, s>>>(a, it);
+    static bool ok1 = false, ok0 = false;
+    if (resid) {
+      allow_smem(k_rows<L, true>, RowsSmem<L, true>::BYTES, ok1);
+      k_rows<L, true><<<grid, kRowNT, RowsSmem<L, true>::BYTES, s>>>(a, it);
+    } else {
+      allow_smem(k_rows<L, false>, RowsSmem<L, false>::BYTES, ok0);
+      k_rows<L, false><<<grid, kRowNT, RowsSmem<L, false>::BYTES, s>>>(a, it);
+    }
   }
   static void inv_cols(const FusedArgs& a, int it, bool update, dim3 grid, cudaStream_t s) {
-    if (update)
-      k_inv_cols<L, true><<<grid, kColNT, 0, s>>>(a, it);
-    else
-      k_inv_cols<L, false><<<grid, kColNT, 0, s>>>(a, it);
+    static bool ok1 = false, ok0 = false;
+    if (update) {
+      allow_smem(k_inv_cols<L, true>, InvColsSmem<L>::BYTES, ok1);
+      k_inv_cols<L, true><<<grid, kColNT, InvColsSmem<L>::BYTES, s>>>(a, it);
+    } else {
+      allow_smem(k_inv_cols<L, false>, InvColsSmem<L>::BYTES, ok0);
+      k_inv_cols<L, false><<<grid, kColNT, InvColsSmem<L>::BYTES, s>>>(a, it);
+    }
   }
   static void fft_rows(const float2* in, float2* out, int nrows, int inv, float scale, const float2* tw, int grid,
                        cudaStream_t s) {

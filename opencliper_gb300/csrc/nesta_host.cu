@@ -182,22 +182,32 @@ __global__ void __launch_bounds__(256) k_maxima(const float2* __restrict__ x, in
 // e_{m+1} = ||D b_m|| / ||b_m|| with b_1 = D^T r and b_{m+1} = D^T D b_m
 // (the reference's per-iteration normalisations and the sign of its adjoint
 // kernel cancel in these ratios).  D acts along frames only, so every pixel's
-// frame vector evolves independently: one thread per pixel runs all 99 steps
-// in registers (scaled by 1/4 per step, exact in binary floating point, to
-// stay in range) and per-step sums of ||b_m||^2 and ||D b_m||^2 are reduced
-// per block; k_normest_final replays the reference's stopping rule on them.
-// part layout: [block][m][2], m in [0, kNeIters), m = 0 holds ||r||^2.
+// frame vector evolves independently: one thread per pixel advances it in
+// registers (scaled by 1/4 per step, exact in binary floating point, to stay
+// in range) and per-step sums of ||b_m||^2 and ||D b_m||^2 are reduced per
+// block.  Steps run in chunks; after each chunk k_normest_check replays the
+// reference's stopping rule on the sums available so far and, once it has
+// stopped, later chunks return immediately.
+// part layout: [block][step - m_begin (+1 for the first chunk)][2]; in the
+// first chunk slot 0 holds ||r||^2.
 // ---------------------------------------------------------------------------
+constexpr int kNeChunks = 3;
+constexpr int kNeBounds[kNeChunks + 1] = {1, 17, 49, kNeIters};
+constexpr int kNeMaxSlots = 52;  // largest chunk (51 steps) + ||r||^2 slot
+
 template <int FMAX>
-__global__ void __launch_bounds__(kNeNT) k_normest_pixels(int N, int F, unsigned long long x0,
-                                                          unsigned long long jumpN_a, unsigned long long jumpN_c,
-                                                          double* __restrict__ part) {
-  __shared__ float sw[kNeNT / 32][kNeIters][2];
+__global__ void __launch_bounds__(kNeNT) k_normest_chunk(int N, int F, unsigned long long x0,
+                                                         unsigned long long jumpN_a, unsigned long long jumpN_c,
+                                                         int m_begin, int m_end, float* __restrict__ bstore,
+                                                         double* __restrict__ part, const NestaDevState* st) {
+  __shared__ float sw[kNeNT / 32][kNeMaxSlots][2];
+  if (st->ne_done) return;
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   const int p = blockIdx.x * kNeNT + t;
   const bool act = p < N;
+  const int slot0 = (m_begin == 1) ? 1 : 0;
   float b[FMAX], d[FMAX];
-  {
+  if (m_begin == 1) {
     // element (f, p) is draw number f*N + p + 1 after the state x0
     const Lcg48 jp = lcg_jump_k(uint64_t(act ? p : 0) + 1);
     uint64_t X = (jp.a * x0 + jp.c) & kMask48;
@@ -210,24 +220,26 @@ __global__ void __launch_bounds__(kNeNT) k_normest_pixels(int N, int F, unsigned
         d[f] = 0.f;
       }
     }
-  }
-  float s0 = 0.f;
+    float s0 = 0.f;
 #pragma unroll
-  for (int f = 0; f < FMAX; ++f) s0 = fmaf(d[f], d[f], s0);
-  // b_1 = D^T r: (D^T v)_f = v_f - v_{f+1 mod F}
+    for (int f = 0; f < FMAX; ++f) s0 = fmaf(d[f], d[f], s0);
+    // b_1 = D^T r: (D^T v)_f = v_f - v_{f+1 mod F}
 #pragma unroll
-  for (int f = 0; f < FMAX; ++f) {
-    const float nx = (f + 1 < FMAX && f + 1 < F) ? d[(f + 1) % FMAX] : d[0];
-    b[f] = (f < F) ? d[f] - nx : 0.f;
-  }
-  float r0 = s0;
+    for (int f = 0; f < FMAX; ++f) {
+      const float nx = (f + 1 < FMAX && f + 1 < F) ? d[(f + 1) % FMAX] : d[0];
+      b[f] = (f < F) ? d[f] - nx : 0.f;
+    }
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) r0 += __shfl_down_sync(0xffffffffu, r0, o);
-  if (lane == 0) {
-    sw[wid][0][0] = r0;
-    sw[wid][0][1] = 0.f;
+    for (int o = 16; o > 0; o >>= 1) s0 += __shfl_down_sync(0xffffffffu, s0, o);
+    if (lane == 0) {
+      sw[wid][0][0] = s0;
+      sw[wid][0][1] = 0.f;
+    }
+  } else {
+#pragma unroll
+    for (int f = 0; f < FMAX; ++f) b[f] = (f < F && act) ? bstore[size_t(f) * N + p] : 0.f;
   }
-  for (int m = 1; m < kNeIters; ++m) {
+  for (int m = m_begin; m < m_end; ++m) {
     float last = b[0];
 #pragma unroll
     for (int f = 1; f < FMAX; ++f)
@@ -246,8 +258,8 @@ __global__ void __launch_bounds__(kNeNT) k_normest_pixels(int N, int F, unsigned
       sd += __shfl_down_sync(0xffffffffu, sd, o);
     }
     if (lane == 0) {
-      sw[wid][m][0] = sb;
-      sw[wid][m][1] = sd;
+      sw[wid][slot0 + m - m_begin][0] = sb;
+      sw[wid][slot0 + m - m_begin][1] = sd;
     }
 #pragma unroll
     for (int f = 0; f < FMAX; ++f) {
@@ -255,39 +267,71 @@ __global__ void __launch_bounds__(kNeNT) k_normest_pixels(int N, int F, unsigned
       b[f] = (f < F) ? (d[f] - nx) * 0.25f : 0.f;
     }
   }
+  if (m_end < kNeIters && act) {
+#pragma unroll
+    for (int f = 0; f < FMAX; ++f)
+      if (f < F) bstore[size_t(f) * N + p] = b[f];
+  }
   __syncthreads();
-  for (int i = t; i < kNeIters * 2; i += kNeNT) {
+  const int nslots = slot0 + m_end - m_begin;
+  for (int i = t; i < nslots * 2; i += kNeNT) {
     double s = 0.0;
     for (int w = 0; w < kNeNT / 32; ++w) s += double(sw[w][i >> 1][i & 1]);
-    part[size_t(blockIdx.x) * kNeIters * 2 + i] = s;
+    part[size_t(blockIdx.x) * kNeMaxSlots * 2 + i] = s;
   }
 }
 
-__global__ void __launch_bounds__(256) k_normest_final(const double* __restrict__ part, int nblk, int N, int F,
-                                                       NestaDevState* st) {
-  __shared__ double tot[kNeIters * 2];
-  for (int i = threadIdx.x; i < kNeIters * 2; i += blockDim.x) {
+// one CTA: reduce the chunk's per-block sums (one warp per sum) and continue
+// the reference's convergence loop (NestaUp.cpp:325-431)
+__global__ void __launch_bounds__(256) k_normest_check(const double* __restrict__ part, int nblk, int m_begin,
+                                                       int m_end, int N, int F, NestaDevState* st) {
+  __shared__ double tot[kNeMaxSlots * 2];
+  if (st->ne_done) return;
+  const int slot0 = (m_begin == 1) ? 1 : 0;
+  const int nsum = (slot0 + m_end - m_begin) * 2;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  for (int i = wid; i < nsum; i += blockDim.x / 32) {
     double s = 0.0;
-    for (int b = 0; b < nblk; ++b) s += part[size_t(b) * kNeIters * 2 + i];
-    tot[i] = s;
+    for (int b = lane; b < nblk; b += 32) s += part[size_t(b) * kNeMaxSlots * 2 + i];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+    if (lane == 0) tot[i] = s;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    const float n = float(unsigned(N) * unsigned(F));
     const float tol = 1e-3f;
-    float e = sqrtf(n);  // ||ones||
-    float e0 = 0.f;
-    int cnt = 0;
-    while (fabsf(e - e0) > tol * e && cnt < kNeIters) {
+    float e, e0;
+    int cnt;
+    if (m_begin == 1) {
+      e = sqrtf(float(unsigned(N) * unsigned(F)));  // ||ones||
+      e0 = 0.f;
+      cnt = 0;
+    } else {
+      e = st->ne_e;
+      e0 = st->ne_e0;
+      cnt = st->ne_cnt;
+    }
+    bool stopped = false;
+    for (;;) {
+      if (!(fabsf(e - e0) > tol * e && cnt < kNeIters)) {
+        stopped = true;
+        break;
+      }
+      if (cnt > 0 && cnt >= m_end) break;  // needs steps of a later chunk
+      const float en = (cnt == 0) ? float(sqrt(tot[0]))
+                                  : float(sqrt(tot[2 * (slot0 + cnt - m_begin) + 1] / tot[2 * (slot0 + cnt - m_begin)]));
       e0 = e;
-      if (cnt == 0)
-        e = float(sqrt(tot[0]));
-      else
-        e = float(sqrt(tot[2 * cnt + 1] / tot[2 * cnt]));
+      e = en;
       ++cnt;
     }
-    st->normU = e;
-    st->normest_iters = cnt;
+    st->ne_e = e;
+    st->ne_e0 = e0;
+    st->ne_cnt = cnt;
+    if (stopped) {
+      st->normU = e;
+      st->normest_iters = cnt;
+      st->ne_done = 1;
+    }
   }
 }
 
@@ -346,6 +390,16 @@ __global__ void k_outer_end(const NestaDevState* st, const float2* __restrict__ 
 // ---------------------------------------------------------------------------
 namespace {
 
+// launch `stmt` (n kernels) as part of profiled group `kind`
+#define GBN_LAUNCH(ctx, kind, n, ...)                    \
+  do {                                                  \
+    cudaEvent_t ev_ = nullptr;                          \
+    if ((ctx)->profile) prof_begin((ctx), (kind), &ev_); \
+    __VA_ARGS__;                                        \
+    if ((ctx)->profile) prof_end((ctx), (kind), ev_);   \
+    (ctx)->launches += (n);                             \
+  } while (0)
+
 template <typename T>
 int grow(T*& p, int& cap, int need) {
   if (need <= cap) return GBN_OK;
@@ -360,15 +414,29 @@ int grow(T*& p, int& cap, int need) {
   return GBN_OK;
 }
 
-int normest_fmax(int F) { return F <= 8 ? 8 : F <= 16 ? 16 : F <= 32 ? 32 : F <= 64 ? 64 : 0; }
+int normest_fmax(int F) {
+  for (int m : {8, 16, 24, 32, 40, 48, 64})
+    if (F <= m) return m;
+  return 0;
+}
 
-void launch_normest(int fmax, int nblk, cudaStream_t s, int N, int F, uint64_t x0, const Lcg48& jN, double* part) {
+void launch_normest_chunk(int fmax, int nblk, cudaStream_t s, int N, int F, uint64_t x0, const Lcg48& jN, int mb,
+                          int me, float* bstore, double* part, const NestaDevState* st) {
+#define GBN_NE_CASE(M)                                                                                  \
+  case M:                                                                                               \
+    k_normest_chunk<M><<<nblk, kNeNT, 0, s>>>(N, F, x0, jN.a, jN.c, mb, me, bstore, part, st); \
+    break;
   switch (fmax) {
-    case 8: k_normest_pixels<8><<<nblk, kNeNT, 0, s>>>(N, F, x0, jN.a, jN.c, part); break;
-    case 16: k_normest_pixels<16><<<nblk, kNeNT, 0, s>>>(N, F, x0, jN.a, jN.c, part); break;
-    case 32: k_normest_pixels<32><<<nblk, kNeNT, 0, s>>>(N, F, x0, jN.a, jN.c, part); break;
-    default: k_normest_pixels<64><<<nblk, kNeNT, 0, s>>>(N, F, x0, jN.a, jN.c, part); break;
+    GBN_NE_CASE(8)
+    GBN_NE_CASE(16)
+    GBN_NE_CASE(24)
+    GBN_NE_CASE(32)
+    GBN_NE_CASE(40)
+    GBN_NE_CASE(48)
+    default:
+      k_normest_chunk<64><<<nblk, kNeNT, 0, s>>>(N, F, x0, jN.a, jN.c, mb, me, bstore, part, st);
   }
+#undef GBN_NE_CASE
 }
 
 }  // namespace
@@ -401,8 +469,9 @@ int problem_alloc(gbn_problem* P) {
 }
 
 void problem_free(gbn_problem* P) {
-  void* ptrs[] = {P->flags, P->full_fh, P->rowmap, P->rowoff, P->rows_h, P->rows_f, P->row_full, P->T,
-                  P->xk0,   P->xk1,     P->wacc,   P->st,     P->fmean,  P->part_tv, P->part_r, P->part_ne};
+  void* ptrs[] = {P->flags, P->full_fh, P->rowmap, P->rowoff,  P->rows_h, P->rows_f,  P->row_full, P->T,
+                  P->xk0,   P->xk1,     P->wacc,   P->st,      P->fmean,  P->part_tv, P->part_r,   P->part_ne,
+                  P->ne_b};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -476,40 +545,46 @@ int nesta_run(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, float2*
   const long long rows_max = (long long)F * H * C;
   const int g2 = int(std::max<long long>(1, std::min<long long>((rows_max + kw->rows_per_cta - 1) / kw->rows_per_cta,
                                                                  (long long)ctx->nsm * ctx->k2_ctas_per_sm)));
-  const dim3 g3(W / kWB, F);
+  const dim3 g3(W / kWB, 2, F);  // clusters of 2 along y
   const int nblk_ne = (N + kNeNT - 1) / kNeNT;
   int rc;
   if ((rc = grow(P->fmean, P->fmean_cap, std::max<int>(1, int(prm->miniter)))) != GBN_OK) return rc;
   if ((rc = grow(P->part_tv, P->part_tv_cap, 2 * nblk_k1)) != GBN_OK) return rc;
   if ((rc = grow(P->part_r, P->part_r_cap, g2)) != GBN_OK) return rc;
-  if ((rc = grow(P->part_ne, P->part_ne_cap, nblk_ne * kNeIters * 2)) != GBN_OK) return rc;
+  if ((rc = grow(P->part_ne, P->part_ne_cap, nblk_ne * kNeMaxSlots * 2)) != GBN_OK) return rc;
+  if ((rc = grow(P->ne_b, P->ne_b_cap, N * F)) != GBN_OK) return rc;
 
   FusedArgs a = make_args(P, x_out);
   a.nblk_k1 = nblk_k1;
   const size_t X = size_t(N) * F;
   const int gx = int(std::min<size_t>((X + 255) / 256, size_t(ctx->nsm) * 8));
 
-  k_state_init<<<1, 1, 0, s>>>(P->st, *prm);
-  launch_row_analysis(P, s);
-  // x0 = E^H y (NestaUp.cpp:465-486)
-  kw->rows(a, 0, false, g2, s);
-  kh->inv_cols(a, 0, false, g3, s);
-  // maxima, norm estimate, constants (NestaUp.cpp:521-583)
-  k_maxima<<<gx, 256, 0, s>>>(x_out, N, F, P->st);
-  const Lcg48 jN = lcg_jump_k(uint64_t(N));
-  launch_normest(fmax, nblk_ne, s, N, F, ctx->rand48, jN, P->part_ne);
-  ctx->rand48 = lcg48_apply(lcg_jump_k(uint64_t(N) * uint64_t(F)), ctx->rand48);
-  k_normest_final<<<1, 256, 0, s>>>(P->part_ne, nblk_ne, N, F, P->st);
-  k_setup<<<1, 1, 0, s>>>(P->st);
+  GBN_LAUNCH(ctx, GBN_PROF_SETUP, 8 + 2 * kNeChunks, {
+    k_state_init<<<1, 1, 0, s>>>(P->st, *prm);
+    launch_row_analysis(P, s);
+    // x0 = E^H y (NestaUp.cpp:465-486)
+    kw->rows(a, 0, false, g2, s);
+    kh->inv_cols(a, 0, false, g3, s);
+    // maxima, norm estimate, constants (NestaUp.cpp:521-583)
+    k_maxima<<<gx, 256, 0, s>>>(x_out, N, F, P->st);
+    const Lcg48 jN = lcg_jump_k(uint64_t(N));
+    for (int ch = 0; ch < kNeChunks; ++ch) {
+      launch_normest_chunk(fmax, nblk_ne, s, N, F, ctx->rand48, jN, kNeBounds[ch], kNeBounds[ch + 1], P->ne_b,
+                           P->part_ne, P->st);
+      k_normest_check<<<1, 256, 0, s>>>(P->part_ne, nblk_ne, kNeBounds[ch], kNeBounds[ch + 1], N, F, P->st);
+    }
+    ctx->rand48 = lcg48_apply(lcg_jump_k(uint64_t(N) * uint64_t(F)), ctx->rand48);
+    k_setup<<<1, 1, 0, s>>>(P->st);
+  });
 
   for (unsigned nl = 1; nl <= prm->maxIntIter; ++nl) {
-    k_outer_begin<<<gx, 256, 0, s>>>(P->st, P->fmean, x_out, P->xk0, P->wacc, X);
+    GBN_LAUNCH(ctx, GBN_PROF_OUTER, 1, (k_outer_begin<<<gx, 256, 0, s>>>(P->st, P->fmean, x_out, P->xk0, P->wacc, X)));
     for (unsigned it = 0; it < prm->maxIter; ++it) {
-      kh->fwd_cols(a, int(it), cpb, g1, s);
-      kw->rows(a, int(it), true, g2, s);
-      kh->inv_cols(a, int(it), true, g3, s);
+      GBN_LAUNCH(ctx, GBN_PROF_FWD_COLS, 1, kh->fwd_cols(a, int(it), cpb, g1, s));
+      GBN_LAUNCH(ctx, GBN_PROF_ROWS, 1, kw->rows(a, int(it), true, g2, s));
+      GBN_LAUNCH(ctx, GBN_PROF_INV_COLS, 1, kh->inv_cols(a, int(it), true, g3, s));
     }
-    k_outer_end<<<gx, 256, 0, s>>>(P->st, P->xk0, P->xk1, x_out, X);
+    GBN_LAUNCH(ctx, GBN_PROF_OUTER, 1, (k_outer_end<<<gx, 256, 0, s>>>(P->st, P->xk0, P->xk1, x_out, X)));
   }
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_status(e, "nesta launch");
@@ -546,7 +621,7 @@ int simple_recon(gbn_ctx* ctx, const float2* y, const float2* S, float2* x, int 
   if (!kh || !kw) return set_error(GBN_ERR_UNSUPPORTED, "unsupported FFT length");
   const size_t FH = size_t(F) * H, K = FH * C * W;
   // scratch: T [F*H][C][W] + rowmap/rowoff/rows_h/rows_f
-  const size_t bytes = K * sizeof(float2) + (3 * FH + F + 1 + FH) * sizeof(int) + 256;
+  const size_t bytes = K * sizeof(float2) + (4 * FH + F + 1) * sizeof(int) + 2 * sizeof(NestaDevState) + 256;
   void* scr = nullptr;
   int rc = ctx_scratch(ctx, bytes, &scr);
   if (rc != GBN_OK) return rc;
@@ -557,9 +632,11 @@ int simple_recon(gbn_ctx* ctx, const float2* y, const float2* S, float2* x, int 
   int* rows_f = rows_h + FH;
   int* row_full = rows_f + FH;
   int* rowoff = row_full + FH;
+  NestaDevState* st = reinterpret_cast<NestaDevState*>(
+      (reinterpret_cast<uintptr_t>(rowoff + F + 1) + alignof(NestaDevState) - 1) & ~uintptr_t(alignof(NestaDevState) - 1));
   cudaStream_t s = ctx->stream;
-  k_rows_identity<<<int(std::min<size_t>((FH + 255) / 256, 1024)), 256, 0, s>>>(H, F, rowmap, rowoff, rows_h, rows_f,
-                                                                                row_full);
+  cudaError_t e0 = cudaMemsetAsync(st, 0, sizeof(NestaDevState), s);
+  if (e0 != cudaSuccess) return cuda_status(e0, "simple recon setup");
   FusedArgs a;
   memset(&a, 0, sizeof(a));
   a.W = W;
@@ -576,14 +653,19 @@ int simple_recon(gbn_ctx* ctx, const float2* y, const float2* S, float2* x, int 
   a.row_full = row_full;
   a.T = T;
   a.xref = x;
+  a.st = st;
   a.twH = ctx_twiddles(ctx, H);
   a.twW = ctx_twiddles(ctx, W);
   a.s_adj = 1.0f / float(W * H);  // clFFT BACKWARD scale
   const long long rows = (long long)FH * C;
   const int g2 = int(std::max<long long>(
       1, std::min<long long>((rows + kw->rows_per_cta - 1) / kw->rows_per_cta, (long long)ctx->nsm * ctx->k2_ctas_per_sm)));
-  kw->rows(a, 0, false, g2, s);
-  kh->inv_cols(a, 0, false, dim3(W / kWB, F), s);
+  GBN_LAUNCH(ctx, GBN_PROF_SETUP, 3, {
+    k_rows_identity<<<int(std::min<size_t>((FH + 255) / 256, 1024)), 256, 0, s>>>(H, F, rowmap, rowoff, rows_h, rows_f,
+                                                                                  row_full);
+    kw->rows(a, 0, false, g2, s);
+    kh->inv_cols(a, 0, false, dim3(W / kWB, 2, F), s);
+  });
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_status(e, "simple recon launch");
   return GBN_OK;

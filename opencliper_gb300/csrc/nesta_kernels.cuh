@@ -12,7 +12,13 @@
 // Column transforms run first in the forward direction so that only the kept
 // (sampled) phase-encode rows ever leave the column pass: T holds G*C rows, not
 // F*C*H.  The adjoint column transform reads only those rows (others are zero).
+//
+// Latency hiding: global loads for the next coil (k_fwd_cols, k_inv_cols) or
+// for the residual's data row (k_rows) are issued before the current stage's
+// arithmetic and barriers, so they are in flight while it runs.
 #pragma once
+
+#include <cooperative_groups.h>
 
 #include "fft.cuh"
 #include "types.h"
@@ -35,22 +41,38 @@ struct Split {
 constexpr int pad_to_8mod16(int v) { return v + ((8 - v % 16) + 16) % 16; }
 constexpr int odd_up(int v) { return (v % 2) ? v : v + 1; }
 constexpr int cdiv(int a, int b) { return (a + b - 1) / b; }
+// exchange-slot stride between k1 groups of the column kernels (kWB lanes each)
+constexpr int col_ks(int q) { return (q * kWB) % 16 == 8 ? q * kWB : q * kWB + 8; }
 
 __device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
-__device__ __forceinline__ float2 ld_tw(const float2* tw, int idx) { return tw[idx]; }
+
+// d / max(mu, |d|) (vectorNormalization.cl:42-56) as d * min(1/mu, 1/|d|):
+// one reciprocal square root instead of a square root and two divisions
+// (within 2 ulp; d = 0 gives 0).
+__device__ __forceinline__ float2 tv_normalize(float2 d, float inv_mu) {
+  const float s = fminf(inv_mu, rsqrtf(fmaf(d.x, d.x, d.y * d.y)));
+  return make_float2(d.x * s, d.y * s);
+}
 
 // ---------------------------------------------------------------------------
 // Reference scalar recurrence of one inner iteration: objective, stopping test
 // and the Nesterov weights (NestaUp.cpp:791-831), executed by one thread.
 // Arithmetic types follow the reference: host floats, std::pow in double.
 // ---------------------------------------------------------------------------
-__device__ inline void nesta_scalar_step(NestaDevState* st, float* fmean, int it, double su2, double sud,
-                                         double sr2) {
+// `fm` is a copy of the first min(miniter, kFmeanCopy) entries of fmean.
+constexpr int kFmeanCopy = 64;
+__device__ inline void nesta_scalar_step(NestaDevState* gst, float* fmean, const float* fm, int it, double su2,
+                                         double sud, double sr2) {
+  // work on a register copy: one batch of loads instead of a chain of round trips
+  NestaDevState loc = *gst;
+  NestaDevState* st = &loc;
   const float normUk = float(sqrt(su2));  // Scnrm2(u)
   const float fxdot = float(sud);         // real part of Cdotc(u, d)
   const float l2 = float(sr2);            // Scsum(|res|^2)
   const float mu = st->mu;
-  const float l1term = float(double(fxdot) - double(mu / 2.0f) * pow(double(normUk), 2.0));
+  // std::pow(normUk, 2) of a float is exactly its square in double
+  const double nu2 = double(normUk) * double(normUk);
+  const float l1term = float(double(fxdot) - double(mu / 2.0f) * nu2);
   const float fx = 0.5f * l2 + st->lambda * l1term;
   int k = it;
   float qp = st->qp;
@@ -59,7 +81,10 @@ __device__ inline void nesta_scalar_step(NestaDevState* st, float* fmean, int it
     bool brk = false;
     if (k >= m) {
       float s = 0.0f;
-      for (int ne = 0; ne < m; ++ne) s += fmean[m - ne - 1];
+      for (int ne = 0; ne < m; ++ne) {
+        const int idx = m - ne - 1;
+        s += (idx < kFmeanCopy) ? fm[idx] : fmean[idx];
+      }
       s = s / float(unsigned(m));
       qp = (s - fx) / s;
       if (qp <= st->tolVar) {
@@ -68,7 +93,7 @@ __device__ inline void nesta_scalar_step(NestaDevState* st, float* fmean, int it
         brk = true;
       }
     } else {
-      qp = fmean[m - 1];
+      qp = (m - 1 < kFmeanCopy) ? fm[m - 1] : fmean[m - 1];
     }
     if (!brk) fmean[(m - 1) - int(unsigned(k + 1) % unsigned(m))] = fx;
   }
@@ -84,21 +109,38 @@ __device__ inline void nesta_scalar_step(NestaDevState* st, float* fmean, int it
   st->l2term = l2;
   st->iters_total += 1;
   if (k >= st->maxIter) st->last_iter = it;  // later inner iterations of this outer loop are skipped
+  *gst = loc;
 }
 
 // ===========================================================================
-// K1: forward column pass.  grid = (W/kWB, coil groups, F)
+// K1: forward column pass.  grid = (W/kWB, coil groups, F), dynamic smem.
+// dit2<A,B> along H: pass-1 items (w, s), s < B, hold rows B*n1 + s; pass-2
+// items (w, k1), k1 < A, produce rows k1 + A*k2.  The S tile of the next coil
+// is copied asynchronously into a second shared buffer while the current coil
+// is transformed.
 // ===========================================================================
 template <int H>
+struct FwdColsSmem {
+  static constexpr int A = Split<H>::A, B = Split<H>::B, KS = col_ks(B);
+  static constexpr int S_OFF = 0;                        // float2 [2][H][kWB]
+  static constexpr int EX_OFF = S_OFF + 2 * H * kWB;     // float2 [A*KS]
+  static constexpr int TW_OFF = EX_OFF + A * KS;         // float2 [H]
+  static constexpr int F2_END = TW_OFF + H;
+  static constexpr int BYTES = F2_END * 8 + (kColNT / 32) * 8 + H * 4;
+};
+
+template <int H>
 __global__ void __launch_bounds__(kColNT) k_fwd_cols(FusedArgs a, int it, int coils_per_block) {
-  constexpr int A = Split<H>::A, B = Split<H>::B;
-  constexpr int KS = (B * kWB) % 16 == 8 ? B * kWB : B * kWB + 8;  // slot (k1, s, w) at k1*KS + s*kWB + w
+  using L = FwdColsSmem<H>;
+  constexpr int A = L::A, B = L::B, KS = L::KS;
   constexpr int N1 = kWB * B, N2 = kWB * A;
   constexpr int NI1 = cdiv(N1, kColNT), NI2 = cdiv(N2, kColNT);
-  __shared__ float2 ex[A * KS];
-  __shared__ float2 tw[H];
-  __shared__ int rmap[H];
-  __shared__ double sred[kColNT / 32];
+  extern __shared__ float4 smem4[];
+  float2* Sb = reinterpret_cast<float2*>(smem4) + L::S_OFF;
+  float2* ex = reinterpret_cast<float2*>(smem4) + L::EX_OFF;
+  float2* tw = reinterpret_cast<float2*>(smem4) + L::TW_OFF;
+  double* sred = reinterpret_cast<double*>(reinterpret_cast<float2*>(smem4) + L::F2_END);
+  int* rmap = reinterpret_cast<int*>(sred + kColNT / 32);
 
   const NestaDevState* st = a.st;
   if (it > st->last_iter) return;
@@ -108,6 +150,19 @@ __global__ void __launch_bounds__(kColNT) k_fwd_cols(FusedArgs a, int it, int co
   const size_t N = size_t(a.N);
   const float2* __restrict__ xk = (it & 1) ? a.xk1 : a.xk0;
   const float2* __restrict__ x = xk + size_t(f) * N;
+  const int c0 = cg * coils_per_block;
+  const int c1 = min(C, c0 + coils_per_block);
+
+  auto issue_S = [&](int c, int buf) {
+    const float2* src = a.S + size_t(c) * N + w0;
+    float2* dst = Sb + buf * H * kWB;
+    for (int q = t; q < H * (kWB / 2); q += kColNT) {
+      const int row = q / (kWB / 2), part = q % (kWB / 2);
+      cp_async16(dst + row * kWB + 2 * part, src + size_t(row) * W + 2 * part);
+    }
+    cp_async_commit();
+  };
+  issue_S(c0, 0);
 
   for (int i = t; i < H; i += kColNT) {
     tw[i] = a.twH[i];
@@ -115,7 +170,7 @@ __global__ void __launch_bounds__(kColNT) k_fwd_cols(FusedArgs a, int it, int co
   }
   const int rowbase = a.rowoff[f];
 
-  // x_k values of this thread's pass-1 items, reused for every coil
+  // x_k for this thread's pass-1 items, reused for every coil
   float2 xv[NI1][A];
 #pragma unroll
   for (int ii = 0; ii < NI1; ++ii) {
@@ -126,12 +181,36 @@ __global__ void __launch_bounds__(kColNT) k_fwd_cols(FusedArgs a, int it, int co
       for (int n1 = 0; n1 < A; ++n1) xv[ii][n1] = x[size_t(B * n1 + s) * W + w0 + w];
     }
   }
-  __syncthreads();
 
-  const int c0 = cg * coils_per_block;
-  const int c1 = min(C, c0 + coils_per_block);
+  // Partial sums of the tTV objective terms over this CTA's tile (coil group 0
+  // only): d = x_f - x_{f-1} (temporalTV.cl:49-76), u = d / max(mu, |d|)
+  // (vectorNormalization.cl:42-56), sum |u|^2 (Scnrm2) and Re<u,d> (Cdotc).
+  float su2 = 0.f, sud = 0.f;
+  if (cg == 0) {
+    const float2* __restrict__ xm = xk + size_t((f + F - 1) % F) * N;
+    const float inv_mu = 1.0f / st->mu;
+#pragma unroll
+    for (int ii = 0; ii < NI1; ++ii) {
+      const int i = t + ii * kColNT;
+      if (i < N1) {
+        const int w = i % kWB, s = i / kWB;
+#pragma unroll
+        for (int n1 = 0; n1 < A; ++n1) {
+          const float2 d = csub(xv[ii][n1], xm[size_t(B * n1 + s) * W + w0 + w]);
+          const float2 u = tv_normalize(d, inv_mu);
+          su2 = fmaf(u.x, u.x, fmaf(u.y, u.y, su2));
+          sud = fmaf(u.x, d.x, fmaf(u.y, d.y, sud));
+        }
+      }
+    }
+  }
+
   for (int c = c0; c < c1; ++c) {
-    const float2* __restrict__ Sc = a.S + size_t(c) * N;
+    const int buf = (c - c0) & 1;
+    cp_async_wait<0>();
+    __syncthreads();  // S tile of coil c visible; previous coil's pass 2 finished
+    if (c + 1 < c1) issue_S(c + 1, buf ^ 1);
+    const float2* Sc = Sb + buf * H * kWB;
 #pragma unroll
     for (int ii = 0; ii < NI1; ++ii) {
       const int i = t + ii * kColNT;
@@ -139,10 +218,10 @@ __global__ void __launch_bounds__(kColNT) k_fwd_cols(FusedArgs a, int it, int co
         const int w = i % kWB, s = i / kWB;
         float2 v[A];
 #pragma unroll
-        for (int n1 = 0; n1 < A; ++n1) v[n1] = cmul(xv[ii][n1], Sc[size_t(B * n1 + s) * W + w0 + w]);
+        for (int n1 = 0; n1 < A; ++n1) v[n1] = cmul(xv[ii][n1], Sc[(B * n1 + s) * kWB + w]);
         dft<A>(v);
 #pragma unroll
-        for (int k1 = 0; k1 < A; ++k1) ex[k1 * KS + s * kWB + w] = (k1 == 0) ? v[k1] : cmul(v[k1], tw[s * k1]);
+        for (int k1 = 0; k1 < A; ++k1) ex[k1 * KS + s * kWB + w] = (k1 == 0) ? v[k1] : cmul(v[k1], tw[k1 * B + s]);
       }
     }
     __syncthreads();
@@ -162,29 +241,8 @@ __global__ void __launch_bounds__(kColNT) k_fwd_cols(FusedArgs a, int it, int co
         }
       }
     }
-    __syncthreads();
   }
 
-  // Partial sums of the tTV objective terms for rows h == cg (mod gridDim.y):
-  // d = x_f - x_{f-1} (temporalTV.cl:49-76), u = d / max(mu, |d|)
-  // (vectorNormalization.cl:42-56), sum |u|^2 (Scnrm2) and Re<u,d> (Cdotc).
-  const int gy = gridDim.y;
-  const float2* __restrict__ xm = xk + size_t((f + F - 1) % F) * N;
-  const float mu = st->mu;
-  float su2 = 0.f, sud = 0.f;
-  {
-    const int w = t % kWB;
-    for (int hr = t / kWB;; hr += kColNT / kWB) {
-      const int h = cg + gy * hr;
-      if (h >= H) break;
-      const size_t p = size_t(h) * W + w0 + w;
-      const float2 d = csub(x[p], xm[p]);
-      const float m = fmaxf(mu, sqrtf(fmaf(d.x, d.x, d.y * d.y)));
-      const float2 u = make_float2(d.x / m, d.y / m);
-      su2 = fmaf(u.x, u.x, fmaf(u.y, u.y, su2));
-      sud = fmaf(u.x, d.x, fmaf(u.y, d.y, sud));
-    }
-  }
   const double t1 = block_sum<kColNT>(double(su2), sred);
   const double t2 = block_sum<kColNT>(double(sud), sred);
   if (t == 0) {
@@ -195,7 +253,9 @@ __global__ void __launch_bounds__(kColNT) k_fwd_cols(FusedArgs a, int it, int co
 }
 
 // ===========================================================================
-// K2: row pass over kept rows, persistent over (g, c) row items.
+// K2: row pass over kept rows; CTAs take RPC-row steps from a device counter
+// and stage the next step's rows (T, y, mask) into shared memory with cp.async
+// while the current step is transformed.
 //   RESID: r = mask * DFT_W(T)/sqrt(N) - y, T = IDFT_W(r), ||r||^2 partials.
 //   !RESID (adjoint of the data, x0 = E^H y): T = IDFT_W(y).
 // ===========================================================================
@@ -206,114 +266,228 @@ struct RowCfg {
   static constexpr int RPC = (kRowNT / MX) > 0 ? kRowNT / MX : 1;  // rows per CTA step
   static constexpr int S1 = odd_up(B), RS1 = pad_to_8mod16(A * S1);   // forward slots (k1, s)
   static constexpr int S2 = odd_up(A), RS2 = pad_to_8mod16(B * S2);   // inverse slots (k1', s')
+  static constexpr int EXN = RPC * (RS1 > RS2 ? RS1 : RS2);           // shared exchange buffer
+};
+
+template <int W, bool RESID>
+struct RowsSmem {
+  using R = RowCfg<W>;
+  static constexpr int Y_OFF = 0;                                 // float2 [2][RPC][W]
+  static constexpr int T_OFF = Y_OFF + 2 * R::RPC * W;            // float2 [RPC][W] (RESID)
+  static constexpr int EX_OFF = T_OFF + (RESID ? R::RPC * W : 0); // float2 [EXN]
+  static constexpr int TW_OFF = EX_OFF + R::EXN;                  // float2 [2W]
+  static constexpr int F2_END = TW_OFF + 2 * W;
+  static constexpr int M_BYTES = RESID ? 2 * R::RPC * W : 0;      // uint8 [2][RPC][W]
+  static constexpr int BYTES = F2_END * 8 + (kRowNT / 32) * 8 + M_BYTES + 16;
 };
 
 template <int W, bool RESID>
 __global__ void __launch_bounds__(kRowNT) k_rows(FusedArgs a, int it) {
   using R = RowCfg<W>;
+  using L = RowsSmem<W, RESID>;
   constexpr int A = R::A, B = R::B, RPC = R::RPC;
-  __shared__ float2 ex1[RESID ? RPC * R::RS1 : 1];
-  __shared__ float2 ex2[RPC * R::RS2];
-  __shared__ float2 tw[W];
-  __shared__ double sred[kRowNT / 32];
+  extern __shared__ float4 smem4[];
+  float2* Yb = reinterpret_cast<float2*>(smem4) + L::Y_OFF;
+  float2* Tb = reinterpret_cast<float2*>(smem4) + L::T_OFF;
+  float2* ex = reinterpret_cast<float2*>(smem4) + L::EX_OFF;
+  float2* tw = reinterpret_cast<float2*>(smem4) + L::TW_OFF;
+  double* sred = reinterpret_cast<double*>(reinterpret_cast<float2*>(smem4) + L::F2_END);
+  uint8_t* Mb = reinterpret_cast<uint8_t*>(sred + kRowNT / 32);
+  __shared__ int s_next;
   __shared__ int am_last;
 
   NestaDevState* st = a.st;
   if (RESID && it > st->last_iter) return;
   const int t = threadIdx.x;
-  for (int i = t; i < W; i += kRowNT) tw[i] = a.twW[i];
-  __syncthreads();
   const int C = a.C, H = a.H;
   const int nitems = a.rowoff[a.F] * C;
+  const int nsteps = (nitems + RPC - 1) / RPC;
   const float s_fwd = a.s_fwd;
-  float racc = 0.f;
 
-  for (int base = blockIdx.x * RPC; base < nitems; base += gridDim.x * RPC) {
+  // y (and mask) rows of a step into buffer `buf`; T rows into Tb.  The row
+  // table lookups of all RPC rows are issued together before the copies.
+  auto issue_y = [&](int step, int buf) {
+    const int base = step * RPC;
+    const float2* ysrc[RPC];
+    const uint8_t* msrc[RPC];
+#pragma unroll
+    for (int r = 0; r < RPC; ++r) {
+      const int item = base + r;
+      ysrc[r] = nullptr;
+      msrc[r] = nullptr;
+      if (item < nitems) {
+        const int g = item / C, c = item % C;
+        const int f = __ldg(a.rows_f + g), h = __ldg(a.rows_h + g);
+        ysrc[r] = a.y + ((size_t(f) * C + c) * H + h) * size_t(W);
+        if (RESID && !__ldg(a.row_full + g)) msrc[r] = a.mask + (size_t(f) * H + h) * size_t(W);
+      }
+    }
+#pragma unroll
+    for (int r = 0; r < RPC; ++r) {
+      if (ysrc[r]) {
+        for (int part = t; part < W / 2; part += kRowNT)
+          cp_async16(Yb + (buf * RPC + r) * W + 2 * part, ysrc[r] + 2 * part);
+        if (RESID && msrc[r]) {
+          for (int part = t; part < W / 8; part += kRowNT)
+            cp_async8(Mb + (buf * RPC + r) * W + 8 * part, msrc[r] + 8 * part);
+        }
+      }
+    }
+  };
+  auto issue_T = [&](int step) {
+    const int base = step * RPC;
+    for (int q = t; q < RPC * (W / 2); q += kRowNT) {
+      const int r = q / (W / 2), part = q % (W / 2), item = base + r;
+      if (item < nitems) cp_async16(Tb + r * W + 2 * part, a.T + size_t(item) * W + 2 * part);
+    }
+  };
+
+  if (t == 0) s_next = atomicAdd(&st->row_next, 1);
+  for (int i = t; i < 2 * W; i += kRowNT) tw[i] = a.twW[i];
+  __syncthreads();
+  int step = s_next;
+  if (step < nsteps) {
+    issue_y(step, 0);
+    if (RESID) issue_T(step);
+  }
+  cp_async_commit();
+  const float2* twab = tw;
+  const float2* twba = tw + W;
+  float racc = 0.f;
+  int buf = 0;
+
+  while (step < nsteps) {
+    __syncthreads();  // all threads hold `step`; s_next may be rewritten
+    if (t == 0) s_next = atomicAdd(&st->row_next, 1);
+    cp_async_wait<0>();
+    __syncthreads();  // rows of `step` visible, next step index visible
+    const int next = s_next;
+    if (next < nsteps) issue_y(next, buf ^ 1);
+    cp_async_commit();
+    const int base = step * RPC;
+    const float2* Yc = Yb + buf * RPC * W;
+    const uint8_t* Mc = Mb + buf * RPC * W;
+
     if constexpr (RESID) {
       for (int i = t; i < RPC * B; i += kRowNT) {
-        const int r = i / B, s = i % B, q = base + r;
-        if (q >= nitems) continue;
-        const float2* __restrict__ src = a.T + size_t(q) * W;
+        const int r = i / B, s = i % B;
+        if (base + r >= nitems) continue;
         float2 v[A];
 #pragma unroll
-        for (int n1 = 0; n1 < A; ++n1) v[n1] = src[B * n1 + s];
+        for (int n1 = 0; n1 < A; ++n1) v[n1] = Tb[r * W + B * n1 + s];
         dft<A>(v);
 #pragma unroll
-        for (int k1 = 0; k1 < A; ++k1) ex1[r * R::RS1 + k1 * R::S1 + s] = (k1 == 0) ? v[k1] : cmul(v[k1], tw[s * k1]);
+        for (int k1 = 0; k1 < A; ++k1)
+          ex[r * R::RS1 + k1 * R::S1 + s] = (k1 == 0) ? v[k1] : cmul(v[k1], twab[k1 * B + s]);
       }
-      __syncthreads();
+      __syncthreads();  // Tb consumed, exchange filled
+      if (next < nsteps) issue_T(next);
+      cp_async_commit();
     }
-    for (int i = t; i < RPC * A; i += kRowNT) {
-      const int r = i / A, k1 = i % A, q = base + r;
-      if (q >= nitems) continue;
-      const int g = q / C, c = q % C;
-      const int f = a.rows_f[g], h = a.rows_h[g];
-      const float2* __restrict__ yrow = a.y + ((size_t(f) * C + c) * H + h) * size_t(W);
-      float2 v[B];
+    // pass B (+ residual) and the first pass of the backward row transform;
+    // RPC*A <= kRowNT so each thread has at most one item
+    const int r = t / A, k1 = t % A, q = base + r;
+    const bool has = (t < RPC * A) && (q < nitems);
+    float2 v[B];
+    if (has) {
       if constexpr (RESID) {
 #pragma unroll
-        for (int s = 0; s < B; ++s) v[s] = ex1[r * R::RS1 + k1 * R::S1 + s];
+        for (int s = 0; s < B; ++s) v[s] = ex[r * R::RS1 + k1 * R::S1 + s];
+      }
+    }
+    if constexpr (RESID) __syncthreads();  // exchange reused by the backward pass
+    if (has) {
+      const int g = q / C;
+      const bool full = RESID ? (a.row_full[g] != 0) : true;
+      if constexpr (RESID) {
         dft<B>(v);  // v[k2] = X[k1 + A*k2]
-        const uint8_t* __restrict__ mrow = a.mask + (size_t(f) * H + h) * size_t(W);
-        const bool full = a.row_full[g] != 0;
 #pragma unroll
         for (int k2 = 0; k2 < B; ++k2) {
           const int kx = k1 + A * k2;
           float2 m = cscale(v[k2], s_fwd);
-          if (!full && mrow[kx] == 0) m = make_float2(0.f, 0.f);
-          const float2 rr = csub(m, yrow[kx]);
+          if (!full && Mc[r * W + kx] == 0) m = make_float2(0.f, 0.f);
+          const float2 rr = csub(m, Yc[r * W + kx]);
           racc = fmaf(rr.x, rr.x, fmaf(rr.y, rr.y, racc));
           v[k2] = conjf2(rr);
         }
       } else {
 #pragma unroll
-        for (int k2 = 0; k2 < B; ++k2) v[k2] = conjf2(yrow[k1 + A * k2]);
+        for (int k2 = 0; k2 < B; ++k2) v[k2] = conjf2(Yc[r * W + k1 + A * k2]);
       }
-      // inverse = conj(forward(conj)); forward dit2<B,A>, pass-1 item s' = k1
+      // backward = conj(forward(conj)); forward dit2<B,A>, pass-1 item s' = k1
       dft<B>(v);
 #pragma unroll
       for (int k1p = 0; k1p < B; ++k1p)
-        ex2[r * R::RS2 + k1p * R::S2 + k1] = (k1p == 0) ? v[k1p] : cmul(v[k1p], tw[k1 * k1p]);
+        ex[r * R::RS2 + k1p * R::S2 + k1] = (k1p == 0) ? v[k1p] : cmul(v[k1p], twba[k1p * A + k1]);
     }
     __syncthreads();
     for (int i = t; i < RPC * B; i += kRowNT) {
-      const int r = i / B, k1p = i % B, q = base + r;
-      if (q >= nitems) continue;
-      float2 v[A];
+      const int rr = i / B, k1p = i % B, qq = base + rr;
+      if (qq >= nitems) continue;
+      float2 u[A];
 #pragma unroll
-      for (int sp = 0; sp < A; ++sp) v[sp] = ex2[r * R::RS2 + k1p * R::S2 + sp];
-      dft<A>(v);
-      float2* __restrict__ dst = a.T + size_t(q) * W;
+      for (int sp = 0; sp < A; ++sp) u[sp] = ex[rr * R::RS2 + k1p * R::S2 + sp];
+      dft<A>(u);
+      float2* __restrict__ dst = a.T + size_t(qq) * W;
 #pragma unroll
-      for (int k2p = 0; k2p < A; ++k2p) dst[k1p + B * k2p] = conjf2(v[k2p]);
+      for (int k2p = 0; k2p < A; ++k2p) dst[k1p + B * k2p] = conjf2(u[k2p]);
     }
-    __syncthreads();
+    step = next;
+    buf ^= 1;
   }
+  cp_async_wait<0>();
 
-  if constexpr (RESID) {
-    const double tot = block_sum<kRowNT>(double(racc), sred);
-    if (t == 0) {
-      a.part_r[blockIdx.x] = tot;
-      __threadfence();
-      const unsigned tk = atomicAdd(&st->ticket, 1u);
-      am_last = (tk == gridDim.x - 1);
-    }
-    __syncthreads();
-    if (am_last) {
-      __threadfence();
+  // last CTA: reset the work counter; in RESID mode also reduce the partial
+  // sums and run the scalar recurrence
+  double tot = 0.0;
+  if constexpr (RESID) tot = block_sum<kRowNT>(double(racc), sred);
+  if (t == 0) {
+    if (RESID) a.part_r[blockIdx.x] = tot;
+    __threadfence();
+    const unsigned tk = atomicAdd(&st->ticket, 1u);
+    am_last = (tk == gridDim.x - 1);
+  }
+  __syncthreads();
+  if (am_last) {
+    __threadfence();
+    if constexpr (RESID) {
+      __shared__ float fm[kFmeanCopy];
+      if (t < kFmeanCopy && t < st->miniter) fm[t] = __ldcg(a.fmean + t);
+      // loads of each batch are issued together; the summation order is fixed
+      constexpr int U = 8;
       double su2 = 0.0, sud = 0.0, sr2 = 0.0;
-      for (int i = t; i < a.nblk_k1; i += kRowNT) {
-        su2 += __ldcg(a.part_tv + 2 * i);
-        sud += __ldcg(a.part_tv + 2 * i + 1);
+      const double2* ptv = reinterpret_cast<const double2*>(a.part_tv);
+      for (int i0 = 0; i0 < a.nblk_k1; i0 += U * kRowNT) {
+        double2 v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int i = i0 + u * kRowNT + t;
+          v[u] = (i < a.nblk_k1) ? __ldcg(ptv + i) : make_double2(0.0, 0.0);
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          su2 += v[u].x;
+          sud += v[u].y;
+        }
       }
-      for (int i = t; i < int(gridDim.x); i += kRowNT) sr2 += __ldcg(a.part_r + i);
+      for (int i0 = 0; i0 < int(gridDim.x); i0 += U * kRowNT) {
+        double v[U];
+#pragma unroll
+        for (int u = 0; u < U; ++u) {
+          const int i = i0 + u * kRowNT + t;
+          v[u] = (i < int(gridDim.x)) ? __ldcg(a.part_r + i) : 0.0;
+        }
+#pragma unroll
+        for (int u = 0; u < U; ++u) sr2 += v[u];
+      }
       su2 = block_sum<kRowNT>(su2, sred);
       sud = block_sum<kRowNT>(sud, sred);
       sr2 = block_sum<kRowNT>(sr2, sred);
-      if (t == 0) {
-        st->ticket = 0;
-        nesta_scalar_step(st, a.fmean, it, su2, sud, sr2);
-      }
+      if (t == 0) nesta_scalar_step(st, a.fmean, fm, it, su2, sud, sr2);
+    }
+    if (t == 0) {
+      st->ticket = 0;
+      st->row_next = 0;
     }
   }
 }
@@ -321,32 +495,77 @@ __global__ void __launch_bounds__(kRowNT) k_rows(FusedArgs a, int it) {
 // ===========================================================================
 // K3: adjoint column pass with coil combination, plus (UPDATE) the tTV
 // gradient and the Nesterov update, or (!UPDATE) x0 = E^H y into x_ref.
-// grid = (W/kWB, F)
+// grid = (W/kWB, 2, F) in clusters of 2 CTAs along y: the two CTAs of a
+// cluster share one (frame, 8-column) tile and take the first and second half
+// of the coils; their accumulators are summed through distributed shared
+// memory and each CTA then finishes half of the tile's rows.
+// backward transform along H = conj(forward dit2<B,A>(conj)): pass-1 items
+// (w, s), s < A, hold rows A*n1 + s; pass-2 items (w, k1'), k1' < B, produce
+// rows k1' + B*k2.  The next coil's S tile and kept T rows are copied
+// asynchronously into second shared buffers while the current coil runs.
 // ===========================================================================
+template <int H>
+struct InvColsSmem {
+  static constexpr int A = Split<H>::A, B = Split<H>::B, KS = col_ks(A);
+  static constexpr int RCAP = H / 2;                     // kept rows staged in shared memory
+  static constexpr int S_OFF = 0;                        // float2 [2][H][kWB]
+  static constexpr int T_OFF = S_OFF + 2 * H * kWB;      // float2 [2][RCAP][kWB] (kept rows, compact)
+  static constexpr int EX_OFF = T_OFF + 2 * RCAP * kWB;  // float2 [B*KS]
+  static constexpr int TW_OFF = EX_OFF + B * KS;         // float2 [H]
+  static constexpr int F2_END = TW_OFF + H;
+  static constexpr int BYTES = F2_END * 8 + H * 4;
+  static_assert(cdiv(kWB * B, kColNT) * A * kColNT <= 2 * H * kWB, "accumulator exchange must fit the S buffers");
+};
+
 template <int H, bool UPDATE>
-__global__ void __launch_bounds__(kColNT) k_inv_cols(FusedArgs a, int it) {
-  constexpr int A = Split<H>::A, B = Split<H>::B;
-  // forward dit2<B, A> on conjugated data: pass-1 items (w, s), s in [0, A),
-  // rows ky = A*n1 + s; pass-2 items (w, k1'), k1' in [0, B), rows h = k1' + B*k2
-  constexpr int KS = (A * kWB) % 16 == 8 ? A * kWB : A * kWB + 8;
+__global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT) k_inv_cols(FusedArgs a, int it) {
+  using L = InvColsSmem<H>;
+  constexpr int A = L::A, B = L::B, KS = L::KS, RCAP = L::RCAP;
   constexpr int N1 = kWB * A, N2 = kWB * B;
   constexpr int NI1 = cdiv(N1, kColNT), NI2 = cdiv(N2, kColNT);
-  __shared__ float2 ex[B * KS];
-  __shared__ float2 tw[H];
-  __shared__ int rmap[H];
+  extern __shared__ float4 smem4[];
+  float2* Sb = reinterpret_cast<float2*>(smem4) + L::S_OFF;
+  float2* Tb = reinterpret_cast<float2*>(smem4) + L::T_OFF;
+  float2* ex = reinterpret_cast<float2*>(smem4) + L::EX_OFF;
+  float2* tw = reinterpret_cast<float2*>(smem4) + L::TW_OFF;
+  int* rmap = reinterpret_cast<int*>(reinterpret_cast<float2*>(smem4) + L::F2_END);
+  namespace cgr = cooperative_groups;
+  cgr::cluster_group cluster = cgr::this_cluster();
 
   const NestaDevState* st = a.st;
-  if (UPDATE && it > st->last_iter) return;
+  if (UPDATE && it > st->last_iter) return;  // uniform over the whole grid
   const int t = threadIdx.x;
-  const int f = blockIdx.y, w0 = blockIdx.x * kWB;
+  const int half = blockIdx.y, f = blockIdx.z, w0 = blockIdx.x * kWB;
   const int W = a.W, C = a.C, F = a.F;
   const size_t N = size_t(a.N);
+  const int rowbase = a.rowoff[f];
+  const int nrows = a.rowoff[f + 1] - rowbase;
+  const bool staged = nrows <= RCAP;  // kept rows fit the shared buffers (uniform per CTA)
+  const int cmid = (C + 1) / 2;
+  const int cbeg = half ? cmid : 0, cend = half ? C : cmid;
+
+  auto issue = [&](int c, int buf) {
+    const float2* src = a.S + size_t(c) * N + w0;
+    float2* dst = Sb + buf * H * kWB;
+    for (int q = t; q < H * (kWB / 2); q += kColNT) {
+      const int row = q / (kWB / 2), part = q % (kWB / 2);
+      cp_async16(dst + row * kWB + 2 * part, src + size_t(row) * W + 2 * part);
+    }
+    if (staged) {
+      const float2* tsrc = a.T + (size_t(rowbase) * C + c) * W + w0;
+      float2* tdst = Tb + buf * RCAP * kWB;
+      for (int q = t; q < nrows * (kWB / 2); q += kColNT) {
+        const int j = q / (kWB / 2), part = q % (kWB / 2);
+        cp_async16(tdst + j * kWB + 2 * part, tsrc + size_t(j) * C * W + 2 * part);
+      }
+    }
+    cp_async_commit();
+  };
+  if (cbeg < cend) issue(cbeg, 0);
   for (int i = t; i < H; i += kColNT) {
-    tw[i] = a.twH[i];
+    tw[i] = a.twH[H + i];
     rmap[i] = a.rowmap[f * H + i];
   }
-  const int rowbase = a.rowoff[f];
-  __syncthreads();
 
   float2 acc[NI2][A];
 #pragma unroll
@@ -354,25 +573,36 @@ __global__ void __launch_bounds__(kColNT) k_inv_cols(FusedArgs a, int it) {
 #pragma unroll
     for (int k2 = 0; k2 < A; ++k2) acc[ii][k2] = make_float2(0.f, 0.f);
 
-  for (int c = 0; c < C; ++c) {
+  for (int c = cbeg; c < cend; ++c) {
+    const int buf = (c - cbeg) & 1;
+    cp_async_wait<0>();
+    __syncthreads();  // coil c staged; previous coil's pass 2 finished
+    if (c + 1 < cend) issue(c + 1, buf ^ 1);
+    const float2* Tc = Tb + buf * RCAP * kWB;
+    const float2* Sc = Sb + buf * H * kWB;
 #pragma unroll
     for (int ii = 0; ii < NI1; ++ii) {
       const int i = t + ii * kColNT;
       if (i < N1) {
         const int w = i % kWB, s = i / kWB;
+        int jv[B];
+#pragma unroll
+        for (int n1 = 0; n1 < B; ++n1) jv[n1] = rmap[A * n1 + s];
         float2 v[B];
 #pragma unroll
         for (int n1 = 0; n1 < B; ++n1) {
-          const int j = rmap[A * n1 + s];
-          v[n1] = (j >= 0) ? conjf2(a.T[(size_t(rowbase + j) * C + c) * W + w0 + w]) : make_float2(0.f, 0.f);
+          float2 e = make_float2(0.f, 0.f);
+          if (jv[n1] >= 0)
+            e = staged ? Tc[jv[n1] * kWB + w] : a.T[(size_t(rowbase + jv[n1]) * C + c) * W + w0 + w];
+          v[n1] = conjf2(e);
         }
         dft<B>(v);
 #pragma unroll
-        for (int k1p = 0; k1p < B; ++k1p) ex[k1p * KS + s * kWB + w] = (k1p == 0) ? v[k1p] : cmul(v[k1p], tw[s * k1p]);
+        for (int k1p = 0; k1p < B; ++k1p)
+          ex[k1p * KS + s * kWB + w] = (k1p == 0) ? v[k1p] : cmul(v[k1p], tw[k1p * A + s]);
       }
     }
     __syncthreads();
-    const float2* __restrict__ Sc = a.S + size_t(c) * N;
 #pragma unroll
     for (int ii = 0; ii < NI2; ++ii) {
       const int i = t + ii * kColNT;
@@ -384,16 +614,39 @@ __global__ void __launch_bounds__(kColNT) k_inv_cols(FusedArgs a, int it) {
         dft<A>(v);
 #pragma unroll
         for (int k2 = 0; k2 < A; ++k2) {
-          const float2 sv = Sc[size_t(k1p + B * k2) * W + w0 + w];
           // conj(v) * conj(S) == conj(v * S)
-          const float2 p = cmul(v[k2], sv);
+          const float2 p = cmul(v[k2], Sc[(k1p + B * k2) * kWB + w]);
           acc[ii][k2].x += p.x;
           acc[ii][k2].y -= p.y;
         }
       }
     }
-    __syncthreads();
   }
+
+  // Sum the two halves' accumulators: each CTA publishes its partial sums in
+  // its own (now idle) S buffers and reads its partner's for the rows it
+  // finishes (k2 < A/2 for the first CTA, the rest for the second).
+  cp_async_wait<0>();
+  __syncthreads();
+  float2* mine = Sb;
+#pragma unroll
+  for (int ii = 0; ii < NI2; ++ii)
+#pragma unroll
+    for (int k2 = 0; k2 < A; ++k2) mine[(ii * A + k2) * kColNT + t] = acc[ii][k2];
+  cluster.sync();
+  const float2* other = cluster.map_shared_rank(mine, half ^ 1);
+  constexpr int KH = A / 2;
+  const int kb = half ? KH : 0, ke = half ? A : KH;
+#pragma unroll
+  for (int ii = 0; ii < NI2; ++ii)
+#pragma unroll
+    for (int k2 = 0; k2 < A; ++k2)
+      if (k2 >= kb && k2 < ke) {
+        // fixed summation order (first half of the coils, then the second)
+        const float2 o = other[(ii * A + k2) * kColNT + t];
+        acc[ii][k2] = half ? cadd(o, acc[ii][k2]) : cadd(acc[ii][k2], o);
+      }
+  cluster.sync();  // partner finished reading this CTA's buffers
 
   const float s_adj = a.s_adj;
   if constexpr (!UPDATE) {
@@ -404,43 +657,58 @@ __global__ void __launch_bounds__(kColNT) k_inv_cols(FusedArgs a, int it) {
         const int w = i % kWB, k1p = i / kWB;
 #pragma unroll
         for (int k2 = 0; k2 < A; ++k2)
-          a.xref[size_t(f) * N + size_t(k1p + B * k2) * W + w0 + w] = cscale(acc[ii][k2], s_adj);
+          if (k2 >= kb && k2 < ke)
+            a.xref[size_t(f) * N + size_t(k1p + B * k2) * W + w0 + w] = cscale(acc[ii][k2], s_adj);
       }
     }
   } else {
     const float2* __restrict__ xk = (it & 1) ? a.xk1 : a.xk0;
     float2* __restrict__ xn = (it & 1) ? a.xk0 : a.xk1;
     const size_t offm = size_t((f + F - 1) % F) * N, off0 = size_t(f) * N, offp = size_t((f + 1) % F) * N;
-    const float mu = st->mu, lambda = st->lambda, nLmu1 = -st->Lmu1, apk = st->apk, tauk = st->tauk;
+    const float inv_mu = 1.0f / st->mu, lambda = st->lambda, nLmu1 = -st->Lmu1, apk = st->apk, tauk = st->tauk;
     const float omt = 1.0f - tauk;
+    constexpr int BATCH = 4;  // outputs whose global loads are issued together
 #pragma unroll
     for (int ii = 0; ii < NI2; ++ii) {
       const int i = t + ii * kColNT;
       if (i < N2) {
         const int w = i % kWB, k1p = i / kWB;
 #pragma unroll
-        for (int k2 = 0; k2 < A; ++k2) {
-          const size_t p = size_t(k1p + B * k2) * W + w0 + w;
-          const float2 xa = xk[off0 + p], xm = xk[offm + p], xp = xk[offp + p];
-          // u_f and u_{f+1} of the normalised temporal difference
-          const float2 d0 = csub(xa, xm), d1 = csub(xp, xa);
-          const float m0 = fmaxf(mu, sqrtf(fmaf(d0.x, d0.x, d0.y * d0.y)));
-          const float m1 = fmaxf(mu, sqrtf(fmaf(d1.x, d1.x, d1.y * d1.y)));
-          const float2 u0 = make_float2(d0.x / m0, d0.y / m0);
-          const float2 u1 = make_float2(d1.x / m1, d1.y / m1);
-          // operator_tTVadj gives u_{f+1} - u_f; NestaUp negates it, scales by lambda, adds A^H r
-          const float2 adj = csub(u1, u0);
-          const float2 ares = cscale(acc[ii][k2], s_adj);
-          const float2 df = make_float2(__fadd_rn(__fmul_rn(-adj.x, lambda), ares.x),
-                                        __fadd_rn(__fmul_rn(-adj.y, lambda), ares.y));
-          const float2 yk = make_float2(fmaf(nLmu1, df.x, xa.x), fmaf(nLmu1, df.y, xa.y));
-          const float2 wo = a.wacc[off0 + p];
-          const float2 wn = make_float2(fmaf(apk, df.x, wo.x), fmaf(apk, df.y, wo.y));
-          const float2 xr = a.xref[off0 + p];
-          const float2 zk = make_float2(fmaf(nLmu1, wn.x, xr.x), fmaf(nLmu1, wn.y, xr.y));
-          const float2 xnew = make_float2(fmaf(omt, yk.x, tauk * zk.x), fmaf(omt, yk.y, tauk * zk.y));
-          a.wacc[off0 + p] = wn;
-          xn[off0 + p] = xnew;
+        for (int k0 = 0; k0 < A; k0 += BATCH) {
+          float2 xa[BATCH], xm[BATCH], xp[BATCH], wo[BATCH], xr[BATCH];
+#pragma unroll
+          for (int b = 0; b < BATCH; ++b) {
+            const int k2 = k0 + b;
+            if (k2 < A && k2 >= kb && k2 < ke) {
+              const size_t p = size_t(k1p + B * k2) * W + w0 + w;
+              xa[b] = xk[off0 + p];
+              xm[b] = xk[offm + p];
+              xp[b] = xk[offp + p];
+              wo[b] = a.wacc[off0 + p];
+              xr[b] = a.xref[off0 + p];
+            }
+          }
+#pragma unroll
+          for (int b = 0; b < BATCH; ++b) {
+            const int k2 = k0 + b;
+            if (k2 < A && k2 >= kb && k2 < ke) {
+              const size_t p = size_t(k1p + B * k2) * W + w0 + w;
+              // u_f and u_{f+1} of the normalised temporal difference
+              const float2 u0 = tv_normalize(csub(xa[b], xm[b]), inv_mu);
+              const float2 u1 = tv_normalize(csub(xp[b], xa[b]), inv_mu);
+              // operator_tTVadj gives u_{f+1} - u_f; NestaUp negates it, scales by lambda, adds A^H r
+              const float2 adj = csub(u1, u0);
+              const float2 ares = cscale(acc[ii][k2], s_adj);
+              const float2 df = make_float2(__fadd_rn(__fmul_rn(-adj.x, lambda), ares.x),
+                                            __fadd_rn(__fmul_rn(-adj.y, lambda), ares.y));
+              const float2 yk = make_float2(fmaf(nLmu1, df.x, xa[b].x), fmaf(nLmu1, df.y, xa[b].y));
+              const float2 wn = make_float2(fmaf(apk, df.x, wo[b].x), fmaf(apk, df.y, wo[b].y));
+              const float2 zk = make_float2(fmaf(nLmu1, wn.x, xr[b].x), fmaf(nLmu1, wn.y, xr[b].y));
+              const float2 xnew = make_float2(fmaf(omt, yk.x, tauk * zk.x), fmaf(omt, yk.y, tauk * zk.y));
+              a.wacc[off0 + p] = wn;
+              xn[off0 + p] = xnew;
+            }
+          }
         }
       }
     }
@@ -476,7 +744,7 @@ __global__ void __launch_bounds__(kRowNT) k_fft_rows_dense(const float2* in, flo
       }
       dft<A>(v);
 #pragma unroll
-      for (int k1 = 0; k1 < A; ++k1) ex1[r * R::RS1 + k1 * R::S1 + s] = (k1 == 0) ? v[k1] : cmul(v[k1], tw[s * k1]);
+      for (int k1 = 0; k1 < A; ++k1) ex1[r * R::RS1 + k1 * R::S1 + s] = (k1 == 0) ? v[k1] : cmul(v[k1], tw[k1 * B + s]);
     }
     __syncthreads();
     for (int i = t; i < RPC * A; i += kRowNT) {
@@ -499,7 +767,7 @@ template <int H>
 __global__ void __launch_bounds__(kColNT) k_fft_cols_dense(const float2* in, float2* out, int W, int inv, float scale,
                                                            const float2* twH) {
   constexpr int A = Split<H>::A, B = Split<H>::B;
-  constexpr int KS = (B * kWB) % 16 == 8 ? B * kWB : B * kWB + 8;
+  constexpr int KS = col_ks(B);
   constexpr int N1 = kWB * B, N2 = kWB * A;
   __shared__ float2 ex[A * KS];
   __shared__ float2 tw[H];
@@ -519,7 +787,7 @@ __global__ void __launch_bounds__(kColNT) k_fft_cols_dense(const float2* in, flo
     }
     dft<A>(v);
 #pragma unroll
-    for (int k1 = 0; k1 < A; ++k1) ex[k1 * KS + s * kWB + w] = (k1 == 0) ? v[k1] : cmul(v[k1], tw[s * k1]);
+    for (int k1 = 0; k1 < A; ++k1) ex[k1 * KS + s * kWB + w] = (k1 == 0) ? v[k1] : cmul(v[k1], tw[k1 * B + s]);
   }
   __syncthreads();
   for (int i = t; i < N2; i += kColNT) {

@@ -30,7 +30,12 @@ struct NestaDevState {
   int qpDone;
   float qp, fx, apk, tauk;
   float normUk, fxdot, l2term;
-  unsigned int ticket;
+  unsigned int ticket;    // last-block detection in the row pass
+  int row_next;           // dynamic work counter of the row pass
+
+  // power-method progress across chunks
+  int ne_done, ne_cnt;
+  float ne_e, ne_e0;
 
   // statistics
   int iters_total;
@@ -58,8 +63,12 @@ struct FusedArgs {
   float* fmean;           // [miniter] rolling objective buffer
   double* part_tv;        // [nblk_k1][2] partial sums of ||u||^2 and Re<u,d>
   double* part_r;         // [nblk_k2] partial sums of ||E x - y||^2
-  const float2* twH;      // twiddles w_H^j (forward sign), j in [0,H)
-  const float2* twW;      // twiddles w_W^j
+  // Twiddle tables for the two-pass transforms, forward sign, 2L entries per
+  // length: [k1*B + s] = w_L^(s*k1) (k1 < A, s < B), then [L + k1'*A + s'] =
+  // w_L^(s'*k1') (k1' < B, s' < A), laid out so that the lanes of a warp read
+  // consecutive words.
+  const float2* twH;
+  const float2* twW;
   float s_fwd;            // 1/sqrt(N) as the reference computes it (double -> float)
   float s_adj;            // sqrt(N)/N: the reference's sqrt(N) pre-scale times clFFT's 1/N
   int nblk_k1;            // number of blocks of the forward column kernel

@@ -199,8 +199,12 @@ def _nrm2sq(v: np.ndarray) -> float:
 
 
 def nesta(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams, precision: str = "f32",
-          rand_state: int = drand48.DEFAULT_STATE, record: bool = False) -> NestaResult:
-    """y: KData [F][C][H][W]; S: [C][H][W]; mask: pixel mask [F][H][W] (uint8)."""
+          rand_state: int = drand48.DEFAULT_STATE, record: bool = False, timings: dict | None = None) -> NestaResult:
+    """y: KData [F][C][H][W]; S: [C][H][W]; mask: pixel mask [F][H][W] (uint8).
+    `timings`, when given, receives wall-clock marks: 'setup' (seconds until the
+    first inner iteration) and 'iters' (seconds of each inner iteration)."""
+    import time as _time
+    _t0 = _time.perf_counter()
     P = _P(precision)
     F, Cn, H, W = y.shape
     N = H * W
@@ -234,6 +238,9 @@ def nesta(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams, prec
     qp = s(0)
     iters = 0
     hist = []
+    if timings is not None:
+        timings["setup"] = _time.perf_counter() - _t0
+        timings["iters"] = []
     for nl in range(1, prm.maxIntIter + 1):
         mu = s(mu * gamma)
         tolVar = s(tolVar * gammat)
@@ -287,6 +294,9 @@ def nesta(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams, prec
             xk = xk.astype(P.c)
             w = w.astype(P.c)
             iters += 1
+            if timings is not None:
+                _t1 = _time.perf_counter()
+                timings["iters"].append(_t1 - _t0 - timings["setup"] - sum(timings["iters"]))
             if record:
                 hist.append(float(fx))
             k += 1

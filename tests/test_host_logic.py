@@ -1,0 +1,73 @@
+"""Host-side logic without a GPU: synthetic workload properties, benchmark
+helpers, and the multi-process (replica) bench path with gloo ranks."""
+from __future__ import annotations
+
+import os
+import socket
+
+import numpy as np
+import pytest
+
+from opencliper_gb300 import synth
+
+
+def test_synthetic_problem_properties():
+    p = synth.make_problem(64, 48, 5, 6, 4, seed=0)
+    F, C, H, W = p.y.shape
+    assert (F, C, H, W) == (5, 6, 48, 64)
+    assert p.y.dtype == np.complex64 and p.S.dtype == np.complex64 and p.mask.dtype == np.uint8
+    assert np.allclose(np.sum(np.abs(p.S) ** 2, axis=0), 1.0, atol=1e-5)
+    for f in range(F):
+        rows = np.flatnonzero(p.rowmask[f])
+        assert len(rows) == max(16, round(H / 4))
+        assert set(range(8)) | set(range(H - 8, H)) <= set(rows)
+    assert np.all(p.y[np.broadcast_to(p.mask[:, None] == 0, p.y.shape)] == 0)
+    assert np.array_equal(p.mask, np.repeat((p.rowmask * 255).astype(np.uint8)[:, :, None], W, axis=2))
+
+
+def test_synthetic_problem_is_seeded():
+    a = synth.make_problem(32, 32, 3, 2, 4, seed=9)
+    b = synth.make_problem(32, 32, 3, 2, 4, seed=9)
+    assert np.array_equal(a.y, b.y) and np.array_equal(a.mask, b.mask)
+
+
+def test_algorithmic_bytes():
+    import bench
+    G = 640
+    assert bench.algorithmic_bytes("rows", G) == 3 * 8 * G * 12 * 256 + G * 256
+    assert bench.algorithmic_bytes("fwd_cols", G) == 8 * 65536 * 20 + 8 * 65536 * 12 + 8 * G * 12 * 256
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _rank_main(rank, world, port, q):
+    os.environ.update(RANK=str(rank), WORLD_SIZE=str(world), LOCAL_RANK=str(rank),
+                      MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    import bench
+    d = bench.Dist()
+    d.barrier()
+    m = d.max(float(rank + 1) * 10.0)
+    d.barrier()
+    d.close()
+    q.put((rank, m))
+
+
+def test_replica_barrier_and_max_over_gloo_ranks():
+    pytest.importorskip("torch")
+    import multiprocessing as mp
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_rank_main, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    res = dict(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+    assert res == {0: 20.0, 1: 20.0}
