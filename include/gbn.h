@@ -165,6 +165,18 @@ GBN_API int gbn_op_encode_adjoint(gbn_ctx* ctx, const float* d_k, const float* d
  * x[f] = sum_c conj(S[c]) * IFFT2(y[f][c]).  The input is not modified. */
 GBN_API int gbn_simple_recon(gbn_ctx* ctx, const float* d_y, const float* d_S, float* d_x, int W, int H, int F, int C);
 
+/* Allocation-free SimpleMRIRecon: same result as gbn_simple_recon, but no
+ * device memory is allocated.  No counterpart in the reference.  For callers
+ * that cannot call cudaMalloc (code running during CUDA-graph stream capture,
+ * hosts that own all device memory in fixed pools): the working memory is a
+ * fixed array inside the library (about 8.2 MiB per device, kept until the
+ * process exits).  Limits: F*H*C*W <= 2^20 and F*H <= 8192, otherwise
+ * GBN_ERR_UNSUPPORTED.  The first call on a device resolves the array's
+ * device address; make that first call before any stream capture.  All calls
+ * share the one array: calls that overlap on the GPU race, so serialise them. */
+GBN_API int gbn_simple_recon_static(gbn_ctx* ctx, const float* d_y, const float* d_S, float* d_x, int W, int H,
+                                    int F, int C);
+
 /* ------------------------------------------------------------------------ */
 /* NESTA (NestaUp::launch, NestaUp.cpp:442-910)                              */
 /* ------------------------------------------------------------------------ */

@@ -92,6 +92,7 @@ SIGNATURES: dict[str, list] = {
     "gbn_op_encode": [_vp, _vp, _vp, _vp, _vp, _i, _i, _i, _i],
     "gbn_op_encode_adjoint": [_vp, _vp, _vp, _vp, _i, _i, _i, _i],
     "gbn_simple_recon": [_vp, _vp, _vp, _vp, _i, _i, _i, _i],
+    "gbn_simple_recon_static": [_vp, _vp, _vp, _vp, _i, _i, _i, _i],
     "gbn_problem_create": [_vp, _i, _i, _i, _i, _vp, _vp, _vp, C.POINTER(_vp)],
     "gbn_problem_destroy": [_vp],
     "gbn_nesta_run": [_vp, _vp, C.POINTER(NestaParams), _vp, C.POINTER(NestaStats)],

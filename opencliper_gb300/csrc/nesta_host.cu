@@ -671,4 +671,12 @@ int simple_recon(gbn_ctx* ctx, const float2* y, const float2* S, float2* x, int 
   return GBN_OK;
 }
 
+// Launches the identity row numbering (every row kept) for F frames of H rows.
+void launch_rows_identity(int H, int F, int* rowmap, int* rowoff, int* rows_h, int* rows_f, int* row_full,
+                          cudaStream_t s) {
+  const size_t FH = size_t(F) * H;
+  k_rows_identity<<<int(std::min<size_t>((FH + 255) / 256, 1024)), 256, 0, s>>>(H, F, rowmap, rowoff, rows_h, rows_f,
+                                                                                row_full);
+}
+
 }  // namespace gbn
