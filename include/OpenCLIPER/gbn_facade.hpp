@@ -1,0 +1,485 @@
+// C++ facade with OpenCLIPER's Process-style API over the GB300 C ABI (gbn.h).
+//
+// Callers written against the reference (tests/MRIRecon.cpp,
+// examples/simpleMRIRecon.cpp) keep their structure: create the runtime with
+// CLapp::create, wrap k-space, sensitivity maps and sampling masks in
+// KData/SensitivityMapsData/SamplingMasksData, create processes with
+// Process::create<T>(app), set input/output and parameters, then init() and
+// launch().  Differences from the reference:
+//  - device buffers are CUDA allocations: Data::getDeviceBuffer() returning a
+//    cl::Buffer* becomes Data::getDevicePtr() returning void*;
+//  - data objects are built from host vectors (file loaders are not part of
+//    this library);
+//  - NestaUp does not support motion compensation (argsMC must be nullptr).
+// Errors are thrown as CLError (code = GBN_ERR_*) or std::invalid_argument,
+// like the reference's BTTHROW (LPISupport/include/LPISupport/Utils.hpp:67-83).
+#pragma once
+
+#include <complex>
+#include <cstdint>
+#include <memory>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../gbn.h"
+
+namespace OpenCLIPER {
+
+using dimIndexType = uint32_t;
+using realType = float;
+using complexType = std::complex<float>;
+
+/// CLError (include/OpenCLIPER/CLapp.hpp:114-144): a runtime failure with a status code.
+class CLError : public std::runtime_error {
+ public:
+  CLError(int code, const std::string& what) : std::runtime_error(what), code_(code) {}
+  int err() const { return code_; }
+
+ private:
+  int code_;
+};
+
+inline void gbnCheck(int rc, const char* where) {
+  if (rc == GBN_OK) return;
+  const std::string msg = std::string(where) + ": " + gbn_last_error_string();
+  if (rc == GBN_ERR_INVALID) throw std::invalid_argument(msg);
+  throw CLError(rc, msg);
+}
+
+/// CLapp (src/CLapp.cpp:188-575): device, stream and allocation layer.
+class CLapp {
+ public:
+  struct PlatformTraits {};
+  struct DeviceTraits {
+    int device;
+    DeviceTraits() : device(0) {}
+    explicit DeviceTraits(int d) : device(d) {}
+  };
+  static std::shared_ptr<CLapp> create() { return create(PlatformTraits(), DeviceTraits()); }
+  static std::shared_ptr<CLapp> create(const PlatformTraits&, const DeviceTraits& dt) {
+    return std::shared_ptr<CLapp>(new CLapp(dt.device));
+  }
+  ~CLapp() {
+    if (ctx_) gbn_ctx_destroy(ctx_);
+  }
+  CLapp(const CLapp&) = delete;
+  CLapp& operator=(const CLapp&) = delete;
+  gbn_ctx* ctx() const { return ctx_; }
+  /// kernels are compiled ahead of time; kept for source compatibility
+  void loadKernels() {}
+  /// getCommandQueue().finish()
+  void finish() { gbnCheck(gbn_ctx_sync(ctx_), "CLapp::finish"); }
+
+ private:
+  explicit CLapp(int device) { gbnCheck(gbn_ctx_create(device, &ctx_), "CLapp::create"); }
+  gbn_ctx* ctx_ = nullptr;
+};
+
+/// Data (src/Data.cpp): one contiguous device buffer mirroring a host array.
+class Data {
+ public:
+  virtual ~Data() {
+    if (dev_ && app_) gbn_free(app_->ctx(), dev_);
+  }
+  void* getDevicePtr() const { return dev_; }
+  size_t getBytes() const { return bytes_; }
+  const std::shared_ptr<CLapp>& getApp() const { return app_; }
+
+ protected:
+  Data(const std::shared_ptr<CLapp>& app, size_t bytes) : app_(app), bytes_(bytes) {
+    gbnCheck(gbn_alloc(app->ctx(), bytes, &dev_), "Data: device allocation");
+  }
+  void upload(const void* host) {
+    gbnCheck(gbn_upload(app_->ctx(), dev_, host, bytes_), "Data::host2Device");
+    app_->finish();
+  }
+  void download(void* host) const { gbnCheck(gbn_download(app_->ctx(), host, dev_, bytes_), "Data::device2Host"); }
+  std::shared_ptr<CLapp> app_;
+  void* dev_ = nullptr;
+  size_t bytes_ = 0;
+};
+
+/// SensitivityMapsData: coil maps [C][H][W].
+class SensitivityMapsData : public Data {
+ public:
+  SensitivityMapsData(const std::shared_ptr<CLapp>& app, dimIndexType W, dimIndexType H, dimIndexType C,
+                      const std::vector<complexType>& maps)
+      : Data(app, sizeof(complexType) * size_t(W) * H * C), W_(W), H_(H), C_(C) {
+    if (maps.size() != size_t(W) * H * C) throw std::invalid_argument("SensitivityMapsData: size mismatch");
+    upload(maps.data());
+  }
+  dimIndexType getNCoils() const { return C_; }
+
+ private:
+  dimIndexType W_, H_, C_;
+};
+
+/// SamplingMasksData: pixel mask [F][H][W], 0 = not sampled.  The row-mask
+/// form (0/1 per phase-encode line, [F][H]) is expanded on the device like
+/// SamplingMasksData::rowmask2pixelmask (SamplingMasksData.cpp:389-441).
+class SamplingMasksData : public Data {
+ public:
+  SamplingMasksData(const std::shared_ptr<CLapp>& app, dimIndexType W, dimIndexType H, dimIndexType F,
+                    const std::vector<uint8_t>& pixelMask)
+      : Data(app, size_t(W) * H * F) {
+    if (pixelMask.size() != size_t(W) * H * F) throw std::invalid_argument("SamplingMasksData: size mismatch");
+    upload(pixelMask.data());
+  }
+  static std::shared_ptr<SamplingMasksData> fromRowMask(const std::shared_ptr<CLapp>& app, dimIndexType W,
+                                                        dimIndexType H, dimIndexType F,
+                                                        const std::vector<uint32_t>& rowMask) {
+    if (rowMask.size() != size_t(H) * F) throw std::invalid_argument("SamplingMasksData: row mask size mismatch");
+    auto m = std::shared_ptr<SamplingMasksData>(new SamplingMasksData(app, W, H, F));
+    void* tmp = nullptr;
+    gbnCheck(gbn_alloc(app->ctx(), rowMask.size() * 4, &tmp), "SamplingMasksData: row mask");
+    int rc = gbn_upload(app->ctx(), tmp, rowMask.data(), rowMask.size() * 4);
+    if (rc == GBN_OK)
+      rc = gbn_op_rowmask_to_pixelmask(app->ctx(), static_cast<const uint32_t*>(tmp), static_cast<uint8_t*>(m->dev_),
+                                       int(W), int(H), int(F));
+    gbn_free(app->ctx(), tmp);
+    gbnCheck(rc, "SamplingMasksData::rowmask2pixelmask");
+    return m;
+  }
+
+ private:
+  SamplingMasksData(const std::shared_ptr<CLapp>& app, dimIndexType W, dimIndexType H, dimIndexType F)
+      : Data(app, size_t(W) * H * F) {}
+};
+
+/// KData: multicoil k-space [F][C][H][W] with its sensitivity maps and masks.
+class KData : public Data {
+ public:
+  KData(const std::shared_ptr<CLapp>& app, dimIndexType W, dimIndexType H, dimIndexType F, dimIndexType C,
+        const std::vector<complexType>& data, std::shared_ptr<SensitivityMapsData> sens = nullptr,
+        std::shared_ptr<SamplingMasksData> masks = nullptr)
+      : Data(app, sizeof(complexType) * size_t(W) * H * F * C), W_(W), H_(H), F_(F), C_(C), sens_(sens), masks_(masks) {
+    if (W % 8 != 0) throw std::invalid_argument("NDArray dimension 0 is not multiple of 8");
+    if (data.size() != size_t(W) * H * F * C) throw std::invalid_argument("KData: size mismatch");
+    upload(data.data());
+  }
+  std::shared_ptr<SensitivityMapsData> getSensitivityMapsData() const { return sens_; }
+  std::shared_ptr<SamplingMasksData> getSamplingMasksData() const { return masks_; }
+  dimIndexType getNCoils() const { return C_; }
+  dimIndexType getDynDimsTotalSize() const { return F_; }
+  dimIndexType width() const { return W_; }
+  dimIndexType height() const { return H_; }
+  void device2Host(std::vector<complexType>& out) const {
+    out.resize(size_t(W_) * H_ * F_ * C_);
+    download(out.data());
+  }
+
+ private:
+  dimIndexType W_, H_, F_, C_;
+  std::shared_ptr<SensitivityMapsData> sens_;
+  std::shared_ptr<SamplingMasksData> masks_;
+};
+
+/// XData: image series [F][H][W]; XData(app, kdata) sizes it like the input
+/// k-space (XData.cpp:425-440).
+class XData : public Data {
+ public:
+  XData(const std::shared_ptr<CLapp>& app, const std::shared_ptr<KData>& k)
+      : Data(app, sizeof(complexType) * size_t(k->width()) * k->height() * k->getDynDimsTotalSize()),
+        W_(k->width()), H_(k->height()), F_(k->getDynDimsTotalSize()) {}
+  XData(const std::shared_ptr<CLapp>& app, dimIndexType W, dimIndexType H, dimIndexType F,
+        const std::vector<complexType>& data)
+      : Data(app, sizeof(complexType) * size_t(W) * H * F), W_(W), H_(H), F_(F) {
+    if (W % 8 != 0) throw std::invalid_argument("NDArray dimension 0 is not multiple of 8");
+    if (data.size() != size_t(W) * H * F) throw std::invalid_argument("XData: size mismatch");
+    upload(data.data());
+  }
+  dimIndexType getDynDimsTotalSize() const { return F_; }
+  dimIndexType width() const { return W_; }
+  dimIndexType height() const { return H_; }
+  void device2Host(std::vector<complexType>& out) const {
+    out.resize(size_t(W_) * H_ * F_);
+    download(out.data());
+  }
+
+ private:
+  dimIndexType W_, H_, F_;
+};
+
+/// Process / ProcessCore (include/OpenCLIPER/Process.hpp:49-108,
+/// ProcessCore.hpp:56-270).
+class Process {
+ public:
+  struct InitParameters {
+    virtual ~InitParameters() {}
+  };
+  struct LaunchParameters {
+    virtual ~LaunchParameters() {}
+  };
+  struct ProfileParameters {
+    bool enable = false;
+    unsigned long loops = 1;
+    ProfileParameters() {}
+    ProfileParameters(bool e, unsigned long l) : enable(e), loops(l) {}
+    virtual ~ProfileParameters() {}
+  };
+  virtual ~Process() {}
+  template <typename T>
+  static std::shared_ptr<T> create(const std::shared_ptr<CLapp>& app,
+                                   const std::shared_ptr<ProfileParameters>& pp = nullptr) {
+    static_assert(std::is_base_of<Process, T>::value, "Process::create: class does not derive from Process");
+    auto p = std::shared_ptr<T>(new T());
+    p->app_ = app;
+    p->pp_ = pp;
+    return p;
+  }
+  void setInput(std::shared_ptr<Data> in) { in_ = std::move(in); }
+  void setOutput(std::shared_ptr<Data> out) { out_ = std::move(out); }
+  virtual void setInitParameters(const std::shared_ptr<InitParameters>& p) { ip_ = p; }
+  virtual void setLaunchParameters(const std::shared_ptr<LaunchParameters>& p) { lp_ = p; }
+  virtual void init() {
+    if (!app_) throw std::invalid_argument("Invalid CLapp pointer");
+  }
+  virtual void launch() = 0;
+
+ protected:
+  Process() {}
+  gbn_ctx* ctx() const { return app_->ctx(); }
+  template <typename D>
+  std::shared_ptr<D> inputAs(const char* who) const {
+    auto d = std::dynamic_pointer_cast<D>(in_);
+    if (!d) throw std::invalid_argument(std::string(who) + ": input data has the wrong type");
+    return d;
+  }
+  template <typename D>
+  std::shared_ptr<D> outputAs(const char* who) const {
+    auto d = std::dynamic_pointer_cast<D>(out_);
+    if (!d) throw std::invalid_argument(std::string(who) + ": output data has the wrong type");
+    return d;
+  }
+  std::shared_ptr<CLapp> app_;
+  std::shared_ptr<ProfileParameters> pp_;
+  std::shared_ptr<Data> in_, out_;
+  std::shared_ptr<InitParameters> ip_;
+  std::shared_ptr<LaunchParameters> lp_;
+};
+
+/// TemporalTV (src/processes/nesta/TemporalTV.cpp:49-86) on XData.
+class TemporalTV : public Process {
+ public:
+  enum Direction { FORWARD = 1, ADJOINT = 0 };
+  struct InitParameters : Process::InitParameters {
+    Direction dir;
+    InitParameters(Direction d) : dir(d) {}
+  };
+  void launch() override {
+    auto ip = std::dynamic_pointer_cast<InitParameters>(ip_);
+    if (!ip) throw std::invalid_argument("TemporalTV: missing InitParameters");
+    auto x = inputAs<XData>("TemporalTV");
+    auto y = outputAs<XData>("TemporalTV");
+    gbnCheck(gbn_op_ttv(ctx(), int(ip->dir), static_cast<const float*>(x->getDevicePtr()),
+                        static_cast<float*>(y->getDevicePtr()), int(x->width()), int(x->height()),
+                        int(x->getDynDimsTotalSize())),
+             "TemporalTV::launch");
+  }
+};
+
+/// VectorNormalization (src/processes/nesta/VectorNormalization.cpp:56-87).
+class VectorNormalization : public Process {
+ public:
+  struct LaunchParameters : Process::LaunchParameters {
+    float mu;
+    LaunchParameters(float m) : mu(m) {}
+  };
+  void launch() override {
+    auto lp = std::dynamic_pointer_cast<LaunchParameters>(lp_);
+    if (!lp) throw std::invalid_argument("VectorNormalization: missing LaunchParameters");
+    gbnCheck(gbn_op_normalize(ctx(), static_cast<const float*>(in_->getDevicePtr()), static_cast<float*>(out_->getDevicePtr()),
+                              in_->getBytes() / sizeof(complexType), lp->mu),
+             "VectorNormalization::launch");
+  }
+};
+
+/// FFT process, 2-D over each image (src/processes/FFT.cpp:59-542).
+class FFT : public Process {
+ public:
+  enum Direction { FORWARD = GBN_FFT_FORWARD, BACKWARD = GBN_FFT_BACKWARD };
+  struct InitParameters : Process::InitParameters {
+    int dim;
+    std::shared_ptr<SamplingMasksData> samplingMask;
+    explicit InitParameters(int d = -1, std::shared_ptr<SamplingMasksData> s = nullptr) : dim(d), samplingMask(s) {}
+  };
+  struct LaunchParameters : Process::LaunchParameters {
+    Direction dir;
+    explicit LaunchParameters(Direction d = FORWARD) : dir(d) {}
+  };
+  void init() override {
+    Process::init();
+    auto ip = std::dynamic_pointer_cast<InitParameters>(ip_);
+    if (ip && (ip->dim != -1 || ip->samplingMask))
+      throw CLError(GBN_ERR_UNSUPPORTED, "FFT::init: only full 2-D transforms (dim = -1) are implemented");
+  }
+  void launch() override {
+    auto lp = std::dynamic_pointer_cast<LaunchParameters>(lp_);
+    const Direction d = lp ? lp->dir : FORWARD;
+    int W, H, batch;
+    if (auto k = std::dynamic_pointer_cast<KData>(in_)) {
+      W = int(k->width()), H = int(k->height()), batch = int(k->getDynDimsTotalSize() * k->getNCoils());
+    } else {
+      auto x = inputAs<XData>("FFT");
+      W = int(x->width()), H = int(x->height()), batch = int(x->getDynDimsTotalSize());
+    }
+    if (in_->getBytes() != out_->getBytes())
+      throw CLError(GBN_ERR_INVALID, "FFT: inputData and outputData must have the same number of images");
+    gbnCheck(gbn_op_fft2(ctx(), int(d), static_cast<const float*>(in_->getDevicePtr()),
+                         static_cast<float*>(out_->getDevicePtr()), W, H, batch),
+             "FFT::launch");
+  }
+};
+
+/// ComplexElementProd (src/processes/ComplexElementProd.cpp:64-131).
+class ComplexElementProd : public Process {
+ public:
+  enum ConjugateSensMap_t { notConjugate = 0, conjugate = 1 };
+  struct LaunchParameters : Process::LaunchParameters {
+    ConjugateSensMap_t conjugateSensMap;
+    std::shared_ptr<SensitivityMapsData> sensitivityMapsData;
+    LaunchParameters(ConjugateSensMap_t c, const std::shared_ptr<SensitivityMapsData>& m)
+        : conjugateSensMap(c), sensitivityMapsData(m) {}
+  };
+  void launch() override {
+    auto lp = std::dynamic_pointer_cast<LaunchParameters>(lp_);
+    if (!lp || !lp->sensitivityMapsData)
+      throw std::invalid_argument("ComplexElementProd::launch: non-existing SensitivityMaps");
+    auto out = outputAs<KData>("ComplexElementProd");
+    const bool inK = bool(std::dynamic_pointer_cast<KData>(in_));
+    gbnCheck(gbn_op_sensmul(ctx(), int(lp->conjugateSensMap), static_cast<const float*>(in_->getDevicePtr()), inK ? 1 : 0,
+                            static_cast<const float*>(lp->sensitivityMapsData->getDevicePtr()),
+                            static_cast<float*>(out->getDevicePtr()), int(out->width()), int(out->height()),
+                            int(out->getDynDimsTotalSize()), int(out->getNCoils())),
+             "ComplexElementProd::launch");
+  }
+};
+
+/// XImageSum (src/processes/XImageSum.cpp:79-96): coil sum.
+class XImageSum : public Process {
+ public:
+  void launch() override {
+    auto k = inputAs<KData>("XImageSum");
+    gbnCheck(gbn_op_coilsum(ctx(), static_cast<const float*>(k->getDevicePtr()), static_cast<float*>(out_->getDevicePtr()),
+                            int(k->width()), int(k->height()), int(k->getDynDimsTotalSize()), int(k->getNCoils())),
+             "XImageSum::launch");
+  }
+};
+
+/// ApplyMask (src/processes/ApplyMask.cpp:21-51), in place on the input KData.
+class ApplyMask : public Process {
+ public:
+  struct LaunchParameters : Process::LaunchParameters {
+    std::shared_ptr<SamplingMasksData> samplingMasksData;
+    explicit LaunchParameters(const std::shared_ptr<SamplingMasksData>& m) : samplingMasksData(m) {}
+  };
+  void launch() override {
+    auto lp = std::dynamic_pointer_cast<LaunchParameters>(lp_);
+    if (!lp || !lp->samplingMasksData) throw std::invalid_argument("Empty sampling masks data");
+    auto k = inputAs<KData>("ApplyMask");
+    gbnCheck(gbn_op_mask(ctx(), static_cast<float*>(k->getDevicePtr()),
+                         static_cast<const uint8_t*>(lp->samplingMasksData->getDevicePtr()), int(k->width()),
+                         int(k->height()), int(k->getDynDimsTotalSize()), int(k->getNCoils())),
+             "ApplyMask::launch");
+  }
+};
+
+/// ComplexAbs / ComplexAbsPow2 (complexAbs.cl:43-70, complexAbsPow2.cl:43-71).
+class ComplexAbs : public Process {
+ public:
+  void launch() override {
+    gbnCheck(gbn_op_abs(ctx(), static_cast<const float*>(in_->getDevicePtr()), static_cast<float*>(out_->getDevicePtr()),
+                        in_->getBytes() / sizeof(complexType)),
+             "ComplexAbs::launch");
+  }
+};
+class ComplexAbsPow2 : public Process {
+ public:
+  void launch() override {
+    gbnCheck(gbn_op_abs2(ctx(), static_cast<const float*>(in_->getDevicePtr()), static_cast<float*>(out_->getDevicePtr()),
+                         in_->getBytes() / sizeof(complexType)),
+             "ComplexAbsPow2::launch");
+  }
+};
+
+/// SimpleMRIRecon (src/processes/examples/SimpleMRIRecon.cpp:58-101).
+class SimpleMRIRecon : public Process {
+ public:
+  void launch() override {
+    auto k = inputAs<KData>("SimpleMRIRecon");
+    if (!k->getSensitivityMapsData()) throw std::invalid_argument("SimpleMRIRecon: missing sensitivity maps");
+    gbnCheck(gbn_simple_recon(ctx(), static_cast<const float*>(k->getDevicePtr()),
+                              static_cast<const float*>(k->getSensitivityMapsData()->getDevicePtr()),
+                              static_cast<float*>(out_->getDevicePtr()), int(k->width()), int(k->height()),
+                              int(k->getDynDimsTotalSize()), int(k->getNCoils())),
+             "SimpleMRIRecon::launch");
+  }
+};
+
+struct ArgumentsMotionCompensation;  // motion compensation is not part of this library
+
+/// NestaUp (src/processes/nesta/NestaUp.cpp:81-910, NestaUp.hpp:67-83).
+class NestaUp : public Process {
+ public:
+  struct LaunchParameters : Process::LaunchParameters {
+    float lambda_i;
+    float mu_f;
+    float La;
+    unsigned int maxIntIter;
+    float tolVar;
+    int verbose;
+    unsigned int maxIter;
+    unsigned int stoptest;
+    unsigned int miniter;
+    ArgumentsMotionCompensation* argsMC;
+    bool showProgress;
+    LaunchParameters(float lambda_i, float mu_f, float La, unsigned int maxIntIter, float tolVar, int verbose,
+                     int maxIter, unsigned int stoptest, unsigned int miniter, ArgumentsMotionCompensation* args,
+                     bool sp = false)
+        : lambda_i(lambda_i), mu_f(mu_f), La(La), maxIntIter(maxIntIter), tolVar(tolVar), verbose(verbose),
+          maxIter(unsigned(maxIter)), stoptest(stoptest), miniter(miniter), argsMC(args), showProgress(sp) {}
+  };
+  ~NestaUp() override {
+    if (prob_) gbn_problem_destroy(prob_);
+  }
+  void init() override {
+    Process::init();
+    bind();
+  }
+  void launch() override {
+    auto lp = std::dynamic_pointer_cast<LaunchParameters>(lp_);
+    if (!lp) throw std::invalid_argument("NestaUp::launch: missing LaunchParameters");
+    if (lp->argsMC) throw CLError(GBN_ERR_UNSUPPORTED, "NestaUp: motion compensation is not supported");
+    bind();
+    const gbn_nesta_params prm{lp->lambda_i, lp->mu_f, lp->La, lp->maxIntIter, lp->tolVar,
+                               lp->verbose, lp->maxIter, lp->stoptest, lp->miniter};
+    gbnCheck(gbn_nesta_run(ctx(), prob_, &prm, static_cast<float*>(out_->getDevicePtr()), &stats_), "NestaUp::launch");
+    lp->tolVar = stats_.tolVar_final;  // the reference updates LaunchParameters::tolVar in place
+  }
+  const gbn_nesta_stats& getStats() const { return stats_; }
+
+ private:
+  void bind() {
+    auto k = inputAs<KData>("NestaUp");
+    outputAs<XData>("NestaUp");
+    if (!k->getSensitivityMapsData() || !k->getSamplingMasksData())
+      throw std::invalid_argument("NestaUp: KData needs sensitivity maps and sampling masks");
+    if (prob_ && bound_in_ == in_.get() && bound_k_ == k->getDevicePtr()) return;
+    if (prob_) gbn_problem_destroy(prob_);
+    prob_ = nullptr;
+    gbnCheck(gbn_problem_create(ctx(), int(k->width()), int(k->height()), int(k->getDynDimsTotalSize()),
+                                int(k->getNCoils()), static_cast<const float*>(k->getDevicePtr()),
+                                static_cast<const float*>(k->getSensitivityMapsData()->getDevicePtr()),
+                                static_cast<const uint8_t*>(k->getSamplingMasksData()->getDevicePtr()), &prob_),
+             "NestaUp::init");
+    bound_in_ = in_.get();
+    bound_k_ = k->getDevicePtr();
+  }
+  gbn_problem* prob_ = nullptr;
+  const Data* bound_in_ = nullptr;
+  const void* bound_k_ = nullptr;
+  gbn_nesta_stats stats_{};
+};
+
+}  // namespace OpenCLIPER

@@ -6,6 +6,10 @@ drand48_libc.npz : values drawn from the C library's drand48 after resetting
 nesta_*.npz      : inputs, parameters and outputs of the CPU restatement of
                    NestaUp::launch for small seeded problems
 simple_*.npz     : SimpleMRIRecon on a small fully sampled problem
+ops_refkernels.npz : outputs of the reference's own operator kernels
+                   (src/kernels/*.cl compiled for the host by oracle/refkernels)
+                   on seeded inputs; written only where the reference sources
+                   are available
 
     python tests/golden/make_golden.py
 """
@@ -56,5 +60,22 @@ def main():
                                                                           s.S.astype(np.complex128)))
 
 
+def refkernel_ops():
+    from oracle import refkernels as K
+    if K.build() is None or not K.available():
+        print("reference kernel sources unavailable: ops_refkernels.npz not regenerated")
+        return
+    rng = np.random.default_rng(77)
+    W, H, F, C = 24, 16, 3, 2
+    c = lambda shape: (rng.standard_normal(shape) + 1j * rng.standard_normal(shape)).astype(np.complex64)
+    x, k, S = c((F, H, W)), c((F, C, H, W)), c((C, H, W))
+    mask = ((rng.random((F, H, W)) > 0.5) * 255).astype(np.uint8)
+    save("ops_refkernels.npz", kind="refkernels", x=x, k=k, S=S, mask=mask, mu=np.float32(0.6),
+         ttv_fwd=K.ttv(x, True), ttv_adj=K.ttv(x, False), normalize=K.normalize(x, 0.6),
+         sensmul_x=K.sensmul(x, S, False), sensmul_k_conj=K.sensmul(k, S, True), coilsum=K.coilsum(k),
+         mask_k=K.apply_mask(k, mask), abs2=K.abs2(k), abs=K.cabs(x))
+
+
 if __name__ == "__main__":
     main()
+    refkernel_ops()

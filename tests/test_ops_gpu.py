@@ -134,3 +134,34 @@ def test_errors_are_reported(ctx):
     assert ei.value.code == -1
     with pytest.raises(g.GbnError):
         api.op_fft2(ctx, 7, k, k)
+
+
+def test_operators_match_reference_kernel_outputs(ctx):
+    """GPU operators against outputs of the reference's own OpenCL kernels
+    compiled for the host (tests/golden/ops_refkernels.npz)."""
+    import os
+    from tests.conftest import ROOT
+    d = np.load(os.path.join(ROOT, "tests", "golden", "ops_refkernels.npz"))
+    x, k, S, mask = d["x"], d["k"], d["S"], d["mask"]
+    F, C, H, W = k.shape
+    dx, dk, dS, dm = ctx.to_device(x), ctx.to_device(k), ctx.to_device(S), ctx.to_device(mask)
+    ox, ok = ctx.empty(x.shape, np.complex64), ctx.empty(k.shape, np.complex64)
+    api.op_ttv(ctx, 1, dx, ox)
+    assert np.array_equal(ox.get(), d["ttv_fwd"])
+    api.op_ttv(ctx, 0, dx, ox)
+    assert np.array_equal(ox.get(), d["ttv_adj"])
+    api.op_normalize(ctx, dx, ox, float(d["mu"]))
+    assert rel_l2(ox.get(), d["normalize"]) < TOL
+    api.op_sensmul(ctx, False, dx, dS, ok)
+    assert rel_l2(ok.get(), d["sensmul_x"]) < TOL
+    api.op_sensmul(ctx, True, dk, dS, ok)
+    assert rel_l2(ok.get(), d["sensmul_k_conj"]) < TOL
+    api.op_coilsum(ctx, dk, ox)
+    assert rel_l2(ox.get(), d["coilsum"]) < TOL
+    dk2 = ctx.to_device(k)
+    api.op_mask(ctx, dk2, dm)
+    assert np.array_equal(dk2.get(), d["mask_k"])
+    api.op_abs(ctx, dk, ok, squared=True)
+    assert rel_l2(ok.get(), d["abs2"]) < TOL
+    api.op_abs(ctx, dx, ox)
+    assert rel_l2(ox.get(), d["abs"]) < TOL

@@ -159,5 +159,14 @@ def test_oracle_reproduces_golden(name):
         assert r.stats["inner_iters"] == int(d["inner_iters"])
     elif kind == "simple":
         assert rel_l2(R.simple_recon(d["y"], d["S"]), d["x"]) < 1e-6
+    elif kind == "refkernels":
+        x, k, S = d["x"].astype(np.complex128), d["k"].astype(np.complex128), d["S"].astype(np.complex128)
+        assert rel_l2(R.ttv(x, True), d["ttv_fwd"]) < 1e-6 and rel_l2(R.ttv(x, False), d["ttv_adj"]) < 1e-6
+        assert rel_l2(R.normalize(x, float(d["mu"])), d["normalize"]) < 1e-6
+        assert rel_l2(R.sensmul(x, S, False), d["sensmul_x"]) < 1e-6
+        assert rel_l2(R.sensmul(k, S, True), d["sensmul_k_conj"]) < 1e-6
+        assert rel_l2(R.coilsum(k), d["coilsum"]) < 1e-6
+        assert np.array_equal(R.apply_mask(d["k"], d["mask"]), d["mask_k"])
+        assert rel_l2(R.complex_abs2(k), d["abs2"]) < 1e-6 and rel_l2(R.complex_abs(x), d["abs"]) < 1e-6
     else:
         raise AssertionError(kind)
