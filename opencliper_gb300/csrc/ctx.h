@@ -22,7 +22,7 @@ struct gbn_ctx {
   uint64_t rand48 = 0x1234ABCD330EULL;  // drand48 state (glibc default before any seeding)
   void* scratch = nullptr;            // grow-only scratch for per-operator entry points
   size_t scratch_bytes = 0;
-  int k1_coils_per_block = 2;         // tuning: coils per CTA in the forward column pass
+  int k1_coils_per_block = 4;         // tuning: coils per CTA in the forward column pass
   int k2_ctas_per_sm = 4;             // tuning: persistent CTAs per SM in the row pass
   unsigned long long launches = 0;    // kernels launched by this context
   // event profiling of kernel groups (reference: ProcessCore::getKernelGroupExecutionTimes)

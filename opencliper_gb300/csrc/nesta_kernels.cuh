@@ -205,6 +205,17 @@ __global__ void __launch_bounds__(kColNT) k_fwd_cols(FusedArgs a, int it, int co
     }
   }
 
+  __syncthreads();
+  // inter-pass twiddles of this thread's pass-1 items, identical for every coil
+  float2 twr[NI1][A];
+#pragma unroll
+  for (int ii = 0; ii < NI1; ++ii) {
+    const int i = t + ii * kColNT;
+    const int s = (i < N1) ? i / kWB : 0;
+#pragma unroll
+    for (int k1 = 0; k1 < A; ++k1) twr[ii][k1] = tw[k1 * B + s];
+  }
+
   for (int c = c0; c < c1; ++c) {
     const int buf = (c - c0) & 1;
     cp_async_wait<0>();
@@ -221,7 +232,7 @@ __global__ void __launch_bounds__(kColNT) k_fwd_cols(FusedArgs a, int it, int co
         for (int n1 = 0; n1 < A; ++n1) v[n1] = cmul(xv[ii][n1], Sc[(B * n1 + s) * kWB + w]);
         dft<A>(v);
 #pragma unroll
-        for (int k1 = 0; k1 < A; ++k1) ex[k1 * KS + s * kWB + w] = (k1 == 0) ? v[k1] : cmul(v[k1], tw[k1 * B + s]);
+        for (int k1 = 0; k1 < A; ++k1) ex[k1 * KS + s * kWB + w] = (k1 == 0) ? v[k1] : cmul(v[k1], twr[ii][k1]);
       }
     }
     __syncthreads();
@@ -351,8 +362,13 @@ __global__ void __launch_bounds__(kRowNT) k_rows(FusedArgs a, int it) {
     if (RESID) issue_T(step);
   }
   cp_async_commit();
-  const float2* twab = tw;
-  const float2* twba = tw + W;
+  // inter-pass twiddles: pass-A items keep s = t % B and backward pass-1 items
+  // keep k1 = t % A at every step, so their twiddles live in registers
+  float2 twa[A], twb[B];
+#pragma unroll
+  for (int k1 = 0; k1 < A; ++k1) twa[k1] = tw[k1 * B + (t % B)];
+#pragma unroll
+  for (int k1p = 0; k1p < B; ++k1p) twb[k1p] = tw[W + k1p * A + (t % A)];
   float racc = 0.f;
   int buf = 0;
 
@@ -378,7 +394,7 @@ __global__ void __launch_bounds__(kRowNT) k_rows(FusedArgs a, int it) {
         dft<A>(v);
 #pragma unroll
         for (int k1 = 0; k1 < A; ++k1)
-          ex[r * R::RS1 + k1 * R::S1 + s] = (k1 == 0) ? v[k1] : cmul(v[k1], twab[k1 * B + s]);
+          ex[r * R::RS1 + k1 * R::S1 + s] = (k1 == 0) ? v[k1] : cmul(v[k1], (RPC * B <= kRowNT) ? twa[k1] : tw[k1 * B + s]);
       }
       __syncthreads();  // Tb consumed, exchange filled
       if (next < nsteps) issue_T(next);
@@ -418,7 +434,7 @@ __global__ void __launch_bounds__(kRowNT) k_rows(FusedArgs a, int it) {
       dft<B>(v);
 #pragma unroll
       for (int k1p = 0; k1p < B; ++k1p)
-        ex[r * R::RS2 + k1p * R::S2 + k1] = (k1p == 0) ? v[k1p] : cmul(v[k1p], twba[k1p * A + k1]);
+        ex[r * R::RS2 + k1p * R::S2 + k1] = (k1p == 0) ? v[k1p] : cmul(v[k1p], twb[k1p]);
     }
     __syncthreads();
     for (int i = t; i < RPC * B; i += kRowNT) {
@@ -572,6 +588,16 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT) k_inv_cols(F
   for (int ii = 0; ii < NI2; ++ii)
 #pragma unroll
     for (int k2 = 0; k2 < A; ++k2) acc[ii][k2] = make_float2(0.f, 0.f);
+  __syncthreads();
+  // inter-pass twiddles of this thread's pass-1 items, identical for every coil
+  float2 twr[NI1][B];
+#pragma unroll
+  for (int ii = 0; ii < NI1; ++ii) {
+    const int i = t + ii * kColNT;
+    const int s = (i < N1) ? i / kWB : 0;
+#pragma unroll
+    for (int k1p = 0; k1p < B; ++k1p) twr[ii][k1p] = tw[k1p * A + s];
+  }
 
   for (int c = cbeg; c < cend; ++c) {
     const int buf = (c - cbeg) & 1;
@@ -599,7 +625,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT) k_inv_cols(F
         dft<B>(v);
 #pragma unroll
         for (int k1p = 0; k1p < B; ++k1p)
-          ex[k1p * KS + s * kWB + w] = (k1p == 0) ? v[k1p] : cmul(v[k1p], tw[k1p * A + s]);
+          ex[k1p * KS + s * kWB + w] = (k1p == 0) ? v[k1p] : cmul(v[k1p], twr[ii][k1p]);
       }
     }
     __syncthreads();
