@@ -185,7 +185,10 @@ def run_ours(args, dist: Dist) -> dict | None:
     from opencliper_gb300 import synth
 
     torch.cuda.set_device(dist.local)
-    stream = torch.cuda.current_stream()
+    # one explicit stream for the library, the L2 flush and the timing events
+    # (the legacy default stream would not order them with the library's work)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     prob_h = synth.make_problem(WL["W"], WL["H"], WL["F"], WL["C"], WL["R"], seed=WL["seed"] + dist.rank)
     ctx = g.Context(dist.local)
     ctx.set_stream(stream.cuda_stream)
@@ -277,10 +280,13 @@ def run_ours(args, dist: Dist) -> dict | None:
             "share_of_step": round(ms_dom / max(total_prof, 1e-9), 3),
             "groups_us_per_launch": {k: round(v[1] * 1e3 / max(v[0], 1), 2) for k, v in prof.items()}}
 
-    ctx.set_stream(None)
     prob.close()
     for a in (y, S, m, x):
         a.free()
+    forms = {}
+    if not args.no_forms and dist.ws == 1:
+        forms["batched_fp32"] = batched_form(ctx, stream)
+    ctx.set_stream(None)
     ctx.close()
     n = dist.ws
     out = {"metric": METRIC, "value": round(n * K / (t_max / 1e3), 3), "unit": UNIT, "n_gpus": n, "steps": K,
@@ -291,7 +297,65 @@ def run_ours(args, dist: Dist) -> dict | None:
                    "d2h_bytes_per_step": int(bo)},
            "gpu_launches": int(launches), "roofline": roof, "clocks": clk,
            "wall_s_timed_region": round(wall, 3)}
+    if forms:
+        out["forms"] = forms
     return out
+
+
+BATCH_WL = dict(n=64, sizes=(128, 192, 256, 320, 384), frames=(12, 40), coils=(8, 32), accel=(4, 12), seed0=1000)
+
+
+def batched_form(ctx, stream, reps: int = 2) -> dict:
+    """The batched form on the uneven workload: 64 reconstructions, each with
+    its own seed 1000+i drawing W=H from {128..384}, F ~ U{12..40},
+    C ~ U{8..32}, R ~ U{4..12}, solved by one captured CUDA graph (gbn_batch_*)
+    with the same NESTA settings as the headline workload.  Device-resident
+    inputs; events on the library's stream around each graph replay."""
+    import torch
+
+    import opencliper_gb300 as g
+    from opencliper_gb300 import synth
+    B = BATCH_WL
+    probs, outs, arrays, shapes = [], [], [], []
+    n_units = 0
+    for i in range(B["n"]):
+        r = np.random.default_rng(B["seed0"] + i)
+        Wd = int(r.choice(B["sizes"]))
+        F = int(r.integers(B["frames"][0], B["frames"][1] + 1))
+        Cc = int(r.integers(B["coils"][0], B["coils"][1] + 1))
+        Rr = int(r.integers(B["accel"][0], B["accel"][1] + 1))
+        p = synth.make_problem_device(ctx, Wd, Wd, F, Cc, Rr, seed=B["seed0"] + i)
+        x = ctx.empty((F, Wd, Wd), np.complex64)
+        probs.append(g.Problem(ctx, p.y, p.S, p.mask))
+        outs.append(x)
+        arrays += [p.y, p.S, p.mask, x]
+        shapes.append((Wd, F, Cc, Rr))
+        n_units += Wd * Wd * F * Cc
+    b = g.Batch(ctx, probs, g.nesta_params(**NESTA), outs)
+    b.capture()
+    b.launch()
+    torch.cuda.synchronize()
+    n0 = ctx.launch_count()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for k in range(reps):
+        ev[k][0].record(stream)
+        b.launch()
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(c) for a, c in ev) / reps
+    launches = (ctx.launch_count() - n0) // reps
+    kept = sum(b.stats(i)["kept_rows"] for i in range(B["n"]))
+    b.close()
+    for pr in probs:
+        pr.close()
+    for a in arrays:
+        a.free()
+    return {"workload": f"{B['n']} uneven reconstructions, W=H in {list(B['sizes'])}, F U{{12..40}}, "
+                        f"C U{{8..32}}, R U{{4..12}}, seeds {B['seed0']}+i, plain FP32, one CUDA graph",
+            "value": round(B["n"] / (ms / 1e3), 3), "unit": UNIT, "ms_per_batch": round(ms, 2),
+            "reps": reps, "pixel_coil_frames": int(n_units), "kept_rows_total": int(kept),
+            "sizes_seen": sorted(set(s[0] for s in shapes)),
+            "host_launch_calls_per_replay": int(launches)}
 
 
 def cpu_port_sample(iters: int = 3) -> dict:
@@ -343,6 +407,7 @@ def main(argv=None) -> int:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU restatement timing")
+    ap.add_argument("--no-forms", action="store_true", help="skip the batched-form measurement")
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3

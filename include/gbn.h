@@ -63,6 +63,7 @@ enum { GBN_NOT_CONJUGATE = 0, GBN_CONJUGATE = 1 };
 
 typedef struct gbn_ctx gbn_ctx;
 typedef struct gbn_problem gbn_problem;
+typedef struct gbn_batch gbn_batch;
 
 /* ------------------------------------------------------------------------ */
 /* Runtime: replaces CLapp (src/CLapp.cpp:188-575: platform/device/context/  */
@@ -221,6 +222,37 @@ GBN_API int gbn_nesta_run(gbn_ctx* ctx, gbn_problem* p, const gbn_nesta_params* 
  * downloads x, and returns when x is on the host. */
 GBN_API int gbn_nesta_run_host(gbn_ctx* ctx, int W, int H, int F, int C, const float* h_y, const float* h_S,
                        const uint8_t* h_mask, const gbn_nesta_params* params, float* h_x, gbn_nesta_stats* stats);
+
+/* ------------------------------------------------------------------------ */
+/* Batched form.  No reference counterpart: the reference runs one           */
+/* NestaUp::launch at a time; a batch gives the same results as running its  */
+/* problems one after another in batch order (power-method draws included).  */
+/* ------------------------------------------------------------------------ */
+#define GBN_PRECISION_FP32 0  /* complex64 data and arithmetic, as the reference */
+#define GBN_PRECISION_MIXED 1 /* reduced-precision storage (not available in this build) */
+
+/* Plans n reconstructions: problems[i] (from gbn_problem_create on ctx, each
+ * at most once), params[i], output image d_outputs[i] ([F][H][W] complex).
+ * Problems of equal (W, H) share the launches of every solver pass (up to 64
+ * per group); groups run concurrently.  A problem must not be run elsewhere
+ * while a launch of the batch is in flight. */
+GBN_API int gbn_batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_nesta_params* params,
+                             float* const* d_outputs, int precision_mode, gbn_batch** out);
+/* Enqueues the whole batch on the context stream (asynchronous); replays the
+ * captured graph when gbn_batch_capture was called. */
+GBN_API int gbn_batch_launch(gbn_batch* b);
+/* Captures the whole batch solve into one CUDA graph (nothing runs). */
+GBN_API int gbn_batch_capture(gbn_batch* b);
+/* Waits for the context stream, then fills *stats for problem i of the batch. */
+GBN_API int gbn_batch_stats(gbn_batch* b, int i, gbn_nesta_stats* stats);
+GBN_API int gbn_batch_destroy(gbn_batch* b);
+/* create + launch (+ stats for every problem when stats != NULL, which waits)
+ * + destroy */
+GBN_API int gbn_batch_run(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_nesta_params* params,
+                          float* const* d_outputs, int precision_mode, gbn_nesta_stats* stats);
+/* CUDA-graph names for the same operations: capture a batch, replay it. */
+GBN_API int gbn_graph_capture(gbn_batch* b);
+GBN_API int gbn_graph_replay(gbn_batch* b);
 
 #ifdef __cplusplus
 }

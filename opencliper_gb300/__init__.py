@@ -5,8 +5,8 @@ include/gbn.h).  This package holds its in-tree build recipe and a ctypes
 binding; there is no CPU fallback.
 """
 from ._abi import GbnError, NestaParams, NestaStats, lib  # noqa: F401
-from .api import (Context, DeviceArray, Problem, nesta_params, nesta_run_host,  # noqa: F401
-                  supported_lengths)
+from .api import (PRECISION_FP32, PRECISION_MIXED, Batch, Context, DeviceArray, Problem,  # noqa: F401
+                  nesta_params, nesta_run_host, supported_lengths)
 
-__all__ = ["GbnError", "NestaParams", "NestaStats", "lib", "Context", "DeviceArray", "Problem",
-           "nesta_params", "nesta_run_host", "supported_lengths"]
+__all__ = ["GbnError", "NestaParams", "NestaStats", "lib", "Context", "DeviceArray", "Problem", "Batch",
+           "PRECISION_FP32", "PRECISION_MIXED", "nesta_params", "nesta_run_host", "supported_lengths"]

@@ -98,6 +98,14 @@ SIGNATURES: dict[str, list] = {
     "gbn_nesta_run": [_vp, _vp, C.POINTER(NestaParams), _vp, C.POINTER(NestaStats)],
     "gbn_nesta_run_host": [_vp, _i, _i, _i, _i, _vp, _vp, _vp, C.POINTER(NestaParams), _vp,
                            C.POINTER(NestaStats)],
+    "gbn_batch_create": [_vp, _i, C.POINTER(_vp), C.POINTER(NestaParams), C.POINTER(_vp), _i, C.POINTER(_vp)],
+    "gbn_batch_launch": [_vp],
+    "gbn_batch_capture": [_vp],
+    "gbn_batch_stats": [_vp, _i, C.POINTER(NestaStats)],
+    "gbn_batch_destroy": [_vp],
+    "gbn_batch_run": [_vp, _i, C.POINTER(_vp), C.POINTER(NestaParams), C.POINTER(_vp), _i, C.POINTER(NestaStats)],
+    "gbn_graph_capture": [_vp],
+    "gbn_graph_replay": [_vp],
 }
 _RESTYPE = {"gbn_last_error_string": C.c_char_p}
 

@@ -245,6 +245,54 @@ class Problem:
             pass
 
 
+PRECISION_FP32 = 0
+PRECISION_MIXED = 1
+
+
+class Batch:
+    """Many reconstructions solved together (gbn_batch_*): problems of equal
+    (W, H) share every solver launch; the whole solve can be captured into one
+    CUDA graph and replayed."""
+
+    def __init__(self, ctx: Context, problems: list[Problem], params: list[NestaParams] | NestaParams,
+                 outputs: list[DeviceArray], precision: int = PRECISION_FP32):
+        n = len(problems)
+        if isinstance(params, NestaParams):
+            params = [params] * n
+        if len(params) != n or len(outputs) != n:
+            raise ValueError("problems, params and outputs must have the same length")
+        hp = (C.c_void_p * n)(*[p.handle for p in problems])
+        pp = (NestaParams * n)(*params)
+        op = (C.c_void_p * n)(*[_ck(o, np.complex64) for o in outputs])
+        h = C.c_void_p()
+        call("gbn_batch_create", ctx.handle, n, hp, pp, op, int(precision), C.byref(h))
+        self.handle = h.value
+        self.ctx, self.n = ctx, n
+        self._keep = (problems, outputs)
+
+    def capture(self) -> None:
+        call("gbn_batch_capture", self.handle)
+
+    def launch(self) -> None:
+        call("gbn_batch_launch", self.handle)
+
+    def stats(self, i: int) -> dict:
+        st = NestaStats()
+        call("gbn_batch_stats", self.handle, int(i), C.byref(st))
+        return st.as_dict()
+
+    def close(self) -> None:
+        if self.handle:
+            call("gbn_batch_destroy", self.handle)
+            self.handle = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
 def nesta_params(lambda_i=1e-2, mu_f=3e-4, La=1.0, maxIntIter=4, tolVar=3e-4, verbose=1, maxIter=100,
                  stoptest=1, miniter=7) -> NestaParams:
     """NestaUp::LaunchParameters (NestaUp.hpp:67-83); defaults are tests/MRIRecon.cpp:105-114."""

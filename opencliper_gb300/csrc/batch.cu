@@ -1,0 +1,276 @@
+// Batched tTV-NESTA: many reconstructions of uneven size, frame count and coil
+// count solved together, optionally captured into one CUDA graph.
+//
+// Problems are grouped by their transform lengths (W, H), at most kMaxBatch
+// per group.  Each group has a device table of its instances (FusedArgs) and
+// a control block, and every pass of an inner iteration is ONE launch over
+// all of the group's frames: the column kernels map grid z to (instance,
+// frame), the persistent row kernel numbers the steps of all instances in one
+// sequence and runs each instance's scalar recurrence when its last step is
+// done.  Instances that stop early (stoptest) or run fewer iterations skip
+// their work inside the launches.  Groups run on their own streams, forked
+// from and joined back to the context stream.
+//
+// Power-method restart draws follow the reference's process-wide drand48
+// sequence as if the problems were solved one after another in batch order:
+// instance i starts sum_{j<i} W_j*H_j*F_j draws after the context state.  A
+// captured graph reads that state from device memory, written just before
+// each replay, so replays continue the sequence.
+#include <algorithm>
+#include <map>
+#include <utility>
+#include <vector>
+
+#include "ctx.h"
+#include "nesta_kernels.cuh"
+#include "solver.h"
+
+struct gbn_batch {
+  gbn_ctx* ctx = nullptr;
+  int precision = GBN_PRECISION_FP32;
+  std::vector<gbn_problem*> probs;
+  std::vector<gbn_nesta_params> prm;
+  std::vector<float2*> out;
+  std::vector<unsigned long long> rand_off;  // draws before instance i
+  unsigned long long rand_total = 0;
+  struct Group {
+    int W = 0, H = 0;
+    std::vector<int> idx;  // members (indices into probs)
+    gbn::FusedArgs* tab = nullptr;
+    gbn::ClassCtl* ctl = nullptr;
+    gbn::BatchMap bm{};
+    int cpb = 1, g2 = 1;
+    dim3 g1, g3;
+    unsigned maxIntIter = 0, maxIter = 0;
+    cudaStream_t stream = nullptr;
+    cudaEvent_t done = nullptr;
+  };
+  std::vector<Group> groups;
+  cudaEvent_t fork = nullptr;
+  unsigned long long* d_rand = nullptr;  // generator state read by a captured graph
+  cudaGraphExec_t graph = nullptr;
+};
+
+namespace gbn {
+
+namespace {
+
+void batch_release(gbn_batch* b) {
+  if (b->graph) cudaGraphExecDestroy(b->graph);
+  for (auto& g : b->groups) {
+    if (g.tab) cudaFree(g.tab);
+    if (g.ctl) cudaFree(g.ctl);
+    if (g.stream) cudaStreamDestroy(g.stream);
+    if (g.done) cudaEventDestroy(g.done);
+  }
+  if (b->fork) cudaEventDestroy(b->fork);
+  if (b->d_rand) cudaFree(b->d_rand);
+}
+
+// Enqueues the whole solve of every instance.  graph_mode: restart draws start
+// from *d_rand (see above) instead of the host-side context state.
+int batch_enqueue(gbn_batch* b, bool graph_mode) {
+  gbn_ctx* ctx = b->ctx;
+  cudaError_t e = cudaEventRecord(b->fork, ctx->stream);
+  if (e != cudaSuccess) return cuda_status(e, "batch fork");
+  unsigned long long n_launch = 0;
+  for (auto& g : b->groups) {
+    if ((e = cudaStreamWaitEvent(g.stream, b->fork, 0)) != cudaSuccess) return cuda_status(e, "batch fork");
+    cudaStream_t s = g.stream;
+    const SizeKernels* kh = find_size(g.H);
+    const SizeKernels* kw = find_size(g.W);
+    for (int i : g.idx) n_launch += launch_pre(b->probs[i], b->prm[i], s);
+    n_launch += launch_group_init(g.tab, int(g.idx.size()), kw->rows_per_cta, g.ctl, s);
+    // x0 = E^H y of all members (NestaUp.cpp:465-486)
+    kw->rows(g.tab, g.bm, 0, false, g.g2, s);
+    kh->inv_cols(g.tab, g.bm, 0, false, g.g3, s);
+    n_launch += 2;
+    for (int i : g.idx) {
+      const Lcg48 j = lcg48_jump(b->rand_off[i]);
+      const RandStart rs = graph_mode ? RandStart{0, b->d_rand, j.a, j.c}
+                                      : RandStart{lcg48_apply(j, ctx->rand48), nullptr, 1, 0};
+      n_launch += launch_constants(ctx, b->probs[i], b->out[i], rs, s);
+    }
+    for (unsigned nl = 1; nl <= g.maxIntIter; ++nl) {
+      for (int i : g.idx) n_launch += launch_outer_begin(ctx, b->probs[i], int(nl), b->out[i], s);
+      for (unsigned it = 0; it < g.maxIter; ++it) {
+        kh->fwd_cols(g.tab, g.bm, int(it), g.cpb, g.g1, s);
+        kw->rows(g.tab, g.bm, int(it), true, g.g2, s);
+        kh->inv_cols(g.tab, g.bm, int(it), true, g.g3, s);
+        n_launch += 3;
+      }
+      for (int i : g.idx) n_launch += launch_outer_end(ctx, b->probs[i], b->out[i], s);
+    }
+    if ((e = cudaEventRecord(g.done, s)) != cudaSuccess) return cuda_status(e, "batch join");
+    if ((e = cudaStreamWaitEvent(ctx->stream, g.done, 0)) != cudaSuccess) return cuda_status(e, "batch join");
+  }
+  ctx->launches += n_launch;
+  if ((e = cudaGetLastError()) != cudaSuccess) return cuda_status(e, "batch launch");
+  return GBN_OK;
+}
+
+}  // namespace
+
+int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_nesta_params* params,
+                 float* const* outputs, int precision, gbn_batch** out) {
+  if (!ctx || !problems || !params || !outputs || !out) return set_error(GBN_ERR_INVALID, "null argument");
+  if (n <= 0) return set_error(GBN_ERR_INVALID, "batch needs at least one problem");
+  if (precision != GBN_PRECISION_FP32)
+    return set_error(GBN_ERR_UNSUPPORTED, "precision mode not available in this build (use GBN_PRECISION_FP32)");
+  *out = nullptr;
+  gbn_batch* b = new gbn_batch();
+  b->ctx = ctx;
+  b->precision = precision;
+  int rc = GBN_OK;
+  std::map<std::pair<int, int>, std::vector<int>> by_size;  // (W, H) -> members, in batch order
+  std::vector<std::pair<int, int>> order;
+  for (int i = 0; i < n && rc == GBN_OK; ++i) {
+    gbn_problem* P = problems[i];
+    if (!P || !outputs[i]) {
+      rc = set_error(GBN_ERR_INVALID, "null problem or output in batch");
+      break;
+    }
+    if (P->ctx != ctx) {
+      rc = set_error(GBN_ERR_INVALID, "batch problems must belong to the batch's context");
+      break;
+    }
+    for (int j = 0; j < i; ++j)
+      if (problems[j] == P) rc = set_error(GBN_ERR_INVALID, "a problem appears twice in the batch");
+    if (rc != GBN_OK) break;
+    if ((rc = run_prepare(ctx, P, &params[i])) != GBN_OK) break;
+    b->probs.push_back(P);
+    b->prm.push_back(params[i]);
+    b->out.push_back(reinterpret_cast<float2*>(outputs[i]));
+    b->rand_off.push_back(b->rand_total);
+    b->rand_total += (unsigned long long)P->W * P->H * P->F;
+    const auto key = std::make_pair(P->W, P->H);
+    auto& v = by_size[key];
+    if (v.empty()) order.push_back(key);
+    v.push_back(i);
+  }
+  cudaError_t e = cudaSuccess;
+  if (rc == GBN_OK) {
+    for (const auto& key : order) {
+      const auto& members = by_size[key];
+      for (size_t c0 = 0; c0 < members.size(); c0 += kMaxBatch) {
+        gbn_batch::Group g;
+        g.W = key.first;
+        g.H = key.second;
+        g.idx.assign(members.begin() + c0, members.begin() + std::min(members.size(), c0 + kMaxBatch));
+        b->groups.push_back(g);
+      }
+    }
+    if ((e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess)
+      rc = cuda_status(e, "batch event");
+    if (rc == GBN_OK && (e = cudaMalloc(&b->d_rand, sizeof(unsigned long long))) != cudaSuccess)
+      rc = set_error(GBN_ERR_NOMEM, "batch allocation failed");
+  }
+  for (auto& g : b->groups) {
+    if (rc != GBN_OK) break;
+    const SizeKernels* kw = find_size(g.W);
+    const int ng = int(g.idx.size());
+    if ((e = cudaMalloc(&g.tab, sizeof(FusedArgs) * ng)) != cudaSuccess ||
+        (e = cudaMalloc(&g.ctl, sizeof(ClassCtl))) != cudaSuccess) {
+      cudaGetLastError();
+      rc = set_error(GBN_ERR_NOMEM, "batch allocation failed");
+      break;
+    }
+    if ((e = cudaStreamCreateWithFlags(&g.stream, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&g.done, cudaEventDisableTiming)) != cudaSuccess) {
+      rc = cuda_status(e, "batch stream");
+      break;
+    }
+    memset(&g.bm, 0, sizeof(g.bm));
+    g.bm.n = ng;
+    g.bm.ctl = g.ctl;
+    int frames = 0, maxC = 1;
+    long long steps = 0;
+    for (int k = 0; k < ng; ++k) {
+      const int i = g.idx[k];
+      gbn_problem* P = b->probs[i];
+      g.bm.fbase[k] = frames;
+      frames += P->F;
+      maxC = std::max(maxC, P->C);
+      steps += ((long long)P->F * P->H * P->C + kw->rows_per_cta - 1) / kw->rows_per_cta;
+      g.maxIntIter = std::max(g.maxIntIter, b->prm[i].maxIntIter);
+      g.maxIter = std::max(g.maxIter, b->prm[i].maxIter);
+      ctx->launches += launch_store_args(g.tab + k, make_args(P, b->out[i]), ctx->stream);
+    }
+    g.bm.fbase[ng] = frames;
+    g.cpb = std::max(1, std::min(ctx->k1_coils_per_block, maxC));
+    g.g1 = dim3(g.W / kWB, (maxC + g.cpb - 1) / g.cpb, frames);
+    g.g2 = row_grid(ctx, steps);
+    g.g3 = dim3(g.W / kWB, 2, frames);
+  }
+  if (rc == GBN_OK && (e = cudaGetLastError()) != cudaSuccess) rc = cuda_status(e, "batch tables");
+  if (rc != GBN_OK) {
+    batch_release(b);
+    delete b;
+    return rc;
+  }
+  *out = b;
+  return GBN_OK;
+}
+
+int batch_launch(gbn_batch* b) {
+  if (!b) return set_error(GBN_ERR_INVALID, "null batch");
+  gbn_ctx* ctx = b->ctx;
+  int rc;
+  if (b->graph) {
+    ctx->launches += launch_set_rand(b->d_rand, ctx->rand48, ctx->stream);
+    const cudaError_t e = cudaGraphLaunch(b->graph, ctx->stream);
+    if (e != cudaSuccess) return cuda_status(e, "graph launch");
+    rc = GBN_OK;
+  } else {
+    rc = batch_enqueue(b, false);
+  }
+  if (rc == GBN_OK) ctx->rand48 = lcg48_apply(lcg48_jump(b->rand_total), ctx->rand48);
+  return rc;
+}
+
+int batch_capture(gbn_batch* b) {
+  if (!b) return set_error(GBN_ERR_INVALID, "null batch");
+  gbn_ctx* ctx = b->ctx;
+  if (b->graph) {
+    cudaGraphExecDestroy(b->graph);
+    b->graph = nullptr;
+  }
+  if (ctx->profile) return set_error(GBN_ERR_INVALID, "disable profiling before capturing a graph");
+  cudaError_t e = cudaStreamBeginCapture(ctx->stream, cudaStreamCaptureModeRelaxed);
+  if (e != cudaSuccess) return cuda_status(e, "begin capture");
+  const unsigned long long launches0 = ctx->launches;
+  const int rc = batch_enqueue(b, true);
+  cudaGraph_t graph = nullptr;
+  e = cudaStreamEndCapture(ctx->stream, &graph);
+  ctx->launches = launches0;  // nothing ran yet
+  if (rc != GBN_OK) {
+    if (graph) cudaGraphDestroy(graph);
+    return rc;
+  }
+  if (e != cudaSuccess) return cuda_status(e, "end capture");
+  e = cudaGraphInstantiate(&b->graph, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) {
+    b->graph = nullptr;
+    return cuda_status(e, "graph instantiate");
+  }
+  return GBN_OK;
+}
+
+int batch_stats(gbn_batch* b, int i, gbn_nesta_stats* stats) {
+  if (!b || !stats) return set_error(GBN_ERR_INVALID, "null argument");
+  if (i < 0 || i >= int(b->probs.size())) return set_error(GBN_ERR_INVALID, "batch index out of range");
+  return read_stats(b->probs[i], b->ctx->stream, stats);
+}
+
+gbn_ctx* batch_ctx(gbn_batch* b) { return b->ctx; }
+
+int batch_destroy(gbn_batch* b) {
+  if (!b) return GBN_OK;
+  cudaStreamSynchronize(b->ctx->stream);  // work of this batch may still be queued
+  batch_release(b);
+  delete b;
+  return GBN_OK;
+}
+
+}  // namespace gbn

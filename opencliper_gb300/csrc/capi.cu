@@ -24,6 +24,13 @@ int problem_alloc(gbn_problem*);
 void problem_free(gbn_problem*);
 int validate_problem_dims(int, int, int, int);
 int nesta_run(gbn_ctx*, gbn_problem*, const gbn_nesta_params*, float2*, gbn_nesta_stats*);
+int batch_create(gbn_ctx*, int, gbn_problem* const*, const gbn_nesta_params*, float* const*, int, gbn_batch**);
+int batch_launch(gbn_batch*);
+int batch_capture(gbn_batch*);
+int batch_stats(gbn_batch*, int, gbn_nesta_stats*);
+int batch_destroy(gbn_batch*);
+gbn_ctx* batch_ctx(gbn_batch*);
+int read_stats(gbn_problem*, cudaStream_t, gbn_nesta_stats*);
 
 namespace {
 thread_local std::string g_err;
@@ -568,30 +575,54 @@ int gbn_nesta_run_host(gbn_ctx* ctx, int W, int H, int F, int C, const float* h_
   if ((rc = nesta_run(ctx, c->prob, params, c->x, nullptr)) != GBN_OK) return rc;
   if ((e = cudaMemcpyAsync(h_x, c->x, X * sizeof(float2), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
     return cuda_status(e, "download");
-  if (stats) {
-    // statistics need the device state: re-read it after completion
-    NestaDevState h;
-    int G = 0;
-    if ((e = cudaMemcpyAsync(&h, c->prob->st, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-        (e = cudaMemcpyAsync(&G, c->prob->rowoff + F, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
-      return cuda_status(e, "stats copy");
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e, "nesta run");
-    stats->normU = h.normU;
-    stats->maxX = h.maxX;
-    stats->maxUX = h.maxUX;
-    stats->lambda = h.lambda;
-    stats->muf = h.muf;
-    stats->mu0 = h.mu0;
-    stats->mu_final = h.mu;
-    stats->tolVar_final = h.tolVar;
-    stats->fx_final = h.fx;
-    stats->qp_final = h.qp;
-    stats->inner_iters = h.iters_total;
-    stats->normest_iters = h.normest_iters;
-    stats->kept_rows = G;
-    return GBN_OK;
-  }
+  if (stats) return read_stats(c->prob, s, stats);  // waits for the download too
   return cuda_status(cudaStreamSynchronize(s), "nesta run");
 }
+
+#define CHECK_BATCH(b) \
+  if (!(b)) return set_error(GBN_ERR_INVALID, "null batch"); \
+  DeviceGuard guard_(batch_ctx(b)->device)
+
+int gbn_batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_nesta_params* params,
+                     float* const* d_outputs, int precision_mode, gbn_batch** out) {
+  CHECK_CTX(ctx);
+  return batch_create(ctx, n, problems, params, d_outputs, precision_mode, out);
+}
+
+int gbn_batch_launch(gbn_batch* b) {
+  CHECK_BATCH(b);
+  return batch_launch(b);
+}
+
+int gbn_batch_capture(gbn_batch* b) {
+  CHECK_BATCH(b);
+  return batch_capture(b);
+}
+
+int gbn_batch_stats(gbn_batch* b, int i, gbn_nesta_stats* stats) {
+  CHECK_BATCH(b);
+  return batch_stats(b, i, stats);
+}
+
+int gbn_batch_destroy(gbn_batch* b) {
+  if (!b) return GBN_OK;
+  DeviceGuard guard_(batch_ctx(b)->device);
+  return batch_destroy(b);
+}
+
+int gbn_batch_run(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_nesta_params* params,
+                  float* const* d_outputs, int precision_mode, gbn_nesta_stats* stats) {
+  CHECK_CTX(ctx);
+  gbn_batch* b = nullptr;
+  int rc = batch_create(ctx, n, problems, params, d_outputs, precision_mode, &b);
+  if (rc != GBN_OK) return rc;
+  rc = batch_launch(b);
+  for (int i = 0; rc == GBN_OK && stats && i < n; ++i) rc = batch_stats(b, i, &stats[i]);
+  const int rd = batch_destroy(b);
+  return rc != GBN_OK ? rc : rd;
+}
+
+int gbn_graph_capture(gbn_batch* b) { return gbn_batch_capture(b); }
+int gbn_graph_replay(gbn_batch* b) { return gbn_batch_launch(b); }
 
 }  // extern "C"

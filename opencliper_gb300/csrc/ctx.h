@@ -66,6 +66,8 @@ struct gbn_problem {
   int part_ne_cap = 0;
   float* ne_b = nullptr;              // power-method frame vectors between chunks [F][N]
   int ne_b_cap = 0;
+  gbn::FusedArgs* d_args = nullptr;   // one-entry instance table of the fused kernels
+  gbn::ClassCtl* ctl = nullptr;       // row-pass control block
 };
 
 namespace gbn {

@@ -15,31 +15,49 @@ inline void allow_smem(K kernel, int bytes, bool& done) {
   }
 }
 
+// launch with programmatic stream serialisation (the kernel may start while
+// its predecessor in the stream drains; it waits in-kernel before reading the
+// predecessor's results)
+template <typename... KArgs, typename... Args>
+inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, int threads, int smem, cudaStream_t s, Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = dim3(threads);
+  cfg.dynamicSmemBytes = size_t(smem);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 template <int L>
 struct Launchers {
-  static void fwd_cols(const FusedArgs& a, int it, int cpb, dim3 grid, cudaStream_t s) {
+  static void fwd_cols(const FusedArgs* tab, const BatchMap& bm, int it, int cpb, dim3 grid, cudaStream_t s) {
     static bool ok = false;
     allow_smem(k_fwd_cols<L>, FwdColsSmem<L>::BYTES, ok);
-    k_fwd_cols<L><<<grid, kColNT, FwdColsSmem<L>::BYTES, s>>>(a, it, cpb);
+    launch_pdl(k_fwd_cols<L>, grid, kColNT, FwdColsSmem<L>::BYTES, s, tab, bm, it, cpb);
   }
-  static void rows(const FusedArgs& a, int it, bool resid, int grid, cudaStream_t s) {
+  static void rows(const FusedArgs* tab, const BatchMap& bm, int it, bool resid, int grid, cudaStream_t s) {
     static bool ok1 = false, ok0 = false;
     if (resid) {
       allow_smem(k_rows<L, true>, RowsSmem<L, true>::BYTES, ok1);
-      k_rows<L, true><<<grid, kRowNT, RowsSmem<L, true>::BYTES, s>>>(a, it);
+      launch_pdl(k_rows<L, true>, dim3(grid), kRowNT, RowsSmem<L, true>::BYTES, s, tab, bm, it);
     } else {
       allow_smem(k_rows<L, false>, RowsSmem<L, false>::BYTES, ok0);
-      k_rows<L, false><<<grid, kRowNT, RowsSmem<L, false>::BYTES, s>>>(a, it);
+      launch_pdl(k_rows<L, false>, dim3(grid), kRowNT, RowsSmem<L, false>::BYTES, s, tab, bm, it);
     }
   }
-  static void inv_cols(const FusedArgs& a, int it, bool update, dim3 grid, cudaStream_t s) {
+  static void inv_cols(const FusedArgs* tab, const BatchMap& bm, int it, bool update, dim3 grid, cudaStream_t s) {
     static bool ok1 = false, ok0 = false;
     if (update) {
       allow_smem(k_inv_cols<L, true>, InvColsSmem<L>::BYTES, ok1);
-      k_inv_cols<L, true><<<grid, kColNT, InvColsSmem<L>::BYTES, s>>>(a, it);
+      launch_pdl(k_inv_cols<L, true>, grid, kColNT, InvColsSmem<L>::BYTES, s, tab, bm, it);
     } else {
       allow_smem(k_inv_cols<L, false>, InvColsSmem<L>::BYTES, ok0);
-      k_inv_cols<L, false><<<grid, kColNT, InvColsSmem<L>::BYTES, s>>>(a, it);
+      launch_pdl(k_inv_cols<L, false>, grid, kColNT, InvColsSmem<L>::BYTES, s, tab, bm, it);
     }
   }
   static void fft_rows(const float2* in, float2* out, int nrows, int inv, float scale, const float2* tw, int grid,

@@ -10,6 +10,7 @@
 
 #include "ctx.h"
 #include "nesta_kernels.cuh"
+#include "solver.h"
 
 namespace gbn {
 
@@ -122,6 +123,32 @@ __global__ void k_rows_identity(int H, int F, int* __restrict__ rowmap, int* __r
 }
 
 // ---------------------------------------------------------------------------
+// Instance tables of a launch group.  k_store_args writes one entry from its
+// by-value parameter (no host buffer has to outlive the call); k_group_init
+// numbers the row-pass steps of every instance from its kept-row count and
+// clears the group's counters.
+// ---------------------------------------------------------------------------
+__global__ void k_store_args(FusedArgs* __restrict__ dst, FusedArgs v) { *dst = v; }
+__global__ void k_set_u64(unsigned long long* dst, unsigned long long v) { *dst = v; }
+
+__global__ void k_group_init(const FusedArgs* __restrict__ tab, int n, int rpc, ClassCtl* __restrict__ ctl) {
+  if (threadIdx.x == 0) {
+    int base = 0;
+    for (int i = 0; i < n; ++i) {
+      const FusedArgs& a = tab[i];
+      const int items = a.rowoff[a.F] * a.C;
+      ctl->step_base[i] = base;
+      ctl->nitems[i] = items;
+      base += (items + rpc - 1) / rpc;
+    }
+    ctl->step_base[n] = base;
+    ctl->row_next = 0;
+    ctl->ticket = 0;
+  }
+  for (int i = threadIdx.x; i < kMaxBatch; i += blockDim.x) ctl->done[i] = 0;
+}
+
+// ---------------------------------------------------------------------------
 // State initialisation from the launch parameters (one thread).
 // ---------------------------------------------------------------------------
 __global__ void k_state_init(NestaDevState* st, gbn_nesta_params p) {
@@ -196,7 +223,7 @@ constexpr int kNeBounds[kNeChunks + 1] = {1, 17, 49, kNeIters};
 constexpr int kNeMaxSlots = 52;  // largest chunk (51 steps) + ||r||^2 slot
 
 template <int FMAX>
-__global__ void __launch_bounds__(kNeNT) k_normest_chunk(int N, int F, unsigned long long x0,
+__global__ void __launch_bounds__(kNeNT) k_normest_chunk(int N, int F, RandStart rs,
                                                          unsigned long long jumpN_a, unsigned long long jumpN_c,
                                                          int m_begin, int m_end, float* __restrict__ bstore,
                                                          double* __restrict__ part, const NestaDevState* st) {
@@ -208,6 +235,7 @@ __global__ void __launch_bounds__(kNeNT) k_normest_chunk(int N, int F, unsigned 
   const int slot0 = (m_begin == 1) ? 1 : 0;
   float b[FMAX], d[FMAX];
   if (m_begin == 1) {
+    const unsigned long long x0 = rs.p ? ((rs.ja * *rs.p + rs.jc) & kMask48) : rs.x0;
     // element (f, p) is draw number f*N + p + 1 after the state x0
     const Lcg48 jp = lcg_jump_k(uint64_t(act ? p : 0) + 1);
     uint64_t X = (jp.a * x0 + jp.c) & kMask48;
@@ -355,11 +383,20 @@ __global__ void k_setup(NestaDevState* st) {
 
 // Start of an outer (continuation) loop (NestaUp.cpp:604-648):
 // mu and tolVar updates, Lmu, w = 0, x_k = x_ref.
-__global__ void k_outer_begin(NestaDevState* st, float* fmean, const float2* __restrict__ xref,
+__global__ void k_outer_begin(NestaDevState* st, int nl, float* fmean, const float2* __restrict__ xref,
                               float2* __restrict__ xk0, float2* __restrict__ wacc, size_t n) {
+  if (nl > st->maxIntIter) {
+    // this instance has run all its outer loops (a batch runs the largest count)
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      st->outer_active = 0;
+      st->last_iter = -1;
+    }
+    return;
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     NestaDevState& s = *st;
-    s.nl += 1;
+    s.outer_active = 1;
+    s.nl = nl;
     s.mu = s.mu * s.gamma;
     s.tolVar = s.tolVar * s.gammat;
     s.Ak = 0.0f;
@@ -380,6 +417,7 @@ __global__ void k_outer_begin(NestaDevState* st, float* fmean, const float2* __r
 // End of an outer loop: x_ref = x_k (NestaUp.cpp:889).
 __global__ void k_outer_end(const NestaDevState* st, const float2* __restrict__ xk0, const float2* __restrict__ xk1,
                             float2* __restrict__ xref, size_t n) {
+  if (!st->outer_active) return;
   const float2* src = ((st->last_iter + 1) & 1) ? xk1 : xk0;
   for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x)
     xref[i] = src[i];
@@ -389,16 +427,6 @@ __global__ void k_outer_end(const NestaDevState* st, const float2* __restrict__ 
 // Host side
 // ---------------------------------------------------------------------------
 namespace {
-
-// launch `stmt` (n kernels) as part of profiled group `kind`
-#define GBN_LAUNCH(ctx, kind, n, ...)                    \
-  do {                                                  \
-    cudaEvent_t ev_ = nullptr;                          \
-    if ((ctx)->profile) prof_begin((ctx), (kind), &ev_); \
-    __VA_ARGS__;                                        \
-    if ((ctx)->profile) prof_end((ctx), (kind), ev_);   \
-    (ctx)->launches += (n);                             \
-  } while (0)
 
 template <typename T>
 int grow(T*& p, int& cap, int need) {
@@ -420,7 +448,7 @@ int normest_fmax(int F) {
   return 0;
 }
 
-void launch_normest_chunk(int fmax, int nblk, cudaStream_t s, int N, int F, uint64_t x0, const Lcg48& jN, int mb,
+void launch_normest_chunk(int fmax, int nblk, cudaStream_t s, int N, int F, const RandStart& x0, const Lcg48& jN, int mb,
                           int me, float* bstore, double* part, const NestaDevState* st) {
 #define GBN_NE_CASE(M)                                                                                  \
   case M:                                                                                               \
@@ -461,6 +489,8 @@ int problem_alloc(gbn_problem* P) {
   A((void**)&P->xk1, X * sizeof(float2));
   A((void**)&P->wacc, X * sizeof(float2));
   A((void**)&P->st, sizeof(NestaDevState));
+  A((void**)&P->d_args, sizeof(FusedArgs));
+  A((void**)&P->ctl, sizeof(ClassCtl));
   if (e != cudaSuccess) {
     cudaGetLastError();
     return set_error(GBN_ERR_NOMEM, std::string("problem workspace allocation failed: ") + cudaGetErrorString(e));
@@ -471,7 +501,7 @@ int problem_alloc(gbn_problem* P) {
 void problem_free(gbn_problem* P) {
   void* ptrs[] = {P->flags, P->full_fh, P->rowmap, P->rowoff,  P->rows_h, P->rows_f,  P->row_full, P->T,
                   P->xk0,   P->xk1,     P->wacc,   P->st,      P->fmean,  P->part_tv, P->part_r,   P->part_ne,
-                  P->ne_b};
+                  P->ne_b,  P->d_args,  P->ctl};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -514,7 +544,18 @@ FusedArgs make_args(gbn_problem* P, float2* xref) {
   const unsigned N = unsigned(P->W) * unsigned(P->H);
   a.s_fwd = float(1.0 / std::sqrt(double(N)));               // NestaUp.cpp:712: 1/(sqrt(cols*rows*slices))
   a.s_adj = std::sqrt(float(N)) * (1.0f / float(N));        // NestaUp.cpp:749 sqrt(float(N)) times clFFT 1/N
+  a.ntv = P->F * (P->W / kWB);
   return a;
+}
+
+BatchMap single_map(int F, ClassCtl* ctl) {
+  BatchMap bm;
+  memset(&bm, 0, sizeof(bm));
+  bm.n = 1;
+  bm.fbase[0] = 0;
+  bm.fbase[1] = F;
+  bm.ctl = ctl;
+  return bm;
 }
 
 int validate_problem_dims(int W, int H, int F, int C) {
@@ -527,116 +568,182 @@ int validate_problem_dims(int W, int H, int F, int C) {
   return GBN_OK;
 }
 
-int nesta_run(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, float2* x_out, gbn_nesta_stats* stats) {
-  if (!ctx || !P || !prm || !x_out) return set_error(GBN_ERR_INVALID, "null argument");
+int run_prepare(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm) {
+  if (!ctx || !P || !prm) return set_error(GBN_ERR_INVALID, "null argument");
   if (P->F < 2) return set_error(GBN_ERR_INVALID, "temporal TV needs at least 2 frames (F=1 makes ||U|| undefined)");
   if (prm->stoptest == 1 && prm->miniter == 0) return set_error(GBN_ERR_INVALID, "miniter must be >= 1 when stoptest == 1");
-  const int fmax = normest_fmax(P->F);
-  if (!fmax) return set_error(GBN_ERR_UNSUPPORTED, "more than 64 frames is not supported");
+  if (!normest_fmax(P->F)) return set_error(GBN_ERR_UNSUPPORTED, "more than 64 frames is not supported");
   const SizeKernels* kh = find_size(P->H);
   const SizeKernels* kw = find_size(P->W);
   if (!kh || !kw) return set_error(GBN_ERR_UNSUPPORTED, "unsupported FFT length");
   const int W = P->W, H = P->H, F = P->F, C = P->C, N = W * H;
-  cudaStream_t s = ctx->stream;
-
-  const int cpb = std::max(1, std::min(ctx->k1_coils_per_block, C));
-  const dim3 g1(W / kWB, (C + cpb - 1) / cpb, F);
-  const int nblk_k1 = int(g1.x * g1.y * g1.z);
-  const long long rows_max = (long long)F * H * C;
-  const int g2 = int(std::max<long long>(1, std::min<long long>((rows_max + kw->rows_per_cta - 1) / kw->rows_per_cta,
-                                                                 (long long)ctx->nsm * ctx->k2_ctas_per_sm)));
-  const dim3 g3(W / kWB, 2, F);  // clusters of 2 along y
+  const long long steps_max = ((long long)F * H * C + kw->rows_per_cta - 1) / kw->rows_per_cta;
   const int nblk_ne = (N + kNeNT - 1) / kNeNT;
   int rc;
   if ((rc = grow(P->fmean, P->fmean_cap, std::max<int>(1, int(prm->miniter)))) != GBN_OK) return rc;
-  if ((rc = grow(P->part_tv, P->part_tv_cap, 2 * nblk_k1)) != GBN_OK) return rc;
-  if ((rc = grow(P->part_r, P->part_r_cap, g2)) != GBN_OK) return rc;
+  if ((rc = grow(P->part_tv, P->part_tv_cap, 2 * F * (W / kWB))) != GBN_OK) return rc;
+  if ((rc = grow(P->part_r, P->part_r_cap, int(steps_max) * kRowWarps)) != GBN_OK) return rc;
   if ((rc = grow(P->part_ne, P->part_ne_cap, nblk_ne * kNeMaxSlots * 2)) != GBN_OK) return rc;
   if ((rc = grow(P->ne_b, P->ne_b_cap, N * F)) != GBN_OK) return rc;
-
-  FusedArgs a = make_args(P, x_out);
-  a.nblk_k1 = nblk_k1;
-  const size_t X = size_t(N) * F;
-  const int gx = int(std::min<size_t>((X + 255) / 256, size_t(ctx->nsm) * 8));
-
-  GBN_LAUNCH(ctx, GBN_PROF_SETUP, 8 + 2 * kNeChunks, {
-    k_state_init<<<1, 1, 0, s>>>(P->st, *prm);
-    launch_row_analysis(P, s);
-    // x0 = E^H y (NestaUp.cpp:465-486)
-    kw->rows(a, 0, false, g2, s);
-    kh->inv_cols(a, 0, false, g3, s);
-    // maxima, norm estimate, constants (NestaUp.cpp:521-583)
-    k_maxima<<<gx, 256, 0, s>>>(x_out, N, F, P->st);
-    const Lcg48 jN = lcg_jump_k(uint64_t(N));
-    for (int ch = 0; ch < kNeChunks; ++ch) {
-      launch_normest_chunk(fmax, nblk_ne, s, N, F, ctx->rand48, jN, kNeBounds[ch], kNeBounds[ch + 1], P->ne_b,
-                           P->part_ne, P->st);
-      k_normest_check<<<1, 256, 0, s>>>(P->part_ne, nblk_ne, kNeBounds[ch], kNeBounds[ch + 1], N, F, P->st);
-    }
-    ctx->rand48 = lcg48_apply(lcg_jump_k(uint64_t(N) * uint64_t(F)), ctx->rand48);
-    k_setup<<<1, 1, 0, s>>>(P->st);
-  });
-
-  for (unsigned nl = 1; nl <= prm->maxIntIter; ++nl) {
-    GBN_LAUNCH(ctx, GBN_PROF_OUTER, 1, (k_outer_begin<<<gx, 256, 0, s>>>(P->st, P->fmean, x_out, P->xk0, P->wacc, X)));
-    for (unsigned it = 0; it < prm->maxIter; ++it) {
-      GBN_LAUNCH(ctx, GBN_PROF_FWD_COLS, 1, kh->fwd_cols(a, int(it), cpb, g1, s));
-      GBN_LAUNCH(ctx, GBN_PROF_ROWS, 1, kw->rows(a, int(it), true, g2, s));
-      GBN_LAUNCH(ctx, GBN_PROF_INV_COLS, 1, kh->inv_cols(a, int(it), true, g3, s));
-    }
-    GBN_LAUNCH(ctx, GBN_PROF_OUTER, 1, (k_outer_end<<<gx, 256, 0, s>>>(P->st, P->xk0, P->xk1, x_out, X)));
-  }
-  cudaError_t e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_status(e, "nesta launch");
-  if (stats) {
-    NestaDevState h;
-    int G = 0;
-    if ((e = cudaMemcpyAsync(&h, P->st, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
-      return cuda_status(e, "stats copy");
-    if ((e = cudaMemcpyAsync(&G, P->rowoff + F, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
-      return cuda_status(e, "stats copy");
-    if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e, "nesta run");
-    stats->normU = h.normU;
-    stats->maxX = h.maxX;
-    stats->maxUX = h.maxUX;
-    stats->lambda = h.lambda;
-    stats->muf = h.muf;
-    stats->mu0 = h.mu0;
-    stats->mu_final = h.mu;
-    stats->tolVar_final = h.tolVar;
-    stats->fx_final = h.fx;
-    stats->qp_final = h.qp;
-    stats->inner_iters = h.iters_total;
-    stats->normest_iters = h.normest_iters;
-    stats->kept_rows = G;
-  }
   return GBN_OK;
 }
 
-// SimpleMRIRecon: x = sum_c conj(S_c) ifft2(y_c) through the adjoint row and
-// column passes with every row kept.
-int simple_recon(gbn_ctx* ctx, const float2* y, const float2* S, float2* x, int W, int H, int F, int C) {
+int row_grid(gbn_ctx* ctx, long long steps) {
+  return int(std::max<long long>(1, std::min<long long>(steps, (long long)ctx->nsm * ctx->k2_ctas_per_sm)));
+}
+
+int launch_store_args(FusedArgs* dst, const FusedArgs& a, cudaStream_t s) {
+  k_store_args<<<1, 1, 0, s>>>(dst, a);
+  return 1;
+}
+
+int launch_group_init(const FusedArgs* tab, int n, int rows_per_cta, ClassCtl* ctl, cudaStream_t s) {
+  k_group_init<<<1, 64, 0, s>>>(tab, n, rows_per_cta, ctl);
+  return 1;
+}
+
+int launch_set_rand(unsigned long long* dst, unsigned long long v, cudaStream_t s) {
+  k_set_u64<<<1, 1, 0, s>>>(dst, v);
+  return 1;
+}
+
+int launch_pre(gbn_problem* P, const gbn_nesta_params& prm, cudaStream_t s) {
+  k_state_init<<<1, 1, 0, s>>>(P->st, prm);
+  launch_row_analysis(P, s);
+  return 3;
+}
+
+namespace {
+int elementwise_grid(gbn_ctx* ctx, size_t n) { return int(std::min<size_t>((n + 255) / 256, size_t(ctx->nsm) * 8)); }
+}  // namespace
+
+int launch_constants(gbn_ctx* ctx, gbn_problem* P, const float2* xref, const RandStart& rs, cudaStream_t s) {
+  const int N = P->W * P->H, F = P->F;
+  const int nblk_ne = (N + kNeNT - 1) / kNeNT;
+  // maxima, norm estimate, constants (NestaUp.cpp:521-583)
+  k_maxima<<<elementwise_grid(ctx, size_t(N) * F), 256, 0, s>>>(xref, N, F, P->st);
+  const Lcg48 jN = lcg_jump_k(uint64_t(N));
+  for (int ch = 0; ch < kNeChunks; ++ch) {
+    launch_normest_chunk(normest_fmax(F), nblk_ne, s, N, F, rs, jN, kNeBounds[ch], kNeBounds[ch + 1], P->ne_b,
+                         P->part_ne, P->st);
+    k_normest_check<<<1, 256, 0, s>>>(P->part_ne, nblk_ne, kNeBounds[ch], kNeBounds[ch + 1], N, F, P->st);
+  }
+  k_setup<<<1, 1, 0, s>>>(P->st);
+  return 2 + 2 * kNeChunks;
+}
+
+int launch_outer_begin(gbn_ctx* ctx, gbn_problem* P, int nl, const float2* xref, cudaStream_t s) {
+  const size_t X = size_t(P->W) * P->H * P->F;
+  k_outer_begin<<<elementwise_grid(ctx, X), 256, 0, s>>>(P->st, nl, P->fmean, xref, P->xk0, P->wacc, X);
+  return 1;
+}
+
+int launch_outer_end(gbn_ctx* ctx, gbn_problem* P, float2* xref, cudaStream_t s) {
+  const size_t X = size_t(P->W) * P->H * P->F;
+  k_outer_end<<<elementwise_grid(ctx, X), 256, 0, s>>>(P->st, P->xk0, P->xk1, xref, X);
+  return 1;
+}
+
+int read_stats(gbn_problem* P, cudaStream_t s, gbn_nesta_stats* stats) {
+  NestaDevState h;
+  int G = 0;
+  cudaError_t e;
+  if ((e = cudaMemcpyAsync(&h, P->st, sizeof(h), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+    return cuda_status(e, "stats copy");
+  if ((e = cudaMemcpyAsync(&G, P->rowoff + P->F, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess)
+    return cuda_status(e, "stats copy");
+  if ((e = cudaStreamSynchronize(s)) != cudaSuccess) return cuda_status(e, "nesta run");
+  stats->normU = h.normU;
+  stats->maxX = h.maxX;
+  stats->maxUX = h.maxUX;
+  stats->lambda = h.lambda;
+  stats->muf = h.muf;
+  stats->mu0 = h.mu0;
+  stats->mu_final = h.mu;
+  stats->tolVar_final = h.tolVar;
+  stats->fx_final = h.fx;
+  stats->qp_final = h.qp;
+  stats->inner_iters = h.iters_total;
+  stats->normest_iters = h.normest_iters;
+  stats->kept_rows = G;
+  return GBN_OK;
+}
+
+int nesta_run(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, float2* x_out, gbn_nesta_stats* stats) {
+  if (!x_out) return set_error(GBN_ERR_INVALID, "null argument");
+  int rc = run_prepare(ctx, P, prm);
+  if (rc != GBN_OK) return rc;
+  const SizeKernels* kh = find_size(P->H);
+  const SizeKernels* kw = find_size(P->W);
+  const int W = P->W, H = P->H, F = P->F, C = P->C;
+  cudaStream_t s = ctx->stream;
+  const int cpb = std::max(1, std::min(ctx->k1_coils_per_block, C));
+  const dim3 g1(W / kWB, (C + cpb - 1) / cpb, F);
+  const int g2 = row_grid(ctx, ((long long)F * H * C + kw->rows_per_cta - 1) / kw->rows_per_cta);
+  const dim3 g3(W / kWB, 2, F);  // clusters of 2 along y
+  const FusedArgs a = make_args(P, x_out);
+  const FusedArgs* tab = P->d_args;
+  const BatchMap bm = single_map(F, P->ctl);
+
+  int n_setup = 0;
+  GBN_LAUNCH(ctx, GBN_PROF_SETUP, n_setup, {
+    n_setup += launch_pre(P, *prm, s);
+    n_setup += launch_store_args(P->d_args, a, s);
+    n_setup += launch_group_init(tab, 1, kw->rows_per_cta, P->ctl, s);
+    // x0 = E^H y (NestaUp.cpp:465-486)
+    kw->rows(tab, bm, 0, false, g2, s);
+    kh->inv_cols(tab, bm, 0, false, g3, s);
+    n_setup += 2;
+    n_setup += launch_constants(ctx, P, x_out, RandStart{ctx->rand48, nullptr, 1, 0}, s);
+    ctx->rand48 = lcg48_apply(lcg_jump_k(uint64_t(W) * uint64_t(H) * uint64_t(F)), ctx->rand48);
+  });
+
+  for (unsigned nl = 1; nl <= prm->maxIntIter; ++nl) {
+    GBN_LAUNCH(ctx, GBN_PROF_OUTER, 1, launch_outer_begin(ctx, P, int(nl), x_out, s));
+    for (unsigned it = 0; it < prm->maxIter; ++it) {
+      GBN_LAUNCH(ctx, GBN_PROF_FWD_COLS, 1, kh->fwd_cols(tab, bm, int(it), cpb, g1, s));
+      GBN_LAUNCH(ctx, GBN_PROF_ROWS, 1, kw->rows(tab, bm, int(it), true, g2, s));
+      GBN_LAUNCH(ctx, GBN_PROF_INV_COLS, 1, kh->inv_cols(tab, bm, int(it), true, g3, s));
+    }
+    GBN_LAUNCH(ctx, GBN_PROF_OUTER, 1, launch_outer_end(ctx, P, x_out, s));
+  }
+  const cudaError_t e = cudaGetLastError();
+  if (e != cudaSuccess) return cuda_status(e, "nesta launch");
+  if (stats) return read_stats(P, s, stats);
+  return GBN_OK;
+}
+
+// Adjoint-only pass (rows without residual, then columns without update) of
+// one instance with every row kept: SimpleMRIRecon.  `ws` provides the
+// intermediates and tables (simple_recon_bytes); no allocation happens here.
+size_t simple_recon_bytes(int W, int H, int F, int C) {
+  const size_t FH = size_t(F) * H, K = FH * C * W;
+  auto up = [](size_t v) { return (v + 255) / 256 * 256; };
+  return up(K * sizeof(float2)) + up((4 * FH + F + 1) * sizeof(int)) + up(sizeof(NestaDevState)) +
+         up(sizeof(FusedArgs)) + up(sizeof(ClassCtl));
+}
+
+int simple_recon_in(gbn_ctx* ctx, void* ws, const float2* y, const float2* S, float2* x, int W, int H, int F, int C) {
   const SizeKernels* kh = find_size(H);
   const SizeKernels* kw = find_size(W);
   if (!kh || !kw) return set_error(GBN_ERR_UNSUPPORTED, "unsupported FFT length");
   const size_t FH = size_t(F) * H, K = FH * C * W;
-  // scratch: T [F*H][C][W] + rowmap/rowoff/rows_h/rows_f
-  const size_t bytes = K * sizeof(float2) + (4 * FH + F + 1) * sizeof(int) + 2 * sizeof(NestaDevState) + 256;
-  void* scr = nullptr;
-  int rc = ctx_scratch(ctx, bytes, &scr);
-  if (rc != GBN_OK) return rc;
-  float2* T = reinterpret_cast<float2*>(scr);
-  int* ip = reinterpret_cast<int*>(T + K);
-  int* rowmap = ip;
+  auto up = [](size_t v) { return (v + 255) / 256 * 256; };
+  unsigned char* b = static_cast<unsigned char*>(ws);
+  float2* T = reinterpret_cast<float2*>(b);
+  b += up(K * sizeof(float2));
+  int* rowmap = reinterpret_cast<int*>(b);
   int* rows_h = rowmap + FH;
   int* rows_f = rows_h + FH;
   int* row_full = rows_f + FH;
   int* rowoff = row_full + FH;
-  NestaDevState* st = reinterpret_cast<NestaDevState*>(
-      (reinterpret_cast<uintptr_t>(rowoff + F + 1) + alignof(NestaDevState) - 1) & ~uintptr_t(alignof(NestaDevState) - 1));
+  b += up((4 * FH + F + 1) * sizeof(int));
+  NestaDevState* st = reinterpret_cast<NestaDevState*>(b);
+  b += up(sizeof(NestaDevState));
+  FusedArgs* tab = reinterpret_cast<FusedArgs*>(b);
+  b += up(sizeof(FusedArgs));
+  ClassCtl* ctl = reinterpret_cast<ClassCtl*>(b);
   cudaStream_t s = ctx->stream;
-  cudaError_t e0 = cudaMemsetAsync(st, 0, sizeof(NestaDevState), s);
-  if (e0 != cudaSuccess) return cuda_status(e0, "simple recon setup");
   FusedArgs a;
   memset(&a, 0, sizeof(a));
   a.W = W;
@@ -657,26 +764,31 @@ int simple_recon(gbn_ctx* ctx, const float2* y, const float2* S, float2* x, int 
   a.twH = ctx_twiddles(ctx, H);
   a.twW = ctx_twiddles(ctx, W);
   a.s_adj = 1.0f / float(W * H);  // clFFT BACKWARD scale
-  const long long rows = (long long)FH * C;
-  const int g2 = int(std::max<long long>(
-      1, std::min<long long>((rows + kw->rows_per_cta - 1) / kw->rows_per_cta, (long long)ctx->nsm * ctx->k2_ctas_per_sm)));
-  GBN_LAUNCH(ctx, GBN_PROF_SETUP, 3, {
+  a.ntv = F * (W / kWB);
+  const long long steps = ((long long)FH * C + kw->rows_per_cta - 1) / kw->rows_per_cta;
+  const int g2 = int(std::max<long long>(1, std::min<long long>(steps, (long long)ctx->nsm * ctx->k2_ctas_per_sm)));
+  const BatchMap bm = single_map(F, ctl);
+  GBN_LAUNCH(ctx, GBN_PROF_SETUP, 5, {
     k_rows_identity<<<int(std::min<size_t>((FH + 255) / 256, 1024)), 256, 0, s>>>(H, F, rowmap, rowoff, rows_h, rows_f,
                                                                                   row_full);
-    kw->rows(a, 0, false, g2, s);
-    kh->inv_cols(a, 0, false, dim3(W / kWB, 2, F), s);
+    k_store_args<<<1, 1, 0, s>>>(tab, a);
+    k_group_init<<<1, 64, 0, s>>>(tab, 1, kw->rows_per_cta, ctl);
+    kw->rows(tab, bm, 0, false, g2, s);
+    kh->inv_cols(tab, bm, 0, false, dim3(W / kWB, 2, F), s);
   });
   const cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_status(e, "simple recon launch");
   return GBN_OK;
 }
 
-// Launches the identity row numbering (every row kept) for F frames of H rows.
-void launch_rows_identity(int H, int F, int* rowmap, int* rowoff, int* rows_h, int* rows_f, int* row_full,
-                          cudaStream_t s) {
-  const size_t FH = size_t(F) * H;
-  k_rows_identity<<<int(std::min<size_t>((FH + 255) / 256, 1024)), 256, 0, s>>>(H, F, rowmap, rowoff, rows_h, rows_f,
-                                                                                row_full);
+// SimpleMRIRecon: x = sum_c conj(S_c) ifft2(y_c) through the adjoint row and
+// column passes with every row kept, working memory from the context scratch.
+int simple_recon(gbn_ctx* ctx, const float2* y, const float2* S, float2* x, int W, int H, int F, int C) {
+  if (!find_size(H) || !find_size(W)) return set_error(GBN_ERR_UNSUPPORTED, "unsupported FFT length");
+  void* scr = nullptr;
+  const int rc = ctx_scratch(ctx, simple_recon_bytes(W, H, F, C), &scr);
+  if (rc != GBN_OK) return rc;
+  return simple_recon_in(ctx, scr, y, S, x, W, H, F, C);
 }
 
 }  // namespace gbn

@@ -28,6 +28,15 @@ namespace gbn {
 constexpr int kWB = 8;       // columns per CTA in the column kernels
 constexpr int kColNT = 128;  // threads per CTA in the column kernels
 constexpr int kRowNT = 128;  // threads per CTA in the row kernels
+constexpr int kRowWarps = kRowNT / 32;
+
+// Programmatic dependent launch: a kernel launched with programmatic stream
+// serialisation may start while its predecessor drains.  Each fused kernel
+// reads nothing its predecessor writes before grid_dep_wait(), and releases
+// its successor only after that wait, so a successor's early part never runs
+// before the kernel two launches back has completed.
+__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
+__device__ __forceinline__ void grid_dep_release() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
 
 template <int L>
 struct Split {
@@ -45,6 +54,17 @@ constexpr int cdiv(int a, int b) { return (a + b - 1) / b; }
 constexpr int col_ks(int q) { return (q * kWB) % 16 == 8 ? q * kWB : q * kWB + 8; }
 
 __device__ __forceinline__ float2 conjf2(float2 a) { return make_float2(a.x, -a.y); }
+
+// instance owning grid z index `z` (largest i with fbase[i] <= z)
+__device__ __forceinline__ int find_inst(const BatchMap& bm, int z) {
+  int lo = 0, hi = bm.n - 1;
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (bm.fbase[mid] <= z) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
 
 // d / max(mu, |d|) (vectorNormalization.cl:42-56) as d * min(1/mu, 1/|d|):
 // one reciprocal square root instead of a square root and two divisions
@@ -129,8 +149,12 @@ struct FwdColsSmem {
   static constexpr int BYTES = F2_END * 8 + (kColNT / 32) * 8 + H * 4;
 };
 
+// power-of-two lengths up to 256 fit 4 CTAs per SM without spilling
+constexpr int fwd_min_blocks(int H) { return (H <= 256 && (H & (H - 1)) == 0) ? 4 : 1; }
+
 template <int H>
-__global__ void __launch_bounds__(kColNT) k_fwd_cols(FusedArgs a, int it, int coils_per_block) {
+__global__ void __launch_bounds__(kColNT, fwd_min_blocks(H))
+    k_fwd_cols(const FusedArgs* __restrict__ tab, const __grid_constant__ BatchMap bm, int it, int coils_per_block) {
   using L = FwdColsSmem<H>;
   constexpr int A = L::A, B = L::B, KS = L::KS;
   constexpr int N1 = kWB * B, N2 = kWB * A;
@@ -142,16 +166,18 @@ __global__ void __launch_bounds__(kColNT) k_fwd_cols(FusedArgs a, int it, int co
   double* sred = reinterpret_cast<double*>(reinterpret_cast<float2*>(smem4) + L::F2_END);
   int* rmap = reinterpret_cast<int*>(sred + kColNT / 32);
 
+  const int inst = find_inst(bm, blockIdx.z);
+  const FusedArgs& a = tab[inst];
   const NestaDevState* st = a.st;
-  if (it > st->last_iter) return;
   const int t = threadIdx.x;
-  const int f = blockIdx.z, cg = blockIdx.y, w0 = blockIdx.x * kWB;
+  const int f = blockIdx.z - bm.fbase[inst], cg = blockIdx.y, w0 = blockIdx.x * kWB;
   const int W = a.W, C = a.C, F = a.F;
+  const int c0 = cg * coils_per_block;
+  if (c0 >= C || it > st->last_iter) return;
+  const int c1 = min(C, c0 + coils_per_block);
   const size_t N = size_t(a.N);
   const float2* __restrict__ xk = (it & 1) ? a.xk1 : a.xk0;
   const float2* __restrict__ x = xk + size_t(f) * N;
-  const int c0 = cg * coils_per_block;
-  const int c1 = min(C, c0 + coils_per_block);
 
   auto issue_S = [&](int c, int buf) {
     const float2* src = a.S + size_t(c) * N + w0;
@@ -169,6 +195,8 @@ __global__ void __launch_bounds__(kColNT) k_fwd_cols(FusedArgs a, int it, int co
     rmap[i] = a.rowmap[f * H + i];
   }
   const int rowbase = a.rowoff[f];
+  grid_dep_wait();  // x_k comes from the previous adjoint column pass
+  grid_dep_release();
 
   // x_k for this thread's pass-1 items, reused for every coil
   float2 xv[NI1][A];
@@ -254,12 +282,14 @@ __global__ void __launch_bounds__(kColNT) k_fwd_cols(FusedArgs a, int it, int co
     }
   }
 
-  const double t1 = block_sum<kColNT>(double(su2), sred);
-  const double t2 = block_sum<kColNT>(double(sud), sred);
-  if (t == 0) {
-    const int blk = (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
-    a.part_tv[2 * blk] = t1;
-    a.part_tv[2 * blk + 1] = t2;
+  if (cg == 0) {
+    const double t1 = block_sum<kColNT>(double(su2), sred);
+    const double t2 = block_sum<kColNT>(double(sud), sred);
+    if (t == 0) {
+      const int blk = f * gridDim.x + blockIdx.x;
+      a.part_tv[2 * blk] = t1;
+      a.part_tv[2 * blk + 1] = t2;
+    }
   }
 }
 
@@ -293,7 +323,8 @@ struct RowsSmem {
 };
 
 template <int W, bool RESID>
-__global__ void __launch_bounds__(kRowNT) k_rows(FusedArgs a, int it) {
+__global__ void __launch_bounds__(kRowNT)
+    k_rows(const FusedArgs* __restrict__ tab, const __grid_constant__ BatchMap bm, int it) {
   using R = RowCfg<W>;
   using L = RowsSmem<W, RESID>;
   constexpr int A = R::A, B = R::B, RPC = R::RPC;
@@ -304,21 +335,50 @@ __global__ void __launch_bounds__(kRowNT) k_rows(FusedArgs a, int it) {
   float2* tw = reinterpret_cast<float2*>(smem4) + L::TW_OFF;
   double* sred = reinterpret_cast<double*>(reinterpret_cast<float2*>(smem4) + L::F2_END);
   uint8_t* Mb = reinterpret_cast<uint8_t*>(sred + kRowNT / 32);
-  __shared__ int s_next;
-  __shared__ int am_last;
+  __shared__ int s_next, s_fin;
+  __shared__ int sb[kMaxBatch + 1];  // step_base of the launch's instances
+  __shared__ int sn[kMaxBatch];      // their kept rows x coils
 
-  NestaDevState* st = a.st;
-  if (RESID && it > st->last_iter) return;
+  ClassCtl* ctl = bm.ctl;
+  const int n = bm.n;
+  if (RESID && n == 1 && it > tab[0].st->last_iter) return;  // uniform: the only instance has finished
   const int t = threadIdx.x;
-  const int C = a.C, H = a.H;
-  const int nitems = a.rowoff[a.F] * C;
-  const int nsteps = (nitems + RPC - 1) / RPC;
-  const float s_fwd = a.s_fwd;
+  for (int i = t; i <= n; i += kRowNT) {
+    sb[i] = ctl->step_base[i];
+    if (i < n) sn[i] = ctl->nitems[i];
+  }
+  __syncthreads();
+  const int nsteps = sb[n];
+  auto inst_of = [&](int step) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+      const int mid = (lo + hi + 1) >> 1;
+      if (sb[mid] <= step) lo = mid;
+      else hi = mid - 1;
+    }
+    return lo;
+  };
+  // next step of a running instance (thread 0); steps of instances that have
+  // finished their iterations are skipped by moving the counter past them
+  auto claim = [&]() {
+    int s = atomicAdd(&ctl->row_next, 1);
+    if (RESID && n > 1) {
+      while (s < nsteps) {
+        const int i = inst_of(s);
+        if (it <= tab[i].st->last_iter) break;
+        atomicMax(&ctl->row_next, sb[i + 1]);
+        s = atomicAdd(&ctl->row_next, 1);
+      }
+    }
+    return s;
+  };
 
   // y (and mask) rows of a step into buffer `buf`; T rows into Tb.  The row
   // table lookups of all RPC rows are issued together before the copies.
   auto issue_y = [&](int step, int buf) {
-    const int base = step * RPC;
+    const int i = inst_of(step);
+    const FusedArgs& ai = tab[i];
+    const int base = (step - sb[i]) * RPC, nitems = sn[i], C = ai.C, H = ai.H;
     const float2* ysrc[RPC];
     const uint8_t* msrc[RPC];
 #pragma unroll
@@ -328,9 +388,9 @@ __global__ void __launch_bounds__(kRowNT) k_rows(FusedArgs a, int it) {
       msrc[r] = nullptr;
       if (item < nitems) {
         const int g = item / C, c = item % C;
-        const int f = __ldg(a.rows_f + g), h = __ldg(a.rows_h + g);
-        ysrc[r] = a.y + ((size_t(f) * C + c) * H + h) * size_t(W);
-        if (RESID && !__ldg(a.row_full + g)) msrc[r] = a.mask + (size_t(f) * H + h) * size_t(W);
+        const int f = __ldg(ai.rows_f + g), h = __ldg(ai.rows_h + g);
+        ysrc[r] = ai.y + ((size_t(f) * C + c) * H + h) * size_t(W);
+        if (RESID && !__ldg(ai.row_full + g)) msrc[r] = ai.mask + (size_t(f) * H + h) * size_t(W);
       }
     }
 #pragma unroll
@@ -346,21 +406,23 @@ __global__ void __launch_bounds__(kRowNT) k_rows(FusedArgs a, int it) {
     }
   };
   auto issue_T = [&](int step) {
-    const int base = step * RPC;
+    const int i = inst_of(step);
+    const int base = (step - sb[i]) * RPC, nitems = sn[i];
+    const float2* T = tab[i].T;
     for (int q = t; q < RPC * (W / 2); q += kRowNT) {
       const int r = q / (W / 2), part = q % (W / 2), item = base + r;
-      if (item < nitems) cp_async16(Tb + r * W + 2 * part, a.T + size_t(item) * W + 2 * part);
+      if (item < nitems) cp_async16(Tb + r * W + 2 * part, T + size_t(item) * W + 2 * part);
     }
   };
 
-  if (t == 0) s_next = atomicAdd(&st->row_next, 1);
-  for (int i = t; i < 2 * W; i += kRowNT) tw[i] = a.twW[i];
+  if (t == 0) s_next = claim();
+  for (int i = t; i < 2 * W; i += kRowNT) tw[i] = tab[0].twW[i];
   __syncthreads();
   int step = s_next;
-  if (step < nsteps) {
-    issue_y(step, 0);
-    if (RESID) issue_T(step);
-  }
+  if (step < nsteps) issue_y(step, 0);  // data rows: inputs, not written by the predecessor
+  grid_dep_wait();
+  grid_dep_release();
+  if (RESID && step < nsteps) issue_T(step);
   cp_async_commit();
   // inter-pass twiddles: pass-A items keep s = t % B and backward pass-1 items
   // keep k1 = t % A at every step, so their twiddles live in registers
@@ -369,18 +431,22 @@ __global__ void __launch_bounds__(kRowNT) k_rows(FusedArgs a, int it) {
   for (int k1 = 0; k1 < A; ++k1) twa[k1] = tw[k1 * B + (t % B)];
 #pragma unroll
   for (int k1p = 0; k1p < B; ++k1p) twb[k1p] = tw[W + k1p * A + (t % A)];
-  float racc = 0.f;
+  const float s_fwd = tab[0].s_fwd;
   int buf = 0;
+  int run = 0;  // steps of the current instance since the last count
 
   while (step < nsteps) {
     __syncthreads();  // all threads hold `step`; s_next may be rewritten
-    if (t == 0) s_next = atomicAdd(&st->row_next, 1);
+    if (t == 0) s_next = claim();
     cp_async_wait<0>();
     __syncthreads();  // rows of `step` visible, next step index visible
     const int next = s_next;
     if (next < nsteps) issue_y(next, buf ^ 1);
     cp_async_commit();
-    const int base = step * RPC;
+    const int inst = inst_of(step);
+    const FusedArgs& ai = tab[inst];
+    const int lstep = step - sb[inst];
+    const int base = lstep * RPC, nitems = sn[inst], C = ai.C;
     const float2* Yc = Yb + buf * RPC * W;
     const uint8_t* Mc = Mb + buf * RPC * W;
 
@@ -404,6 +470,7 @@ __global__ void __launch_bounds__(kRowNT) k_rows(FusedArgs a, int it) {
     // RPC*A <= kRowNT so each thread has at most one item
     const int r = t / A, k1 = t % A, q = base + r;
     const bool has = (t < RPC * A) && (q < nitems);
+    float racc = 0.f;
     float2 v[B];
     if (has) {
       if constexpr (RESID) {
@@ -414,7 +481,7 @@ __global__ void __launch_bounds__(kRowNT) k_rows(FusedArgs a, int it) {
     if constexpr (RESID) __syncthreads();  // exchange reused by the backward pass
     if (has) {
       const int g = q / C;
-      const bool full = RESID ? (a.row_full[g] != 0) : true;
+      const bool full = RESID ? (ai.row_full[g] != 0) : true;
       if constexpr (RESID) {
         dft<B>(v);  // v[k2] = X[k1 + A*k2]
 #pragma unroll
@@ -444,66 +511,90 @@ __global__ void __launch_bounds__(kRowNT) k_rows(FusedArgs a, int it) {
 #pragma unroll
       for (int sp = 0; sp < A; ++sp) u[sp] = ex[rr * R::RS2 + k1p * R::S2 + sp];
       dft<A>(u);
-      float2* __restrict__ dst = a.T + size_t(qq) * W;
+      float2* __restrict__ dst = ai.T + size_t(qq) * W;
 #pragma unroll
       for (int k2p = 0; k2p < A; ++k2p) dst[k1p + B * k2p] = conjf2(u[k2p]);
+    }
+
+    if constexpr (RESID) {
+      // ||r||^2 of this step, one partial per warp (fixed slots, so the final
+      // sum does not depend on which CTA ran which step)
+      double pr = double(racc);
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) pr += __shfl_down_sync(0xffffffffu, pr, o);
+      if ((t & 31) == 0) ai.part_r[lstep * kRowWarps + (t >> 5)] = pr;
+      ++run;
+      // at the end of a run of steps of one instance, count them; the CTA that
+      // completes the instance reduces its partial sums and runs its scalar
+      // recurrence
+      const int nst = sb[inst + 1] - sb[inst];
+      const bool run_ends = (next >= nsteps) || (inst_of(next) != inst);
+      if (run_ends) {
+        if ((t & 31) == 0) __threadfence();  // this warp's partials before the count
+        __syncthreads();
+        if (t == 0) {
+          const unsigned dn = atomicAdd(&ctl->done[inst], unsigned(run));
+          s_fin = (dn + unsigned(run) == unsigned(nst)) ? 1 : 0;
+        }
+        run = 0;
+        __syncthreads();
+      }
+      if (run_ends && s_fin) {
+        __threadfence();
+        NestaDevState* st = ai.st;
+        __shared__ float fm[kFmeanCopy];
+        if (t < kFmeanCopy && t < st->miniter) fm[t] = __ldcg(ai.fmean + t);
+        // loads of each batch are issued together; the summation order is fixed
+        constexpr int U = 8;
+        double su2 = 0.0, sud = 0.0, sr2 = 0.0;
+        const double2* ptv = reinterpret_cast<const double2*>(ai.part_tv);
+        const int ntv = ai.ntv;
+        for (int i0 = 0; i0 < ntv; i0 += U * kRowNT) {
+          double2 vv[U];
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const int i = i0 + u * kRowNT + t;
+            vv[u] = (i < ntv) ? __ldcg(ptv + i) : make_double2(0.0, 0.0);
+          }
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            su2 += vv[u].x;
+            sud += vv[u].y;
+          }
+        }
+        const int npr = nst * kRowWarps;
+        for (int i0 = 0; i0 < npr; i0 += U * kRowNT) {
+          double vv[U];
+#pragma unroll
+          for (int u = 0; u < U; ++u) {
+            const int i = i0 + u * kRowNT + t;
+            vv[u] = (i < npr) ? __ldcg(ai.part_r + i) : 0.0;
+          }
+#pragma unroll
+          for (int u = 0; u < U; ++u) sr2 += vv[u];
+        }
+        su2 = block_sum<kRowNT>(su2, sred);
+        sud = block_sum<kRowNT>(sud, sred);
+        sr2 = block_sum<kRowNT>(sr2, sred);
+        if (t == 0) {
+          nesta_scalar_step(st, ai.fmean, fm, it, su2, sud, sr2);
+          ctl->done[inst] = 0;
+        }
+        __syncthreads();
+      }
     }
     step = next;
     buf ^= 1;
   }
   cp_async_wait<0>();
 
-  // last CTA: reset the work counter; in RESID mode also reduce the partial
-  // sums and run the scalar recurrence
-  double tot = 0.0;
-  if constexpr (RESID) tot = block_sum<kRowNT>(double(racc), sred);
+  // the last CTA to finish resets the step counter for the next launch
   if (t == 0) {
-    if (RESID) a.part_r[blockIdx.x] = tot;
     __threadfence();
-    const unsigned tk = atomicAdd(&st->ticket, 1u);
-    am_last = (tk == gridDim.x - 1);
-  }
-  __syncthreads();
-  if (am_last) {
-    __threadfence();
-    if constexpr (RESID) {
-      __shared__ float fm[kFmeanCopy];
-      if (t < kFmeanCopy && t < st->miniter) fm[t] = __ldcg(a.fmean + t);
-      // loads of each batch are issued together; the summation order is fixed
-      constexpr int U = 8;
-      double su2 = 0.0, sud = 0.0, sr2 = 0.0;
-      const double2* ptv = reinterpret_cast<const double2*>(a.part_tv);
-      for (int i0 = 0; i0 < a.nblk_k1; i0 += U * kRowNT) {
-        double2 v[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int i = i0 + u * kRowNT + t;
-          v[u] = (i < a.nblk_k1) ? __ldcg(ptv + i) : make_double2(0.0, 0.0);
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          su2 += v[u].x;
-          sud += v[u].y;
-        }
-      }
-      for (int i0 = 0; i0 < int(gridDim.x); i0 += U * kRowNT) {
-        double v[U];
-#pragma unroll
-        for (int u = 0; u < U; ++u) {
-          const int i = i0 + u * kRowNT + t;
-          v[u] = (i < int(gridDim.x)) ? __ldcg(a.part_r + i) : 0.0;
-        }
-#pragma unroll
-        for (int u = 0; u < U; ++u) sr2 += v[u];
-      }
-      su2 = block_sum<kRowNT>(su2, sred);
-      sud = block_sum<kRowNT>(sud, sred);
-      sr2 = block_sum<kRowNT>(sr2, sred);
-      if (t == 0) nesta_scalar_step(st, a.fmean, fm, it, su2, sud, sr2);
-    }
-    if (t == 0) {
-      st->ticket = 0;
-      st->row_next = 0;
+    const unsigned tk = atomicAdd(&ctl->ticket, 1u);
+    if (tk == gridDim.x - 1) {
+      ctl->row_next = 0;
+      ctl->ticket = 0;
     }
   }
 }
@@ -534,7 +625,8 @@ struct InvColsSmem {
 };
 
 template <int H, bool UPDATE>
-__global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT) k_inv_cols(FusedArgs a, int it) {
+__global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT)
+    k_inv_cols(const FusedArgs* __restrict__ tab, const __grid_constant__ BatchMap bm, int it) {
   using L = InvColsSmem<H>;
   constexpr int A = L::A, B = L::B, KS = L::KS, RCAP = L::RCAP;
   constexpr int N1 = kWB * A, N2 = kWB * B;
@@ -548,10 +640,11 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT) k_inv_cols(F
   namespace cgr = cooperative_groups;
   cgr::cluster_group cluster = cgr::this_cluster();
 
+  const int inst = find_inst(bm, blockIdx.z);
+  const FusedArgs& a = tab[inst];
   const NestaDevState* st = a.st;
-  if (UPDATE && it > st->last_iter) return;  // uniform over the whole grid
   const int t = threadIdx.x;
-  const int half = blockIdx.y, f = blockIdx.z, w0 = blockIdx.x * kWB;
+  const int half = blockIdx.y, f = blockIdx.z - bm.fbase[inst], w0 = blockIdx.x * kWB;
   const int W = a.W, C = a.C, F = a.F;
   const size_t N = size_t(a.N);
   const int rowbase = a.rowoff[f];
@@ -560,13 +653,15 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT) k_inv_cols(F
   const int cmid = (C + 1) / 2;
   const int cbeg = half ? cmid : 0, cend = half ? C : cmid;
 
-  auto issue = [&](int c, int buf) {
+  auto issue_S = [&](int c, int buf) {
     const float2* src = a.S + size_t(c) * N + w0;
     float2* dst = Sb + buf * H * kWB;
     for (int q = t; q < H * (kWB / 2); q += kColNT) {
       const int row = q / (kWB / 2), part = q % (kWB / 2);
       cp_async16(dst + row * kWB + 2 * part, src + size_t(row) * W + 2 * part);
     }
+  };
+  auto issue_T = [&](int c, int buf) {
     if (staged) {
       const float2* tsrc = a.T + (size_t(rowbase) * C + c) * W + w0;
       float2* tdst = Tb + buf * RCAP * kWB;
@@ -575,13 +670,21 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT) k_inv_cols(F
         cp_async16(tdst + j * kWB + 2 * part, tsrc + size_t(j) * C * W + 2 * part);
       }
     }
-    cp_async_commit();
   };
-  if (cbeg < cend) issue(cbeg, 0);
+  if (cbeg < cend) issue_S(cbeg, 0);
   for (int i = t; i < H; i += kColNT) {
     tw[i] = a.twH[H + i];
     rmap[i] = a.rowmap[f * H + i];
   }
+  grid_dep_wait();  // T and the scalar state come from the row pass
+  grid_dep_release();
+  if (UPDATE && it > st->last_iter) {  // uniform over the instance, so over each cluster
+    cp_async_commit();
+    cp_async_wait<0>();
+    return;
+  }
+  if (cbeg < cend) issue_T(cbeg, 0);
+  cp_async_commit();
 
   float2 acc[NI2][A];
 #pragma unroll
@@ -603,7 +706,11 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT) k_inv_cols(F
     const int buf = (c - cbeg) & 1;
     cp_async_wait<0>();
     __syncthreads();  // coil c staged; previous coil's pass 2 finished
-    if (c + 1 < cend) issue(c + 1, buf ^ 1);
+    if (c + 1 < cend) {
+      issue_S(c + 1, buf ^ 1);
+      issue_T(c + 1, buf ^ 1);
+    }
+    cp_async_commit();
     const float2* Tc = Tb + buf * RCAP * kWB;
     const float2* Sc = Sb + buf * H * kWB;
 #pragma unroll

@@ -11,10 +11,11 @@
 // library, held until the process exits).
 //
 // The scratch holds the row-pass intermediates (F*H*C*W complex values), the
-// row tables and a small state block.  Every call reuses it: the state block
-// is cleared at the start of each call, the rest is fully rewritten before it
-// is read.  Calls whose work overlaps on the GPU (different streams, or several
-// host threads) share the one array and race; serialise them.
+// row tables, the one-entry instance table and the row pass's control block.
+// Every call reuses it: kernels of the call rewrite the tables and reset the
+// control block before anything reads them.  Calls whose work overlaps on the
+// GPU (different streams, or several host threads) share the one array and
+// race; serialise them.
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -25,8 +26,8 @@
 
 namespace gbn {
 
-void launch_rows_identity(int H, int F, int* rowmap, int* rowoff, int* rows_h, int* rows_f, int* row_full,
-                          cudaStream_t s);
+size_t simple_recon_bytes(int W, int H, int F, int C);
+int simple_recon_in(gbn_ctx* ctx, void* ws, const float2* y, const float2* S, float2* x, int W, int H, int F, int C);
 
 namespace {
 
@@ -34,9 +35,13 @@ namespace {
 constexpr size_t kStaticMaxT = size_t(1) << 20;  // complex elements of the intermediates: F*H*C*W
 constexpr size_t kStaticMaxRows = 8192;          // F*H
 constexpr size_t kStaticTBytes = kStaticMaxT * sizeof(float2);
-constexpr size_t kStaticIntBytes = (4 * kStaticMaxRows + kStaticMaxRows + 1) * sizeof(int);
-constexpr size_t kStaticStateOff = ((kStaticTBytes + kStaticIntBytes + 255) / 256) * 256;
-constexpr size_t kStaticScratchBytes = kStaticStateOff + ((sizeof(NestaDevState) + 255) / 256) * 256;
+constexpr size_t kStaticIntBytes = ((5 * kStaticMaxRows + 1) * sizeof(int) + 255) / 256 * 256;
+// state block, instance table and control block, each rounded to 256 bytes
+constexpr size_t kStaticSmallBytes = 4096;
+static_assert(((sizeof(NestaDevState) + 255) / 256 + (sizeof(FusedArgs) + 255) / 256 + (sizeof(ClassCtl) + 255) / 256) *
+                      256 <= kStaticSmallBytes,
+              "static scratch tail too small");
+constexpr size_t kStaticScratchBytes = kStaticTBytes + kStaticIntBytes + kStaticSmallBytes;
 
 __device__ __align__(256) unsigned char g_static_scratch[kStaticScratchBytes];
 
@@ -60,9 +65,7 @@ int static_scratch(int device, void** out) {
 }  // namespace
 
 int simple_recon_static(gbn_ctx* ctx, const float2* y, const float2* S, float2* x, int W, int H, int F, int C) {
-  const SizeKernels* kh = find_size(H);
-  const SizeKernels* kw = find_size(W);
-  if (!kh || !kw) return set_error(GBN_ERR_UNSUPPORTED, "unsupported FFT length");
+  if (!find_size(H) || !find_size(W)) return set_error(GBN_ERR_UNSUPPORTED, "unsupported FFT length");
   const size_t FH = size_t(F) * H, K = FH * C * W;
   if (K > kStaticMaxT || FH > kStaticMaxRows)
     return set_error(GBN_ERR_UNSUPPORTED,
@@ -70,51 +73,11 @@ int simple_recon_static(gbn_ctx* ctx, const float2* y, const float2* S, float2* 
                          std::to_string(kStaticMaxT) + " and F*H <= " + std::to_string(kStaticMaxRows) +
                          "; got " + std::to_string(K) + " and " + std::to_string(FH) + ")");
   void* base = nullptr;
-  int rc = static_scratch(ctx->device, &base);
+  const int rc = static_scratch(ctx->device, &base);
   if (rc != GBN_OK) return rc;
-  unsigned char* b = static_cast<unsigned char*>(base);
-  float2* T = reinterpret_cast<float2*>(b);
-  int* rowmap = reinterpret_cast<int*>(b + kStaticTBytes);
-  int* rows_h = rowmap + kStaticMaxRows;
-  int* rows_f = rows_h + kStaticMaxRows;
-  int* row_full = rows_f + kStaticMaxRows;
-  int* rowoff = row_full + kStaticMaxRows;
-  NestaDevState* st = reinterpret_cast<NestaDevState*>(b + kStaticStateOff);
-  cudaStream_t s = ctx->stream;
-  // the row pass's work counter and ticket must start at zero on every call
-  cudaError_t e = cudaMemsetAsync(st, 0, sizeof(NestaDevState), s);
-  if (e != cudaSuccess) return cuda_status(e, "static scratch reset");
-
-  FusedArgs a;
-  memset(&a, 0, sizeof(a));
-  a.W = W;
-  a.H = H;
-  a.F = F;
-  a.C = C;
-  a.N = W * H;
-  a.y = y;
-  a.S = S;
-  a.rowmap = rowmap;
-  a.rowoff = rowoff;
-  a.rows_h = rows_h;
-  a.rows_f = rows_f;
-  a.row_full = row_full;
-  a.T = T;
-  a.xref = x;
-  a.st = st;
-  a.twH = ctx_twiddles(ctx, H);
-  a.twW = ctx_twiddles(ctx, W);
-  a.s_adj = 1.0f / float(W * H);  // clFFT BACKWARD scale
-  const long long rows = (long long)FH * C;
-  const int g2 = int(std::max<long long>(
-      1, std::min<long long>((rows + kw->rows_per_cta - 1) / kw->rows_per_cta, (long long)ctx->nsm * ctx->k2_ctas_per_sm)));
-  launch_rows_identity(H, F, rowmap, rowoff, rows_h, rows_f, row_full, s);
-  kw->rows(a, 0, false, g2, s);
-  kh->inv_cols(a, 0, false, dim3(W / kWB, 2, F), s);
-  ctx->launches += 3;
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return cuda_status(e, "static simple recon launch");
-  return GBN_OK;
+  if (simple_recon_bytes(W, H, F, C) > kStaticScratchBytes)
+    return set_error(GBN_ERR_UNSUPPORTED, "gbn_simple_recon_static: problem exceeds the static scratch");
+  return simple_recon_in(ctx, base, y, S, x, W, H, F, C);
 }
 
 }  // namespace gbn

@@ -9,12 +9,14 @@ namespace gbn {
 
 struct SizeKernels {
   int L;
-  // forward column pass (k_fwd_cols<L>), grid (W/8, coil groups, F)
-  void (*fwd_cols)(const FusedArgs& a, int it, int coils_per_block, dim3 grid, cudaStream_t s);
+  // The fused kernels take a device table of instances (all with H = L for the
+  // column passes, W = L for the row pass) and the launch's BatchMap.
+  // forward column pass (k_fwd_cols<L>), grid (W/8, coil groups, total frames)
+  void (*fwd_cols)(const FusedArgs* tab, const BatchMap& bm, int it, int coils_per_block, dim3 grid, cudaStream_t s);
   // row pass (k_rows<L, resid>), 1-D persistent grid
-  void (*rows)(const FusedArgs& a, int it, bool resid, int grid, cudaStream_t s);
-  // adjoint column pass (k_inv_cols<L, update>), grid (W/8, F)
-  void (*inv_cols)(const FusedArgs& a, int it, bool update, dim3 grid, cudaStream_t s);
+  void (*rows)(const FusedArgs* tab, const BatchMap& bm, int it, bool resid, int grid, cudaStream_t s);
+  // adjoint column pass (k_inv_cols<L, update>), grid (W/8, 2, total frames) in clusters of 2
+  void (*inv_cols)(const FusedArgs* tab, const BatchMap& bm, int it, bool update, dim3 grid, cudaStream_t s);
   // dense FFT passes
   void (*fft_rows)(const float2* in, float2* out, int nrows, int inv, float scale, const float2* tw, int grid,
                    cudaStream_t s);

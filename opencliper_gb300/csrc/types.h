@@ -30,8 +30,7 @@ struct NestaDevState {
   int qpDone;
   float qp, fx, apk, tauk;
   float normUk, fxdot, l2term;
-  unsigned int ticket;    // last-block detection in the row pass
-  int row_next;           // dynamic work counter of the row pass
+  int outer_active;       // this instance runs the current outer loop
 
   // power-method progress across chunks
   int ne_done, ne_cnt;
@@ -61,8 +60,8 @@ struct FusedArgs {
   float2* wacc;           // Nesterov weighted gradient sum w_k
   NestaDevState* st;
   float* fmean;           // [miniter] rolling objective buffer
-  double* part_tv;        // [nblk_k1][2] partial sums of ||u||^2 and Re<u,d>
-  double* part_r;         // [nblk_k2] partial sums of ||E x - y||^2
+  double* part_tv;        // [ntv][2] partial sums of ||u||^2 and Re<u,d>, one per (frame, column tile)
+  double* part_r;         // [row steps] partial sums of ||E x - y||^2, one per row-pass step
   // Twiddle tables for the two-pass transforms, forward sign, 2L entries per
   // length: [k1*B + s] = w_L^(s*k1) (k1 < A, s < B), then [L + k1'*A + s'] =
   // w_L^(s'*k1') (k1' < B, s' < A), laid out so that the lanes of a warp read
@@ -71,7 +70,27 @@ struct FusedArgs {
   const float2* twW;
   float s_fwd;            // 1/sqrt(N) as the reference computes it (double -> float)
   float s_adj;            // sqrt(N)/N: the reference's sqrt(N) pre-scale times clFFT's 1/N
-  int nblk_k1;            // number of blocks of the forward column kernel
+  int ntv;                // F * (W / 8): number of tTV partial sums
+};
+
+// Instances covered by one launch of the fused kernels.  All of them share the
+// transform lengths (W, H); frames of instance i occupy grid z indices
+// [fbase[i], fbase[i+1]).
+constexpr int kMaxBatch = 64;
+
+// Device-resident control block of one launch group (one set of instances).
+struct ClassCtl {
+  int row_next;                   // dynamic step counter of the row pass
+  unsigned int ticket;            // CTAs of the row pass that have finished
+  int step_base[kMaxBatch + 1];   // prefix sums of the instances' row-pass steps
+  int nitems[kMaxBatch];          // kept rows x coils of each instance
+  unsigned int done[kMaxBatch];   // finished row-pass steps of each instance in this launch
+};
+
+struct BatchMap {
+  int n;                          // instances
+  int fbase[kMaxBatch + 1];       // prefix sums of their frame counts
+  ClassCtl* ctl;
 };
 
 }  // namespace gbn

@@ -127,3 +127,55 @@ def make_fully_sampled(W: int, H: int, C: int, seed: int, noise: float = 1e-3) -
     k = k + sig * (rng.standard_normal(k.shape) + 1j * rng.standard_normal(k.shape)) / np.sqrt(2)
     mask = np.full((1, H, W), 255, np.uint8)
     return Problem(k.astype(np.complex64), S, mask, np.ones((1, H), np.uint32), x, seed)
+
+
+@dataclass
+class DeviceProblem:
+    y: object            # DeviceArray KData [F][C][H][W] complex64
+    S: object            # DeviceArray [C][H][W] complex64
+    mask: object         # DeviceArray [F][H][W] uint8
+    rowmask: np.ndarray  # row mask [F][H] uint32 (host)
+    seed: int
+
+
+class _CudaView:
+    """__cuda_array_interface__ over a DeviceArray's memory with another element
+    type (complex64 as float32 pairs), for zero-copy torch views."""
+
+    def __init__(self, d, typestr: str, shape):
+        self.__cuda_array_interface__ = {"shape": tuple(shape), "typestr": typestr, "data": (int(d.ptr), False),
+                                         "version": 3, "strides": None}
+
+
+def make_problem_device(ctx, W: int, H: int, F: int, C: int, R: float, seed: int,
+                        noise: float = 1e-3) -> DeviceProblem:
+    """The distributions of make_problem with the k-space formed on the device:
+    the library's forward operator (gbn_op_encode, mask * FFT2_ortho(S_c x_f))
+    plus masked complex Gaussian noise drawn by torch from `seed`.  For
+    benchmark workloads too large to generate with numpy FFTs; the noise stream
+    differs from make_problem's."""
+    import torch
+
+    from . import api
+    rng = np.random.default_rng(np.random.PCG64(seed))
+    x = phantom_series(W, H, F, rng)
+    S = coil_maps(W, H, C)
+    rm = row_masks(H, F, R, rng)
+    mask = np.repeat((rm.astype(np.uint8) * 255)[:, :, None], W, axis=2)
+    dx, dS, dm = ctx.to_device(x), ctx.to_device(S), ctx.to_device(mask)
+    dy = ctx.empty((F, C, H, W), np.complex64)
+    api.op_encode(ctx, dx, dS, dm, dy)
+    ctx.sync()
+    dev = torch.device("cuda", ctx.device)
+    k = torch.as_tensor(_CudaView(dy, "<f4", (F, C, H, W, 2)), device=dev)
+    m = torch.as_tensor(_CudaView(dm, "|u1", (F, H, W)), device=dev)
+    gen = torch.Generator(device=dev)
+    gen.manual_seed(int(seed))
+    sig = float(noise) * float(k.square().sum(-1).sqrt().max())
+    for f in range(F):  # one frame at a time bounds the temporary
+        n = torch.randn(k[f].shape, generator=gen, device=dev) * (sig / np.sqrt(2.0))
+        k[f] += n * (m[f] != 0)[None, :, :, None]
+    torch.cuda.synchronize(dev)
+    dx.free()
+    return DeviceProblem(dy, dS, dm, rm, int(seed))
+
