@@ -39,7 +39,7 @@ struct gbn_batch {
     gbn::FusedArgs* tab = nullptr;
     gbn::ClassCtl* ctl = nullptr;
     gbn::BatchMap bm{};
-    int cpb = 1, g2 = 1;
+    int cpb = 1, g2 = 1, g2a = 1;  // row grids with / without the residual
     dim3 g1, g3;
     unsigned maxIntIter = 0, maxIter = 0;
     cudaStream_t stream = nullptr;
@@ -82,7 +82,7 @@ int batch_enqueue(gbn_batch* b, bool graph_mode) {
     for (int i : g.idx) n_launch += launch_pre(b->probs[i], b->prm[i], s);
     n_launch += launch_group_init(g.tab, int(g.idx.size()), kw->rows_per_cta, g.ctl, s);
     // x0 = E^H y of all members (NestaUp.cpp:465-486)
-    kw->rows(g.tab, g.bm, 0, false, g.g2, s);
+    kw->rows(g.tab, g.bm, 0, false, g.g2a, s);
     kh->inv_cols(g.tab, g.bm, 0, false, g.g3, s);
     n_launch += 2;
     for (int i : g.idx) {
@@ -199,7 +199,8 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
     g.bm.fbase[ng] = frames;
     g.cpb = std::max(1, std::min(ctx->k1_coils_per_block, maxC));
     g.g1 = dim3(g.W / kWB, (maxC + g.cpb - 1) / g.cpb, frames);
-    g.g2 = row_grid(ctx, steps);
+    g.g2 = row_grid(ctx, kw, true, steps);
+    g.g2a = row_grid(ctx, kw, false, steps);
     g.g3 = dim3(g.W / kWB, 2, frames);
   }
   if (rc == GBN_OK && (e = cudaGetLastError()) != cudaSuccess) rc = cuda_status(e, "batch tables");

@@ -40,6 +40,24 @@ struct Launchers {
     allow_smem(k_fwd_cols<L>, FwdColsSmem<L>::BYTES, ok);
     launch_pdl(k_fwd_cols<L>, grid, kColNT, FwdColsSmem<L>::BYTES, s, tab, bm, it, cpb);
   }
+  // resident CTAs per SM of the row kernel (queried once)
+  static int rows_occupancy(bool resid) {
+    static int occ1 = 0, occ0 = 0;
+    int& o = resid ? occ1 : occ0;
+    if (o == 0) {
+      static bool ok1 = false, ok0 = false;
+      int nb = 0;
+      if (resid) {
+        allow_smem(k_rows<L, true>, RowsSmem<L, true>::BYTES, ok1);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_rows<L, true>, kRowNT, RowsSmem<L, true>::BYTES);
+      } else {
+        allow_smem(k_rows<L, false>, RowsSmem<L, false>::BYTES, ok0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, k_rows<L, false>, kRowNT, RowsSmem<L, false>::BYTES);
+      }
+      o = nb > 0 ? nb : 1;
+    }
+    return o;
+  }
   static void rows(const FusedArgs* tab, const BatchMap& bm, int it, bool resid, int grid, cudaStream_t s) {
     static bool ok1 = false, ok0 = false;
     if (resid) {
@@ -70,7 +88,7 @@ struct Launchers {
   }
   static SizeKernels entry() {
     static_assert(fft_size_ok(L), "unsupported transform length");
-    return SizeKernels{L, &fwd_cols, &rows, &inv_cols, &fft_rows, &fft_cols, RowCfg<L>::RPC};
+    return SizeKernels{L, &fwd_cols, &rows, &inv_cols, &fft_rows, &fft_cols, RowCfg<L>::RPC, &rows_occupancy};
   }
 };
 

@@ -588,8 +588,9 @@ int run_prepare(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm) {
   return GBN_OK;
 }
 
-int row_grid(gbn_ctx* ctx, long long steps) {
-  return int(std::max<long long>(1, std::min<long long>(steps, (long long)ctx->nsm * ctx->k2_ctas_per_sm)));
+int row_grid(gbn_ctx* ctx, const SizeKernels* kw, bool resid, long long steps) {
+  const int per_sm = std::max(1, std::min(ctx->k2_ctas_per_sm, kw->rows_occupancy(resid)));
+  return int(std::max<long long>(1, std::min<long long>(steps, (long long)ctx->nsm * per_sm)));
 }
 
 int launch_store_args(FusedArgs* dst, const FusedArgs& a, cudaStream_t s) {
@@ -679,7 +680,8 @@ int nesta_run(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, float2*
   cudaStream_t s = ctx->stream;
   const int cpb = std::max(1, std::min(ctx->k1_coils_per_block, C));
   const dim3 g1(W / kWB, (C + cpb - 1) / cpb, F);
-  const int g2 = row_grid(ctx, ((long long)F * H * C + kw->rows_per_cta - 1) / kw->rows_per_cta);
+  const long long steps = ((long long)F * H * C + kw->rows_per_cta - 1) / kw->rows_per_cta;
+  const int g2 = row_grid(ctx, kw, true, steps), g2a = row_grid(ctx, kw, false, steps);
   const dim3 g3(W / kWB, 2, F);  // clusters of 2 along y
   const FusedArgs a = make_args(P, x_out);
   const FusedArgs* tab = P->d_args;
@@ -691,7 +693,7 @@ int nesta_run(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, float2*
     n_setup += launch_store_args(P->d_args, a, s);
     n_setup += launch_group_init(tab, 1, kw->rows_per_cta, P->ctl, s);
     // x0 = E^H y (NestaUp.cpp:465-486)
-    kw->rows(tab, bm, 0, false, g2, s);
+    kw->rows(tab, bm, 0, false, g2a, s);
     kh->inv_cols(tab, bm, 0, false, g3, s);
     n_setup += 2;
     n_setup += launch_constants(ctx, P, x_out, RandStart{ctx->rand48, nullptr, 1, 0}, s);
@@ -766,7 +768,7 @@ int simple_recon_in(gbn_ctx* ctx, void* ws, const float2* y, const float2* S, fl
   a.s_adj = 1.0f / float(W * H);  // clFFT BACKWARD scale
   a.ntv = F * (W / kWB);
   const long long steps = ((long long)FH * C + kw->rows_per_cta - 1) / kw->rows_per_cta;
-  const int g2 = int(std::max<long long>(1, std::min<long long>(steps, (long long)ctx->nsm * ctx->k2_ctas_per_sm)));
+  const int g2 = row_grid(ctx, kw, false, steps);
   const BatchMap bm = single_map(F, ctl);
   GBN_LAUNCH(ctx, GBN_PROF_SETUP, 5, {
     k_rows_identity<<<int(std::min<size_t>((FH + 255) / 256, 1024)), 256, 0, s>>>(H, F, rowmap, rowoff, rows_h, rows_f,

@@ -144,8 +144,7 @@ struct FwdColsSmem {
   static constexpr int A = Split<H>::A, B = Split<H>::B, KS = col_ks(B);
   static constexpr int S_OFF = 0;                        // float2 [2][H][kWB]
   static constexpr int EX_OFF = S_OFF + 2 * H * kWB;     // float2 [A*KS]
-  static constexpr int TW_OFF = EX_OFF + A * KS;         // float2 [H]
-  static constexpr int F2_END = TW_OFF + H;
+  static constexpr int F2_END = EX_OFF + A * KS;
   static constexpr int BYTES = F2_END * 8 + (kColNT / 32) * 8 + H * 4;
 };
 
@@ -162,7 +161,6 @@ __global__ void __launch_bounds__(kColNT, fwd_min_blocks(H))
   extern __shared__ float4 smem4[];
   float2* Sb = reinterpret_cast<float2*>(smem4) + L::S_OFF;
   float2* ex = reinterpret_cast<float2*>(smem4) + L::EX_OFF;
-  float2* tw = reinterpret_cast<float2*>(smem4) + L::TW_OFF;
   double* sred = reinterpret_cast<double*>(reinterpret_cast<float2*>(smem4) + L::F2_END);
   int* rmap = reinterpret_cast<int*>(sred + kColNT / 32);
 
@@ -190,10 +188,7 @@ __global__ void __launch_bounds__(kColNT, fwd_min_blocks(H))
   };
   issue_S(c0, 0);
 
-  for (int i = t; i < H; i += kColNT) {
-    tw[i] = a.twH[i];
-    rmap[i] = a.rowmap[f * H + i];
-  }
+  for (int i = t; i < H; i += kColNT) rmap[i] = a.rowmap[f * H + i];
   const int rowbase = a.rowoff[f];
   grid_dep_wait();  // x_k comes from the previous adjoint column pass
   grid_dep_release();
@@ -233,7 +228,6 @@ __global__ void __launch_bounds__(kColNT, fwd_min_blocks(H))
     }
   }
 
-  __syncthreads();
   // inter-pass twiddles of this thread's pass-1 items, identical for every coil
   float2 twr[NI1][A];
 #pragma unroll
@@ -241,7 +235,7 @@ __global__ void __launch_bounds__(kColNT, fwd_min_blocks(H))
     const int i = t + ii * kColNT;
     const int s = (i < N1) ? i / kWB : 0;
 #pragma unroll
-    for (int k1 = 0; k1 < A; ++k1) twr[ii][k1] = tw[k1 * B + s];
+    for (int k1 = 0; k1 < A; ++k1) twr[ii][k1] = __ldg(a.twH + k1 * B + s);
   }
 
   for (int c = c0; c < c1; ++c) {
@@ -294,9 +288,9 @@ __global__ void __launch_bounds__(kColNT, fwd_min_blocks(H))
 }
 
 // ===========================================================================
-// K2: row pass over kept rows; CTAs take RPC-row steps from a device counter
-// and stage the next step's rows (T, y, mask) into shared memory with cp.async
-// while the current step is transformed.
+// K2: row pass over kept rows in steps of RPC rows taken by a persistent grid
+// from a device counter; the next step's rows (T, y, mask) are staged into
+// shared memory with cp.async while the current step is transformed.
 //   RESID: r = mask * DFT_W(T)/sqrt(N) - y, T = IDFT_W(r), ||r||^2 partials.
 //   !RESID (adjoint of the data, x0 = E^H y): T = IDFT_W(y).
 // ===========================================================================
@@ -316,8 +310,7 @@ struct RowsSmem {
   static constexpr int Y_OFF = 0;                                 // float2 [2][RPC][W]
   static constexpr int T_OFF = Y_OFF + 2 * R::RPC * W;            // float2 [RPC][W] (RESID)
   static constexpr int EX_OFF = T_OFF + (RESID ? R::RPC * W : 0); // float2 [EXN]
-  static constexpr int TW_OFF = EX_OFF + R::EXN;                  // float2 [2W]
-  static constexpr int F2_END = TW_OFF + 2 * W;
+  static constexpr int F2_END = EX_OFF + R::EXN;
   static constexpr int M_BYTES = RESID ? 2 * R::RPC * W : 0;      // uint8 [2][RPC][W]
   static constexpr int BYTES = F2_END * 8 + (kRowNT / 32) * 8 + M_BYTES + 16;
 };
@@ -332,20 +325,26 @@ __global__ void __launch_bounds__(kRowNT)
   float2* Yb = reinterpret_cast<float2*>(smem4) + L::Y_OFF;
   float2* Tb = reinterpret_cast<float2*>(smem4) + L::T_OFF;
   float2* ex = reinterpret_cast<float2*>(smem4) + L::EX_OFF;
-  float2* tw = reinterpret_cast<float2*>(smem4) + L::TW_OFF;
   double* sred = reinterpret_cast<double*>(reinterpret_cast<float2*>(smem4) + L::F2_END);
   uint8_t* Mb = reinterpret_cast<uint8_t*>(sred + kRowNT / 32);
-  __shared__ int s_next, s_fin;
-  __shared__ int sb[kMaxBatch + 1];  // step_base of the launch's instances
-  __shared__ int sn[kMaxBatch];      // their kept rows x coils
+  __shared__ int s_fin, s_last;
+  __shared__ int s_q[2];                    // claimed steps: current and next
+  __shared__ int sb[kMaxBatch + 1];         // step_base of the launch's instances
+  __shared__ int sn[kMaxBatch];             // their kept rows x coils
+  __shared__ unsigned char sact[kMaxBatch];  // instance runs this iteration
+  // rows of the two staged steps: data row, mask row (nullptr: fully sampled)
+  __shared__ const float2* meta_y[2][RPC];
+  __shared__ const uint8_t* meta_m[2][RPC];
 
-  ClassCtl* ctl = bm.ctl;
   const int n = bm.n;
   if (RESID && n == 1 && it > tab[0].st->last_iter) return;  // uniform: the only instance has finished
   const int t = threadIdx.x;
   for (int i = t; i <= n; i += kRowNT) {
-    sb[i] = ctl->step_base[i];
-    if (i < n) sn[i] = ctl->nitems[i];
+    sb[i] = bm.ctl->step_base[i];
+    if (i < n) {
+      sn[i] = bm.ctl->nitems[i];
+      sact[i] = (!RESID || it <= tab[i].st->last_iter) ? 1 : 0;
+    }
   }
   __syncthreads();
   const int nsteps = sb[n];
@@ -358,14 +357,17 @@ __global__ void __launch_bounds__(kRowNT)
     }
     return lo;
   };
-  // next step of a running instance (thread 0); steps of instances that have
-  // finished their iterations are skipped by moving the counter past them
+  // Dynamic assignment from the group's step counter, one step ahead: while
+  // a CTA transforms step k it already knows step k+1 (whose rows it is
+  // staging) and claims step k+2.  Steps of instances that have finished their
+  // iterations are skipped by moving the counter past them.  (thread 0)
+  ClassCtl* ctl = bm.ctl;
   auto claim = [&]() {
     int s = atomicAdd(&ctl->row_next, 1);
     if (RESID && n > 1) {
       while (s < nsteps) {
         const int i = inst_of(s);
-        if (it <= tab[i].st->last_iter) break;
+        if (sact[i]) break;
         atomicMax(&ctl->row_next, sb[i + 1]);
         s = atomicAdd(&ctl->row_next, 1);
       }
@@ -373,34 +375,38 @@ __global__ void __launch_bounds__(kRowNT)
     return s;
   };
 
-  // y (and mask) rows of a step into buffer `buf`; T rows into Tb.  The row
-  // table lookups of all RPC rows are issued together before the copies.
-  auto issue_y = [&](int step, int buf) {
-    const int i = inst_of(step);
-    const FusedArgs& ai = tab[i];
-    const int base = (step - sb[i]) * RPC, nitems = sn[i], C = ai.C, H = ai.H;
-    const float2* ysrc[RPC];
-    const uint8_t* msrc[RPC];
-#pragma unroll
-    for (int r = 0; r < RPC; ++r) {
-      const int item = base + r;
-      ysrc[r] = nullptr;
-      msrc[r] = nullptr;
-      if (item < nitems) {
-        const int g = item / C, c = item % C;
+  // Row lookups of step `step` for row r (thread r < RPC): data and mask rows.
+  struct RowRef {
+    const float2* y;
+    const uint8_t* m;
+  };
+  auto lookup = [&](int step, int r) {
+    RowRef rr{nullptr, nullptr};
+    if (step < nsteps) {
+      const int i = inst_of(step);
+      const FusedArgs& ai = tab[i];
+      const int item = (step - sb[i]) * RPC + r;
+      if (item < sn[i]) {
+        const int C = ai.C, H = ai.H, g = item / C, c = item % C;
         const int f = __ldg(ai.rows_f + g), h = __ldg(ai.rows_h + g);
-        ysrc[r] = ai.y + ((size_t(f) * C + c) * H + h) * size_t(W);
-        if (RESID && !__ldg(ai.row_full + g)) msrc[r] = ai.mask + (size_t(f) * H + h) * size_t(W);
+        rr.y = ai.y + ((size_t(f) * C + c) * H + h) * size_t(W);
+        if (RESID && !__ldg(ai.row_full + g)) rr.m = ai.mask + (size_t(f) * H + h) * size_t(W);
       }
     }
+    return rr;
+  };
+  // copies of the staged rows of a step (metadata in slot `buf`)
+  auto issue_y = [&](int buf) {
 #pragma unroll
     for (int r = 0; r < RPC; ++r) {
-      if (ysrc[r]) {
+      const float2* ys = meta_y[buf][r];
+      const uint8_t* ms = meta_m[buf][r];
+      if (ys) {
         for (int part = t; part < W / 2; part += kRowNT)
-          cp_async16(Yb + (buf * RPC + r) * W + 2 * part, ysrc[r] + 2 * part);
-        if (RESID && msrc[r]) {
+          cp_async16(Yb + (buf * RPC + r) * W + 2 * part, ys + 2 * part);
+        if (RESID && ms) {
           for (int part = t; part < W / 8; part += kRowNT)
-            cp_async8(Mb + (buf * RPC + r) * W + 8 * part, msrc[r] + 8 * part);
+            cp_async8(Mb + (buf * RPC + r) * W + 8 * part, ms + 8 * part);
         }
       }
     }
@@ -415,38 +421,49 @@ __global__ void __launch_bounds__(kRowNT)
     }
   };
 
-  if (t == 0) s_next = claim();
-  for (int i = t; i < 2 * W; i += kRowNT) tw[i] = tab[0].twW[i];
+  if (t == 0) {
+    s_q[0] = claim();
+    s_q[1] = claim();
+  }
   __syncthreads();
-  int step = s_next;
-  if (step < nsteps) issue_y(step, 0);  // data rows: inputs, not written by the predecessor
+  int step = s_q[0];
+  if (t < RPC) {
+    const RowRef rr = lookup(step, t);
+    meta_y[0][t] = rr.y;
+    meta_m[0][t] = rr.m;
+  }
+  // inter-pass twiddles: RPC * max(A, B) <= kRowNT, so every thread has at
+  // most one item per pass and keeps it at every step (pass A: s = t % B,
+  // backward pass 1: k1 = t % A); their twiddles live in registers
+  static_assert(RPC * B <= kRowNT && RPC * A <= kRowNT, "one item per thread and pass");
+  const float2* __restrict__ twW = tab[0].twW;
+  float2 twa[A], twb[B];
+#pragma unroll
+  for (int k1 = 0; k1 < A; ++k1) twa[k1] = __ldg(twW + k1 * B + (t % B));
+#pragma unroll
+  for (int k1p = 0; k1p < B; ++k1p) twb[k1p] = __ldg(twW + W + k1p * A + (t % A));
+  __syncthreads();
+  if (step < nsteps) issue_y(0);  // data rows: inputs, not written by the predecessor
   grid_dep_wait();
   grid_dep_release();
   if (RESID && step < nsteps) issue_T(step);
   cp_async_commit();
-  // inter-pass twiddles: pass-A items keep s = t % B and backward pass-1 items
-  // keep k1 = t % A at every step, so their twiddles live in registers
-  float2 twa[A], twb[B];
-#pragma unroll
-  for (int k1 = 0; k1 < A; ++k1) twa[k1] = tw[k1 * B + (t % B)];
-#pragma unroll
-  for (int k1p = 0; k1p < B; ++k1p) twb[k1p] = tw[W + k1p * A + (t % A)];
   const float s_fwd = tab[0].s_fwd;
   int buf = 0;
   int run = 0;  // steps of the current instance since the last count
 
   while (step < nsteps) {
-    __syncthreads();  // all threads hold `step`; s_next may be rewritten
-    if (t == 0) s_next = claim();
-    cp_async_wait<0>();
-    __syncthreads();  // rows of `step` visible, next step index visible
-    const int next = s_next;
-    if (next < nsteps) issue_y(next, buf ^ 1);
-    cp_async_commit();
+    const int next = s_q[buf ^ 1];
+    // the next step's row lookups and the claim of the one after are in
+    // flight while this step is transformed
+    const RowRef nref = (t < RPC) ? lookup(next, t) : RowRef{nullptr, nullptr};
+    const int after = (t == 0 && next < nsteps) ? claim() : nsteps;
     const int inst = inst_of(step);
     const FusedArgs& ai = tab[inst];
     const int lstep = step - sb[inst];
     const int base = lstep * RPC, nitems = sn[inst], C = ai.C;
+    cp_async_wait<0>();
+    __syncthreads();  // rows of `step` visible; slot buf^1 and the exchange are free
     const float2* Yc = Yb + buf * RPC * W;
     const uint8_t* Mc = Mb + buf * RPC * W;
 
@@ -459,15 +476,22 @@ __global__ void __launch_bounds__(kRowNT)
         for (int n1 = 0; n1 < A; ++n1) v[n1] = Tb[r * W + B * n1 + s];
         dft<A>(v);
 #pragma unroll
-        for (int k1 = 0; k1 < A; ++k1)
-          ex[r * R::RS1 + k1 * R::S1 + s] = (k1 == 0) ? v[k1] : cmul(v[k1], (RPC * B <= kRowNT) ? twa[k1] : tw[k1 * B + s]);
+        for (int k1 = 0; k1 < A; ++k1) ex[r * R::RS1 + k1 * R::S1 + s] = (k1 == 0) ? v[k1] : cmul(v[k1], twa[k1]);
       }
-      __syncthreads();  // Tb consumed, exchange filled
-      if (next < nsteps) issue_T(next);
-      cp_async_commit();
     }
+    if (t < RPC) {
+      meta_y[buf ^ 1][t] = nref.y;
+      meta_m[buf ^ 1][t] = nref.m;
+    }
+    if (t == 0) s_q[buf] = after;  // every thread read s_q before the first barrier
+    __syncthreads();  // Tb consumed, exchange filled, next step's rows known
+    if (next < nsteps) {
+      issue_y(buf ^ 1);
+      if (RESID) issue_T(next);
+    }
+    cp_async_commit();
     // pass B (+ residual) and the first pass of the backward row transform;
-    // RPC*A <= kRowNT so each thread has at most one item
+    // each thread has at most one item
     const int r = t / A, k1 = t % A, q = base + r;
     const bool has = (t < RPC * A) && (q < nitems);
     float racc = 0.f;
@@ -480,9 +504,8 @@ __global__ void __launch_bounds__(kRowNT)
     }
     if constexpr (RESID) __syncthreads();  // exchange reused by the backward pass
     if (has) {
-      const int g = q / C;
-      const bool full = RESID ? (ai.row_full[g] != 0) : true;
       if constexpr (RESID) {
+        const bool full = meta_m[buf][r] == nullptr;
         dft<B>(v);  // v[k2] = X[k1 + A*k2]
 #pragma unroll
         for (int k2 = 0; k2 < B; ++k2) {
@@ -545,7 +568,7 @@ __global__ void __launch_bounds__(kRowNT)
         __shared__ float fm[kFmeanCopy];
         if (t < kFmeanCopy && t < st->miniter) fm[t] = __ldcg(ai.fmean + t);
         // loads of each batch are issued together; the summation order is fixed
-        constexpr int U = 8;
+        constexpr int U = 16;
         double su2 = 0.0, sud = 0.0, sr2 = 0.0;
         const double2* ptv = reinterpret_cast<const double2*>(ai.part_tv);
         const int ntv = ai.ntv;
@@ -563,15 +586,15 @@ __global__ void __launch_bounds__(kRowNT)
           }
         }
         const int npr = nst * kRowWarps;
-        for (int i0 = 0; i0 < npr; i0 += U * kRowNT) {
-          double vv[U];
+        for (int i0 = 0; i0 < npr; i0 += 2 * U * kRowNT) {
+          double vv[2 * U];
 #pragma unroll
-          for (int u = 0; u < U; ++u) {
+          for (int u = 0; u < 2 * U; ++u) {
             const int i = i0 + u * kRowNT + t;
             vv[u] = (i < npr) ? __ldcg(ai.part_r + i) : 0.0;
           }
 #pragma unroll
-          for (int u = 0; u < U; ++u) sr2 += vv[u];
+          for (int u = 0; u < 2 * U; ++u) sr2 += vv[u];
         }
         su2 = block_sum<kRowNT>(su2, sred);
         sud = block_sum<kRowNT>(sud, sred);
@@ -591,8 +614,8 @@ __global__ void __launch_bounds__(kRowNT)
   // the last CTA to finish resets the step counter for the next launch
   if (t == 0) {
     __threadfence();
-    const unsigned tk = atomicAdd(&ctl->ticket, 1u);
-    if (tk == gridDim.x - 1) {
+    s_last = (atomicAdd(&ctl->ticket, 1u) == gridDim.x - 1) ? 1 : 0;
+    if (s_last) {
       ctl->row_next = 0;
       ctl->ticket = 0;
     }
@@ -618,8 +641,7 @@ struct InvColsSmem {
   static constexpr int S_OFF = 0;                        // float2 [2][H][kWB]
   static constexpr int T_OFF = S_OFF + 2 * H * kWB;      // float2 [2][RCAP][kWB] (kept rows, compact)
   static constexpr int EX_OFF = T_OFF + 2 * RCAP * kWB;  // float2 [B*KS]
-  static constexpr int TW_OFF = EX_OFF + B * KS;         // float2 [H]
-  static constexpr int F2_END = TW_OFF + H;
+  static constexpr int F2_END = EX_OFF + B * KS;
   static constexpr int BYTES = F2_END * 8 + H * 4;
   static_assert(cdiv(kWB * B, kColNT) * A * kColNT <= 2 * H * kWB, "accumulator exchange must fit the S buffers");
 };
@@ -635,7 +657,6 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT)
   float2* Sb = reinterpret_cast<float2*>(smem4) + L::S_OFF;
   float2* Tb = reinterpret_cast<float2*>(smem4) + L::T_OFF;
   float2* ex = reinterpret_cast<float2*>(smem4) + L::EX_OFF;
-  float2* tw = reinterpret_cast<float2*>(smem4) + L::TW_OFF;
   int* rmap = reinterpret_cast<int*>(reinterpret_cast<float2*>(smem4) + L::F2_END);
   namespace cgr = cooperative_groups;
   cgr::cluster_group cluster = cgr::this_cluster();
@@ -672,10 +693,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT)
     }
   };
   if (cbeg < cend) issue_S(cbeg, 0);
-  for (int i = t; i < H; i += kColNT) {
-    tw[i] = a.twH[H + i];
-    rmap[i] = a.rowmap[f * H + i];
-  }
+  for (int i = t; i < H; i += kColNT) rmap[i] = a.rowmap[f * H + i];
   grid_dep_wait();  // T and the scalar state come from the row pass
   grid_dep_release();
   if (UPDATE && it > st->last_iter) {  // uniform over the instance, so over each cluster
@@ -699,7 +717,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT)
     const int i = t + ii * kColNT;
     const int s = (i < N1) ? i / kWB : 0;
 #pragma unroll
-    for (int k1p = 0; k1p < B; ++k1p) twr[ii][k1p] = tw[k1p * A + s];
+    for (int k1p = 0; k1p < B; ++k1p) twr[ii][k1p] = __ldg(a.twH + H + k1p * A + s);
   }
 
   for (int c = cbeg; c < cend; ++c) {

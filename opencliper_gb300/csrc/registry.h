@@ -23,6 +23,7 @@ struct SizeKernels {
   void (*fft_cols)(const float2* in, float2* out, int W, int nimg, int inv, float scale, const float2* tw,
                    cudaStream_t s);
   int rows_per_cta;  // rows processed per CTA step by the row kernels
+  int (*rows_occupancy)(bool resid);  // resident row-kernel CTAs per SM
 };
 
 // Returns the table entry for length L or nullptr when L is unsupported.

@@ -34,8 +34,9 @@ int run_prepare(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm);
 FusedArgs make_args(gbn_problem* P, float2* xref);
 BatchMap single_map(int F, ClassCtl* ctl);
 
-// grid of the persistent row pass for `steps` row-pass steps
-int row_grid(gbn_ctx* ctx, long long steps);
+// grid of the persistent row pass (length-W kernels `kw`) for `steps` steps:
+// at most as many CTAs as fit on the GPU at once
+int row_grid(gbn_ctx* ctx, const SizeKernels* kw, bool resid, long long steps);
 
 int launch_store_args(FusedArgs* dst, const FusedArgs& a, cudaStream_t s);
 int launch_group_init(const FusedArgs* tab, int n, int rows_per_cta, ClassCtl* ctl, cudaStream_t s);
