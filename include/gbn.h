@@ -254,6 +254,22 @@ GBN_API int gbn_batch_run(gbn_ctx* ctx, int n, gbn_problem* const* problems, con
 GBN_API int gbn_graph_capture(gbn_batch* b);
 GBN_API int gbn_graph_replay(gbn_batch* b);
 
+/* ------------------------------------------------------------------------ */
+/* Launch-shape autotuner (no reference counterpart).                        */
+/* ------------------------------------------------------------------------ */
+/* For each shape (W, H, F, C) of `shapes` (n x 4 ints) times the run-time
+ * launch shapes (coils per forward-column CTA, row-pass CTAs per SM) on a
+ * synthetic problem and keeps the fastest in the context; later runs and
+ * batches of that shape use it (the nearest tuned F, C of the same W, H
+ * otherwise).  With a cache_path, shapes found in that text file are loaded
+ * instead of measured and new results are appended.  The drand48 state is
+ * left unchanged. */
+GBN_API int gbn_autotune(gbn_ctx* ctx, int n, const int* shapes, const char* cache_path);
+/* loads a cache file written by gbn_autotune */
+GBN_API int gbn_autotune_load(gbn_ctx* ctx, const char* cache_path);
+/* launch shapes a run of this shape would use */
+GBN_API int gbn_autotune_lookup(gbn_ctx* ctx, int W, int H, int F, int C, int* k1_coils_per_block, int* k2_ctas_per_sm);
+
 #ifdef __cplusplus
 }
 #endif

@@ -106,6 +106,9 @@ SIGNATURES: dict[str, list] = {
     "gbn_batch_run": [_vp, _i, C.POINTER(_vp), C.POINTER(NestaParams), C.POINTER(_vp), _i, C.POINTER(NestaStats)],
     "gbn_graph_capture": [_vp],
     "gbn_graph_replay": [_vp],
+    "gbn_autotune": [_vp, _i, _vp, C.c_char_p],
+    "gbn_autotune_load": [_vp, C.c_char_p],
+    "gbn_autotune_lookup": [_vp, _i, _i, _i, _i, C.POINTER(_i), C.POINTER(_i)],
 }
 _RESTYPE = {"gbn_last_error_string": C.c_char_p}
 

@@ -121,6 +121,21 @@ class Context:
     def set_tuning(self, key: str, value: int) -> None:
         call("gbn_ctx_set_tuning", self.handle, key.encode(), int(value))
 
+    def autotune(self, shapes, cache_path: str | None = None) -> None:
+        """gbn_autotune over shapes [(W, H, F, C), ...]."""
+        flat = np.ascontiguousarray(np.asarray(shapes, np.int32).reshape(-1, 4))
+        call("gbn_autotune", self.handle, int(flat.shape[0]), flat.ctypes.data,
+             cache_path.encode() if cache_path else None)
+
+    def autotune_load(self, cache_path: str) -> None:
+        call("gbn_autotune_load", self.handle, cache_path.encode())
+
+    def tuning_for(self, W: int, H: int, F: int, Cc: int) -> tuple[int, int]:
+        """(k1_coils_per_block, k2_ctas_per_sm) a run of this shape uses."""
+        a, b = C.c_int(), C.c_int()
+        call("gbn_autotune_lookup", self.handle, int(W), int(H), int(F), int(Cc), C.byref(a), C.byref(b))
+        return a.value, b.value
+
     def launch_count(self) -> int:
         n = C.c_ulonglong()
         call("gbn_ctx_launch_count", self.handle, C.byref(n))

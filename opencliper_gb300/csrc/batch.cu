@@ -183,7 +183,7 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
     memset(&g.bm, 0, sizeof(g.bm));
     g.bm.n = ng;
     g.bm.ctl = g.ctl;
-    int frames = 0, maxC = 1;
+    int frames = 0, maxC = 1, maxF = 2;
     long long steps = 0;
     for (int k = 0; k < ng; ++k) {
       const int i = g.idx[k];
@@ -191,16 +191,19 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
       g.bm.fbase[k] = frames;
       frames += P->F;
       maxC = std::max(maxC, P->C);
+      maxF = std::max(maxF, P->F);
       steps += ((long long)P->F * P->H * P->C + kw->rows_per_cta - 1) / kw->rows_per_cta;
       g.maxIntIter = std::max(g.maxIntIter, b->prm[i].maxIntIter);
       g.maxIter = std::max(g.maxIter, b->prm[i].maxIter);
       ctx->launches += launch_store_args(g.tab + k, make_args(P, b->out[i]), ctx->stream);
     }
     g.bm.fbase[ng] = frames;
-    g.cpb = std::max(1, std::min(ctx->k1_coils_per_block, maxC));
+    int cpb, k2;
+    tuning_for(ctx, g.W, g.H, maxF, maxC, &cpb, &k2);
+    g.cpb = std::max(1, std::min(cpb, maxC));
     g.g1 = dim3(g.W / kWB, (maxC + g.cpb - 1) / g.cpb, frames);
-    g.g2 = row_grid(ctx, kw, true, steps);
-    g.g2a = row_grid(ctx, kw, false, steps);
+    g.g2 = row_grid(ctx, kw, true, steps, k2);
+    g.g2a = row_grid(ctx, kw, false, steps, k2);
     g.g3 = dim3(g.W / kWB, 2, frames);
   }
   if (rc == GBN_OK && (e = cudaGetLastError()) != cudaSuccess) rc = cuda_status(e, "batch tables");

@@ -30,6 +30,9 @@ int batch_capture(gbn_batch*);
 int batch_stats(gbn_batch*, int, gbn_nesta_stats*);
 int batch_destroy(gbn_batch*);
 gbn_ctx* batch_ctx(gbn_batch*);
+int autotune(gbn_ctx*, int, const int*, const char*);
+int autotune_load(gbn_ctx*, const char*);
+void tuning_for(gbn_ctx*, int, int, int, int, int*, int*);
 int read_stats(gbn_problem*, cudaStream_t, gbn_nesta_stats*);
 
 namespace {
@@ -624,5 +627,22 @@ int gbn_batch_run(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_n
 
 int gbn_graph_capture(gbn_batch* b) { return gbn_batch_capture(b); }
 int gbn_graph_replay(gbn_batch* b) { return gbn_batch_launch(b); }
+
+int gbn_autotune(gbn_ctx* ctx, int n, const int* shapes, const char* cache_path) {
+  CHECK_CTX(ctx);
+  return autotune(ctx, n, shapes, cache_path);
+}
+
+int gbn_autotune_load(gbn_ctx* ctx, const char* cache_path) {
+  CHECK_CTX(ctx);
+  return autotune_load(ctx, cache_path);
+}
+
+int gbn_autotune_lookup(gbn_ctx* ctx, int W, int H, int F, int C, int* k1_coils_per_block, int* k2_ctas_per_sm) {
+  CHECK_CTX(ctx);
+  if (!k1_coils_per_block || !k2_ctas_per_sm) return set_error(GBN_ERR_INVALID, "null output pointer");
+  tuning_for(ctx, W, H, F, C, k1_coils_per_block, k2_ctas_per_sm);
+  return GBN_OK;
+}
 
 }  // extern "C"

@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <map>
 #include <string>
+#include <tuple>
 #include <vector>
 
 #include "gbn.h"
@@ -24,6 +25,13 @@ struct gbn_ctx {
   size_t scratch_bytes = 0;
   int k1_coils_per_block = 4;         // tuning: coils per CTA in the forward column pass
   int k2_ctas_per_sm = 4;             // tuning: persistent CTAs per SM in the row pass
+  // autotuned launch shapes per problem shape (W, H, F, C) (autotune.cu)
+  struct Tuned {
+    int cpb, k2;
+    float us;  // measured time per inner iteration
+  };
+  std::map<std::tuple<int, int, int, int>, Tuned> tuned;
+  bool use_tuned = true;
   unsigned long long launches = 0;    // kernels launched by this context
   // event profiling of kernel groups (reference: ProcessCore::getKernelGroupExecutionTimes)
   bool profile = false;

@@ -588,8 +588,8 @@ int run_prepare(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm) {
   return GBN_OK;
 }
 
-int row_grid(gbn_ctx* ctx, const SizeKernels* kw, bool resid, long long steps) {
-  const int per_sm = std::max(1, std::min(ctx->k2_ctas_per_sm, kw->rows_occupancy(resid)));
+int row_grid(gbn_ctx* ctx, const SizeKernels* kw, bool resid, long long steps, int k2_per_sm) {
+  const int per_sm = std::max(1, std::min(k2_per_sm, kw->rows_occupancy(resid)));
   return int(std::max<long long>(1, std::min<long long>(steps, (long long)ctx->nsm * per_sm)));
 }
 
@@ -678,10 +678,12 @@ int nesta_run(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, float2*
   const SizeKernels* kw = find_size(P->W);
   const int W = P->W, H = P->H, F = P->F, C = P->C;
   cudaStream_t s = ctx->stream;
-  const int cpb = std::max(1, std::min(ctx->k1_coils_per_block, C));
+  int cpb, k2;
+  tuning_for(ctx, W, H, F, C, &cpb, &k2);
+  cpb = std::max(1, std::min(cpb, C));
   const dim3 g1(W / kWB, (C + cpb - 1) / cpb, F);
   const long long steps = ((long long)F * H * C + kw->rows_per_cta - 1) / kw->rows_per_cta;
-  const int g2 = row_grid(ctx, kw, true, steps), g2a = row_grid(ctx, kw, false, steps);
+  const int g2 = row_grid(ctx, kw, true, steps, k2), g2a = row_grid(ctx, kw, false, steps, k2);
   const dim3 g3(W / kWB, 2, F);  // clusters of 2 along y
   const FusedArgs a = make_args(P, x_out);
   const FusedArgs* tab = P->d_args;
@@ -768,7 +770,7 @@ int simple_recon_in(gbn_ctx* ctx, void* ws, const float2* y, const float2* S, fl
   a.s_adj = 1.0f / float(W * H);  // clFFT BACKWARD scale
   a.ntv = F * (W / kWB);
   const long long steps = ((long long)FH * C + kw->rows_per_cta - 1) / kw->rows_per_cta;
-  const int g2 = row_grid(ctx, kw, false, steps);
+  const int g2 = row_grid(ctx, kw, false, steps, ctx->k2_ctas_per_sm);
   const BatchMap bm = single_map(F, ctl);
   GBN_LAUNCH(ctx, GBN_PROF_SETUP, 5, {
     k_rows_identity<<<int(std::min<size_t>((FH + 255) / 256, 1024)), 256, 0, s>>>(H, F, rowmap, rowoff, rows_h, rows_f,

@@ -35,8 +35,12 @@ FusedArgs make_args(gbn_problem* P, float2* xref);
 BatchMap single_map(int F, ClassCtl* ctl);
 
 // grid of the persistent row pass (length-W kernels `kw`) for `steps` steps:
-// at most as many CTAs as fit on the GPU at once
-int row_grid(gbn_ctx* ctx, const SizeKernels* kw, bool resid, long long steps);
+// at most k2_per_sm CTAs per SM and no more than fit on the GPU at once
+int row_grid(gbn_ctx* ctx, const SizeKernels* kw, bool resid, long long steps, int k2_per_sm);
+
+// launch shapes for a problem shape: autotuned entry (exact, else nearest of
+// the same W, H) or the context's defaults (autotune.cu)
+void tuning_for(gbn_ctx* ctx, int W, int H, int F, int C, int* k1_coils_per_block, int* k2_ctas_per_sm);
 
 int launch_store_args(FusedArgs* dst, const FusedArgs& a, cudaStream_t s);
 int launch_group_init(const FusedArgs* tab, int n, int rows_per_cta, ClassCtl* ctl, cudaStream_t s);

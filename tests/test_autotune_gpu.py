@@ -1,0 +1,63 @@
+"""Launch-shape autotuner (gbn_autotune): chosen shapes are valid candidates,
+the cache file round-trips, tuning leaves the drand48 state alone, and a run
+with tuned shapes gives the same image as one with the defaults (launch shapes
+change how work is cut into CTAs, never the arithmetic)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import opencliper_gb300 as g
+from opencliper_gb300 import synth
+
+pytestmark = pytest.mark.gpu
+
+
+def test_autotune_cache_roundtrip_and_results(tmp_path):
+    shapes = [(32, 32, 6, 5), (48, 40, 4, 3)]
+    cache = tmp_path / "tune.txt"
+    with g.Context(0) as ctx:
+        r0 = ctx.rand48()
+        ctx.autotune(shapes, str(cache))
+        assert ctx.rand48() == r0
+        tuned = {s: ctx.tuning_for(*s) for s in shapes}
+        for (W, H, F, C), (cpb, k2) in tuned.items():
+            assert cpb in (1, 2, 3, 4, 6, 8) and cpb <= C
+            assert 1 <= k2 <= 8
+        lines = [ln for ln in cache.read_text().splitlines() if not ln.startswith("#")]
+        assert len(lines) == len(shapes)
+        # same image with tuned shapes and with every other candidate pair
+        p = synth.make_problem(32, 32, 6, 5, 4, seed=3)
+        dy, dS, dm = ctx.to_device(p.y), ctx.to_device(p.S), ctx.to_device(p.mask)
+        prob = g.Problem(ctx, dy, dS, dm)
+        prm = g.nesta_params(lambda_i=0.01, mu_f=1e-3, maxIntIter=1, maxIter=20, stoptest=0)
+        x = ctx.empty((6, 32, 32), np.complex64)
+        ctx.seed48((1, 2, 3))
+        prob.run(prm, x)
+        ref = x.get()
+        prob.close()
+    with g.Context(0) as ctx2:
+        ctx2.autotune_load(str(cache))
+        assert {s: ctx2.tuning_for(*s) for s in shapes} == tuned
+        # nearest entry of the same transform lengths for an untuned shape
+        assert ctx2.tuning_for(32, 32, 7, 5) == tuned[(32, 32, 6, 5)]
+        dy, dS, dm = ctx2.to_device(p.y), ctx2.to_device(p.S), ctx2.to_device(p.mask)
+        prob2 = g.Problem(ctx2, dy, dS, dm)
+        x2 = ctx2.empty((6, 32, 32), np.complex64)
+        for cpb in (1, 2, 5):
+            for k2 in (1, 3):
+                ctx2.set_tuning("k1_coils_per_block", cpb)
+                ctx2.set_tuning("k2_ctas_per_sm", k2)
+                ctx2.autotune_load(str(cache))  # tuned entry still wins for this shape
+                ctx2.seed48((1, 2, 3))
+                prob2.run(prm, x2)
+                assert np.array_equal(x2.get(), ref)
+        prob2.close()
+
+
+def test_autotune_rejects_bad_shapes():
+    with g.Context(0) as ctx:
+        with pytest.raises(g.GbnError):
+            ctx.autotune([(30, 32, 4, 2)])  # width not a multiple of 8
+        with pytest.raises(g.GbnError):
+            ctx.autotune_load("/nonexistent/tune.txt")
