@@ -206,6 +206,7 @@ typedef struct gbn_nesta_stats {
   int inner_iters;    /* inner iterations executed, all outer loops */
   int normest_iters;
   int kept_rows;      /* k-space rows carried by the solver (sampled or nonzero) */
+  int status;         /* 0; nonzero when the device reported a failure of this run */
 } gbn_nesta_stats;
 
 /* Binds the caller's device buffers (not copied, not modified):
@@ -229,7 +230,7 @@ GBN_API int gbn_nesta_run_host(gbn_ctx* ctx, int W, int H, int F, int C, const f
 /* problems one after another in batch order (power-method draws included).  */
 /* ------------------------------------------------------------------------ */
 #define GBN_PRECISION_FP32 0  /* complex64 data and arithmetic, as the reference */
-#define GBN_PRECISION_MIXED 1 /* reduced-precision storage (not available in this build) */
+#define GBN_PRECISION_MIXED 1 /* forward column transform on the tensor cores with split fp16 operands */
 
 /* Plans n reconstructions: problems[i] (from gbn_problem_create on ctx, each
  * at most once), params[i], output image d_outputs[i] ([F][H][W] complex).

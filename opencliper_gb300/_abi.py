@@ -44,7 +44,7 @@ class NestaStats(C.Structure):
                 ("lambda_", C.c_float), ("muf", C.c_float), ("mu0", C.c_float),
                 ("mu_final", C.c_float), ("tolVar_final", C.c_float), ("fx_final", C.c_float),
                 ("qp_final", C.c_float), ("inner_iters", C.c_int), ("normest_iters", C.c_int),
-                ("kept_rows", C.c_int)]
+                ("kept_rows", C.c_int), ("status", C.c_int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -2,6 +2,7 @@
 from __future__ import annotations
 
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -25,6 +26,7 @@ class DeviceArray:
         else:
             self._owned = False
         self.ptr = int(ptr)
+        ctx._children.add(self)
 
     @property
     def size(self) -> int:
@@ -67,9 +69,17 @@ class Context:
         call("gbn_ctx_create", int(device), C.byref(h))
         self.handle = h.value
         self.device = device
+        self._children = weakref.WeakSet()  # batches, problems and arrays of this context
 
     def close(self) -> None:
         if self.handle:
+            # objects that refer to the context go first, whatever order the
+            # garbage collector would pick
+            kids = list(self._children)
+            for kind in (Batch, Problem, DeviceArray):
+                for k in kids:
+                    if isinstance(k, kind):
+                        k.close() if kind is not DeviceArray else k.free()
             call("gbn_ctx_destroy", self.handle)
             self.handle = None
 
@@ -241,6 +251,7 @@ class Problem:
         self.handle = h.value
         self.ctx, self.shape = ctx, (F, Cc, H, W)
         self._keep = (y, S, mask)
+        ctx._children.add(self)
 
     def run(self, params: NestaParams, out: DeviceArray, stats: bool = True) -> dict | None:
         st = NestaStats() if stats else None
@@ -284,6 +295,7 @@ class Batch:
         self.handle = h.value
         self.ctx, self.n = ctx, n
         self._keep = (problems, outputs)
+        ctx._children.add(self)
 
     def capture(self) -> None:
         call("gbn_batch_capture", self.handle)

@@ -40,6 +40,7 @@ struct gbn_batch {
     gbn::ClassCtl* ctl = nullptr;
     gbn::BatchMap bm{};
     int cpb = 1, g2 = 1, g2a = 1;  // row grids with / without the residual
+    int npad_max = 0;              // mixed form: widest DFT operand of the group
     dim3 g1, g3;
     unsigned maxIntIter = 0, maxIter = 0;
     cudaStream_t stream = nullptr;
@@ -52,6 +53,14 @@ struct gbn_batch {
 };
 
 namespace gbn {
+
+// mixed-precision form (mixed.cu)
+int mixed_prepare(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params& prm);
+void mixed_args(gbn_problem* P, FusedArgs* a);
+int launch_mixed_setup(gbn_ctx* ctx, gbn_problem* P, cudaStream_t s);
+int launch_mixed_colmax(gbn_problem* P, cudaStream_t s);
+dim3 fwd_cols_tc_grid(int W, int maxC, int frames);
+void launch_fwd_cols_tc(const FusedArgs* tab, const BatchMap& bm, int it, int npad_max, dim3 grid, cudaStream_t s);
 
 namespace {
 
@@ -79,7 +88,11 @@ int batch_enqueue(gbn_batch* b, bool graph_mode) {
     cudaStream_t s = g.stream;
     const SizeKernels* kh = find_size(g.H);
     const SizeKernels* kw = find_size(g.W);
-    for (int i : g.idx) n_launch += launch_pre(b->probs[i], b->prm[i], s);
+    const bool mixed = b->precision == GBN_PRECISION_MIXED;
+    for (int i : g.idx) {
+      n_launch += launch_pre(b->probs[i], b->prm[i], s);
+      if (mixed) n_launch += launch_mixed_setup(ctx, b->probs[i], s);
+    }
     n_launch += launch_group_init(g.tab, int(g.idx.size()), kw->rows_per_cta, g.ctl, s);
     // x0 = E^H y of all members (NestaUp.cpp:465-486)
     kw->rows(g.tab, g.bm, 0, false, g.g2a, s);
@@ -92,9 +105,15 @@ int batch_enqueue(gbn_batch* b, bool graph_mode) {
       n_launch += launch_constants(ctx, b->probs[i], b->out[i], rs, s);
     }
     for (unsigned nl = 1; nl <= g.maxIntIter; ++nl) {
-      for (int i : g.idx) n_launch += launch_outer_begin(ctx, b->probs[i], int(nl), b->out[i], s);
+      for (int i : g.idx) {
+        n_launch += launch_outer_begin(ctx, b->probs[i], int(nl), b->out[i], s);
+        if (mixed) n_launch += launch_mixed_colmax(b->probs[i], s);
+      }
       for (unsigned it = 0; it < g.maxIter; ++it) {
-        kh->fwd_cols(g.tab, g.bm, int(it), g.cpb, g.g1, s);
+        if (mixed)
+          launch_fwd_cols_tc(g.tab, g.bm, int(it), g.npad_max, g.g1, s);
+        else
+          kh->fwd_cols(g.tab, g.bm, int(it), g.cpb, g.g1, s);
         kw->rows(g.tab, g.bm, int(it), true, g.g2, s);
         kh->inv_cols(g.tab, g.bm, int(it), true, g.g3, s);
         n_launch += 3;
@@ -115,8 +134,8 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
                  float* const* outputs, int precision, gbn_batch** out) {
   if (!ctx || !problems || !params || !outputs || !out) return set_error(GBN_ERR_INVALID, "null argument");
   if (n <= 0) return set_error(GBN_ERR_INVALID, "batch needs at least one problem");
-  if (precision != GBN_PRECISION_FP32)
-    return set_error(GBN_ERR_UNSUPPORTED, "precision mode not available in this build (use GBN_PRECISION_FP32)");
+  if (precision != GBN_PRECISION_FP32 && precision != GBN_PRECISION_MIXED)
+    return set_error(GBN_ERR_INVALID, "unknown precision mode");
   *out = nullptr;
   gbn_batch* b = new gbn_batch();
   b->ctx = ctx;
@@ -138,6 +157,7 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
       if (problems[j] == P) rc = set_error(GBN_ERR_INVALID, "a problem appears twice in the batch");
     if (rc != GBN_OK) break;
     if ((rc = run_prepare(ctx, P, &params[i])) != GBN_OK) break;
+    if (precision == GBN_PRECISION_MIXED && (rc = mixed_prepare(ctx, P, params[i])) != GBN_OK) break;
     b->probs.push_back(P);
     b->prm.push_back(params[i]);
     b->out.push_back(reinterpret_cast<float2*>(outputs[i]));
@@ -195,13 +215,19 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
       steps += ((long long)P->F * P->H * P->C + kw->rows_per_cta - 1) / kw->rows_per_cta;
       g.maxIntIter = std::max(g.maxIntIter, b->prm[i].maxIntIter);
       g.maxIter = std::max(g.maxIter, b->prm[i].maxIter);
-      ctx->launches += launch_store_args(g.tab + k, make_args(P, b->out[i]), ctx->stream);
+      FusedArgs fa = make_args(P, b->out[i]);
+      if (precision == GBN_PRECISION_MIXED) {
+        mixed_args(P, &fa);
+        g.npad_max = std::max(g.npad_max, P->npad);
+      }
+      ctx->launches += launch_store_args(g.tab + k, fa, ctx->stream);
     }
     g.bm.fbase[ng] = frames;
     int cpb, k2;
     tuning_for(ctx, g.W, g.H, maxF, maxC, &cpb, &k2);
     g.cpb = std::max(1, std::min(cpb, maxC));
-    g.g1 = dim3(g.W / kWB, (maxC + g.cpb - 1) / g.cpb, frames);
+    g.g1 = (precision == GBN_PRECISION_MIXED) ? fwd_cols_tc_grid(g.W, maxC, frames)
+                                              : dim3(g.W / kWB, (maxC + g.cpb - 1) / g.cpb, frames);
     g.g2 = row_grid(ctx, kw, true, steps, k2);
     g.g2a = row_grid(ctx, kw, false, steps, k2);
     g.g3 = dim3(g.W / kWB, 2, frames);

@@ -74,6 +74,12 @@ struct gbn_problem {
   int part_ne_cap = 0;
   float* ne_b = nullptr;              // power-method frame vectors between chunks [F][N]
   int ne_b_cap = 0;
+  // mixed-precision form (mixed.cu)
+  unsigned char* fk = nullptr;        // kept-row DFT operand
+  size_t fk_bytes = 0;
+  float* colmax = nullptr;            // [2][F][W]
+  float* smax = nullptr;              // [C][W]
+  int npad = 0, nch = 0;
   gbn::FusedArgs* d_args = nullptr;   // one-entry instance table of the fused kernels
   gbn::ClassCtl* ctl = nullptr;       // row-pass control block
 };

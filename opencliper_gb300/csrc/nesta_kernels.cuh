@@ -818,6 +818,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT)
     const size_t offm = size_t((f + F - 1) % F) * N, off0 = size_t(f) * N, offp = size_t((f + 1) % F) * N;
     const float inv_mu = 1.0f / st->mu, lambda = st->lambda, nLmu1 = -st->Lmu1, apk = st->apk, tauk = st->tauk;
     const float omt = 1.0f - tauk;
+    float cmx = 0.f;  // max |x_{k+1}|^2 of this thread's column (mixed form)
     constexpr int BATCH = 4;  // outputs whose global loads are issued together
 #pragma unroll
     for (int ii = 0; ii < NI2; ++ii) {
@@ -858,10 +859,20 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT)
               const float2 xnew = make_float2(fmaf(omt, yk.x, tauk * zk.x), fmaf(omt, yk.y, tauk * zk.y));
               a.wacc[off0 + p] = wn;
               xn[off0 + p] = xnew;
+              cmx = fmaxf(cmx, fmaf(xnew.x, xnew.x, xnew.y * xnew.y));
             }
           }
         }
       }
+    }
+    if (a.colmax) {
+      // column maxima for the next tensor-core forward pass: lanes l, l^8,
+      // l^16, l^24 share a column (i % kWB)
+      cmx = fmaxf(cmx, __shfl_xor_sync(0xffffffffu, cmx, 8));
+      cmx = fmaxf(cmx, __shfl_xor_sync(0xffffffffu, cmx, 16));
+      if ((t & 31) < kWB)
+        atomicMax(reinterpret_cast<unsigned int*>(a.colmax) + size_t((it + 1) & 1) * F * W + size_t(f) * W + w0 + (t & 31),
+                  __float_as_uint(sqrtf(cmx)));
     }
   }
 }

@@ -70,7 +70,12 @@ struct FusedArgs {
   const float2* twW;
   float s_fwd;            // 1/sqrt(N) as the reference computes it (double -> float)
   float s_adj;            // sqrt(N)/N: the reference's sqrt(N) pre-scale times clFFT's 1/N
-  int ntv;                // F * (W / 8): number of tTV partial sums
+  int ntv;                // number of tTV partial sums (F * W/8; mixed form F * ceil(W/32))
+  // mixed-precision form (nullptr / 0 otherwise)
+  const unsigned char* fk;  // kept-row DFT operand, fp16 hi/lo, per frame and chunk
+  float* colmax;          // [2][F][W] column maxima of |x_k| (iteration parity)
+  const float* smax;      // [C][W] column maxima of |S_c|
+  int npad, nch;          // operand rows (2G padded to 16) and K chunks
 };
 
 // Instances covered by one launch of the fused kernels.  All of them share the
