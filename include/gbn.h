@@ -88,7 +88,9 @@ GBN_API int gbn_ctx_sync(gbn_ctx* ctx);
  * (glibc's default state, as if seed48 were never called). */
 GBN_API int gbn_ctx_seed48(gbn_ctx* ctx, const unsigned short seed16v[3]);
 GBN_API int gbn_ctx_get_rand48(gbn_ctx* ctx, unsigned short state16v[3]);
-/* tuning knobs: "k1_coils_per_block", "k2_ctas_per_sm" */
+/* tuning knobs: "k1_coils_per_block", "k2_ctas_per_sm" (>= 1) and
+ * "mixed_adjoint_tc" (0/1: the mixed form also runs the adjoint column pass on
+ * the tensor cores; read when a batch is created) */
 GBN_API int gbn_ctx_set_tuning(gbn_ctx* ctx, const char* key, int value);
 /* number of kernels this context has launched so far */
 GBN_API int gbn_ctx_launch_count(gbn_ctx* ctx, unsigned long long* count);
@@ -230,7 +232,7 @@ GBN_API int gbn_nesta_run_host(gbn_ctx* ctx, int W, int H, int F, int C, const f
 /* problems one after another in batch order (power-method draws included).  */
 /* ------------------------------------------------------------------------ */
 #define GBN_PRECISION_FP32 0  /* complex64 data and arithmetic, as the reference */
-#define GBN_PRECISION_MIXED 1 /* forward column transform on the tensor cores with split fp16 operands */
+#define GBN_PRECISION_MIXED 1 /* column transforms on the tensor cores (split fp16 operands, FP32 accumulation) */
 
 /* Plans n reconstructions: problems[i] (from gbn_problem_create on ctx, each
  * at most once), params[i], output image d_outputs[i] ([F][H][W] complex).

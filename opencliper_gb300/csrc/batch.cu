@@ -40,7 +40,10 @@ struct gbn_batch {
     gbn::ClassCtl* ctl = nullptr;
     gbn::BatchMap bm{};
     int cpb = 1, g2 = 1, g2a = 1;  // row grids with / without the residual
-    int npad_max = 0;              // mixed form: widest DFT operand of the group
+    int npad_max = 0;              // mixed form: widest forward DFT operand of the group
+    int nmax_ac = 0;               // mixed form: widest adjoint B operand of the group
+    dim3 g3tc;                     // mixed form: grid of the adjoint tensor-core kernel
+    bool adjoint_tc = false;       // mixed form: adjoint column pass on the tensor cores
     dim3 g1, g3;
     unsigned maxIntIter = 0, maxIter = 0;
     cudaStream_t stream = nullptr;
@@ -55,7 +58,10 @@ struct gbn_batch {
 namespace gbn {
 
 // mixed-precision form (mixed.cu)
-int mixed_prepare(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params& prm);
+int mixed_prepare(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params& prm, const float2* out);
+int inv_cols_tc_rows(int C);
+dim3 inv_cols_tc_grid(int W, int H, int frames);
+void launch_inv_cols_tc(const FusedArgs* tab, const BatchMap& bm, int it, int nmax, dim3 grid, cudaStream_t s);
 void mixed_args(gbn_problem* P, FusedArgs* a);
 int launch_mixed_setup(gbn_ctx* ctx, gbn_problem* P, cudaStream_t s);
 int launch_mixed_colmax(gbn_problem* P, cudaStream_t s);
@@ -115,7 +121,10 @@ int batch_enqueue(gbn_batch* b, bool graph_mode) {
         else
           kh->fwd_cols(g.tab, g.bm, int(it), g.cpb, g.g1, s);
         kw->rows(g.tab, g.bm, int(it), true, g.g2, s);
-        kh->inv_cols(g.tab, g.bm, int(it), true, g.g3, s);
+        if (g.adjoint_tc)
+          launch_inv_cols_tc(g.tab, g.bm, int(it), g.nmax_ac, g.g3tc, s);
+        else
+          kh->inv_cols(g.tab, g.bm, int(it), true, g.g3, s);
         n_launch += 3;
       }
       for (int i : g.idx) n_launch += launch_outer_end(ctx, b->probs[i], b->out[i], s);
@@ -157,7 +166,9 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
       if (problems[j] == P) rc = set_error(GBN_ERR_INVALID, "a problem appears twice in the batch");
     if (rc != GBN_OK) break;
     if ((rc = run_prepare(ctx, P, &params[i])) != GBN_OK) break;
-    if (precision == GBN_PRECISION_MIXED && (rc = mixed_prepare(ctx, P, params[i])) != GBN_OK) break;
+    if (precision == GBN_PRECISION_MIXED &&
+        (rc = mixed_prepare(ctx, P, params[i], reinterpret_cast<const float2*>(outputs[i]))) != GBN_OK)
+      break;
     b->probs.push_back(P);
     b->prm.push_back(params[i]);
     b->out.push_back(reinterpret_cast<float2*>(outputs[i]));
@@ -219,6 +230,7 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
       if (precision == GBN_PRECISION_MIXED) {
         mixed_args(P, &fa);
         g.npad_max = std::max(g.npad_max, P->npad);
+        g.nmax_ac = std::max(g.nmax_ac, inv_cols_tc_rows(P->C));
       }
       ctx->launches += launch_store_args(g.tab + k, fa, ctx->stream);
     }
@@ -231,6 +243,8 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
     g.g2 = row_grid(ctx, kw, true, steps, k2);
     g.g2a = row_grid(ctx, kw, false, steps, k2);
     g.g3 = dim3(g.W / kWB, 2, frames);
+    g.g3tc = inv_cols_tc_grid(g.W, g.H, frames);
+    g.adjoint_tc = precision == GBN_PRECISION_MIXED && ctx->mixed_adjoint_tc != 0;
   }
   if (rc == GBN_OK && (e = cudaGetLastError()) != cudaSuccess) rc = cuda_status(e, "batch tables");
   if (rc != GBN_OK) {

@@ -290,6 +290,11 @@ int gbn_ctx_get_rand48(gbn_ctx* ctx, unsigned short state16v[3]) {
 int gbn_ctx_set_tuning(gbn_ctx* ctx, const char* key, int value) {
   CHECK_CTX(ctx);
   if (!key) return set_error(GBN_ERR_INVALID, "null key");
+  if (!std::strcmp(key, "mixed_adjoint_tc")) {
+    if (value != 0 && value != 1) return set_error(GBN_ERR_INVALID, "mixed_adjoint_tc is 0 or 1");
+    ctx->mixed_adjoint_tc = value;
+    return GBN_OK;
+  }
   if (value < 1) return set_error(GBN_ERR_INVALID, "tuning values must be >= 1");
   if (!std::strcmp(key, "k1_coils_per_block"))
     ctx->k1_coils_per_block = value;

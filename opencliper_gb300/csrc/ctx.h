@@ -25,6 +25,7 @@ struct gbn_ctx {
   size_t scratch_bytes = 0;
   int k1_coils_per_block = 4;         // tuning: coils per CTA in the forward column pass
   int k2_ctas_per_sm = 4;             // tuning: persistent CTAs per SM in the row pass
+  int mixed_adjoint_tc = 0;           // tuning: mixed form runs the adjoint column pass on the tensor cores
   // autotuned launch shapes per problem shape (W, H, F, C) (autotune.cu)
   struct Tuned {
     int cpb, k2;
@@ -80,6 +81,9 @@ struct gbn_problem {
   float* colmax = nullptr;            // [2][F][W]
   float* smax = nullptr;              // [C][W]
   int npad = 0, nch = 0;
+  unsigned char* fa = nullptr;        // adjoint kept-row DFT operand
+  size_t fa_bytes = 0;
+  int ncha = 0;
   gbn::FusedArgs* d_args = nullptr;   // one-entry instance table of the fused kernels
   gbn::ClassCtl* ctl = nullptr;       // row-pass control block
 };

@@ -501,7 +501,7 @@ int problem_alloc(gbn_problem* P) {
 void problem_free(gbn_problem* P) {
   void* ptrs[] = {P->flags, P->full_fh, P->rowmap, P->rowoff,  P->rows_h, P->rows_f,  P->row_full, P->T,
                   P->xk0,   P->xk1,     P->wacc,   P->st,      P->fmean,  P->part_tv, P->part_r,   P->part_ne,
-                  P->ne_b,  P->d_args,  P->ctl,      P->fk,     P->colmax, P->smax};
+                  P->ne_b,  P->d_args,  P->ctl,      P->fk,     P->colmax, P->smax,   P->fa};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }

@@ -75,7 +75,9 @@ struct FusedArgs {
   const unsigned char* fk;  // kept-row DFT operand, fp16 hi/lo, per frame and chunk
   float* colmax;          // [2][F][W] column maxima of |x_k| (iteration parity)
   const float* smax;      // [C][W] column maxima of |S_c|
-  int npad, nch;          // operand rows (2G padded to 16) and K chunks
+  int npad, nch;          // forward operand rows (2G padded to 16) and K chunks
+  const unsigned char* fa;  // adjoint kept-row DFT operand, fp16 hi/lo, per frame, row tile and chunk
+  int ncha;               // adjoint K chunks (32 kept rows each)
 };
 
 // Instances covered by one launch of the fused kernels.  All of them share the

@@ -25,14 +25,19 @@ CASES = [(32, 32, 6, 4, 4, FIXED), (48, 40, 5, 3, 4, FIXED), (64, 64, 8, 5, 2, F
          (96, 64, 6, 6, 4, DRIVER)]
 
 
-@pytest.mark.parametrize("W,H,F,C,Rr,prm", CASES)
-def test_mixed_against_oracle(ctx, W, H, F, C, Rr, prm):
+@pytest.mark.parametrize("adjoint_tc", [0, 1])
+@pytest.mark.parametrize("W,H,F,C,Rr,prm", CASES + [(32, 24, 4, 19, 2, FIXED)])
+def test_mixed_against_oracle(ctx, W, H, F, C, Rr, prm, adjoint_tc):
+    """Forward column pass on the tensor cores, and optionally the adjoint one
+    (C = 19 takes two coil groups through tensor memory)."""
+    ctx.set_tuning("mixed_adjoint_tc", adjoint_tc)
     p = synth.make_problem(W, H, F, C, Rr, seed=40 + W + C)
     dy, dS, dm = ctx.to_device(p.y), ctx.to_device(p.S), ctx.to_device(p.mask)
     prob = g.Problem(ctx, dy, dS, dm)
     x = ctx.empty((F, H, W), np.complex64)
     s0 = drand48.seed16v_to_state(ctx.rand48())
     b = g.Batch(ctx, [prob], g.nesta_params(**prm), [x], precision=g.PRECISION_MIXED)
+    ctx.set_tuning("mixed_adjoint_tc", 0)
     b.launch()
     got = x.get()
     st = b.stats(0)
