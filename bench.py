@@ -285,7 +285,8 @@ def run_ours(args, dist: Dist) -> dict | None:
         a.free()
     forms = {}
     if not args.no_forms and dist.ws == 1:
-        forms["batched_fp32"] = batched_form(ctx, stream)
+        forms["mixed"] = mixed_forms(ctx, stream)
+        forms["batched"] = batched_form(ctx, stream)
     ctx.set_stream(None)
     ctx.close()
     n = dist.ws
@@ -305,14 +306,69 @@ def run_ours(args, dist: Dist) -> dict | None:
 BATCH_WL = dict(n=64, sizes=(128, 192, 256, 320, 384), frames=(12, 40), coils=(8, 32), accel=(4, 12), seed0=1000)
 
 
+def _graph_rate(ctx, stream, batch, n: int, reps: int) -> tuple[float, float]:
+    """(recons/s, ms per replay) of a captured batch, events on the library's stream."""
+    import torch
+    batch.capture()
+    batch.launch()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
+    for k in range(reps):
+        ev[k][0].record(stream)
+        batch.launch()
+        ev[k][1].record(stream)
+    torch.cuda.synchronize()
+    ms = sum(a.elapsed_time(c) for a, c in ev) / reps
+    return n / (ms / 1e3), ms
+
+
+def _nrmse(a: np.ndarray, b: np.ndarray) -> float:
+    return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-30))
+
+
+def mixed_forms(ctx, stream, reps: int = 5) -> dict:
+    """The mixed-precision form (column transforms on the tensor cores, split
+    fp16 operands, FP32 accumulation) against the plain FP32 path on the
+    headline workload and on the 384x384 x 30 frames x 16 coils workload, same
+    inputs and drand48 state for both; NRMSE of the mixed image against the
+    plain FP32 one."""
+    import opencliper_gb300 as g
+    from opencliper_gb300 import synth
+    out = {}
+    for tag, (W, H, F, Cc, Rr) in (("256x256x20c12", (256, 256, 20, 12, 8)), ("384x384x30c16", (384, 384, 30, 16, 8))):
+        p = synth.make_problem_device(ctx, W, H, F, Cc, Rr, seed=7)
+        prob = g.Problem(ctx, p.y, p.S, p.mask)
+        x = ctx.empty((F, H, W), np.complex64)
+        res, imgs = {}, {}
+        for name, prec in (("fp32", g.PRECISION_FP32), ("mixed", g.PRECISION_MIXED)):
+            ctx.seed48((0x330E, 0xABCD, 0x1234))
+            b = g.Batch(ctx, [prob], g.nesta_params(**NESTA), [x], precision=prec)
+            b.launch()
+            imgs[name] = x.get()
+            status = b.stats(0)["status"]
+            rate, ms = _graph_rate(ctx, stream, b, 1, reps)
+            res[name] = {"value": round(rate, 3), "ms_per_recon": round(ms, 3), "status": int(status)}
+            b.close()
+        res["speedup_mixed_over_fp32"] = round(res["mixed"]["value"] / res["fp32"]["value"], 3)
+        res["nrmse_mixed_vs_fp32"] = float(f"{_nrmse(imgs['mixed'], imgs['fp32']):.3e}")
+        res["unit"] = UNIT
+        out[tag] = res
+        prob.close()
+        for a in (p.y, p.S, p.mask, x):
+            a.free()
+    return out
+
+
+BATCH_WL = dict(n=64, sizes=(128, 192, 256, 320, 384), frames=(12, 40), coils=(8, 32), accel=(4, 12), seed0=1000)
+
+
 def batched_form(ctx, stream, reps: int = 2) -> dict:
     """The batched form on the uneven workload: 64 reconstructions, each with
     its own seed 1000+i drawing W=H from {128..384}, F ~ U{12..40},
     C ~ U{8..32}, R ~ U{4..12}, solved by one captured CUDA graph (gbn_batch_*)
-    with the same NESTA settings as the headline workload.  Device-resident
-    inputs; events on the library's stream around each graph replay."""
-    import torch
-
+    with the same NESTA settings as the headline workload, in plain FP32 and in
+    the mixed form.  Device-resident inputs; events on the library's stream
+    around each graph replay."""
     import opencliper_gb300 as g
     from opencliper_gb300 import synth
     B = BATCH_WL
@@ -331,31 +387,27 @@ def batched_form(ctx, stream, reps: int = 2) -> dict:
         arrays += [p.y, p.S, p.mask, x]
         shapes.append((Wd, F, Cc, Rr))
         n_units += Wd * Wd * F * Cc
-    b = g.Batch(ctx, probs, g.nesta_params(**NESTA), outs)
-    b.capture()
-    b.launch()
-    torch.cuda.synchronize()
-    n0 = ctx.launch_count()
-    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(reps)]
-    for k in range(reps):
-        ev[k][0].record(stream)
-        b.launch()
-        ev[k][1].record(stream)
-    torch.cuda.synchronize()
-    ms = sum(a.elapsed_time(c) for a, c in ev) / reps
-    launches = (ctx.launch_count() - n0) // reps
-    kept = sum(b.stats(i)["kept_rows"] for i in range(B["n"]))
-    b.close()
+    res = {"workload": f"{B['n']} uneven reconstructions, W=H in {list(B['sizes'])}, F U{{12..40}}, "
+                       f"C U{{8..32}}, R U{{4..12}}, seeds {B['seed0']}+i, one CUDA graph",
+           "unit": UNIT, "pixel_coil_frames": int(n_units), "sizes_seen": sorted(set(s[0] for s in shapes))}
+    for name, prec in (("fp32", g.PRECISION_FP32), ("mixed", g.PRECISION_MIXED)):
+        try:
+            b = g.Batch(ctx, probs, g.nesta_params(**NESTA), outs, precision=prec)
+        except g.GbnError as e:  # e.g. a frame with more kept rows than the mixed operand takes
+            res[name] = {"unavailable": str(e)}
+            continue
+        n0 = ctx.launch_count()
+        rate, ms = _graph_rate(ctx, stream, b, B["n"], reps)
+        res[name] = {"value": round(rate, 3), "ms_per_batch": round(ms, 2), "reps": reps,
+                     "kept_rows_total": int(sum(b.stats(i)["kept_rows"] for i in range(B["n"]))),
+                     "status_nonzero": int(sum(b.stats(i)["status"] != 0 for i in range(B["n"]))),
+                     "host_launch_calls_per_replay": int((ctx.launch_count() - n0) // (reps + 1))}
+        b.close()
     for pr in probs:
         pr.close()
     for a in arrays:
         a.free()
-    return {"workload": f"{B['n']} uneven reconstructions, W=H in {list(B['sizes'])}, F U{{12..40}}, "
-                        f"C U{{8..32}}, R U{{4..12}}, seeds {B['seed0']}+i, plain FP32, one CUDA graph",
-            "value": round(B["n"] / (ms / 1e3), 3), "unit": UNIT, "ms_per_batch": round(ms, 2),
-            "reps": reps, "pixel_coil_frames": int(n_units), "kept_rows_total": int(kept),
-            "sizes_seen": sorted(set(s[0] for s in shapes)),
-            "host_launch_calls_per_replay": int(launches)}
+    return res
 
 
 def cpu_port_sample(iters: int = 3) -> dict:
