@@ -123,8 +123,35 @@ bool run_case(unsigned seed) {
   return rel < 1e-5;
 }
 
+// An mbarrier that nothing arrives at: the bounded wait gives up and reports
+// it instead of hanging the CTA.
+__global__ void k_wait_gives_up(int* __restrict__ out) {
+  __shared__ uint64_t mbar;
+  if (threadIdx.x == 0) {
+    tc::mbar_init(&mbar, 1);
+    tc::fence_mbar_init();
+  }
+  __syncthreads();
+  const bool done = tc::mbar_wait(&mbar, 0, 1000);
+  if (threadIdx.x == 0) *out = done ? 1 : 2;
+}
+
+bool run_wait_case() {
+  int* d;
+  int h = 0;
+  cudaMalloc(&d, 4);
+  cudaMemset(d, 0, 4);
+  k_wait_gives_up<<<1, 32>>>(d);
+  const cudaError_t e = cudaDeviceSynchronize();
+  cudaMemcpy(&h, d, 4, cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  const bool ok = e == cudaSuccess && h == 2;
+  printf("bounded wait on an mbarrier nobody completes: %s\n", ok ? "gave up, ok" : "FAIL");
+  return ok;
+}
+
 int main() {
-  bool ok = true;
+  bool ok = run_wait_case();
   ok &= run_case<16, 32>(1);
   ok &= run_case<64, 64>(2);
   ok &= run_case<128, 128>(3);
