@@ -17,7 +17,9 @@
 
 #include <complex>
 #include <cstdint>
+#include <fstream>
 #include <memory>
+#include <sstream>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -100,6 +102,28 @@ class Data {
   size_t bytes_ = 0;
 };
 
+namespace cfl {
+// LPISupport::Utils::basename (LPISupport/src/Utils.cpp:123-132): the name
+// without its last extension
+inline std::string basename(const std::string& f) {
+  const size_t p = f.find_last_of('.');
+  return p == std::string::npos ? f : f.substr(0, p);
+}
+inline bool exists(const std::string& f) { return std::ifstream(f).good(); }
+// reads exactly `count` elements of T from the start of a raw file
+template <typename T>
+std::vector<T> read_raw(const std::string& f, size_t count, const char* who) {
+  std::ifstream in(f, std::ios::binary);
+  if (!in) throw std::invalid_argument(std::string(who) + ": cannot open " + f);
+  std::vector<T> v(count);
+  in.read(reinterpret_cast<char*>(v.data()), std::streamsize(count * sizeof(T)));
+  if (size_t(in.gcount()) != count * sizeof(T))
+    throw std::invalid_argument(std::string(who) + ": " + f + " holds fewer than the expected " +
+                                std::to_string(count) + " elements");
+  return v;
+}
+}  // namespace cfl
+
 /// SensitivityMapsData: coil maps [C][H][W].
 class SensitivityMapsData : public Data {
  public:
@@ -158,6 +182,17 @@ class KData : public Data {
     if (data.size() != size_t(W) * H * F * C) throw std::invalid_argument("KData: size mismatch");
     upload(data.data());
   }
+  /// KData(app, fileName, asyncLoad) in its CFL form (KData.cpp:246-351):
+  /// header <base>.hdr (first line not starting with '#': "W H C F"), data
+  /// `fileName` as raw complex float [F][C][H][W], sensitivity maps
+  /// <base>_SensitivityMaps.cfl [C][H][W] and the sampling masks
+  /// <base>_SamplingMasks.u32 (row mask [F][H], expanded to pixels) or else
+  /// <base>_SamplingMasks.u8 (pixel mask [F][H][W]), each when present.  MATLAB
+  /// files are not supported (no matio); the load is synchronous.
+  KData(const std::shared_ptr<CLapp>& app, const std::string& fileName, bool asyncLoad = false)
+      : KData(load(app, fileName)) {
+    (void)asyncLoad;
+  }
   std::shared_ptr<SensitivityMapsData> getSensitivityMapsData() const { return sens_; }
   std::shared_ptr<SamplingMasksData> getSamplingMasksData() const { return masks_; }
   dimIndexType getNCoils() const { return C_; }
@@ -170,6 +205,52 @@ class KData : public Data {
   }
 
  private:
+  struct Loaded {
+    std::shared_ptr<CLapp> app;
+    dimIndexType W, H, F, C;
+    std::vector<complexType> data;
+    std::shared_ptr<SensitivityMapsData> sens;
+    std::shared_ptr<SamplingMasksData> masks;
+  };
+  explicit KData(Loaded&& l) : KData(l.app, l.W, l.H, l.F, l.C, l.data, l.sens, l.masks) {}
+  static Loaded load(const std::shared_ptr<CLapp>& app, const std::string& fileName) {
+    {
+      std::ifstream probe(fileName, std::ios::binary);
+      char magic[6] = {0};
+      probe.read(magic, 6);
+      if (probe.gcount() == 6 && std::string(magic, 6) == "MATLAB")
+        throw std::invalid_argument("KData: MATLAB files are not supported by this library (use the CFL form)");
+    }
+    const std::string base = cfl::basename(fileName);
+    std::ifstream hdr(base + ".hdr");
+    if (!hdr) throw std::invalid_argument("KData: cannot open " + base + ".hdr");
+    Loaded l{app, 0, 0, 0, 0, {}, nullptr, nullptr};
+    std::string line;
+    bool ok = false;
+    while (std::getline(hdr, line)) {
+      if (line.empty() || line[0] == '#') continue;
+      std::istringstream iss(line);
+      if (!(iss >> l.W >> l.H >> l.C >> l.F))
+        throw std::invalid_argument("Invalid line format: " + line + " (should be <width> <depth> <numCoils> <numFrames>)");
+      ok = true;
+      break;
+    }
+    if (!ok) throw std::invalid_argument("KData: no dimensions in " + base + ".hdr");
+    l.data = cfl::read_raw<complexType>(fileName, size_t(l.W) * l.H * l.F * l.C, "KData");
+    const std::string sname = base + "_SensitivityMaps.cfl";
+    if (cfl::exists(sname))
+      l.sens = std::make_shared<SensitivityMapsData>(
+          app, l.W, l.H, l.C, cfl::read_raw<complexType>(sname, size_t(l.W) * l.H * l.C, "SensitivityMapsData"));
+    const std::string rname = base + "_SamplingMasks.u32", pname = base + "_SamplingMasks.u8";
+    if (cfl::exists(rname))
+      l.masks = SamplingMasksData::fromRowMask(app, l.W, l.H, l.F,
+                                               cfl::read_raw<uint32_t>(rname, size_t(l.H) * l.F, "SamplingMasksData"));
+    else if (cfl::exists(pname))
+      l.masks = std::make_shared<SamplingMasksData>(
+          app, l.W, l.H, l.F, cfl::read_raw<uint8_t>(pname, size_t(l.W) * l.H * l.F, "SamplingMasksData"));
+    return l;
+  }
+
   dimIndexType W_, H_, F_, C_;
   std::shared_ptr<SensitivityMapsData> sens_;
   std::shared_ptr<SamplingMasksData> masks_;
@@ -195,6 +276,19 @@ class XData : public Data {
   void device2Host(std::vector<complexType>& out) const {
     out.resize(size_t(W_) * H_ * F_);
     download(out.data());
+  }
+  /// XData::saveCFLData (XData.cpp:851-881): `fileName`.cfl raw complex float
+  /// [F][H][W] and <basename(fileName)>.hdr "W H 1 F 1"; synchronous.
+  void saveCFLData(const std::string& fileName, bool asyncSave = false) const {
+    (void)asyncSave;
+    std::vector<complexType> h;
+    device2Host(h);
+    std::ofstream out(fileName + ".cfl", std::ios::binary | std::ios::trunc);
+    if (!out) throw std::invalid_argument("XData::saveCFLData: cannot write " + fileName + ".cfl");
+    out.write(reinterpret_cast<const char*>(h.data()), std::streamsize(h.size() * sizeof(complexType)));
+    std::ofstream hdr(cfl::basename(fileName) + ".hdr", std::ios::trunc);
+    if (!hdr) throw std::invalid_argument("XData::saveCFLHeader: cannot write header");
+    hdr << W_ << " " << H_ << " " << "1 " << F_ << " " << "1" << std::endl;
   }
 
  private:
@@ -414,6 +508,32 @@ class SimpleMRIRecon : public Process {
                               static_cast<float*>(out_->getDevicePtr()), int(k->width()), int(k->height()),
                               int(k->getDynDimsTotalSize()), int(k->getNCoils())),
              "SimpleMRIRecon::launch");
+  }
+};
+
+/// RSoS (src/processes/RSoS.cpp:43-85): root sum of squares over the coils of a
+/// KData input into an XData output.
+class RSoS : public Process {
+ public:
+  void launch() override {
+    auto k = inputAs<KData>("RSoS");
+    gbnCheck(gbn_op_rss(ctx(), static_cast<const float*>(k->getDevicePtr()), static_cast<float*>(out_->getDevicePtr()),
+                        int(k->width()), int(k->height()), int(k->getDynDimsTotalSize()), int(k->getNCoils())),
+             "RSoS::launch");
+  }
+};
+
+/// SimpleMRIReconSOS (src/processes/examples/SimpleMRIReconSOS.cpp:54-118):
+/// inverse FFT of every coil image, then RSoS.  The input KData is left as it
+/// was (the reference transforms it in place and writes .mat / timing files).
+class SimpleMRIReconSOS : public Process {
+ public:
+  void launch() override {
+    auto k = inputAs<KData>("SimpleMRIReconSOS");
+    gbnCheck(gbn_simple_recon_sos(ctx(), static_cast<const float*>(k->getDevicePtr()),
+                                  static_cast<float*>(out_->getDevicePtr()), int(k->width()), int(k->height()),
+                                  int(k->getDynDimsTotalSize()), int(k->getNCoils())),
+             "SimpleMRIReconSOS::launch");
   }
 };
 

@@ -168,6 +168,14 @@ GBN_API int gbn_op_encode_adjoint(gbn_ctx* ctx, const float* d_k, const float* d
  * x[f] = sum_c conj(S[c]) * IFFT2(y[f][c]).  The input is not modified. */
 GBN_API int gbn_simple_recon(gbn_ctx* ctx, const float* d_y, const float* d_S, float* d_x, int W, int H, int F, int C);
 
+/* RSoS (src/processes/RSoS.cpp:58-85, src/kernels/rss.cl:43-74):
+ * x[f] = (sqrt(sum_c |k[f][c]|^2), 0) for KData k [F][C][H][W]. */
+GBN_API int gbn_op_rss(gbn_ctx* ctx, const float* d_k, float* d_x, int W, int H, int F, int C);
+/* SimpleMRIReconSOS (src/processes/examples/SimpleMRIReconSOS.cpp:54-118):
+ * x[f] = RSoS(IFFT2(y[f][c])).  Unlike the reference, the input is not
+ * transformed in place, and no .mat or timing files are written. */
+GBN_API int gbn_simple_recon_sos(gbn_ctx* ctx, const float* d_y, float* d_x, int W, int H, int F, int C);
+
 /* Allocation-free SimpleMRIRecon: same result as gbn_simple_recon, but no
  * device memory is allocated.  No counterpart in the reference.  For callers
  * that cannot call cudaMalloc (code running during CUDA-graph stream capture,

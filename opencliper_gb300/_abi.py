@@ -98,6 +98,8 @@ SIGNATURES: dict[str, list] = {
     "gbn_nesta_run": [_vp, _vp, C.POINTER(NestaParams), _vp, C.POINTER(NestaStats)],
     "gbn_nesta_run_host": [_vp, _i, _i, _i, _i, _vp, _vp, _vp, C.POINTER(NestaParams), _vp,
                            C.POINTER(NestaStats)],
+    "gbn_op_rss": [_vp, _vp, _vp, _i, _i, _i, _i],
+    "gbn_simple_recon_sos": [_vp, _vp, _vp, _i, _i, _i, _i],
     "gbn_batch_create": [_vp, _i, C.POINTER(_vp), C.POINTER(NestaParams), C.POINTER(_vp), _i, C.POINTER(_vp)],
     "gbn_batch_launch": [_vp],
     "gbn_batch_capture": [_vp],

@@ -240,6 +240,16 @@ def simple_recon(ctx: Context, y: DeviceArray, S: DeviceArray, out: DeviceArray)
          _ck(out, np.complex64), W, H, F, Cc)
 
 
+def op_rss(ctx: Context, k: DeviceArray, out: DeviceArray) -> None:
+    F, Cc, H, W = k.shape
+    call("gbn_op_rss", ctx.handle, _ck(k, np.complex64), _ck(out, np.complex64), W, H, F, Cc)
+
+
+def simple_recon_sos(ctx: Context, y: DeviceArray, out: DeviceArray) -> None:
+    F, Cc, H, W = y.shape
+    call("gbn_simple_recon_sos", ctx.handle, _ck(y, np.complex64), _ck(out, np.complex64), W, H, F, Cc)
+
+
 class Problem:
     """Solver workspace bound to device-resident y, S and pixel mask."""
 

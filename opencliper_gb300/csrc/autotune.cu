@@ -129,7 +129,8 @@ int tune_shape(gbn_ctx* ctx, int W, int H, int F, int C, gbn_ctx::Tuned* out) {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   if (rc == GBN_OK && ((e = cudaEventCreate(&e0)) != cudaSuccess || (e = cudaEventCreate(&e1)) != cudaSuccess))
     rc = cuda_status(e, "autotune events");
-  gbn_nesta_params prm{0.01f, 1e-3f, 1.0f, 1u, 3e-4f, 0, 12u, 0u, 7u};
+  // 40 inner iterations per timed run, so the per-run setup does not decide the ranking
+  gbn_nesta_params prm{0.01f, 1e-3f, 1.0f, 1u, 3e-4f, 0, 40u, 0u, 7u};
   const int saved_cpb = ctx->k1_coils_per_block, saved_k2 = ctx->k2_ctas_per_sm;
   const bool saved_use = ctx->use_tuned, saved_prof = ctx->profile;
   const uint64_t saved_rand = ctx->rand48;

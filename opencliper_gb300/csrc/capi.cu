@@ -17,6 +17,8 @@ int op_mask(gbn_ctx*, float2*, const uint8_t*, int, int, int, int);
 int op_rowmask(gbn_ctx*, const uint32_t*, uint8_t*, int, int, int);
 int op_abs(gbn_ctx*, const float2*, float2*, size_t, int);
 int op_fft2(gbn_ctx*, int, const float2*, float2*, int, int, int);
+int op_rss(gbn_ctx*, const float2*, float2*, int, int, int, int);
+int simple_recon_sos(gbn_ctx*, const float2*, float2*, int, int, int, int);
 int op_encode(gbn_ctx*, const float2*, const float2*, const uint8_t*, float2*, int, int, int, int);
 int op_encode_adjoint(gbn_ctx*, const float2*, const float2*, float2*, int, int, int, int);
 int simple_recon(gbn_ctx*, const float2*, const float2*, float2*, int, int, int, int);
@@ -494,6 +496,23 @@ int gbn_simple_recon(gbn_ctx* ctx, const float* d_y, const float* d_S, float* d_
   if (rc) return rc;
   if ((rc = check_fft(W, H))) return rc;
   return simple_recon(ctx, CF2(d_y), CF2(d_S), F2(d_x), W, H, F, C);
+}
+
+int gbn_op_rss(gbn_ctx* ctx, const float* d_k, float* d_x, int W, int H, int F, int C) {
+  CHECK_CTX(ctx);
+  NONNULL2(d_k, d_x);
+  const int rc = check_dims(W, H, F, C);
+  if (rc) return rc;
+  return op_rss(ctx, CF2(d_k), F2(d_x), W, H, F, C);
+}
+
+int gbn_simple_recon_sos(gbn_ctx* ctx, const float* d_y, float* d_x, int W, int H, int F, int C) {
+  CHECK_CTX(ctx);
+  NONNULL2(d_y, d_x);
+  int rc = check_dims(W, H, F, C);
+  if (rc) return rc;
+  if ((rc = check_fft(W, H))) return rc;
+  return simple_recon_sos(ctx, CF2(d_y), F2(d_x), W, H, F, C);
 }
 
 int gbn_problem_create(gbn_ctx* ctx, int W, int H, int F, int C, const float* d_y, const float* d_S,

@@ -151,6 +151,41 @@ int op_rowmask(gbn_ctx* ctx, const uint32_t* rm, uint8_t* pm, int W, int H, int 
   return GBN_OK;
 }
 
+// rss.cl:43-74 (RSoS): out[f][p] = (sqrt(sum_c |k[f][c][p]|^2), 0), the sum in
+// coil order in FP32
+__global__ void k_rss(const float2* __restrict__ k, float2* __restrict__ out, int N, int F, int C) {
+  const size_t n = size_t(N) * F;
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+    const size_t f = i / N, p = i - f * N;
+    const float2* src = k + f * size_t(C) * N + p;
+    float acc = 0.f;
+    for (int c = 0; c < C; ++c) {
+      const float2 v = src[size_t(c) * N];
+      acc = __fadd_rn(acc, __fadd_rn(__fmul_rn(v.x, v.x), __fmul_rn(v.y, v.y)));
+    }
+    out[i] = make_float2(sqrtf(acc), 0.f);
+  }
+}
+
+int op_rss(gbn_ctx* ctx, const float2* k, float2* out, int W, int H, int F, int C) {
+  k_rss<<<grid_for(ctx, size_t(W) * H * F), 256, 0, ctx->stream>>>(k, out, W * H, F, C);
+  ctx->launches += 1;
+  return cuda_status(cudaGetLastError(), "rss");
+}
+
+int op_fft2(gbn_ctx* ctx, int direction, const float2* in, float2* out, int W, int H, int batch);
+
+// SimpleMRIReconSOS: backward FFT of every coil image into the context scratch
+// (the input stays untouched), then the root sum of squares
+int simple_recon_sos(gbn_ctx* ctx, const float2* y, float2* x, int W, int H, int F, int C) {
+  void* scr = nullptr;
+  int rc = ctx_scratch(ctx, size_t(W) * H * F * C * sizeof(float2), &scr);
+  if (rc != GBN_OK) return rc;
+  float2* t = static_cast<float2*>(scr);
+  if ((rc = op_fft2(ctx, GBN_FFT_BACKWARD, y, t, W, H, F * C)) != GBN_OK) return rc;
+  return op_rss(ctx, t, x, W, H, F, C);
+}
+
 int op_abs(gbn_ctx* ctx, const float2* in, float2* out, size_t n, int squared) {
   k_abs<<<grid_for(ctx, n), 256, 0, ctx->stream>>>(in, out, n, squared);
   return cuda_status(cudaGetLastError(), "abs");

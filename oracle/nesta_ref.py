@@ -135,6 +135,23 @@ def simple_recon(y, S):
     return coilsum(sensmul(fft2(y, False), S, True))
 
 
+def rss(k: np.ndarray) -> np.ndarray:
+    """RSoS::launch + rss.cl:43-74 on KData [F][C][H][W]: (sqrt(sum_c |k_c|^2), 0),
+    the sum accumulated in the data's real type in coil order."""
+    F, Cn, H, W = k.shape
+    acc = np.zeros((F, H, W), k.real.dtype)
+    for c in range(Cn):
+        kc = k[:, c]
+        acc = acc + (kc.real * kc.real + kc.imag * kc.imag)
+    return np.sqrt(acc).astype(k.dtype)
+
+
+def simple_recon_sos(y: np.ndarray) -> np.ndarray:
+    """SimpleMRIReconSOS::launch (SimpleMRIReconSOS.cpp:65-118): backward FFT of
+    every coil image, then the root sum of squares over coils."""
+    return rss(fft2(y, False))
+
+
 # ---------------------------------------------------------------------------
 # Power method (myNormest, NestaUp.cpp:291-439)
 # ---------------------------------------------------------------------------

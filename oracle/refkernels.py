@@ -3,7 +3,7 @@ INFRASTRUCTURE (oracle).
 
 build() compiles src/kernels/{hostKernelFunctions,temporalTV,
 vectorNormalization,complexElementProd,xImageSum,applyMask,complexAbsPow2,
-complexAbs}.cl from the reference tree, with the host shim in
+complexAbs,rss}.cl from the reference tree, with the host shim in
 oracle/refkernels/shim and the harness oracle/refkernels/harness.cpp, into
 oracle/_ref/librefkernels.so.  The reference tree is only read when present
 (REFERENCE_ROOT, default /root/reference); elsewhere the library is simply
@@ -24,7 +24,7 @@ HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref" / "librefkernels.so"
 REF = Path(os.environ.get("REFERENCE_ROOT", "/root/reference"))
 SOURCES = ["hostKernelFunctions.cl", "temporalTV.cl", "vectorNormalization.cl", "complexElementProd.cl",
-           "xImageSum.cl", "applyMask.cl", "complexAbsPow2.cl", "complexAbs.cl"]
+           "xImageSum.cl", "applyMask.cl", "complexAbsPow2.cl", "complexAbs.cl", "rss.cl"]
 
 
 def build(force: bool = False) -> Path | None:
@@ -65,6 +65,7 @@ def lib() -> C.CDLL:
         L.ref_mask.argtypes = [vp, vp, i, i, i, i]
         L.ref_abs2.argtypes = [vp, i, i, i, i]
         L.ref_abs.argtypes = [vp, vp, i, i, i]
+        L.ref_rss.argtypes = [vp, vp, i, i, i, i]
         _lib = L
     return _lib
 
@@ -126,4 +127,12 @@ def cabs(x: np.ndarray) -> np.ndarray:
     F, H, W = x.shape
     out = np.empty_like(x)
     lib().ref_abs(x.ctypes.data, out.ctypes.data, W, H, F)
+    return out
+
+
+def rss(k: np.ndarray) -> np.ndarray:
+    k = _c64(k)
+    F, Cc, H, W = k.shape
+    out = np.empty((F, H, W), np.complex64)
+    lib().ref_rss(k.ctypes.data, out.ctypes.data, W, H, F, Cc)
     return out

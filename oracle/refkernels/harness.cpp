@@ -18,6 +18,7 @@ thread_local size_t gbnref_gid[3];
 #include "applyMask.cl"
 #include "complexAbsPow2.cl"
 #include "complexAbs.cl"
+#include "rss.cl"
 
 #include <vector>
 
@@ -124,6 +125,13 @@ void ref_abs2(float* data, int W, int H, int F, int C) {
 void ref_abs(const float* in, float* out, int W, int H, int F) {
   RefBuf a = make(W, H, 0, F, 8, in), b = make(W, H, 0, F, 8, nullptr);
   ndrange(W, H, 1, [&] { complexAbs((float2*)a.data(), (float2*)b.data()); });
+  std::memcpy(out, b.data(), size_t(W) * H * F * 8);
+}
+
+// RSoS::launch (RSoS.cpp:58-85): global (W, H, dynamic dims), KData in, XData out
+void ref_rss(const float* in, float* out, int W, int H, int F, int C) {
+  RefBuf a = make(W, H, C, F, 8, in), b = make(W, H, 0, F, 8, nullptr);
+  ndrange(W, H, F, [&] { rss_kernel((float2*)a.data(), (float2*)b.data()); });
   std::memcpy(out, b.data(), size_t(W) * H * F * 8);
 }
 

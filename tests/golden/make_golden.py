@@ -73,7 +73,7 @@ def refkernel_ops():
     save("ops_refkernels.npz", kind="refkernels", x=x, k=k, S=S, mask=mask, mu=np.float32(0.6),
          ttv_fwd=K.ttv(x, True), ttv_adj=K.ttv(x, False), normalize=K.normalize(x, 0.6),
          sensmul_x=K.sensmul(x, S, False), sensmul_k_conj=K.sensmul(k, S, True), coilsum=K.coilsum(k),
-         mask_k=K.apply_mask(k, mask), abs2=K.abs2(k), abs=K.cabs(x))
+         mask_k=K.apply_mask(k, mask), abs2=K.abs2(k), abs=K.cabs(x), rss=K.rss(k))
 
 
 if __name__ == "__main__":

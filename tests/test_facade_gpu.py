@@ -56,3 +56,38 @@ def test_facade_matches_c_abi(ctx, driver, tmp_path):
     out = ctx.empty((F, H, W), np.complex64)
     api.simple_recon(ctx, ctx.to_device(p.y), ctx.to_device(p.S), out)
     assert rel_l2(simple_cpp, out.get()) == 0.0
+
+
+def test_facade_cfl_files(ctx, tmp_path):
+    """KData(app, fileName) from the reference's CFL form (row mask file),
+    SimpleMRIRecon, SimpleMRIReconSOS and NestaUp through the facade, results
+    written by XData::saveCFLData and checked against the oracle."""
+    from opencliper_gb300 import cfl
+    from oracle import nesta_ref as R
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("g++ not available")
+    exe = tmp_path / "cfl_facade"
+    libdir = os.path.join(ROOT, "opencliper_gb300")
+    subprocess.run([cxx, "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "cfl_facade.cpp"), "-L", libdir, "-lgbnesta",
+                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    W, H, F, C = 32, 24, 4, 3
+    p = synth.make_problem(W, H, F, C, 2, seed=31)
+    kfile = str(tmp_path / "series.cfl")
+    cfl.write_kdata(kfile, p.y, p.S, rowmask=p.rowmask)
+    r = subprocess.run([str(exe), kfile, str(tmp_path / "out")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    simple = cfl.read_xdata(str(tmp_path / "out_simple"))
+    sos = cfl.read_xdata(str(tmp_path / "out_sos"))
+    nesta = cfl.read_xdata(str(tmp_path / "out_nesta"))
+    y64 = p.y.astype(np.complex128)
+    assert rel_l2(simple, R.simple_recon(y64, p.S.astype(np.complex128))) < 1e-5
+    assert rel_l2(sos, R.simple_recon_sos(y64)) < 1e-5
+    r64 = R.nesta(p.y, p.S, p.mask, R.NestaParams(lambda_i=0.01, mu_f=1e-3, La=1.0, maxIntIter=1, maxIter=20,
+                                                   stoptest=0, miniter=7, tolVar=3e-4), "f64")
+    r32 = R.nesta(p.y, p.S, p.mask, R.NestaParams(lambda_i=0.01, mu_f=1e-3, La=1.0, maxIntIter=1, maxIter=20,
+                                                   stoptest=0, miniter=7, tolVar=3e-4), "f32")
+    assert R.nrmse(nesta, r64.x) <= 2.0 * R.nrmse(r32.x, r64.x) + 5e-6
+    hdr = (tmp_path / "out_nesta.hdr").read_text().split()
+    assert hdr == [str(W), str(H), "1", str(F), "1"]

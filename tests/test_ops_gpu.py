@@ -165,3 +165,19 @@ def test_operators_match_reference_kernel_outputs(ctx):
     assert rel_l2(ok.get(), d["abs2"]) < TOL
     api.op_abs(ctx, dx, ox)
     assert rel_l2(ox.get(), d["abs"]) < TOL
+    api.op_rss(ctx, dk, ox)
+    assert rel_l2(ox.get(), d["rss"]) < TOL
+
+
+@pytest.mark.parametrize("W,H,F,C", [(32, 32, 1, 8), (48, 40, 3, 5), (256, 256, 1, 8)])
+def test_simple_recon_sos(ctx, W, H, F, C):
+    """SimpleMRIReconSOS: inverse FFT per coil, root sum of squares; input untouched."""
+    rng = np.random.default_rng(W + C)
+    y = _rand(rng, (F, C, H, W))
+    dy, ox = ctx.to_device(y), ctx.empty((F, H, W), np.complex64)
+    api.simple_recon_sos(ctx, dy, ox)
+    ref = R.simple_recon_sos(_c128(y))
+    out = ox.get()
+    assert rel_l2(out, ref) < TOL
+    assert not out.imag.any()
+    assert np.array_equal(dy.get(), y)

@@ -32,6 +32,8 @@ def test_operators_match_reference_kernels(W, H, F, C):
     assert np.array_equal(K.apply_mask(k, mask), R.apply_mask(k, mask))
     assert rel_l2(K.abs2(k), R.complex_abs2(k.astype(np.complex128))) < 1e-6
     assert rel_l2(K.cabs(x), R.complex_abs(x.astype(np.complex128))) < 1e-6
+    # RSoS: the FP32 restatement follows the kernel's accumulation order exactly
+    assert np.array_equal(K.rss(k), R.rss(k))
 
 
 def test_ttv_edge_frames_follow_reference_kernel():
