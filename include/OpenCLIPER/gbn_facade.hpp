@@ -10,7 +10,10 @@
 //    cl::Buffer* becomes Data::getDevicePtr() returning void*;
 //  - data objects are built from host vectors (file loaders are not part of
 //    this library);
-//  - NestaUp does not support motion compensation (argsMC must be nullptr).
+//  - the motion-compensation meshes of ArgumentsMotionCompensation are
+//    ArrayData<float> / ArrayData<int> built from host vectors (the reference
+//    builds them inside GroupwiseRegistration, which is not part of this
+//    library).
 // Errors are thrown as CLError (code = GBN_ERR_*) or std::invalid_argument,
 // like the reference's BTTHROW (LPISupport/include/LPISupport/Utils.hpp:67-83).
 #pragma once
@@ -537,7 +540,84 @@ class SimpleMRIReconSOS : public Process {
   }
 };
 
-struct ArgumentsMotionCompensation;  // motion compensation is not part of this library
+/// A typed device array built from a host vector: the meshes of
+/// ArgumentsMotionCompensation.
+template <typename T>
+class ArrayData : public Data {
+ public:
+  ArrayData(const std::shared_ptr<CLapp>& app, const std::vector<T>& host)
+      : Data(app, sizeof(T) * host.size()), n_(host.size()) {
+    if (host.empty()) throw std::invalid_argument("ArrayData: empty array");
+    upload(host.data());
+  }
+  size_t size() const { return n_; }
+
+ private:
+  size_t n_;
+};
+
+/// ArgumentsMotionCompensation (include/OpenCLIPER/processes/
+/// GroupwiseRegistration.hpp:95-100): xnData = deformed mesh [2][F][H][W]
+/// float, xData = original mesh [2][W][H] int, both 1-based; bound_box = the
+/// four 1-based bounding-box coordinates.  TData (the registration's B-spline
+/// coefficients) is not read by the motion-compensation operators.
+struct ArgumentsMotionCompensation {
+  std::shared_ptr<Data> xnData;
+  std::shared_ptr<Data> TData;
+  std::shared_ptr<Data> xData;
+  std::vector<dimIndexType>* bound_box;
+};
+
+namespace detail {
+struct MotionArgs {
+  const float* xn;
+  const int* xmesh;
+  int bb[4];
+};
+inline MotionArgs motion_args(const ArgumentsMotionCompensation* a, dimIndexType W, dimIndexType H,
+                              dimIndexType F, const char* who) {
+  if (!a || !a->xnData || !a->xData || !a->bound_box)
+    throw std::invalid_argument(std::string(who) + ": ArgumentsMotionCompensation needs xnData, xData and bound_box");
+  if (a->bound_box->size() != 4) throw std::invalid_argument(std::string(who) + ": bound_box must hold 4 values");
+  if (a->xnData->getBytes() != sizeof(float) * 2 * size_t(F) * H * W)
+    throw std::invalid_argument(std::string(who) + ": xnData must be float [2][F][H][W]");
+  if (a->xData->getBytes() != sizeof(int) * 2 * size_t(W) * H)
+    throw std::invalid_argument(std::string(who) + ": xData must be int [2][W][H]");
+  MotionArgs m{static_cast<const float*>(a->xnData->getDevicePtr()), static_cast<const int*>(a->xData->getDevicePtr()),
+               {0, 0, 0, 0}};
+  for (int i = 0; i < 4; ++i) m.bb[i] = int((*a->bound_box)[size_t(i)]);
+  return m;
+}
+}  // namespace detail
+
+/// MotionCompensation (src/processes/MotionCompensation.cpp:57-78) and
+/// AdjointMotionCompensation (src/processes/AdjointMotionCompensation.cpp:
+/// 59-86): XData -> XData through the registration's meshes.
+template <int Direction>
+class MotionCompensationProcess : public Process {
+ public:
+  struct LaunchParameters : Process::LaunchParameters {
+    ArgumentsMotionCompensation* argsMC;
+    explicit LaunchParameters(ArgumentsMotionCompensation* args) : argsMC(args) {}
+  };
+  void launch() override {
+    const char* who = Direction == GBN_TTV_FORWARD ? "MotionCompensation::launch" : "AdjointMotionCompensation::launch";
+    auto lp = std::dynamic_pointer_cast<LaunchParameters>(lp_);
+    if (!lp) throw std::invalid_argument(std::string(who) + ": missing LaunchParameters");
+    auto in = inputAs<XData>(who);
+    auto out = outputAs<XData>(who);
+    if (in->width() != out->width() || in->height() != out->height() ||
+        in->getDynDimsTotalSize() != out->getDynDimsTotalSize())
+      throw std::invalid_argument(std::string(who) + ": input and output sizes differ");
+    const auto m = detail::motion_args(lp->argsMC, in->width(), in->height(), in->getDynDimsTotalSize(), who);
+    gbnCheck(gbn_op_motion(ctx(), Direction, static_cast<const float*>(in->getDevicePtr()),
+                           static_cast<float*>(out->getDevicePtr()), m.xn, m.xmesh, m.bb, int(in->width()),
+                           int(in->height()), int(in->getDynDimsTotalSize())),
+             who);
+  }
+};
+using MotionCompensation = MotionCompensationProcess<GBN_TTV_FORWARD>;
+using AdjointMotionCompensation = MotionCompensationProcess<GBN_TTV_ADJOINT>;
 
 /// NestaUp (src/processes/nesta/NestaUp.cpp:81-910, NestaUp.hpp:67-83).
 class NestaUp : public Process {
@@ -570,8 +650,17 @@ class NestaUp : public Process {
   void launch() override {
     auto lp = std::dynamic_pointer_cast<LaunchParameters>(lp_);
     if (!lp) throw std::invalid_argument("NestaUp::launch: missing LaunchParameters");
-    if (lp->argsMC) throw CLError(GBN_ERR_UNSUPPORTED, "NestaUp: motion compensation is not supported");
     bind();
+    // with argsMC the sparsity operator is tTV after motion compensation and
+    // the solve starts from the output's current image (NestaUp.cpp:201-278, 483-486)
+    if (lp->argsMC) {
+      auto k = inputAs<KData>("NestaUp");
+      const auto m = detail::motion_args(lp->argsMC, k->width(), k->height(), k->getDynDimsTotalSize(),
+                                         "NestaUp::launch");
+      gbnCheck(gbn_problem_set_motion(prob_, m.xn, m.xmesh, m.bb), "NestaUp::launch");
+    } else {
+      gbnCheck(gbn_problem_set_motion(prob_, nullptr, nullptr, nullptr), "NestaUp::launch");
+    }
     const gbn_nesta_params prm{lp->lambda_i, lp->mu_f, lp->La, lp->maxIntIter, lp->tolVar,
                                lp->verbose, lp->maxIter, lp->stoptest, lp->miniter};
     gbnCheck(gbn_nesta_run(ctx(), prob_, &prm, static_cast<float*>(out_->getDevicePtr()), &stats_), "NestaUp::launch");

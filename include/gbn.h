@@ -225,6 +225,23 @@ typedef struct gbn_nesta_stats {
 GBN_API int gbn_problem_create(gbn_ctx* ctx, int W, int H, int F, int C, const float* d_y, const float* d_S,
                        const uint8_t* d_mask, gbn_problem** out);
 GBN_API int gbn_problem_destroy(gbn_problem* p);
+/* MotionCompensation (direction GBN_TTV_FORWARD, MotionCompensation.cpp:57-78)
+ * or AdjointMotionCompensation (GBN_TTV_ADJOINT, AdjointMotionCompensation.cpp:
+ * 59-86) of XData [F][H][W]; meshes and bounding box as for
+ * gbn_problem_set_motion.  Waits for completion; a mesh point interpolating
+ * outside the image is an error. */
+GBN_API int gbn_op_motion(gbn_ctx* ctx, int direction, const float* d_in, float* d_out, const float* d_xn,
+                          const int* d_xmesh, const int bound_box[4], int W, int H, int F);
+/* Motion-compensated sparsity operator for later runs of p (NestaUp with
+ * argsMC, NestaUp.cpp:201-278; ArgumentsMotionCompensation,
+ * GroupwiseRegistration.hpp:95-100): d_xn = deformed mesh [2][F][H][W] float,
+ * d_xmesh = original mesh [2][W][H] int, both 1-based (not copied, kept
+ * alive by the caller), bound_box = the 1-based bounding box (host, 4 ints).
+ * As in the reference, such a run starts from the image already in its output
+ * buffer instead of E^H y.  All three NULL switches motion compensation off.
+ * Mesh points whose interpolation leaves the image are skipped and reported
+ * in gbn_nesta_stats::status. */
+GBN_API int gbn_problem_set_motion(gbn_problem* p, const float* d_xn, const int* d_xmesh, const int bound_box[4]);
 /* One reconstruction into d_x ([F][H][W], the reference's output XData).
  * Runs asynchronously; when stats != NULL the call waits for completion and
  * fills *stats. */

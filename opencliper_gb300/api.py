@@ -240,6 +240,14 @@ def simple_recon(ctx: Context, y: DeviceArray, S: DeviceArray, out: DeviceArray)
          _ck(out, np.complex64), W, H, F, Cc)
 
 
+def op_motion(ctx: Context, direction: int, x: DeviceArray, out: DeviceArray, xn: DeviceArray, xmesh: DeviceArray,
+              bound_box) -> None:
+    F, H, W = x.shape
+    bb = (C.c_int * 4)(*[int(v) for v in bound_box])
+    call("gbn_op_motion", ctx.handle, int(direction), _ck(x, np.complex64), _ck(out, np.complex64),
+         _ck(xn, np.float32), _ck(xmesh, np.int32), bb, W, H, F)
+
+
 def op_rss(ctx: Context, k: DeviceArray, out: DeviceArray) -> None:
     F, Cc, H, W = k.shape
     call("gbn_op_rss", ctx.handle, _ck(k, np.complex64), _ck(out, np.complex64), W, H, F, Cc)
@@ -262,6 +270,17 @@ class Problem:
         self.ctx, self.shape = ctx, (F, Cc, H, W)
         self._keep = (y, S, mask)
         ctx._children.add(self)
+
+    def set_motion(self, xn: DeviceArray | None, xmesh: DeviceArray | None, bound_box=None) -> None:
+        """Motion-compensated sparsity operator (gbn_problem_set_motion); the
+        run then starts from the image already in its output buffer."""
+        if xn is None:
+            call("gbn_problem_set_motion", self.handle, None, None, None)
+            self._motion = None
+            return
+        bb = (C.c_int * 4)(*[int(v) for v in bound_box])
+        call("gbn_problem_set_motion", self.handle, _ck(xn, np.float32), _ck(xmesh, np.int32), bb)
+        self._motion = (xn, xmesh)
 
     def run(self, params: NestaParams, out: DeviceArray, stats: bool = True) -> dict | None:
         st = NestaStats() if stats else None

@@ -165,6 +165,10 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
     for (int j = 0; j < i; ++j)
       if (problems[j] == P) rc = set_error(GBN_ERR_INVALID, "a problem appears twice in the batch");
     if (rc != GBN_OK) break;
+    if (P->mc_on) {
+      rc = set_error(GBN_ERR_UNSUPPORTED, "batches do not take motion-compensated problems (use gbn_nesta_run)");
+      break;
+    }
     if ((rc = run_prepare(ctx, P, &params[i])) != GBN_OK) break;
     if (precision == GBN_PRECISION_MIXED &&
         (rc = mixed_prepare(ctx, P, params[i], reinterpret_cast<const float2*>(outputs[i]))) != GBN_OK)

@@ -32,6 +32,8 @@ int batch_capture(gbn_batch*);
 int batch_stats(gbn_batch*, int, gbn_nesta_stats*);
 int batch_destroy(gbn_batch*);
 gbn_ctx* batch_ctx(gbn_batch*);
+int motion_set(gbn_problem*, const float*, const int*, const int*);
+int motion_op(gbn_ctx*, int, const float2*, float2*, const float*, const int*, const int*, int, int, int);
 int autotune(gbn_ctx*, int, const int*, const char*);
 int autotune_load(gbn_ctx*, const char*);
 void tuning_for(gbn_ctx*, int, int, int, int, int*, int*);
@@ -541,6 +543,24 @@ int gbn_problem_create(gbn_ctx* ctx, int W, int H, int F, int C, const float* d_
   }
   *out = p;
   return GBN_OK;
+}
+
+int gbn_op_motion(gbn_ctx* ctx, int direction, const float* d_in, float* d_out, const float* d_xn, const int* d_xmesh,
+                  const int bound_box[4], int W, int H, int F) {
+  CHECK_CTX(ctx);
+  NONNULL2(d_in, d_out);
+  if (!d_xn || !d_xmesh || !bound_box) return set_error(GBN_ERR_INVALID, "null mesh or bounding box");
+  if (direction != GBN_TTV_FORWARD && direction != GBN_TTV_ADJOINT)
+    return set_error(GBN_ERR_INVALID, "direction must be FORWARD or ADJOINT");
+  const int rc = check_dims(W, H, F, 1);
+  if (rc) return rc;
+  return motion_op(ctx, direction, CF2(d_in), F2(d_out), d_xn, d_xmesh, bound_box, W, H, F);
+}
+
+int gbn_problem_set_motion(gbn_problem* p, const float* d_xn, const int* d_xmesh, const int bound_box[4]) {
+  if (!p) return set_error(GBN_ERR_INVALID, "null problem");
+  DeviceGuard guard(p->ctx->device);
+  return motion_set(p, d_xn, d_xmesh, bound_box);
 }
 
 int gbn_problem_destroy(gbn_problem* p) {

@@ -84,6 +84,15 @@ struct gbn_problem {
   unsigned char* fa = nullptr;        // adjoint kept-row DFT operand
   size_t fa_bytes = 0;
   int ncha = 0;
+  // motion-compensated form (motion.cu): caller's meshes, not owned
+  bool mc_on = false;
+  const float* mc_xn = nullptr;       // deformed mesh [2][F][H][W], 1-based
+  const int* mc_xmesh = nullptr;      // original mesh [2][W][H], 1-based
+  int mc_bb[4] = {0, 0, 0, 0};        // bounding box (1-based)
+  float2* mc_xw = nullptr;            // M x_k
+  float2* mc_g = nullptr;             // tTVadj(normalise(D M x_k))
+  float2* mc_gm = nullptr;            // M^T of it
+  double* mc_part = nullptr;          // power-method norm partials
   gbn::FusedArgs* d_args = nullptr;   // one-entry instance table of the fused kernels
   gbn::ClassCtl* ctl = nullptr;       // row-pass control block
 };

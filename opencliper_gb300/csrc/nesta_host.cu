@@ -170,7 +170,10 @@ __global__ void k_state_init(NestaDevState* st, gbn_nesta_params p) {
 // max|x0| and max|U x0| (NestaUp.cpp:521-568: ComplexAbs + host loop).  Values
 // are non-negative, so float order equals unsigned order of their bits.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(256) k_maxima(const float2* __restrict__ x, int N, int F, NestaDevState* st) {
+// xu: the image the sparsity operator is applied to (x itself, or M x with
+// motion compensation)
+__global__ void __launch_bounds__(256) k_maxima(const float2* __restrict__ x, const float2* __restrict__ xu, int N,
+                                                int F, NestaDevState* st) {
   __shared__ float s1[8], s2[8];
   const size_t total = size_t(N) * F;
   float m1 = 0.f, m2 = 0.f;
@@ -178,8 +181,7 @@ __global__ void __launch_bounds__(256) k_maxima(const float2* __restrict__ x, in
     const int f = int(i / N);
     const size_t p = i - size_t(f) * N;
     const float2 a = x[i];
-    const float2 b = x[size_t((f + F - 1) % F) * N + p];
-    const float2 d = csub(a, b);
+    const float2 d = csub(xu[i], xu[size_t((f + F - 1) % F) * N + p]);
     m1 = fmaxf(m1, sqrtf(a.x * a.x + a.y * a.y));
     m2 = fmaxf(m2, sqrtf(d.x * d.x + d.y * d.y));
   }
@@ -501,7 +503,8 @@ int problem_alloc(gbn_problem* P) {
 void problem_free(gbn_problem* P) {
   void* ptrs[] = {P->flags, P->full_fh, P->rowmap, P->rowoff,  P->rows_h, P->rows_f,  P->row_full, P->T,
                   P->xk0,   P->xk1,     P->wacc,   P->st,      P->fmean,  P->part_tv, P->part_r,   P->part_ne,
-                  P->ne_b,  P->d_args,  P->ctl,      P->fk,     P->colmax, P->smax,   P->fa};
+                  P->ne_b,  P->d_args,  P->ctl,      P->fk,     P->colmax, P->smax,   P->fa,
+                  P->mc_xw, P->mc_g,    P->mc_gm,    P->mc_part};
   for (void* p : ptrs)
     if (p) cudaFree(p);
 }
@@ -622,7 +625,7 @@ int launch_constants(gbn_ctx* ctx, gbn_problem* P, const float2* xref, const Ran
   const int N = P->W * P->H, F = P->F;
   const int nblk_ne = (N + kNeNT - 1) / kNeNT;
   // maxima, norm estimate, constants (NestaUp.cpp:521-583)
-  k_maxima<<<elementwise_grid(ctx, size_t(N) * F), 256, 0, s>>>(xref, N, F, P->st);
+  k_maxima<<<elementwise_grid(ctx, size_t(N) * F), 256, 0, s>>>(xref, xref, N, F, P->st);
   const Lcg48 jN = lcg_jump_k(uint64_t(N));
   for (int ch = 0; ch < kNeChunks; ++ch) {
     launch_normest_chunk(normest_fmax(F), nblk_ne, s, N, F, rs, jN, kNeBounds[ch], kNeBounds[ch + 1], P->ne_b,
@@ -631,6 +634,17 @@ int launch_constants(gbn_ctx* ctx, gbn_problem* P, const float2* xref, const Ran
   }
   k_setup<<<1, 1, 0, s>>>(P->st);
   return 2 + 2 * kNeChunks;
+}
+
+int launch_maxima(gbn_ctx* ctx, gbn_problem* P, const float2* x0, const float2* xu, cudaStream_t s) {
+  const size_t X = size_t(P->W) * P->H * P->F;
+  k_maxima<<<elementwise_grid(ctx, X), 256, 0, s>>>(x0, xu, P->W * P->H, P->F, P->st);
+  return 1;
+}
+
+int launch_setup(gbn_problem* P, cudaStream_t s) {
+  k_setup<<<1, 1, 0, s>>>(P->st);
+  return 1;
 }
 
 int launch_outer_begin(gbn_ctx* ctx, gbn_problem* P, int nl, const float2* xref, cudaStream_t s) {
@@ -671,10 +685,16 @@ int read_stats(gbn_problem* P, cudaStream_t s, gbn_nesta_stats* stats) {
   return GBN_OK;
 }
 
+int nesta_run_mc(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, float2* x_out);
+
 int nesta_run(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, float2* x_out, gbn_nesta_stats* stats) {
   if (!x_out) return set_error(GBN_ERR_INVALID, "null argument");
   int rc = run_prepare(ctx, P, prm);
   if (rc != GBN_OK) return rc;
+  if (P->mc_on) {
+    if ((rc = nesta_run_mc(ctx, P, prm, x_out)) != GBN_OK) return rc;
+    return stats ? read_stats(P, ctx->stream, stats) : GBN_OK;
+  }
   const SizeKernels* kh = find_size(P->H);
   const SizeKernels* kw = find_size(P->W);
   const int W = P->W, H = P->H, F = P->F, C = P->C;

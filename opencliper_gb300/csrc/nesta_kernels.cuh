@@ -208,8 +208,10 @@ __global__ void __launch_bounds__(kColNT, fwd_min_blocks(H))
   // Partial sums of the tTV objective terms over this CTA's tile (coil group 0
   // only): d = x_f - x_{f-1} (temporalTV.cl:49-76), u = d / max(mu, |d|)
   // (vectorNormalization.cl:42-56), sum |u|^2 (Scnrm2) and Re<u,d> (Cdotc).
+  // (with motion compensation the gradient kernel writes these sums instead)
   float su2 = 0.f, sud = 0.f;
-  if (cg == 0) {
+  const bool tv_here = (cg == 0) && !a.tv_src;
+  if (tv_here) {
     const float2* __restrict__ xm = xk + size_t((f + F - 1) % F) * N;
     const float inv_mu = 1.0f / st->mu;
 #pragma unroll
@@ -276,7 +278,7 @@ __global__ void __launch_bounds__(kColNT, fwd_min_blocks(H))
     }
   }
 
-  if (cg == 0) {
+  if (tv_here) {
     const double t1 = block_sum<kColNT>(double(su2), sred);
     const double t2 = block_sum<kColNT>(double(sud), sred);
     if (t == 0) {
@@ -834,8 +836,12 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT)
             if (k2 < A && k2 >= kb && k2 < ke) {
               const size_t p = size_t(k1p + B * k2) * W + w0 + w;
               xa[b] = xk[off0 + p];
-              xm[b] = xk[offm + p];
-              xp[b] = xk[offp + p];
+              if (a.grad_ext) {
+                xm[b] = a.grad_ext[off0 + p];  // M^T (tTVadj u) of the motion-compensated form
+              } else {
+                xm[b] = xk[offm + p];
+                xp[b] = xk[offp + p];
+              }
               wo[b] = a.wacc[off0 + p];
               xr[b] = a.xref[off0 + p];
             }
@@ -845,11 +851,16 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT)
             const int k2 = k0 + b;
             if (k2 < A && k2 >= kb && k2 < ke) {
               const size_t p = size_t(k1p + B * k2) * W + w0 + w;
-              // u_f and u_{f+1} of the normalised temporal difference
-              const float2 u0 = tv_normalize(csub(xa[b], xm[b]), inv_mu);
-              const float2 u1 = tv_normalize(csub(xp[b], xa[b]), inv_mu);
-              // operator_tTVadj gives u_{f+1} - u_f; NestaUp negates it, scales by lambda, adds A^H r
-              const float2 adj = csub(u1, u0);
+              // operator_tTVadj gives u_{f+1} - u_f of the normalised temporal
+              // differences; NestaUp negates it, scales by lambda, adds A^H r
+              float2 adj;
+              if (a.grad_ext) {
+                adj = xm[b];
+              } else {
+                const float2 u0 = tv_normalize(csub(xa[b], xm[b]), inv_mu);
+                const float2 u1 = tv_normalize(csub(xp[b], xa[b]), inv_mu);
+                adj = csub(u1, u0);
+              }
               const float2 ares = cscale(acc[ii][k2], s_adj);
               const float2 df = make_float2(__fadd_rn(__fmul_rn(-adj.x, lambda), ares.x),
                                             __fadd_rn(__fmul_rn(-adj.y, lambda), ares.y));

@@ -48,6 +48,10 @@ int launch_group_init(const FusedArgs* tab, int n, int rows_per_cta, ClassCtl* c
 int launch_pre(gbn_problem* P, const gbn_nesta_params& prm, cudaStream_t s);
 // after x0 = E^H y is in xref: maxima, norm estimate and derived constants
 int launch_constants(gbn_ctx* ctx, gbn_problem* P, const float2* xref, const RandStart& rs, cudaStream_t s);
+// max|x0| and max|D xu| into the state block (xu = x0, or M x0 with motion compensation)
+int launch_maxima(gbn_ctx* ctx, gbn_problem* P, const float2* x0, const float2* xu, cudaStream_t s);
+// derived constants (lambda, mu0, gamma, ...) once ||U|| and the maxima are in the state
+int launch_setup(gbn_problem* P, cudaStream_t s);
 // start (w = 0, x_k = x_ref, mu/tolVar/Lmu) and end (x_ref = x_k) of outer loop nl
 int launch_outer_begin(gbn_ctx* ctx, gbn_problem* P, int nl, const float2* xref, cudaStream_t s);
 int launch_outer_end(gbn_ctx* ctx, gbn_problem* P, float2* xref, cudaStream_t s);

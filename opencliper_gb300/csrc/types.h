@@ -78,6 +78,12 @@ struct FusedArgs {
   int npad, nch;          // forward operand rows (2G padded to 16) and K chunks
   const unsigned char* fa;  // adjoint kept-row DFT operand, fp16 hi/lo, per frame, row tile and chunk
   int ncha;               // adjoint K chunks (32 kept rows each)
+  // motion-compensated form (nullptr otherwise): tv_src = M x_k, whose tTV
+  // objective sums a separate kernel writes (the forward column pass skips
+  // them), and grad_ext = M^T (tTVadj u), the tTV gradient the adjoint column
+  // pass takes instead of forming it from x_k
+  const float2* tv_src;
+  const float2* grad_ext;
 };
 
 // Instances covered by one launch of the fused kernels.  All of them share the

@@ -156,12 +156,16 @@ def simple_recon_sos(y: np.ndarray) -> np.ndarray:
 # Power method (myNormest, NestaUp.cpp:291-439)
 # ---------------------------------------------------------------------------
 def normest(F: int, H: int, W: int, precision: str = "f32", rand_state: int = drand48.DEFAULT_STATE,
-            use_libc: bool = False):
+            use_libc: bool = False, U=None, Ut=None):
     """Returns (e, iterations, new drand48 state).
 
     The loop test uses the float overload of abs: CLapp.hpp:54 includes
     <stdlib.h>, whose C++ wrapper brings std::abs(float) into the global
-    namespace that NestaUp.cpp's unqualified abs() call resolves against."""
+    namespace that NestaUp.cpp's unqualified abs() call resolves against.
+    U / Ut: the sparsity operator and its adjoint (default: temporal TV and its
+    adjoint kernel; with motion compensation, NestaUp::operatorU/Ut)."""
+    U = U or (lambda v: ttv(v, True))
+    Ut = Ut or (lambda v: ttv(v, False))
     P = _P(precision)
     n = P.s(np.float32(H * W * F)) if P.f32 else float(H * W * F)
     tol = P.s(1e-3)
@@ -174,14 +178,14 @@ def normest(F: int, H: int, W: int, precision: str = "f32", rand_state: int = dr
     state = rand_state
     while abs(e - e0) > tol * e and cnt < maxiter:
         e0 = e
-        Sx = ttv(x, True)
+        Sx = U(x)
         nnz = np.sum(np.abs(Sx.real) + np.abs(Sx.imag))
         if nnz == 0:
             gen = drand48.libc_sequence if use_libc else drand48.lcg_sequence
             vals, state = gen(F * H * W, state)
             Sx = vals.astype(np.float32).reshape(F, H, W).astype(P.c)  # complexType(drand48(), 0)
         e = P.s(np.sqrt(np.sum(np.abs(Sx) ** 2, dtype=np.float64)))
-        x = ttv(Sx, False)  # operatorUt: tTVadj then copy (no negation here)
+        x = Ut(Sx)  # operatorUt: tTVadj then copy / adjoint motion compensation (no negation here)
         nx = P.s(np.sqrt(np.sum(np.abs(x) ** 2, dtype=np.float64)))
         x = x * P.s(1 / nx)
         cnt += 1
@@ -216,10 +220,15 @@ def _nrm2sq(v: np.ndarray) -> float:
 
 
 def nesta(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams, precision: str = "f32",
-          rand_state: int = drand48.DEFAULT_STATE, record: bool = False, timings: dict | None = None) -> NestaResult:
+          rand_state: int = drand48.DEFAULT_STATE, record: bool = False, timings: dict | None = None,
+          mc=None, x_init: np.ndarray | None = None) -> NestaResult:
     """y: KData [F][C][H][W]; S: [C][H][W]; mask: pixel mask [F][H][W] (uint8).
     `timings`, when given, receives wall-clock marks: 'setup' (seconds until the
-    first inner iteration) and 'iters' (seconds of each inner iteration)."""
+    first inner iteration) and 'iters' (seconds of each inner iteration).
+    `mc` = (xn, xmesh, bb) runs the motion-compensated form (argsMC != nullptr):
+    the sparsity operator becomes U = tTV(M x), Ut = M^T tTVadj (NestaUp.cpp:
+    201-278), and the solve starts from `x_init` (the output XData's current
+    image) instead of E^H y (NestaUp.cpp:483-486)."""
     import time as _time
     _t0 = _time.perf_counter()
     P = _P(precision)
@@ -231,9 +240,25 @@ def nesta(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams, prec
     # y' = copy(y) * sqrt(float(N))   (NestaUp.cpp:465-481)
     sqrtN = s(np.sqrt(np.float32(N))) if P.f32 else np.sqrt(float(N))
     yp = y * sqrtN
-    # x0 = operatorAt(y')  (NestaUp.cpp:484-486)
-    xref = operator_At(yp, S).astype(P.c)
-    Ux0 = ttv(xref, True)
+    if mc is not None:
+        from oracle import motion
+        xn_, xm_, bb_ = mc
+
+        def U(v):
+            return ttv(motion.warp(v, xn_, xm_, bb_), True)
+
+        def Ut(v):
+            return motion.warp_adjoint(ttv(v, False), xn_, xm_, bb_)
+        xref = np.asarray(x_init).astype(P.c)
+    else:
+        def U(v):
+            return ttv(v, True)
+
+        def Ut(v):
+            return ttv(v, False)
+        # x0 = operatorAt(y')  (NestaUp.cpp:484-486)
+        xref = operator_At(yp, S).astype(P.c)
+    Ux0 = U(xref)
     # maxima (NestaUp.cpp:521-568)
     maxX = s(np.max(np.abs(xref)))
     maxUX = s(np.max(np.abs(Ux0)))
@@ -241,7 +266,7 @@ def nesta(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams, prec
     lam = s(s(prm.lambda_i) * maxX)
     muf = s(s(prm.mu_f) * maxX)
     mu0 = s(0.9 * float(maxUX))
-    normU, ne_iters, new_state = normest(F, H, W, precision, rand_state)
+    normU, ne_iters, new_state = normest(F, H, W, precision, rand_state, U=U, Ut=Ut)
     muL = s(lam / s(prm.La))
     if muL > mu0:
         mu0 = muL
@@ -272,11 +297,11 @@ def nesta(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams, prec
         qpDone = False
         k = 0
         while k < prm.maxIter:
-            d = ttv(xk, True)                       # operatorU (669)
+            d = U(xk)                               # operatorU (669)
             u = normalize(d, mu)                    # VectorNormalization (680-683)
             normUk = s(np.sqrt(_nrm2sq(u)))         # Scnrm2 (686)
             fxdot = s(np.sum((np.conj(u) * d).real, dtype=np.float64))  # Cdotc real part (691)
-            Df = -ttv(u, False)                     # operatorUt + Cscal(-1) (696-704)
+            Df = -Ut(u)                             # operatorUt + Cscal(-1) (696-704)
             res = operator_A(xk, S, mask) * inv_sqrtN - y  # operatorA, Cscal(1/sqrt N), Caxpy(-1) (710-727)
             l2 = s(_nrm2sq(res))                    # ComplexAbsPow2 + Scsum (738-746)
             Ares = operator_At(res * sqrtN, S)      # Cscal(sqrt N) + operatorAt (749-756)

@@ -3,7 +3,7 @@ INFRASTRUCTURE (oracle).
 
 build() compiles src/kernels/{hostKernelFunctions,temporalTV,
 vectorNormalization,complexElementProd,xImageSum,applyMask,complexAbsPow2,
-complexAbs,rss}.cl from the reference tree, with the host shim in
+complexAbs,rss,initialize,optimizer}.cl from the reference tree, with the host shim in
 oracle/refkernels/shim and the harness oracle/refkernels/harness.cpp, into
 oracle/_ref/librefkernels.so.  The reference tree is only read when present
 (REFERENCE_ROOT, default /root/reference); elsewhere the library is simply
@@ -24,7 +24,8 @@ HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref" / "librefkernels.so"
 REF = Path(os.environ.get("REFERENCE_ROOT", "/root/reference"))
 SOURCES = ["hostKernelFunctions.cl", "temporalTV.cl", "vectorNormalization.cl", "complexElementProd.cl",
-           "xImageSum.cl", "applyMask.cl", "complexAbsPow2.cl", "complexAbs.cl", "rss.cl"]
+           "xImageSum.cl", "applyMask.cl", "complexAbsPow2.cl", "complexAbs.cl", "rss.cl", "initialize.cl",
+           "optimizer.cl"]
 
 
 def build(force: bool = False) -> Path | None:
@@ -66,6 +67,8 @@ def lib() -> C.CDLL:
         L.ref_abs2.argtypes = [vp, i, i, i, i]
         L.ref_abs.argtypes = [vp, vp, i, i, i]
         L.ref_rss.argtypes = [vp, vp, i, i, i, i]
+        L.ref_mc.argtypes = [vp, vp, vp, vp, i, i, i, vp]
+        L.ref_mc_adjoint.argtypes = [vp, vp, vp, vp, i, i, i, vp]
         _lib = L
     return _lib
 
@@ -136,3 +139,25 @@ def rss(k: np.ndarray) -> np.ndarray:
     out = np.empty((F, H, W), np.complex64)
     lib().ref_rss(k.ctypes.data, out.ctypes.data, W, H, F, Cc)
     return out
+
+
+def _mc(fn, x, xn, xmesh, bb):
+    x = _c64(x)
+    F, H, W = x.shape
+    out = np.empty_like(x)
+    xn = np.ascontiguousarray(xn, np.float32)
+    xm = np.ascontiguousarray(xmesh, np.int32)
+    b = np.ascontiguousarray(bb, np.int32)
+    fn(x.ctypes.data, out.ctypes.data, xn.ctypes.data, xm.ctypes.data, W, H, F, b.ctypes.data)
+    return out
+
+
+def mc(x, xn, xmesh, bb):
+    """MotionCompensation with the reference's kernels (copy + interpolator)."""
+    return _mc(lib().ref_mc, x, xn, xmesh, bb)
+
+
+def mc_adjoint(x, xn, xmesh, bb):
+    """AdjointMotionCompensation with the reference's kernels (copy, zero rectangle, adjoint interpolator)."""
+    return _mc(lib().ref_mc_adjoint, x, xn, xmesh, bb)
+

@@ -9,6 +9,7 @@
 #include <OpenCLIPER/kernels/hostKernelFunctions.h>
 
 thread_local size_t gbnref_gid[3];
+thread_local size_t gbnref_gsz[3];
 
 #include "hostKernelFunctions.cl"
 #include "temporalTV.cl"
@@ -19,6 +20,8 @@ thread_local size_t gbnref_gid[3];
 #include "complexAbsPow2.cl"
 #include "complexAbs.cl"
 #include "rss.cl"
+#include "initialize.cl"
+#include "optimizer.cl"
 
 #include <vector>
 
@@ -55,6 +58,9 @@ RefBuf make(cl_uint W, cl_uint H, cl_uint C, cl_uint F, size_t elem_bytes, const
 
 template <typename Fn>
 void ndrange(size_t g0, size_t g1, size_t g2, Fn fn) {
+  gbnref_gsz[0] = g0;
+  gbnref_gsz[1] = g1;
+  gbnref_gsz[2] = g2;
   for (size_t k = 0; k < g2; ++k)
     for (size_t j = 0; j < g1; ++j)
       for (size_t i = 0; i < g0; ++i) {
@@ -132,6 +138,47 @@ void ref_abs(const float* in, float* out, int W, int H, int F) {
 void ref_rss(const float* in, float* out, int W, int H, int F, int C) {
   RefBuf a = make(W, H, C, F, 8, in), b = make(W, H, 0, F, 8, nullptr);
   ndrange(W, H, F, [&] { rss_kernel((float2*)a.data(), (float2*)b.data()); });
+  std::memcpy(out, b.data(), size_t(W) * H * F * 8);
+}
+
+// Row and column index lists of the motion-compensation rectangle, as
+// Interpolator / AdjointInterpolator / InitZeroRect::launch build them
+// (Interpolator.cpp:63-87): margins H/40, W/40 (integer division) around the
+// 1-based bounding box bb.
+struct McRect {
+  std::vector<int> r1, r2;
+};
+McRect mc_rect(int W, int H, const int* bb) {
+  const int m0 = int(std::ceil(cl_uint(H) / 40)), m1 = int(std::ceil(cl_uint(W) / 40));
+  const int l1 = (bb[3] + m0 + 1) - (bb[1] - m0 - 1) + 1, l2 = (bb[2] + m1 + 1) - (bb[0] - m1 - 1) + 1;
+  McRect r;
+  for (int i = 0; i < l1; ++i) r.r1.push_back((bb[1] - m0 - 1) + i - 1);
+  for (int j = 0; j < l2; ++j) r.r2.push_back((bb[0] - m1 - 1) + j - 1);
+  return r;
+}
+
+// MotionCompensation::launch (MotionCompensation.cpp:57-78): copyDataGPU, then
+// the interpolator over the rectangle.  xn [2][F][H][W], x [2][W][H] (1-based).
+void ref_mc(const float* in, float* out, const float* xn, const int* x, int W, int H, int F, const int* bb) {
+  RefBuf a = make(W, H, 0, F, 8, in), b = make(W, H, 0, F, 8, nullptr);
+  ndrange(size_t(W) * H * F, 1, 1, [&] { copyDataGPU((float2*)b.data(), (float2*)a.data()); });
+  McRect r = mc_rect(W, H, bb);
+  ndrange(r.r1.size(), r.r2.size(), F, [&] {
+    interpolator((float2*)b.data(), (float2*)a.data(), (float*)xn, (int*)x, r.r1.data(), r.r2.data());
+  });
+  std::memcpy(out, b.data(), size_t(W) * H * F * 8);
+}
+
+// AdjointMotionCompensation::launch (AdjointMotionCompensation.cpp:59-86):
+// copyDataGPU, initZeroRect over the rectangle, then adjointInterpolator.
+void ref_mc_adjoint(const float* in, float* out, const float* xn, const int* x, int W, int H, int F, const int* bb) {
+  RefBuf a = make(W, H, 0, F, 8, in), b = make(W, H, 0, F, 8, nullptr);
+  ndrange(size_t(W) * H * F, 1, 1, [&] { copyDataGPU((float2*)b.data(), (float2*)a.data()); });
+  McRect r = mc_rect(W, H, bb);
+  ndrange(r.r1.size(), r.r2.size(), F, [&] { initZeroRect((float2*)b.data(), r.r1.data(), r.r2.data()); });
+  ndrange(r.r1.size(), r.r2.size(), F, [&] {
+    adjointInterpolator((float2*)b.data(), (float2*)a.data(), (float*)xn, (int*)x, r.r1.data(), r.r2.data());
+  });
   std::memcpy(out, b.data(), size_t(W) * H * F * 8);
 }
 

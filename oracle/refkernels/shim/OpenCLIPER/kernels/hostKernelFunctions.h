@@ -37,14 +37,23 @@ inline float2 operator+(float2 a, float2 b) { return float2(a.x + b.x, a.y + b.y
 inline float2 operator-(float2 a, float2 b) { return float2(a.x - b.x, a.y - b.y); }
 inline float2 operator/(float2 a, float s) { return float2(a.x / s, a.y / s); }
 inline float2 operator*(float2 a, float s) { return float2(a.x * s, a.y * s); }
+inline float2 operator*(float s, float2 a) { return float2(s * a.x, s * a.y); }
 struct uint2 {
   cl_uint x, y;
 };
 typedef float2 complexType;
 
-// work-item id of the NDRange being executed by the host harness
+// work-item id and global sizes of the NDRange being executed by the host harness
 extern thread_local size_t gbnref_gid[3];
+extern thread_local size_t gbnref_gsz[3];
 inline size_t get_global_id(int d) { return gbnref_gid[d]; }
+inline size_t get_global_size(int d) { return gbnref_gsz[d]; }
+// the harness runs work-items one after another, so compare-and-swap is plain
+inline cl_uint atomic_cmpxchg(volatile cl_uint* p, cl_uint cmp, cl_uint val) {
+  const cl_uint old = *p;
+  if (old == cmp) *p = val;
+  return old;
+}
 inline float length(float2 v) { return std::sqrt(v.x * v.x + v.y * v.y); }
 inline float as_float(cl_uint u) { float f; std::memcpy(&f, &u, 4); return f; }
 inline cl_uint as_uint(float f) { cl_uint u; std::memcpy(&u, &f, 4); return u; }

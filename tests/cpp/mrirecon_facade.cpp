@@ -2,8 +2,11 @@
 // shape of the reference driver tests/MRIRecon.cpp:94-235 (create the runtime,
 // wrap the data, create the process, init, set launch parameters, launch).
 // Reads raw little-endian inputs written by tests/test_facade_gpu.py:
-//   <dir>/dims.u32 = W H F C, y.c64 [F][C][H][W], S.c64 [C][H][W], rowmask.u32 [F][H]
-// and writes x.c64 [F][H][W], simple.c64 [H][W] (frame 0 data), stats.txt.
+//   <dir>/dims.u32 = W H F C, y.c64 [F][C][H][W], S.c64 [C][H][W], rowmask.u32 [F][H],
+//   xn.f32 [2][F][H][W], xmesh.i32 [2][W][H], bb.u32 [4] (motion compensation)
+// and writes x.c64 [F][H][W], simple.c64 [H][W] (frame 0 data), mc.c64 and
+// mcadj.c64 (MotionCompensation / AdjointMotionCompensation of x), xmc.c64
+// (NestaUp with argsMC started from x), stats.txt.
 #include <cstdio>
 #include <fstream>
 #include <iostream>
@@ -13,6 +16,8 @@
 #include <OpenCLIPER/CLapp.hpp>
 #include <OpenCLIPER/KData.hpp>
 #include <OpenCLIPER/XData.hpp>
+#include <OpenCLIPER/processes/AdjointMotionCompensation.hpp>
+#include <OpenCLIPER/processes/MotionCompensation.hpp>
 #include <OpenCLIPER/processes/examples/SimpleMRIRecon.hpp>
 #include <OpenCLIPER/processes/nesta/NestaUp.hpp>
 
@@ -75,16 +80,48 @@ int main(int argc, char** argv) {
     pSimpleOut->device2Host(xs);
     writeRaw(dir + "/simple.c64", xs);
 
-    // the reference's error behaviour: a non-null motion-compensation argument is refused
-    auto bad = std::make_shared<NestaUp::LaunchParameters>(1e-2f, 3e-4f, 1.0f, 1u, 3e-4f, 1, 1, 0u, 7u,
-                                                           reinterpret_cast<ArgumentsMotionCompensation*>(params.get()));
-    nestaUpProcess->setLaunchParameters(bad);
+    // motion compensation: the operators on x, then NestaUp with argsMC
+    // started from x (the reference's motion-compensated pass reuses the
+    // output XData of the first reconstruction)
+    ArgumentsMotionCompensation args;
+    args.xnData = std::make_shared<ArrayData<float>>(pCLapp, readRaw<float>(dir + "/xn.f32", 2 * size_t(F) * H * W));
+    args.xData = std::make_shared<ArrayData<int>>(pCLapp, readRaw<int>(dir + "/xmesh.i32", 2 * size_t(W) * H));
+    const auto bbv = readRaw<uint32_t>(dir + "/bb.u32", 4);
+    std::vector<dimIndexType> bb(bbv.begin(), bbv.end());
+    args.bound_box = &bb;
+    auto mcOut = std::make_shared<XData>(pCLapp, pInputKData);
+    auto mc = Process::create<MotionCompensation>(pCLapp);
+    mc->setInput(pOutputXData);
+    mc->setOutput(mcOut);
+    mc->setLaunchParameters(std::make_shared<MotionCompensation::LaunchParameters>(&args));
+    mc->init();
+    mc->launch();
+    std::vector<complexType> h;
+    mcOut->device2Host(h);
+    writeRaw(dir + "/mc.c64", h);
+    auto adj = Process::create<AdjointMotionCompensation>(pCLapp);
+    adj->setInput(pOutputXData);
+    adj->setOutput(mcOut);
+    adj->setLaunchParameters(std::make_shared<AdjointMotionCompensation::LaunchParameters>(&args));
+    adj->init();
+    adj->launch();
+    mcOut->device2Host(h);
+    writeRaw(dir + "/mcadj.c64", h);
+    auto mcParams = std::make_shared<NestaUp::LaunchParameters>(1e-2f, 3e-4f, 1.0f, 1u, 3e-4f, 1, 20, 0u, 7u, &args);
+    nestaUpProcess->setLaunchParameters(mcParams);
+    nestaUpProcess->launch();
+    pOutputXData->device2Host(h);
+    writeRaw(dir + "/xmc.c64", h);
+    st << s.normU << " " << s.inner_iters << " " << s.status << "\n";
+
+    // the reference's error behaviour: a bounding box that is not 4 values is refused
+    bb.push_back(1);
     try {
       nestaUpProcess->launch();
-      std::cerr << "expected CLError\n";
+      std::cerr << "expected std::invalid_argument\n";
       return 3;
-    } catch (const CLError& e) {
-      st << "refused " << e.err() << "\n";
+    } catch (const std::invalid_argument& e) {
+      st << "refused bound_box\n";
     }
   } catch (const std::exception& e) {
     std::cerr << "error: " << e.what() << "\n";

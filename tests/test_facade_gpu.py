@@ -13,6 +13,7 @@ import pytest
 import opencliper_gb300 as g
 from opencliper_gb300 import api, synth
 from oracle import drand48
+from oracle import motion as M
 from tests.conftest import ROOT, rel_l2
 
 pytestmark = pytest.mark.gpu
@@ -38,13 +39,18 @@ def test_facade_matches_c_abi(ctx, driver, tmp_path):
     p.y.tofile(tmp_path / "y.c64")
     p.S.tofile(tmp_path / "S.c64")
     p.rowmask.astype(np.uint32).tofile(tmp_path / "rowmask.u32")
+    xn, xm, bb = M.synthetic(W, H, F, seed=5)
+    xn.astype(np.float32).tofile(tmp_path / "xn.f32")
+    xm.astype(np.int32).tofile(tmp_path / "xmesh.i32")
+    np.asarray(bb, np.uint32).tofile(tmp_path / "bb.u32")
     r = subprocess.run([str(driver), str(tmp_path)], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     x_cpp = np.fromfile(tmp_path / "x.c64", np.complex64).reshape(F, H, W)
     simple_cpp = np.fromfile(tmp_path / "simple.c64", np.complex64).reshape(F, H, W)
     lines = (tmp_path / "stats.txt").read_text().split("\n")
     normU, iters, tolvar = lines[0].split()
-    assert lines[1].startswith("refused -2")
+    normU_mc, iters_mc, status_mc = lines[1].split()
+    assert lines[2] == "refused bound_box"
 
     # the same through the C ABI (fresh drand48 state, like the driver's new context)
     ctx.seed48(drand48.state_to_seed16v(drand48.DEFAULT_STATE))
@@ -56,6 +62,25 @@ def test_facade_matches_c_abi(ctx, driver, tmp_path):
     out = ctx.empty((F, H, W), np.complex64)
     api.simple_recon(ctx, ctx.to_device(p.y), ctx.to_device(p.S), out)
     assert rel_l2(simple_cpp, out.get()) == 0.0
+
+    # motion compensation: the operators on x, then NestaUp with argsMC from x
+    mc_cpp = np.fromfile(tmp_path / "mc.c64", np.complex64).reshape(F, H, W)
+    mcadj_cpp = np.fromfile(tmp_path / "mcadj.c64", np.complex64).reshape(F, H, W)
+    assert np.array_equal(mc_cpp, M.warp(x_cpp, xn, xm, bb))
+    assert rel_l2(mcadj_cpp, M.warp_adjoint(x_cpp.astype(np.complex128), xn, xm, bb)) < 1e-6
+    dy, dS, dm = ctx.to_device(p.y), ctx.to_device(p.S), ctx.to_device(p.mask)
+    prob = g.Problem(ctx, dy, dS, dm)
+    prob.set_motion(ctx.to_device(xn), ctx.to_device(xm), bb)
+    xmc = ctx.to_device(x_cpp)
+    st_mc = prob.run(g.nesta_params(lambda_i=1e-2, mu_f=3e-4, La=1.0, maxIntIter=1, maxIter=20, stoptest=0,
+                                    miniter=7, tolVar=3e-4), xmc)
+    prob.close()
+    xmc_cpp = np.fromfile(tmp_path / "xmc.c64", np.complex64).reshape(F, H, W)
+    assert int(status_mc) == 0 and st_mc["status"] == 0
+    assert int(iters_mc) == st_mc["inner_iters"]
+    # the adjoint warp scatters with atomic adds: equal up to summation order
+    assert abs(float(normU_mc) - st_mc["normU"]) <= 2e-3 * st_mc["normU"]
+    assert rel_l2(xmc_cpp, xmc.get()) < 1e-4
 
 
 def test_facade_cfl_files(ctx, tmp_path):

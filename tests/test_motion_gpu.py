@@ -1,0 +1,71 @@
+"""Motion-compensated NESTA on the GPU: the warp and its adjoint against the
+oracle, and the full solve (NestaUp with argsMC) against the FP64 / FP32
+restatement started from the same image.  The warp is a gather with the
+reference kernel's rounding and matches bit for bit; the adjoint scatters with
+atomic adds like the reference's kernel, so its sums are compared with a
+tolerance.  With motion compensation the power method starts from the
+interpolation's rounding residue on a constant image and converges slowly, so
+a last-place difference from the scatter can move its stopping step by one
+(about 1e-3 of ||U||): ||U|| is compared to 2e-3."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+import opencliper_gb300 as g
+from opencliper_gb300 import api, synth
+from oracle import drand48
+from oracle import motion as M
+from oracle import nesta_ref as R
+from tests.conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("W,H,F", [(48, 40, 3), (128, 96, 5)])
+def test_motion_operators(ctx, W, H, F):
+    xn, xm, bb = M.synthetic(W, H, F, seed=W)
+    rng = np.random.default_rng(H)
+    x = (rng.standard_normal((F, H, W)) + 1j * rng.standard_normal((F, H, W))).astype(np.complex64)
+    dx, out = ctx.to_device(x), ctx.empty((F, H, W), np.complex64)
+    dxn, dxm = ctx.to_device(xn), ctx.to_device(xm)
+    api.op_motion(ctx, 1, dx, out, dxn, dxm, bb)  # forward (GBN_TTV_FORWARD): a gather, bit-exact
+    assert np.array_equal(out.get(), M.warp(x, xn, xm, bb))
+    api.op_motion(ctx, 0, dx, out, dxn, dxm, bb)  # adjoint
+    assert rel_l2(out.get(), M.warp_adjoint(x.astype(np.complex128), xn, xm, bb)) < 1e-6
+
+
+def test_motion_rejects_bad_box(ctx):
+    W, H, F = 32, 32, 2
+    xn, xm, bb = M.synthetic(W, H, F, seed=1)
+    x = ctx.zeros((F, H, W), np.complex64)
+    with pytest.raises(g.GbnError):
+        api.op_motion(ctx, 1, x, x, ctx.to_device(xn), ctx.to_device(xm), [1, 1, W + 5, H])
+
+
+@pytest.mark.parametrize("W,H,F,C,Rr", [(48, 40, 6, 3, 4), (64, 64, 8, 4, 4)])
+def test_nesta_motion_compensated(ctx, W, H, F, C, Rr):
+    p = synth.make_problem(W, H, F, C, Rr, seed=W + F)
+    xn, xm, bb = M.synthetic(W, H, F, seed=F)
+    dy, dS, dm = ctx.to_device(p.y), ctx.to_device(p.S), ctx.to_device(p.mask)
+    prob = g.Problem(ctx, dy, dS, dm)
+    prm = dict(lambda_i=0.01, mu_f=1e-3, La=1.0, maxIntIter=1, maxIter=25, stoptest=0, miniter=7, tolVar=3e-4)
+    x = ctx.empty((F, H, W), np.complex64)
+    prob.run(g.nesta_params(**prm), x)            # first reconstruction, without motion
+    x0 = x.get()
+    dxn, dxm = ctx.to_device(xn), ctx.to_device(xm)
+    prob.set_motion(dxn, dxm, bb)
+    s0 = drand48.seed16v_to_state(ctx.rand48())
+    st = prob.run(g.nesta_params(**prm), x)       # starts from x0, the output's content
+    got = x.get()
+    prob.close()
+    assert st["status"] == 0
+    r64 = R.nesta(p.y, p.S, p.mask, R.NestaParams(**prm), "f64", rand_state=s0, mc=(xn, xm, bb), x_init=x0)
+    r32 = R.nesta(p.y, p.S, p.mask, R.NestaParams(**prm), "f32", rand_state=s0, mc=(xn, xm, bb), x_init=x0)
+    e_gpu, e_32 = R.nrmse(got, r64.x), R.nrmse(r32.x, r64.x)
+    print(f"MC NRMSE gpu/f64 {e_gpu:.3e}  f32-oracle/f64 {e_32:.3e}  normU {st['normU']:.5f} vs {r32.stats['normU']:.5f}")
+    assert np.isfinite(got).all()
+    assert abs(st["normU"] - r32.stats["normU"]) <= 2e-3 * r32.stats["normU"]
+    assert abs(st["normest_iters"] - r32.stats["normest_iters"]) <= 1
+    assert e_gpu <= 2.0 * e_32 + 2e-5
+    assert st["inner_iters"] == r32.stats["inner_iters"]
