@@ -305,6 +305,7 @@ def run_ours(args, dist: Dist) -> dict | None:
     if not args.no_forms and dist.ws == 1:
         forms["mixed"] = mixed_forms(ctx, stream)
         forms["batched"] = batched_form(ctx, stream)
+        forms["motion"] = motion_form(ctx, stream)
     ctx.set_stream(None)
     ctx.close()
     n = dist.ws
@@ -377,6 +378,54 @@ def mixed_forms(ctx, stream, reps: int = 5) -> dict:
         for a in (p.y, p.S, p.mask, x):
             a.free()
     return out
+
+
+def motion_form(ctx, stream, reps: int = 3) -> dict:
+    """The motion-compensated form (NestaUp with argsMC) on the headline
+    workload: a seeded smooth motion estimate (synth.make_motion, up to 1.2 px
+    displacements over the whole field of view), started from the plain
+    reconstruction's image as the reference's motion-compensated pass is;
+    same NESTA settings; events on the library's stream around each run, the
+    starting image re-uploaded outside them.  The plain FP32 solve of the same
+    problem is timed alongside."""
+    import opencliper_gb300 as g
+    from opencliper_gb300 import synth
+    W, H, F, Cc, Rr = WL["W"], WL["H"], WL["F"], WL["C"], WL["R"]
+    p = synth.make_problem_device(ctx, W, H, F, Cc, Rr, seed=11)
+    prob = g.Problem(ctx, p.y, p.S, p.mask)
+    x = ctx.empty((F, H, W), np.complex64)
+    prm = g.nesta_params(**NESTA)
+    prob.run(prm, x)
+    x0 = x.get()
+    xn, xm, bb = synth.make_motion(W, H, F, seed=3)
+    dxn, dxm = ctx.to_device(xn), ctx.to_device(xm)
+    res = {"workload": f"{W}x{H} x {F} frames, {Cc} coils, R={Rr}, {NESTA['maxIter']} iterations, "
+                       "motion estimate: identity mesh + sinusoidal displacements <= 1.2 px", "unit": UNIT}
+    for name, mc in (("plain", False), ("motion", True)):
+        prob.set_motion(dxn, dxm, bb) if mc else prob.set_motion(None, None, None)
+        times, st = [], None
+        for k in range(reps + 1):
+            x.set(x0)
+            a, c = torch_events()
+            a.record(stream)
+            st = prob.run(prm, x, stats=False) if k < reps else prob.run(prm, x, stats=True)
+            c.record(stream)
+            stream.synchronize()
+            if k > 0 or reps == 0:
+                times.append(a.elapsed_time(c))
+        ms = sum(times) / len(times)
+        res[name] = {"value": round(1e3 / ms, 3), "ms_per_recon": round(ms, 3), "status": int(st["status"]),
+                     "normU": round(float(st["normU"]), 5), "normest_iters": int(st["normest_iters"])}
+    res["motion_over_plain_time"] = round(res["plain"]["value"] / res["motion"]["value"], 3)
+    prob.close()
+    for a in (p.y, p.S, p.mask, x, dxn, dxm):
+        a.free()
+    return res
+
+
+def torch_events():
+    import torch
+    return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
 
 
 BATCH_WL = dict(n=64, sizes=(128, 192, 256, 320, 384), frames=(12, 40), coils=(8, 32), accel=(4, 12), seed0=1000)

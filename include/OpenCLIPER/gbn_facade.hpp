@@ -21,6 +21,7 @@
 #include <complex>
 #include <cstdint>
 #include <fstream>
+#include <map>
 #include <memory>
 #include <sstream>
 #include <stdexcept>
@@ -28,6 +29,7 @@
 #include <vector>
 
 #include "../gbn.h"
+#include "gbn_matfile.hpp"
 
 namespace OpenCLIPER {
 
@@ -137,6 +139,12 @@ class SensitivityMapsData : public Data {
     upload(maps.data());
   }
   dimIndexType getNCoils() const { return C_; }
+  dimIndexType width() const { return W_; }
+  dimIndexType height() const { return H_; }
+  void device2Host(std::vector<complexType>& out) const {
+    out.resize(size_t(W_) * H_ * C_);
+    download(out.data());
+  }
 
  private:
   dimIndexType W_, H_, C_;
@@ -174,6 +182,82 @@ class SamplingMasksData : public Data {
       : Data(app, size_t(W) * H * F) {}
 };
 
+namespace matio {
+// The Dims variable (MatVarDimsData.cpp:41-67): uint32 [nSpatialDims,
+// allSizesEqual, nCoils, nTemporalDims, temporal dims..., spatial dims...]
+// with the spatial dims as (width, height).
+struct Dims {
+  dimIndexType W = 0, H = 0, C = 0, F = 1, nT = 0;
+};
+inline Dims parse_dims(const std::map<std::string, matfile::Var>& vars, const char* who) {
+  const auto it = vars.find("Dims");
+  if (it == vars.end()) throw std::invalid_argument("Error: no Dims variable in matlab file");
+  const matfile::Var& v = it->second;
+  if (v.complex || v.cls != matfile::kUInt32)
+    throw std::invalid_argument("Matlab dims variable should be an array of 32 bits unsigned integers");
+  const uint32_t* d = v.real<uint32_t>();
+  const size_t n = v.numel();
+  if (n < 4) throw std::invalid_argument(std::string(who) + ": Dims variable too short");
+  const size_t nS = d[0], nT = d[3];
+  if (n < 4 + nT + nS) throw std::invalid_argument(std::string(who) + ": Dims variable too short");
+  if (nS != 2)
+    throw std::invalid_argument(std::string(who) + ": only 2 spatial dimensions are supported (Dims says " +
+                                std::to_string(nS) + ")");
+  Dims r;
+  r.C = d[2];
+  r.nT = dimIndexType(nT);
+  for (size_t i = 0; i < nT; ++i) r.F *= d[4 + i];
+  r.W = d[4 + nT];
+  r.H = d[5 + nT];
+  return r;
+}
+inline matfile::Var dims_var(dimIndexType W, dimIndexType H, dimIndexType C, dimIndexType F) {
+  const uint32_t d[7] = {2u, 1u, uint32_t(C), 1u, uint32_t(F), uint32_t(W), uint32_t(H)};
+  matfile::Var v;
+  v.name = "Dims";
+  v.cls = matfile::kUInt32;
+  v.dims = {1, 7};
+  v.re.assign(reinterpret_cast<const uint8_t*>(d), reinterpret_cast<const uint8_t*>(d) + sizeof(d));
+  return v;
+}
+// MATLAB (rows=H, cols=W, outer...) -> row-major complex [outer][H][W]
+inline std::vector<complexType> complex_rows(const matfile::Var& v, const char* who) {
+  if (v.cls != matfile::kSingle && v.cls != matfile::kDouble)
+    throw std::invalid_argument(std::string(who) + ": Unsupported element data type in matlab data");
+  std::vector<float> re, im;
+  if (v.cls == matfile::kSingle) {
+    matfile::to_row_major<float>(v, re, &im);
+  } else {
+    std::vector<double> r, i;
+    matfile::to_row_major<double>(v, r, &i);
+    re.assign(r.begin(), r.end());
+    im.assign(i.begin(), i.end());
+  }
+  std::vector<complexType> out(re.size());
+  for (size_t k = 0; k < re.size(); ++k) out[k] = complexType(re[k], im[k]);
+  return out;
+}
+inline matfile::Var complex_var(const std::string& name, const std::vector<complexType>& rows, size_t H, size_t W,
+                                const std::vector<uint64_t>& outer) {
+  std::vector<float> re(rows.size()), im(rows.size());
+  for (size_t k = 0; k < rows.size(); ++k) {
+    re[k] = rows[k].real();
+    im[k] = rows[k].imag();
+  }
+  return matfile::from_row_major<float>(name, matfile::kSingle, re.data(), im.data(), H, W, outer);
+}
+// MATLAB dims after (H, W) must equal `want`; trailing singleton dimensions may be absent
+inline void check_dims(const matfile::Var& v, dimIndexType H, dimIndexType W, const std::vector<uint64_t>& want,
+                       const char* who) {
+  if (v.dims.size() < 2 || v.dims[0] != H || v.dims[1] != W)
+    throw std::out_of_range(std::string("Invalid ") + who + " spatial dimensions");
+  std::vector<uint64_t> got(v.dims.begin() + 2, v.dims.end()), w = want;
+  while (!got.empty() && got.back() == 1) got.pop_back();
+  while (!w.empty() && w.back() == 1) w.pop_back();
+  if (got != w) throw std::out_of_range(std::string("Invalid ") + who + " dimensions");
+}
+}  // namespace matio
+
 /// KData: multicoil k-space [F][C][H][W] with its sensitivity maps and masks.
 class KData : public Data {
  public:
@@ -185,13 +269,16 @@ class KData : public Data {
     if (data.size() != size_t(W) * H * F * C) throw std::invalid_argument("KData: size mismatch");
     upload(data.data());
   }
-  /// KData(app, fileName, asyncLoad) in its CFL form (KData.cpp:246-351):
-  /// header <base>.hdr (first line not starting with '#': "W H C F"), data
-  /// `fileName` as raw complex float [F][C][H][W], sensitivity maps
-  /// <base>_SensitivityMaps.cfl [C][H][W] and the sampling masks
-  /// <base>_SamplingMasks.u32 (row mask [F][H], expanded to pixels) or else
-  /// <base>_SamplingMasks.u8 (pixel mask [F][H][W]), each when present.  MATLAB
-  /// files are not supported (no matio); the load is synchronous.
+  /// KData(app, fileName, asyncLoad) (KData.cpp:276-435).  A MAT-file holds
+  /// Dims, KData (single complex, MATLAB dims H x W [x C] x F) and, when
+  /// present, SensitivityMaps (H x W x C) and SamplingMasks (uint32 row mask
+  /// H x F, expanded to pixels, or uint8 pixel mask H x W x F).  Any other
+  /// file is read in the CFL form (KData.cpp:246-351): header <base>.hdr
+  /// (first line not starting with '#': "W H C F"), data `fileName` as raw
+  /// complex float [F][C][H][W], sensitivity maps <base>_SensitivityMaps.cfl
+  /// [C][H][W] and the sampling masks <base>_SamplingMasks.u32 (row mask
+  /// [F][H]) or else <base>_SamplingMasks.u8 (pixel mask [F][H][W]), each
+  /// when present.  Only 2-D Cartesian data; the load is synchronous.
   KData(const std::shared_ptr<CLapp>& app, const std::string& fileName, bool asyncLoad = false)
       : KData(load(app, fileName)) {
     (void)asyncLoad;
@@ -206,6 +293,21 @@ class KData : public Data {
     out.resize(size_t(W_) * H_ * F_ * C_);
     download(out.data());
   }
+  /// KData::matlabSave (KData.cpp:837-884): Dims, KData (H x W x C x F) and
+  /// SensitivityMaps (H x W x C) when present; the sampling masks are not
+  /// saved, as in the reference.  Written uncompressed.
+  void matlabSave(const std::string& fileName) const {
+    std::vector<matfile::Var> vars;
+    vars.push_back(matio::dims_var(W_, H_, C_, F_));
+    std::vector<complexType> h;
+    device2Host(h);
+    vars.push_back(matio::complex_var("KData", h, H_, W_, {C_, F_}));
+    if (sens_) {
+      sens_->device2Host(h);
+      vars.push_back(matio::complex_var("SensitivityMaps", h, H_, W_, {C_}));
+    }
+    matfile::write(fileName, vars);
+  }
 
  private:
   struct Loaded {
@@ -216,14 +318,41 @@ class KData : public Data {
     std::shared_ptr<SamplingMasksData> masks;
   };
   explicit KData(Loaded&& l) : KData(l.app, l.W, l.H, l.F, l.C, l.data, l.sens, l.masks) {}
-  static Loaded load(const std::shared_ptr<CLapp>& app, const std::string& fileName) {
-    {
-      std::ifstream probe(fileName, std::ios::binary);
-      char magic[6] = {0};
-      probe.read(magic, 6);
-      if (probe.gcount() == 6 && std::string(magic, 6) == "MATLAB")
-        throw std::invalid_argument("KData: MATLAB files are not supported by this library (use the CFL form)");
+  static Loaded load_mat(const std::shared_ptr<CLapp>& app, const std::string& fileName) {
+    const auto vars = matfile::read(fileName);
+    const matio::Dims d = matio::parse_dims(vars, "KData::KData");
+    const auto it = vars.find("KData");
+    if (it == vars.end()) throw std::invalid_argument("Error: no KData variable in matlab file");
+    const dimIndexType C = d.C > 1 ? d.C : 1;
+    matio::check_dims(it->second, d.H, d.W, {C, d.F}, "KData");
+    Loaded l{app, d.W, d.H, d.F, C, matio::complex_rows(it->second, "KData"), nullptr, nullptr};
+    const auto sm = vars.find("SensitivityMaps");
+    if (sm != vars.end()) {
+      matio::check_dims(sm->second, d.H, d.W, {C}, "SensitivityMaps");
+      l.sens = std::make_shared<SensitivityMapsData>(app, d.W, d.H, C, matio::complex_rows(sm->second, "SensitivityMaps"));
     }
+    const auto mk = vars.find("SamplingMasks");
+    if (mk != vars.end()) {
+      const matfile::Var& m = mk->second;
+      if (m.complex) throw std::invalid_argument("Invalid mask format (supported: ROWMASK and PIXELMASK");
+      if (m.cls == matfile::kUInt32) {  // row mask: MATLAB dims H x F (one 1-D array per frame)
+        if (m.dims[0] != d.H || m.numel() != size_t(d.H) * d.F)
+          throw std::out_of_range("Invalid SamplingMasks dimensions");
+        const uint32_t* r = m.real<uint32_t>();
+        l.masks = SamplingMasksData::fromRowMask(app, d.W, d.H, d.F, std::vector<uint32_t>(r, r + m.numel()));
+      } else if (m.cls == matfile::kUInt8) {  // pixel mask: H x W x F
+        matio::check_dims(m, d.H, d.W, {d.F}, "SamplingMasks");
+        std::vector<uint8_t> px;
+        matfile::to_row_major<uint8_t>(m, px, nullptr);
+        l.masks = std::make_shared<SamplingMasksData>(app, d.W, d.H, d.F, px);
+      } else {
+        throw std::invalid_argument("Invalid mask format (supported: ROWMASK and PIXELMASK");
+      }
+    }
+    return l;
+  }
+  static Loaded load(const std::shared_ptr<CLapp>& app, const std::string& fileName) {
+    if (matfile::is_mat(fileName)) return load_mat(app, fileName);
     const std::string base = cfl::basename(fileName);
     std::ifstream hdr(base + ".hdr");
     if (!hdr) throw std::invalid_argument("KData: cannot open " + base + ".hdr");
@@ -273,12 +402,23 @@ class XData : public Data {
     if (data.size() != size_t(W) * H * F) throw std::invalid_argument("XData: size mismatch");
     upload(data.data());
   }
+  /// XData(app, fileName) from a MAT-file (XData.cpp:504-558): Dims and XData
+  /// (single, MATLAB dims H x W x F; a real array gets a zero imaginary part).
+  /// Image files (OpenCV) are not supported.
+  XData(const std::shared_ptr<CLapp>& app, const std::string& fileName) : XData(load_mat(app, fileName)) {}
   dimIndexType getDynDimsTotalSize() const { return F_; }
   dimIndexType width() const { return W_; }
   dimIndexType height() const { return H_; }
   void device2Host(std::vector<complexType>& out) const {
     out.resize(size_t(W_) * H_ * F_);
     download(out.data());
+  }
+  /// XData::matlabSave (XData.cpp:886-930): Dims [2, 1, 0, 1, F, W, H] and
+  /// XData (single complex, H x W x F).  Written uncompressed.
+  void matlabSave(const std::string& fileName) const {
+    std::vector<complexType> h;
+    device2Host(h);
+    matfile::write(fileName, {matio::dims_var(W_, H_, 0, F_), matio::complex_var("XData", h, H_, W_, {F_})});
   }
   /// XData::saveCFLData (XData.cpp:851-881): `fileName`.cfl raw complex float
   /// [F][H][W] and <basename(fileName)>.hdr "W H 1 F 1"; synchronous.
@@ -295,6 +435,23 @@ class XData : public Data {
   }
 
  private:
+  struct Loaded {
+    std::shared_ptr<CLapp> app;
+    dimIndexType W, H, F;
+    std::vector<complexType> data;
+  };
+  explicit XData(Loaded&& l) : XData(l.app, l.W, l.H, l.F, l.data) {}
+  static Loaded load_mat(const std::shared_ptr<CLapp>& app, const std::string& fileName) {
+    if (!matfile::is_mat(fileName))
+      throw std::invalid_argument("XData: " + fileName + " is not a MAT-file (image files are not supported)");
+    const auto vars = matfile::read(fileName);
+    const matio::Dims d = matio::parse_dims(vars, "XData::XData");
+    const auto it = vars.find("XData");
+    if (it == vars.end()) throw std::invalid_argument("Error: no XData variable in matlab file");
+    if (d.C > 1) throw std::out_of_range("Invalid XData dimensions (XData has no coil dimension)");
+    matio::check_dims(it->second, d.H, d.W, {d.F}, "XData");
+    return Loaded{app, d.W, d.H, d.F, matio::complex_rows(it->second, "XData")};
+  }
   dimIndexType W_, H_, F_;
 };
 

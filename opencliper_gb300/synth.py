@@ -179,3 +179,29 @@ def make_problem_device(ctx, W: int, H: int, F: int, C: int, R: float, seed: int
     dx.free()
     return DeviceProblem(dy, dS, dm, rm, int(seed))
 
+
+def make_motion(W: int, H: int, F: int, seed: int, amplitude: float = 1.2, border: int = 4):
+    """A seeded smooth stand-in for a motion estimate, in the layouts of
+    ArgumentsMotionCompensation (include/OpenCLIPER/processes/
+    GroupwiseRegistration.hpp:95-100): returns (xn [2][F][H][W] float32 deformed
+    mesh, xmesh [2][W][H] int32 original mesh, bb [4] int32 bounding box), all
+    1-based.  The original mesh is the identity; each frame's deformed mesh adds
+    sinusoidal sub-pixel displacements of at most `amplitude` pixels; the
+    bounding box sits `border` pixels inside the margins (H/40, W/40) that the
+    interpolator adds around it, so every interpolation stays in the image."""
+    rng = np.random.default_rng(seed)
+    m0, m1 = H // 40, W // 40
+    # rectangle rows bb1-m0-2 .. bb3+m0-1 and columns bb0-m1-2 .. bb2+m1-1 (0-based)
+    bb = np.array([m1 + 2 + border, m0 + 2 + border, W - m1 - border, H - m0 - border], np.int32)
+    xmesh = np.empty((2, W, H), np.int32)
+    xmesh[0] = np.arange(W)[:, None] + 1  # horizontal = column + 1
+    xmesh[1] = np.arange(H)[None, :] + 1  # vertical = row + 1
+    rr, cc = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
+    xn = np.empty((2, F, H, W), np.float32)
+    for f in range(F):
+        ph = rng.uniform(0, 2 * np.pi, 4)
+        dx = amplitude * np.sin(2 * np.pi * rr / H + ph[0]) * np.cos(2 * np.pi * cc / W + ph[1])
+        dy = amplitude * np.cos(2 * np.pi * rr / H + ph[2]) * np.sin(2 * np.pi * cc / W + ph[3])
+        xn[0, f] = (cc + 1 + dx).astype(np.float32)
+        xn[1, f] = (rr + 1 + dy).astype(np.float32)
+    return xn, xmesh, bb

@@ -3,7 +3,8 @@
 (src/processes/MotionCompensation.cpp:57-78, AdjointMotionCompensation.cpp:
 59-86) and their kernels (src/kernels/optimizer.cl:832-937 interpolator /
 adjointInterpolator, src/kernels/initialize.cl:55-80 initZeroRect /
-copyDataGPU), plus a seeded synthetic stand-in for the motion estimate.
+copyDataGPU).  Pinned bit for bit against those kernels compiled for the host
+(oracle/refkernels.py).
 
 Layouts (as ArgumentsMotionCompensation holds them, GroupwiseRegistration.hpp:
 95-100): xmesh = original mesh [2][W][H] int32, xn = deformed mesh [2][F][H][W]
@@ -86,26 +87,3 @@ def warp_adjoint(g: np.ndarray, xn, xmesh, bb) -> np.ndarray:
                       part * Whh * Wvv], axis=1).ravel()
         np.add.at(acc, idx, w)  # unbuffered, in index-array order
     return (re + 1j * im).reshape(F, H, W).astype(g.dtype)
-
-
-def synthetic(W: int, H: int, F: int, seed: int, amplitude: float = 1.2, border: int = 4):
-    """A seeded smooth motion estimate: identity original mesh, deformed mesh =
-    identity + sinusoidal sub-pixel displacements per frame, bounding box `border`
-    pixels inside the margins so that every interpolation stays in the image."""
-    rng = np.random.default_rng(seed)
-    m0, m1 = H // 40, W // 40
-    # rows r1 = bb1-m0-2 .. bb3+m0-1 and columns r2 = bb0-m1-2 .. bb2+m1-1 must stay
-    # `border` pixels inside the image
-    bb = np.array([m1 + 2 + border, m0 + 2 + border, W - m1 - border, H - m0 - border], np.int32)
-    xmesh = np.empty((2, W, H), np.int32)
-    xmesh[0] = (np.arange(W)[:, None] + 1)  # horizontal = column + 1
-    xmesh[1] = (np.arange(H)[None, :] + 1)  # vertical = row + 1
-    rr, cc = np.meshgrid(np.arange(H), np.arange(W), indexing="ij")
-    xn = np.empty((2, F, H, W), np.float32)
-    for f in range(F):
-        ph = rng.uniform(0, 2 * np.pi, 4)
-        dx = amplitude * np.sin(2 * np.pi * rr / H + ph[0]) * np.cos(2 * np.pi * cc / W + ph[1])
-        dy = amplitude * np.cos(2 * np.pi * rr / H + ph[2]) * np.sin(2 * np.pi * cc / W + ph[3])
-        xn[0, f] = (cc + 1 + dx).astype(np.float32)
-        xn[1, f] = (rr + 1 + dy).astype(np.float32)
-    return xn, xmesh, bb

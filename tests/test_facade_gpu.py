@@ -39,7 +39,7 @@ def test_facade_matches_c_abi(ctx, driver, tmp_path):
     p.y.tofile(tmp_path / "y.c64")
     p.S.tofile(tmp_path / "S.c64")
     p.rowmask.astype(np.uint32).tofile(tmp_path / "rowmask.u32")
-    xn, xm, bb = M.synthetic(W, H, F, seed=5)
+    xn, xm, bb = synth.make_motion(W, H, F, seed=5)
     xn.astype(np.float32).tofile(tmp_path / "xn.f32")
     xm.astype(np.int32).tofile(tmp_path / "xmesh.i32")
     np.asarray(bb, np.uint32).tofile(tmp_path / "bb.u32")
@@ -116,3 +116,41 @@ def test_facade_cfl_files(ctx, tmp_path):
     assert R.nrmse(nesta, r64.x) <= 2.0 * R.nrmse(r32.x, r64.x) + 5e-6
     hdr = (tmp_path / "out_nesta.hdr").read_text().split()
     assert hdr == [str(W), str(H), "1", str(F), "1"]
+
+
+def test_facade_mat_files(ctx, tmp_path):
+    """KData(app, "x.mat") (compressed MAT-file with Dims, KData,
+    SensitivityMaps and a row-mask SamplingMasks, as KData.cpp:276-435 reads
+    it), SimpleMRIRecon and NestaUp through the facade, results written by
+    XData::matlabSave and KData::matlabSave and read back with scipy.io;
+    XData(app, "x.mat") reloads the saved image exactly."""
+    pytest.importorskip("scipy.io")
+    from opencliper_gb300 import matfile
+    from oracle import nesta_ref as R
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("g++ not available")
+    exe = tmp_path / "mat_facade"
+    libdir = os.path.join(ROOT, "opencliper_gb300")
+    subprocess.run([cxx, "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "mat_facade.cpp"), "-L", libdir, "-lgbnesta",
+                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    W, H, F, C = 40, 32, 4, 3
+    p = synth.make_problem(W, H, F, C, 2, seed=17)
+    kfile = str(tmp_path / "series.mat")
+    matfile.write_kdata(kfile, p.y, p.S, rowmask=p.rowmask)
+    out = str(tmp_path / "out")
+    r = subprocess.run([str(exe), kfile, out], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    assert (tmp_path / "out_stats.txt").read_text().split() == ["reload", "0"]
+    simple = matfile.read_xdata(out + "_simple.mat")
+    nesta = matfile.read_xdata(out + "_nesta.mat")
+    y2, S2 = matfile.read_kdata(out + "_k.mat")
+    assert np.array_equal(y2, p.y) and np.array_equal(S2, p.S.astype(np.complex64))
+    import scipy.io as sio
+    assert sio.loadmat(out + "_simple.mat")["Dims"].ravel().tolist() == [2, 1, 0, 1, F, W, H]
+    assert rel_l2(simple, R.simple_recon(p.y.astype(np.complex128), p.S.astype(np.complex128))) < 1e-5
+    prm = R.NestaParams(lambda_i=0.01, mu_f=1e-3, La=1.0, maxIntIter=1, maxIter=20, stoptest=0, miniter=7, tolVar=3e-4)
+    r64 = R.nesta(p.y, p.S, p.mask, prm, "f64")
+    r32 = R.nesta(p.y, p.S, p.mask, prm, "f32")
+    assert R.nrmse(nesta, r64.x) <= 2.0 * R.nrmse(r32.x, r64.x) + 5e-6

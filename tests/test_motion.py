@@ -6,6 +6,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
+from opencliper_gb300 import synth
 from oracle import motion as M
 from oracle import refkernels as K
 
@@ -14,7 +15,7 @@ pytestmark = pytest.mark.skipif(K.build() is None, reason="reference kernel sour
 
 @pytest.mark.parametrize("W,H,F,seed", [(48, 40, 3, 1), (96, 80, 2, 2), (40, 160, 4, 3)])
 def test_motion_oracle_matches_reference_kernels(W, H, F, seed):
-    xn, xm, bb = M.synthetic(W, H, F, seed=seed)
+    xn, xm, bb = synth.make_motion(W, H, F, seed=seed)
     rng = np.random.default_rng(seed)
     x = (rng.standard_normal((F, H, W)) + 1j * rng.standard_normal((F, H, W))).astype(np.complex64)
     assert np.array_equal(K.mc(x, xn, xm, bb), M.warp(x, xn, xm, bb))
@@ -23,7 +24,7 @@ def test_motion_oracle_matches_reference_kernels(W, H, F, seed):
 
 def test_motion_adjoint_identity():
     W, H, F = 64, 48, 3
-    xn, xm, bb = M.synthetic(W, H, F, seed=9)
+    xn, xm, bb = synth.make_motion(W, H, F, seed=9)
     rng = np.random.default_rng(4)
     x = rng.standard_normal((F, H, W)) + 1j * rng.standard_normal((F, H, W))
     y = rng.standard_normal((F, H, W)) + 1j * rng.standard_normal((F, H, W))

@@ -24,7 +24,7 @@ pytestmark = pytest.mark.gpu
 
 @pytest.mark.parametrize("W,H,F", [(48, 40, 3), (128, 96, 5)])
 def test_motion_operators(ctx, W, H, F):
-    xn, xm, bb = M.synthetic(W, H, F, seed=W)
+    xn, xm, bb = synth.make_motion(W, H, F, seed=W)
     rng = np.random.default_rng(H)
     x = (rng.standard_normal((F, H, W)) + 1j * rng.standard_normal((F, H, W))).astype(np.complex64)
     dx, out = ctx.to_device(x), ctx.empty((F, H, W), np.complex64)
@@ -37,7 +37,7 @@ def test_motion_operators(ctx, W, H, F):
 
 def test_motion_rejects_bad_box(ctx):
     W, H, F = 32, 32, 2
-    xn, xm, bb = M.synthetic(W, H, F, seed=1)
+    xn, xm, bb = synth.make_motion(W, H, F, seed=1)
     x = ctx.zeros((F, H, W), np.complex64)
     with pytest.raises(g.GbnError):
         api.op_motion(ctx, 1, x, x, ctx.to_device(xn), ctx.to_device(xm), [1, 1, W + 5, H])
@@ -46,7 +46,7 @@ def test_motion_rejects_bad_box(ctx):
 @pytest.mark.parametrize("W,H,F,C,Rr", [(48, 40, 6, 3, 4), (64, 64, 8, 4, 4)])
 def test_nesta_motion_compensated(ctx, W, H, F, C, Rr):
     p = synth.make_problem(W, H, F, C, Rr, seed=W + F)
-    xn, xm, bb = M.synthetic(W, H, F, seed=F)
+    xn, xm, bb = synth.make_motion(W, H, F, seed=F)
     dy, dS, dm = ctx.to_device(p.y), ctx.to_device(p.S), ctx.to_device(p.mask)
     prob = g.Problem(ctx, dy, dS, dm)
     prm = dict(lambda_i=0.01, mu_f=1e-3, La=1.0, maxIntIter=1, maxIter=25, stoptest=0, miniter=7, tolVar=3e-4)
