@@ -303,9 +303,10 @@ def run_ours(args, dist: Dist) -> dict | None:
         a.free()
     forms = {}
     if not args.no_forms and dist.ws == 1:
-        forms["mixed"] = mixed_forms(ctx, stream)
-        forms["batched"] = batched_form(ctx, stream)
-        forms["motion"] = motion_form(ctx, stream)
+        wanted = {f.strip() for f in args.forms.split(",") if f.strip()}
+        for name, fn in FORMS:
+            if name in wanted:
+                forms[name] = fn(ctx, stream, args)
     ctx.set_stream(None)
     ctx.close()
     n = dist.ws
@@ -347,7 +348,7 @@ def _nrmse(a: np.ndarray, b: np.ndarray) -> float:
     return float(np.linalg.norm((a - b).ravel()) / max(np.linalg.norm(b.ravel()), 1e-30))
 
 
-def mixed_forms(ctx, stream, reps: int = 5) -> dict:
+def mixed_forms(ctx, stream, args=None, reps: int = 5) -> dict:
     """The mixed-precision form (column transforms on the tensor cores, split
     fp16 operands, FP32 accumulation) against the plain FP32 path on the
     headline workload and on the 384x384 x 30 frames x 16 coils workload, same
@@ -380,7 +381,7 @@ def mixed_forms(ctx, stream, reps: int = 5) -> dict:
     return out
 
 
-def motion_form(ctx, stream, reps: int = 3) -> dict:
+def motion_form(ctx, stream, args=None) -> dict:
     """The motion-compensated form (NestaUp with argsMC) on the headline
     workload: a seeded smooth motion estimate (synth.make_motion, up to 1.2 px
     displacements over the whole field of view), started from the plain
@@ -390,6 +391,7 @@ def motion_form(ctx, stream, reps: int = 3) -> dict:
     problem is timed alongside."""
     import opencliper_gb300 as g
     from opencliper_gb300 import synth
+    reps = args.form_reps if args is not None else 3
     W, H, F, Cc, Rr = WL["W"], WL["H"], WL["F"], WL["C"], WL["R"]
     p = synth.make_problem_device(ctx, W, H, F, Cc, Rr, seed=11)
     prob = g.Problem(ctx, p.y, p.S, p.mask)
@@ -423,6 +425,23 @@ def motion_form(ctx, stream, reps: int = 3) -> dict:
     return res
 
 
+def run_forms_only(args, dist: Dist) -> dict | None:
+    """The forms named by --forms on their own, without the headline timing."""
+    import torch
+
+    import opencliper_gb300 as g
+    torch.cuda.set_device(dist.local)
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    ctx = g.Context(dist.local)
+    ctx.set_stream(stream.cuda_stream)
+    wanted = {f.strip() for f in args.forms.split(",") if f.strip()}
+    forms = {name: fn(ctx, stream, args) for name, fn in FORMS if name in wanted}
+    ctx.set_stream(None)
+    ctx.close()
+    return {"metric": METRIC, "unit": UNIT, "forms_only": True, "forms": forms}
+
+
 def torch_events():
     import torch
     return torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -431,7 +450,7 @@ def torch_events():
 BATCH_WL = dict(n=64, sizes=(128, 192, 256, 320, 384), frames=(12, 40), coils=(8, 32), accel=(4, 12), seed0=1000)
 
 
-def batched_form(ctx, stream, reps: int = 2) -> dict:
+def batched_form(ctx, stream, args=None, reps: int = 2) -> dict:
     """The batched form on the uneven workload: 64 reconstructions, each with
     its own seed 1000+i drawing W=H from {128..384}, F ~ U{12..40},
     C ~ U{8..32}, R ~ U{4..12}, solved by one captured CUDA graph (gbn_batch_*)
@@ -499,6 +518,9 @@ def cpu_port_sample(iters: int = 3) -> dict:
             "est_seconds_per_recon": round(est, 3), "sample_wall_s": round(wall, 2)}
 
 
+FORMS = (("mixed", mixed_forms), ("batched", batched_form), ("motion", motion_form))
+
+
 def run_reference(args, dist: Dist) -> dict | None:
     if dist.rank != 0:
         return None
@@ -528,7 +550,12 @@ def main(argv=None) -> int:
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU restatement timing")
-    ap.add_argument("--no-forms", action="store_true", help="skip the mixed and batched form measurements")
+    ap.add_argument("--no-forms", action="store_true", help="skip the mixed, batched and motion form measurements")
+    ap.add_argument("--forms", default="mixed,batched,motion",
+                    help="comma-separated forms to measure after the headline (mixed, batched, motion)")
+    ap.add_argument("--forms-only", action="store_true",
+                    help="measure only the forms named by --forms (no headline line; for profiling)")
+    ap.add_argument("--form-reps", type=int, default=3, help="timed repetitions of the motion form")
     ap.add_argument("--precision", choices=["fp32", "mixed"], default="fp32",
                     help="form timed as the main workload (the headline is fp32)")
     ap.add_argument("--tuning", action="append", default=[], metavar="KEY=VALUE",
@@ -540,6 +567,8 @@ def main(argv=None) -> int:
     try:
         if args.impl == "reference":
             out = run_reference(args, dist)
+        elif args.forms_only:
+            out = run_forms_only(args, dist)
         else:
             out = run_ours(args, dist)
             if out is not None and dist.rank == 0 and dist.ws == 1:

@@ -46,6 +46,10 @@ struct gbn_ctx {
   unsigned long long prof_count[8] = {0, 0, 0, 0, 0, 0, 0, 0};
 };
 
+namespace gbn {
+struct McTables;
+}
+
 struct gbn_problem {
   gbn_ctx* ctx = nullptr;
   int W = 0, H = 0, F = 0, C = 0;
@@ -93,6 +97,7 @@ struct gbn_problem {
   float2* mc_g = nullptr;             // tTVadj(normalise(D M x_k))
   float2* mc_gm = nullptr;            // M^T of it
   double* mc_part = nullptr;          // power-method norm partials
+  gbn::McTables* mc_tab = nullptr;    // gather tables of the meshes (motion.cu)
   gbn::FusedArgs* d_args = nullptr;   // one-entry instance table of the fused kernels
   gbn::ClassCtl* ctl = nullptr;       // row-pass control block
 };

@@ -7,14 +7,27 @@
 // already in the output buffer (the reference skips x0 = E^H y with argsMC,
 // NestaUp.cpp:483-486).
 //
-// Per inner iteration: x_w = M x_k (copy + gather), then one kernel forms the
-// tTV gradient g = tTVadj(normalise(D x_w)) and the objective's partial sums,
-// the fused forward column and row passes run as in the plain form (the
-// forward pass skips its tTV sums), M^T g (copy, zero rectangle, scatter with
-// atomic adds, as the reference) feeds the adjoint column pass, which takes it
-// as its tTV gradient.  The power method ||U|| cannot use the plain form's
-// per-pixel recurrence (M mixes pixels), so it runs myNormest's loop literally
-// with one host read of the norms per step.
+// Both operators run as gathers over tables built from the meshes at the
+// start of each run:
+//  * inv[p]: the rectangle entry whose warped value lands on pixel p (the
+//    last one in the reference's work-item order when several do), or -1:
+//    (M x)[f][p] = inv[p] < 0 ? x[f][p] : bilinear x[f] at that entry;
+//  * per target pixel and frame, the list of (entry, corner) pairs the
+//    scatter would add there, in the reference's work-item order, with each
+//    entry's source pixel and fractional position: (M^T g)[q] = (q in the
+//    rectangle ? 0 : g[q]) + sum of (g[src] * fa) * fb, each product and sum
+//    rounded as the kernel's.
+// So M^T is deterministic and equals an in-order scatter bit for bit, where
+// the reference's atomic scatter depends on the order of its atomics.
+//
+// Per inner iteration: k_mc_tv (M x_k for three frames on the fly, D, the
+// Huber normalisation, g = D^T u and the objective's partial sums), the fused
+// forward column and row passes as in the plain form (the forward pass skips
+// its tTV sums), k_mc_adjoint (M^T g), and the adjoint column pass, which
+// takes M^T g as its tTV gradient; all chained by programmatic dependent
+// launch.  The power method ||U|| cannot use the plain form's per-pixel
+// recurrence (M mixes pixels), so it runs myNormest's loop literally with one
+// host read of the norms per step.
 //
 // Bounds: the reference reads the image at the interpolation corners without
 // checks; here a corner or target outside the image skips that pixel and sets
@@ -34,10 +47,28 @@ int op_ttv(gbn_ctx* ctx, int dir, const float2* in, float2* out, int W, int H, i
 Lcg48 lcg48_jump(uint64_t k);
 uint64_t lcg48_apply(const Lcg48& j, uint64_t x);
 
+// tables of one problem's meshes (rebuilt at every run)
+struct McTables {
+  int* inv = nullptr;         // [H*W] rectangle entry landing on each pixel, -1 none
+  int* cnt = nullptr;         // [F*H*W] contributions per target (then fill cursors)
+  int* off = nullptr;         // [F*H*W + 1] exclusive prefix sums of cnt
+  int* bsum = nullptr;        // [scan blocks] block totals of the prefix sum
+  int* key = nullptr;         // [4 * l1 * l2 * F] contributions grouped by target, sorted by entry * 4 + corner,
+                              // then rewritten to (the entry's pixel R1*W + R2) * 4 + corner
+  int* srcmap = nullptr;      // [H*W] pixel each entry (by its R1*W + R2) reads in the adjoint
+  float2* wts = nullptr;      // [F][H*W] (Whh, Wvv): each entry's fractional position in frame f
+  double* tvpart = nullptr;   // [F * pixel blocks][2] partial sums of the fused tTV kernel
+  size_t x = 0, entries = 0;  // F*H*W and l1*l2 the buffers were sized for
+  int nbp = 0, nscan = 0;
+};
+
 namespace {
 
 constexpr int kStatusMotionRange = 5;  // NestaDevState::status: a mesh point outside the image
 constexpr int kNT = 256;
+constexpr int kScanItems = 4;                   // prefix-sum elements per thread
+constexpr int kScanBlock = kNT * kScanItems;    // per block
+constexpr int kTvFrames = 2;                    // frames per thread of the fused tTV kernel
 
 // rows r1b .. r1b+l1-1 and columns r2b .. r2b+l2-1 of the rectangle
 // (Interpolator.cpp:63-87: margins H/40 and W/40 in integer division)
@@ -55,24 +86,31 @@ McRect mc_rect(int W, int H, const int* bb) {
   return r;
 }
 
+bool rect_ok(const McRect& r, int W, int H) {
+  return r.l1 > 0 && r.l2 > 0 && r.r1b >= 0 && r.r2b >= 0 && r.r1b + r.l1 <= H && r.r2b + r.l2 <= W;
+}
+
+// deformed position of rectangle entry e = i + l1*j in frame k (0-based) and
+// its upper-left interpolation corner
 struct McPoint {
-  int hor, ver, ph, pv;  // target pixel, upper-left interpolation corner
-  float nh, nv;          // deformed position (0-based)
+  float nh, nv;
+  int ph, pv;
   bool ok;
 };
 
-__device__ __forceinline__ McPoint mc_point(const float* __restrict__ xn, const int* __restrict__ xm, McRect r,
-                                            int W, int H, int F, int i, int j, int k) {
-  McPoint q;
-  const int R1 = r.r1b + i, R2 = r.r2b + j;
+__device__ __forceinline__ int entry_offset(McRect r, int e, int W) {
+  const int i = e % r.l1, j = e / r.l1;
+  return (r.r2b + j) + (r.r1b + i) * W;  // (row R1, column R2) in a [H][W] plane
+}
+
+__device__ __forceinline__ McPoint mc_point(const float* __restrict__ xn, int xo, int k, int W, int H, int F) {
   const size_t HW = size_t(H) * W;
-  q.hor = xm[R1 + size_t(R2) * H] - 1;
-  q.ver = xm[R1 + size_t(R2) * H + HW] - 1;
-  q.nh = xn[R2 + size_t(R1) * W + k * HW] - 1.f;
-  q.nv = xn[R2 + size_t(R1) * W + k * HW + HW * F] - 1.f;
+  McPoint q;
+  q.nh = xn[xo + k * HW] - 1.f;
+  q.nv = xn[xo + k * HW + HW * F] - 1.f;
   q.ph = int(floorf(q.nh));
   q.pv = int(floorf(q.nv));
-  q.ok = q.hor >= 0 && q.hor < W && q.ver >= 0 && q.ver < H && q.ph >= 0 && q.ph + 1 < W && q.pv >= 0 && q.pv + 1 < H;
+  q.ok = q.ph >= 0 && q.ph + 1 < W && q.pv >= 0 && q.pv + 1 < H;
   return q;
 }
 
@@ -81,103 +119,356 @@ __device__ __forceinline__ float lin2(float p, float u, float q, float v) {
   return __fadd_rn(__fmul_rn(p, u), __fmul_rn(q, v));
 }
 
-// interpolator (optimizer.cl:832-877); `out` already holds a copy of `in`
-__global__ void k_mc_warp(const float2* __restrict__ in, float2* __restrict__ out, const float* __restrict__ xn,
-                          const int* __restrict__ xm, McRect r, int W, int H, int F, int* __restrict__ status) {
-  const size_t n = size_t(r.l1) * r.l2 * F;
+// the interpolator's value (optimizer.cl:832-877) at q from frame xf, in the
+// kernel's order with separately rounded products and sums: with motion
+// compensation the power method starts from this interpolation's rounding
+// residue on a constant image, so ||U|| depends on these exact bits
+__device__ __forceinline__ float2 bilinear(const float2* __restrict__ xf, const McPoint& q, int W) {
+  const float2 i1 = xf[q.ph + size_t(q.pv) * W], i2 = xf[q.ph + 1 + size_t(q.pv) * W];
+  const float2 i3 = xf[q.ph + size_t(q.pv + 1) * W], i4 = xf[q.ph + 1 + size_t(q.pv + 1) * W];
+  const float a = float(q.ph + 1) - q.nh, b = q.nh - float(q.ph);
+  const float c = float(q.pv + 1) - q.nv, d = q.nv - float(q.pv);
+  const float2 aux1 = make_float2(lin2(a, i1.x, b, i2.x), lin2(a, i1.y, b, i2.y));
+  const float2 aux2 = make_float2(lin2(a, i3.x, b, i4.x), lin2(a, i3.y, b, i4.y));
+  return make_float2(lin2(c, aux1.x, d, aux2.x), lin2(c, aux1.y, d, aux2.y));
+}
+
+// (M x)[k][p]
+__device__ __forceinline__ float2 warp_at(const float2* __restrict__ x, const float* __restrict__ xn, McRect r, int e,
+                                          int p, int k, int W, int H, int F, int* __restrict__ status) {
+  const float2* xf = x + size_t(k) * H * W;
+  if (e < 0) return xf[p];
+  const McPoint q = mc_point(xn, entry_offset(r, e, W), k, W, H, F);
+  if (!q.ok) {
+    atomicExch(status, kStatusMotionRange);
+    return xf[p];
+  }
+  return bilinear(xf, q, W);
+}
+
+// ---- table construction ------------------------------------------------------
+// inv[ver*W + hor] = the largest entry e whose original-mesh point is (hor, ver);
+// srcmap[R1*W + R2] = that pixel (-1 outside the image)
+__global__ void k_mc_inv(const int* __restrict__ xm, McRect r, int W, int H, int* __restrict__ inv,
+                         int* __restrict__ srcmap, int* __restrict__ status) {
+  const int E = r.l1 * r.l2;
   const size_t HW = size_t(H) * W;
-  for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < n; t += size_t(gridDim.x) * blockDim.x) {
-    const int i = int(t % r.l1), j = int((t / r.l1) % r.l2), k = int(t / (size_t(r.l1) * r.l2));
-    const McPoint q = mc_point(xn, xm, r, W, H, F, i, j, k);
-    if (!q.ok) {
+  for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < E; e += gridDim.x * blockDim.x) {
+    const int R1 = r.r1b + e % r.l1, R2 = r.r2b + e / r.l1;
+    const int hor = xm[R1 + size_t(R2) * H] - 1, ver = xm[R1 + size_t(R2) * H + HW] - 1;
+    if (hor < 0 || hor >= W || ver < 0 || ver >= H) {
+      srcmap[R1 * W + R2] = -1;
       atomicExch(status, kStatusMotionRange);
       continue;
     }
-    const float2* src = in + k * HW;
-    const float2 i1 = src[q.ph + size_t(q.pv) * W], i2 = src[q.ph + 1 + size_t(q.pv) * W];
-    const float2 i3 = src[q.ph + size_t(q.pv + 1) * W], i4 = src[q.ph + 1 + size_t(q.pv + 1) * W];
-    const float a = float(q.ph + 1) - q.nh, b = q.nh - float(q.ph);
-    const float c = float(q.pv + 1) - q.nv, d = q.nv - float(q.pv);
-    // separately rounded products and sums (no contraction), in the kernel's
-    // order: with motion compensation the power method starts from this
-    // interpolation's rounding residue on a constant image, so ||U|| depends
-    // on these exact bits
-    const float2 aux1 = make_float2(lin2(a, i1.x, b, i2.x), lin2(a, i1.y, b, i2.y));
-    const float2 aux2 = make_float2(lin2(a, i3.x, b, i4.x), lin2(a, i3.y, b, i4.y));
-    out[k * HW + size_t(q.ver) * W + q.hor] = make_float2(lin2(c, aux1.x, d, aux2.x), lin2(c, aux1.y, d, aux2.y));
+    srcmap[R1 * W + R2] = ver * W + hor;
+    atomicMax(inv + size_t(ver) * W + hor, e);
   }
 }
 
-// initZeroRect (initialize.cl:55-69)
-__global__ void k_mc_zero_rect(float2* __restrict__ out, McRect r, int W, int H, int F) {
-  const size_t n = size_t(r.l1) * r.l2 * F;
-  for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < n; t += size_t(gridDim.x) * blockDim.x) {
-    const int i = int(t % r.l1), j = int((t / r.l1) % r.l2), k = int(t / (size_t(r.l1) * r.l2));
-    out[k * size_t(H) * W + size_t(r.r1b + i) * W + (r.r2b + j)] = make_float2(0.f, 0.f);
-  }
-}
-
-// adjointInterpolator (optimizer.cl:880-937): scatter with atomic adds
-__global__ void k_mc_scatter(const float2* __restrict__ in, float2* __restrict__ out, const float* __restrict__ xn,
-                             const int* __restrict__ xm, McRect r, int W, int H, int F, int* __restrict__ status) {
-  const size_t n = size_t(r.l1) * r.l2 * F;
+// the (entry, frame) pairs that scatter: target pixel (its original-mesh point) in the image, corners too
+__device__ __forceinline__ bool scatter_point(const float* __restrict__ xn, const int* __restrict__ xm, McRect r, int e,
+                                              int k, int W, int H, int F, McPoint* q, int* src) {
   const size_t HW = size_t(H) * W;
-  float* o = reinterpret_cast<float*>(out);
+  const int R1 = r.r1b + e % r.l1, R2 = r.r2b + e / r.l1;
+  const int hor = xm[R1 + size_t(R2) * H] - 1, ver = xm[R1 + size_t(R2) * H + HW] - 1;
+  *q = mc_point(xn, R2 + R1 * W, k, W, H, F);
+  *src = ver * W + hor;
+  return q->ok && hor >= 0 && hor < W && ver >= 0 && ver < H;
+}
+
+__global__ void k_mc_count(const float* __restrict__ xn, const int* __restrict__ xm, McRect r, int W, int H, int F,
+                           int* __restrict__ cnt, int* __restrict__ status) {
+  const int E = r.l1 * r.l2;
+  const size_t HW = size_t(H) * W, n = size_t(E) * F;
   for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < n; t += size_t(gridDim.x) * blockDim.x) {
-    const int i = int(t % r.l1), j = int((t / r.l1) % r.l2), k = int(t / (size_t(r.l1) * r.l2));
-    const McPoint q = mc_point(xn, xm, r, W, H, F, i, j, k);
-    if (!q.ok) {
+    const int e = int(t % E), k = int(t / E);
+    McPoint q;
+    int src;
+    if (!scatter_point(xn, xm, r, e, k, W, H, F, &q, &src)) {
       atomicExch(status, kStatusMotionRange);
       continue;
     }
-    const float Wvv = q.nv - float(q.pv), Whh = q.nh - float(q.ph);
-    const float2 i0 = in[k * HW + size_t(q.ver) * W + q.hor];
-    const size_t p00 = k * HW + size_t(q.pv) * W + q.ph, p01 = p00 + 1, p10 = p00 + W, p11 = p10 + 1;
-    atomicAdd(o + 2 * p00, i0.x * (1.f - Whh) * (1.f - Wvv));
-    atomicAdd(o + 2 * p01, i0.x * Whh * (1.f - Wvv));
-    atomicAdd(o + 2 * p10, i0.x * (1.f - Whh) * Wvv);
-    atomicAdd(o + 2 * p11, i0.x * Whh * Wvv);
-    atomicAdd(o + 2 * p00 + 1, i0.y * (1.f - Whh) * (1.f - Wvv));
-    atomicAdd(o + 2 * p01 + 1, i0.y * Whh * (1.f - Wvv));
-    atomicAdd(o + 2 * p10 + 1, i0.y * (1.f - Whh) * Wvv);
-    atomicAdd(o + 2 * p11 + 1, i0.y * Whh * Wvv);
+    int* c = cnt + k * HW + size_t(q.pv) * W + q.ph;
+    atomicAdd(c, 1);
+    atomicAdd(c + 1, 1);
+    atomicAdd(c + W, 1);
+    atomicAdd(c + W + 1, 1);
   }
 }
 
-// g = tTVadj(normalise(D x_w)) (temporalTV.cl:78-107 sign: u_{f+1} - u_f) and the
-// objective's partial sums of |u|^2 and Re<u, d> per (frame, 8-column tile),
-// the slots the forward column pass fills in the plain form.  grid (W/8, F)
-__global__ void __launch_bounds__(128) k_mc_tv(const float2* __restrict__ xw, const NestaDevState* __restrict__ st,
-                                               float2* __restrict__ g, double* __restrict__ part_tv, int W, int H,
-                                               int F) {
-  __shared__ double sred[4];
-  const int f = blockIdx.y, w0 = blockIdx.x * 8, t = threadIdx.x;
-  const size_t N = size_t(W) * H;
-  const float2* x0 = xw + size_t(f) * N;
-  const float2* xm = xw + size_t((f + F - 1) % F) * N;
-  const float2* xp = xw + size_t((f + 1) % F) * N;
+// exclusive prefix sum of n ints in three launches: per-block scan, scan of the
+// block totals, add
+__device__ __forceinline__ int block_exclusive_scan(int v, int* swarp, int* total) {
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  int incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int u = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += u;
+  }
+  if (lane == 31) swarp[wid] = incl;
+  __syncthreads();
+  if (wid == 0) {
+    int w = lane < int(blockDim.x >> 5) ? swarp[lane] : 0;
+    int wi = w;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int u = __shfl_up_sync(0xffffffffu, wi, o);
+      if (lane >= o) wi += u;
+    }
+    if (lane < int(blockDim.x >> 5)) swarp[lane] = wi - w;
+    if (lane == int(blockDim.x >> 5) - 1) *total = wi;
+  }
+  __syncthreads();
+  return swarp[wid] + incl - v;
+}
+
+__global__ void __launch_bounds__(kNT) k_scan_blocks(const int* __restrict__ in, size_t n, int* __restrict__ out,
+                                                      int* __restrict__ bsum) {
+  __shared__ int swarp[kNT / 32];
+  __shared__ int total;
+  const size_t base = size_t(blockIdx.x) * kScanBlock + size_t(threadIdx.x) * kScanItems;
+  int v[kScanItems], s = 0;
+#pragma unroll
+  for (int u = 0; u < kScanItems; ++u) {
+    v[u] = base + u < n ? in[base + u] : 0;
+    s += v[u];
+  }
+  int run = block_exclusive_scan(s, swarp, &total);
+#pragma unroll
+  for (int u = 0; u < kScanItems; ++u) {
+    if (base + u < n) out[base + u] = run;
+    run += v[u];
+  }
+  if (threadIdx.x == 0) bsum[blockIdx.x] = total;
+}
+
+// one block: exclusive scan of the nb block totals in place; out[n] = the grand total
+__global__ void __launch_bounds__(1024) k_scan_totals(int* __restrict__ bsum, int nb, int* __restrict__ out, size_t n) {
+  __shared__ int swarp[32];
+  __shared__ int total;
+  int carry = 0;
+  for (int b0 = 0; b0 < nb; b0 += 1024) {
+    const int b = b0 + int(threadIdx.x);
+    const int v = b < nb ? bsum[b] : 0;
+    const int ex = block_exclusive_scan(v, swarp, &total);
+    if (b < nb) bsum[b] = carry + ex;
+    carry += total;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) out[n] = carry;
+}
+
+__global__ void k_scan_add(int* __restrict__ out, size_t n, const int* __restrict__ bsum) {
+  const size_t i = size_t(blockIdx.x) * kScanBlock + threadIdx.x;
+  const int add = bsum[blockIdx.x];
+#pragma unroll
+  for (int u = 0; u < kScanItems; ++u)
+    if (i + size_t(u) * kNT < n) out[i + size_t(u) * kNT] += add;
+}
+
+// the contributions of every scattering (entry, frame) to its four corners,
+// and the entry's fractional position (Whh, Wvv) the weights derive from
+__global__ void k_mc_fill(const float* __restrict__ xn, const int* __restrict__ xm, McRect r, int W, int H, int F,
+                          const int* __restrict__ off, int* __restrict__ cur, int* __restrict__ key,
+                          float2* __restrict__ wts) {
+  const int E = r.l1 * r.l2;
+  const size_t HW = size_t(H) * W, n = size_t(E) * F;
+  for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < n; t += size_t(gridDim.x) * blockDim.x) {
+    const int e = int(t % E), k = int(t / E);
+    McPoint q;
+    int src;
+    if (!scatter_point(xn, xm, r, e, k, W, H, F, &q, &src)) continue;
+    wts[k * HW + entry_offset(r, e, W)] = make_float2(q.nh - float(q.ph), q.nv - float(q.pv));
+    const size_t q00 = k * HW + size_t(q.pv) * W + q.ph;
+    const size_t tq[4] = {q00, q00 + 1, q00 + W, q00 + W + 1};
+#pragma unroll
+    for (int c = 0; c < 4; ++c) key[off[tq[c]] + atomicAdd(cur + tq[c], 1)] = e * 4 + c;
+  }
+}
+
+// each target's contributions into key order (lists are short: insertion sort)
+__global__ void k_mc_sort(const int* __restrict__ off, int* __restrict__ key, size_t n) {
+  for (size_t q = blockIdx.x * size_t(blockDim.x) + threadIdx.x; q < n; q += size_t(gridDim.x) * blockDim.x) {
+    const int b = off[q], e = off[q + 1];
+    for (int i = b + 1; i < e; ++i) {
+      const int v = key[i];
+      int j = i - 1;
+      while (j >= b && key[j] > v) {
+        key[j + 1] = key[j];
+        --j;
+      }
+      key[j + 1] = v;
+    }
+  }
+}
+
+// sorted keys entry * 4 + corner -> (the entry's pixel R1*W + R2) * 4 + corner,
+// so that neighbouring targets read neighbouring table entries
+__global__ void k_mc_rekey(int* __restrict__ key, size_t n, McRect r, int W) {
+  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
+    const int k = key[i];
+    key[i] = entry_offset(r, k >> 2, W) * 4 + (k & 3);
+  }
+}
+
+// ---- the operators -------------------------------------------------------------
+// out = M x (MotionCompensation: copy, then the interpolator), one thread per pixel
+__global__ void k_mc_warp(const float2* __restrict__ x, float2* __restrict__ out, const float* __restrict__ xn,
+                          const int* __restrict__ inv, McRect r, int W, int H, int F, int* __restrict__ status) {
+  const size_t HW = size_t(H) * W, n = HW * F;
+  for (size_t t = blockIdx.x * size_t(blockDim.x) + threadIdx.x; t < n; t += size_t(gridDim.x) * blockDim.x) {
+    const int p = int(t % HW), k = int(t / HW);
+    out[t] = warp_at(x, xn, r, inv[p], p, k, W, H, F, status);
+  }
+}
+
+// out = M^T g (AdjointMotionCompensation: copy, zero the rectangle, scatter),
+// one thread per target, contributions in the reference's order; corner c of
+// an entry's square gets (g * fa) * fb with fa = Whh or 1 - Whh (c & 1), fb =
+// Wvv or 1 - Wvv (c & 2), as optimizer.cl:880-937 rounds them.  Loads of up to
+// four contributions are issued before any of them is accumulated.
+__global__ void __launch_bounds__(kNT) k_mc_adjoint(const float2* __restrict__ g, float2* __restrict__ out,
+                                                     const int* __restrict__ off, const int* __restrict__ key,
+                                                     const int* __restrict__ srcmap, const float2* __restrict__ wts,
+                                                     McRect r, int W, int H, int F, int pdl) {
+  if (pdl) {
+    grid_dep_wait();  // g comes from the fused tTV kernel two launches back
+    grid_dep_release();
+  }
+  const size_t HW = size_t(H) * W, n = HW * F;
+  const size_t q = blockIdx.x * size_t(kNT) + threadIdx.x;
+  if (q >= n) return;
+  const int p = int(q % HW), row = p / W, col = p % W;
+  const bool in_rect = row >= r.r1b && row < r.r1b + r.l1 && col >= r.r2b && col < r.r2b + r.l2;
+  int c = __ldg(off + q);
+  const int ce = __ldg(off + q + 1);
+  float2 acc = in_rect ? make_float2(0.f, 0.f) : g[q];
+  const size_t k = q / HW;
+  const float2* gk = g + k * HW;
+  const float2* wk = wts + k * HW;
+  while (c < ce) {
+    const int m = min(4, ce - c);
+    int kc[4];
+    float2 w[4], v[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) kc[u] = u < m ? __ldg(key + c + u) : 0;
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (u < m) {
+        w[u] = __ldg(wk + (kc[u] >> 2));
+        v[u] = gk[__ldg(srcmap + (kc[u] >> 2))];
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      if (u < m) {
+        const float fa = (kc[u] & 1) ? w[u].x : __fsub_rn(1.f, w[u].x);
+        const float fb = (kc[u] & 2) ? w[u].y : __fsub_rn(1.f, w[u].y);
+        acc.x = __fadd_rn(acc.x, __fmul_rn(__fmul_rn(v[u].x, fa), fb));
+        acc.y = __fadd_rn(acc.y, __fmul_rn(__fmul_rn(v[u].y, fa), fb));
+      }
+    }
+    c += m;
+  }
+  out[q] = acc;
+}
+
+// g = tTVadj(normalise(D M x)) (temporalTV.cl:78-107 sign: u_{f+1} - u_f) and
+// the objective's partial sums of |u|^2 and Re<u, d> per (frame, block of 256
+// pixels).  grid (ceil(H*W/256), ceil(F/kTvFrames)); each thread warps its
+// pixel for kTvFrames+2 consecutive frames (periodic in f) and slides over them.
+__global__ void __launch_bounds__(kNT) k_mc_tv(const float2* __restrict__ x, const float* __restrict__ xn,
+                                                const int* __restrict__ inv, McRect r, const NestaDevState* __restrict__ st,
+                                                float2* __restrict__ g, double* __restrict__ part, int W, int H, int F,
+                                                int* __restrict__ status) {
+  __shared__ double sred[2 * kTvFrames][kNT / 32];
+  const int HW = H * W;
+  const int p = blockIdx.x * kNT + threadIdx.x;
+  const bool live = p < HW;
+  const int e = live ? __ldg(inv + p) : -1;
+  const int f0 = blockIdx.y * kTvFrames, f1 = min(F, f0 + kTvFrames);
+  grid_dep_wait();  // x_k comes from the previous adjoint column pass
+  grid_dep_release();
   const float inv_mu = 1.0f / st->mu;
-  float su2 = 0.f, sud = 0.f;
-  for (int q = t; q < 8 * H; q += 128) {
-    const size_t p = size_t(q / 8) * W + w0 + (q % 8);
-    const float2 a = x0[p];
-    const float2 d0 = csub(a, xm[p]);
-    const float2 u0 = tv_normalize(d0, inv_mu);
-    const float2 u1 = tv_normalize(csub(xp[p], a), inv_mu);
-    su2 = fmaf(u0.x, u0.x, fmaf(u0.y, u0.y, su2));
-    sud = fmaf(u0.x, d0.x, fmaf(u0.y, d0.y, sud));
-    g[size_t(f) * N + p] = csub(u1, u0);
+  float su2[kTvFrames], sud[kTvFrames];
+#pragma unroll
+  for (int u = 0; u < kTvFrames; ++u) su2[u] = sud[u] = 0.f;
+  if (live) {
+    // M x_k at this pixel for frames f0-1 .. f1 (periodic): positions, then
+    // corners, then values, so that the loads of all frames are in flight together
+    constexpr int NW = kTvFrames + 2;
+    const int nw = f1 - f0 + 2;
+    int fr[NW];
+#pragma unroll
+    for (int u = 0; u < NW; ++u) fr[u] = (f0 - 1 + u + F) % F;
+    float2 w[NW];
+    if (e < 0) {
+#pragma unroll
+      for (int u = 0; u < NW; ++u)
+        if (u < nw) w[u] = x[size_t(fr[u]) * HW + p];
+    } else {
+      const int xo = entry_offset(r, e, W);
+      McPoint q[NW];
+#pragma unroll
+      for (int u = 0; u < NW; ++u)
+        if (u < nw) q[u] = mc_point(xn, xo, fr[u], W, H, F);
+#pragma unroll
+      for (int u = 0; u < NW; ++u) {
+        if (u < nw) {
+          const float2* xf = x + size_t(fr[u]) * HW;
+          if (q[u].ok) {
+            w[u] = bilinear(xf, q[u], W);
+          } else {
+            atomicExch(status, kStatusMotionRange);
+            w[u] = xf[p];
+          }
+        }
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < kTvFrames; ++u) {
+      const int f = f0 + u;
+      if (f < f1) {
+        const float2 d0 = csub(w[u + 1], w[u]);
+        const float2 u0 = tv_normalize(d0, inv_mu);
+        const float2 u1 = tv_normalize(csub(w[u + 2], w[u + 1]), inv_mu);
+        su2[u] = fmaf(u0.x, u0.x, u0.y * u0.y);
+        sud[u] = fmaf(u0.x, d0.x, u0.y * d0.y);
+        g[size_t(f) * HW + p] = csub(u1, u0);
+      }
+    }
   }
-  const double t1 = block_sum<128>(double(su2), sred);
-  const double t2 = block_sum<128>(double(sud), sred);
-  if (t == 0) {
-    const int slot = f * gridDim.x + blockIdx.x;
-    part_tv[2 * slot] = t1;
-    part_tv[2 * slot + 1] = t2;
+  // fixed-order reduction: FP32 warp shuffles (32 values), then the warps in
+  // order in FP64 (FP64 throughput is a small fraction of FP32's here)
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+#pragma unroll
+  for (int u = 0; u < kTvFrames; ++u) {
+    float a = su2[u], b = sud[u];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      a += __shfl_down_sync(0xffffffffu, a, o);
+      b += __shfl_down_sync(0xffffffffu, b, o);
+    }
+    if (lane == 0) {
+      sred[2 * u][wid] = double(a);
+      sred[2 * u + 1][wid] = double(b);
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x < 2 * kTvFrames) {
+    const int u = threadIdx.x >> 1;
+    if (f0 + u < f1) {
+      double t = 0.0;
+#pragma unroll
+      for (int w = 0; w < kNT / 32; ++w) t += sred[threadIdx.x][w];
+      part[2 * (size_t(f0 + u) * gridDim.x + blockIdx.x) + (threadIdx.x & 1)] = t;
+    }
   }
 }
 
-// the power method's vector operations
+// ---- the power method's vector operations ----------------------------------------
 __global__ void k_fill(float2* __restrict__ v, size_t n, float2 value) {
   for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) v[i] = value;
 }
@@ -206,29 +497,50 @@ __global__ void k_fill_drand48(float2* __restrict__ v, size_t n, unsigned long l
     v[i] = make_float2(__double2float_rn(double(X) * 0x1p-48), 0.f);
   }
 }
-// sum of |v|^2 and of |Re| + |Im| in FP64: per-block partials in fixed slots
+// sum of |v|^2 and of |Re| + |Im|: FP32 within a thread's few elements and
+// a warp, FP64 across warps and blocks; per-block partials in fixed slots
+__device__ __forceinline__ void warp_sums_to_block(float s2, float s1, double* sred2, double* sred1, double* part) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    s2 += __shfl_down_sync(0xffffffffu, s2, o);
+    s1 += __shfl_down_sync(0xffffffffu, s1, o);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  if (lane == 0) {
+    sred2[wid] = double(s2);
+    sred1[wid] = double(s1);
+  }
+  __syncthreads();
+  if (threadIdx.x < 2) {
+    const double* r = threadIdx.x == 0 ? sred2 : sred1;
+    double t = 0.0;
+#pragma unroll
+    for (int w = 0; w < kNT / 32; ++w) t += r[w];
+    part[2 * blockIdx.x + threadIdx.x] = t;
+  }
+}
 __global__ void __launch_bounds__(kNT) k_sums(const float2* __restrict__ v, size_t n, double* __restrict__ part) {
-  __shared__ double sred[kNT / 32];
-  double s2 = 0.0, s1 = 0.0;
+  __shared__ double sred2[kNT / 32], sred1[kNT / 32];
+  float s2 = 0.f, s1 = 0.f;
   for (size_t i = blockIdx.x * size_t(kNT) + threadIdx.x; i < n; i += size_t(gridDim.x) * kNT) {
     const float2 a = v[i];
-    s2 += double(a.x) * a.x + double(a.y) * a.y;
-    s1 += double(fabsf(a.x)) + double(fabsf(a.y));
+    s2 = fmaf(a.x, a.x, fmaf(a.y, a.y, s2));
+    s1 += fabsf(a.x) + fabsf(a.y);
+  }
+  warp_sums_to_block(s2, s1, sred2, sred1, part);
+}
+// the block partials summed by one block: each thread a strided subset in
+// order, then the threads in order
+__global__ void __launch_bounds__(kNT) k_sums_final(const double* __restrict__ part, int nblk, double* __restrict__ out) {
+  __shared__ double sred[kNT / 32];
+  double s2 = 0.0, s1 = 0.0;
+  for (int b = threadIdx.x; b < nblk; b += kNT) {
+    s2 += part[2 * b];
+    s1 += part[2 * b + 1];
   }
   s2 = block_sum<kNT>(s2, sred);
   s1 = block_sum<kNT>(s1, sred);
   if (threadIdx.x == 0) {
-    part[2 * blockIdx.x] = s2;
-    part[2 * blockIdx.x + 1] = s1;
-  }
-}
-__global__ void k_sums_final(const double* __restrict__ part, int nblk, double* __restrict__ out) {
-  if (threadIdx.x == 0) {
-    double s2 = 0.0, s1 = 0.0;
-    for (int b = 0; b < nblk; ++b) {
-      s2 += part[2 * b];
-      s1 += part[2 * b + 1];
-    }
     out[0] = s2;
     out[1] = s1;
   }
@@ -241,11 +553,79 @@ __global__ void k_set_normest(NestaDevState* st, float e, int iters) {
 
 int grid1(gbn_ctx* ctx, size_t n) { return int(std::min<size_t>((n + kNT - 1) / kNT, size_t(ctx->nsm) * 8)); }
 
-}  // namespace
-
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+void tables_free(McTables* t) {
+  void* ptrs[] = {t->inv, t->cnt, t->off, t->bsum, t->key, t->srcmap, t->wts, t->tvpart};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  *t = McTables{};
+}
+
+// buffers for F*H*W pixels and E rectangle entries (kept when large enough)
+int tables_alloc(McTables* t, int W, int H, int F, int E) {
+  const size_t HW = size_t(H) * W, X = HW * F;
+  const int nbp = int((HW + kNT - 1) / kNT);
+  if (t->inv && t->x == X && size_t(E) <= t->entries) return GBN_OK;
+  tables_free(t);
+  t->x = X;
+  t->entries = size_t(E);
+  t->nbp = nbp;
+  t->nscan = int((X + kScanBlock - 1) / kScanBlock);
+  cudaError_t e = cudaMalloc(&t->inv, HW * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&t->cnt, X * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&t->off, (X + 1) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&t->bsum, size_t(t->nscan) * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&t->key, 4 * size_t(E) * F * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&t->srcmap, HW * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&t->wts, X * sizeof(float2));
+  if (e == cudaSuccess) e = cudaMalloc(&t->tvpart, 2 * size_t(F) * nbp * sizeof(double));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    tables_free(t);
+    return set_error(GBN_ERR_NOMEM, "motion compensation table allocation failed");
+  }
+  return GBN_OK;
+}
+
+// builds inv and the contribution lists from the meshes (asynchronous on s)
+int tables_build(gbn_ctx* ctx, McTables* t, const float* xn, const int* xm, const McRect& r, int W, int H, int F,
+                 int* status, cudaStream_t s) {
+  const size_t HW = size_t(H) * W, X = HW * F;
+  const int E = r.l1 * r.l2;
+  cudaError_t e = cudaMemsetAsync(t->inv, 0xFF, HW * sizeof(int), s);  // -1
+  if (e == cudaSuccess) e = cudaMemsetAsync(t->cnt, 0, X * sizeof(int), s);
+  if (e != cudaSuccess) return cuda_status(e, "motion compensation tables");
+  k_mc_inv<<<grid1(ctx, size_t(E)), kNT, 0, s>>>(xm, r, W, H, t->inv, t->srcmap, status);
+  k_mc_count<<<grid1(ctx, size_t(E) * F), kNT, 0, s>>>(xn, xm, r, W, H, F, t->cnt, status);
+  k_scan_blocks<<<t->nscan, kNT, 0, s>>>(t->cnt, X, t->off, t->bsum);
+  k_scan_totals<<<1, 1024, 0, s>>>(t->bsum, t->nscan, t->off, X);
+  k_scan_add<<<t->nscan, kNT, 0, s>>>(t->off, X, t->bsum);
+  if ((e = cudaMemsetAsync(t->cnt, 0, X * sizeof(int), s)) != cudaSuccess)
+    return cuda_status(e, "motion compensation tables");
+  k_mc_fill<<<grid1(ctx, size_t(E) * F), kNT, 0, s>>>(xn, xm, r, W, H, F, t->off, t->cnt, t->key, t->wts);
+  k_mc_sort<<<grid1(ctx, X), kNT, 0, s>>>(t->off, t->key, X);
+  k_mc_rekey<<<grid1(ctx, 4 * size_t(E) * F), kNT, 0, s>>>(t->key, 4 * size_t(E) * F, r, W);
+  ctx->launches += 9;
+  return GBN_OK;
+}
+
+}  // namespace
+
+void motion_free(gbn_problem* P) {
+  if (P->mc_tab) {
+    tables_free(P->mc_tab);
+    delete P->mc_tab;
+    P->mc_tab = nullptr;
+  }
+  void* ptrs[] = {P->mc_xw, P->mc_g, P->mc_gm, P->mc_part};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  P->mc_xw = P->mc_g = P->mc_gm = nullptr;
+  P->mc_part = nullptr;
+}
+
 int motion_set(gbn_problem* P, const float* xn, const int* xmesh, const int* bb) {
   if (!xn && !xmesh && !bb) {
     P->mc_on = false;
@@ -253,7 +633,7 @@ int motion_set(gbn_problem* P, const float* xn, const int* xmesh, const int* bb)
   }
   if (!xn || !xmesh || !bb) return set_error(GBN_ERR_INVALID, "motion compensation needs xn, the mesh and the bounding box");
   const McRect r = mc_rect(P->W, P->H, bb);
-  if (r.l1 <= 0 || r.l2 <= 0 || r.r1b < 0 || r.r2b < 0 || r.r1b + r.l1 > P->H || r.r2b + r.l2 > P->W)
+  if (!rect_ok(r, P->W, P->H))
     return set_error(GBN_ERR_INVALID, "motion compensation: bounding box plus margins leaves the image");
   const size_t X = size_t(P->W) * P->H * P->F;
   if (!P->mc_xw) {
@@ -263,9 +643,13 @@ int motion_set(gbn_problem* P, const float* xn, const int* xmesh, const int* bb)
     if (e == cudaSuccess) e = cudaMalloc(&P->mc_part, 2 * 1024 * sizeof(double) + 2 * sizeof(double));
     if (e != cudaSuccess) {
       cudaGetLastError();
+      motion_free(P);
       return set_error(GBN_ERR_NOMEM, "motion compensation workspace allocation failed");
     }
   }
+  if (!P->mc_tab) P->mc_tab = new McTables();
+  const int rc = tables_alloc(P->mc_tab, P->W, P->H, P->F, r.l1 * r.l2);
+  if (rc != GBN_OK) return rc;
   P->mc_xn = xn;
   P->mc_xmesh = xmesh;
   std::memcpy(P->mc_bb, bb, sizeof(P->mc_bb));
@@ -275,29 +659,22 @@ int motion_set(gbn_problem* P, const float* xn, const int* xmesh, const int* bb)
 
 namespace {
 
-// out = M in (copy, then the interpolator over the rectangle)
-int mc_apply(gbn_ctx* ctx, gbn_problem* P, const float2* in, float2* out, cudaStream_t s) {
+// out = M in
+void mc_apply(gbn_ctx* ctx, gbn_problem* P, const float2* in, float2* out, cudaStream_t s) {
   const size_t X = size_t(P->W) * P->H * P->F;
   const McRect r = mc_rect(P->W, P->H, P->mc_bb);
-  cudaError_t e = cudaMemcpyAsync(out, in, X * sizeof(float2), cudaMemcpyDeviceToDevice, s);
-  if (e != cudaSuccess) return cuda_status(e, "motion compensation copy");
-  k_mc_warp<<<grid1(ctx, size_t(r.l1) * r.l2 * P->F), kNT, 0, s>>>(in, out, P->mc_xn, P->mc_xmesh, r, P->W, P->H, P->F,
-                                                                    &P->st->status);
+  k_mc_warp<<<grid1(ctx, X), kNT, 0, s>>>(in, out, P->mc_xn, P->mc_tab->inv, r, P->W, P->H, P->F, &P->st->status);
   ctx->launches += 1;
-  return GBN_OK;
 }
 
-// out = M^T in (copy, zero the rectangle, scatter)
-int mc_adjoint(gbn_ctx* ctx, gbn_problem* P, const float2* in, float2* out, cudaStream_t s) {
+// out = M^T in
+void mc_adjoint(gbn_ctx* ctx, gbn_problem* P, const float2* in, float2* out, cudaStream_t s) {
   const size_t X = size_t(P->W) * P->H * P->F;
   const McRect r = mc_rect(P->W, P->H, P->mc_bb);
-  cudaError_t e = cudaMemcpyAsync(out, in, X * sizeof(float2), cudaMemcpyDeviceToDevice, s);
-  if (e != cudaSuccess) return cuda_status(e, "motion compensation copy");
-  const int g = grid1(ctx, size_t(r.l1) * r.l2 * P->F);
-  k_mc_zero_rect<<<g, kNT, 0, s>>>(out, r, P->W, P->H, P->F);
-  k_mc_scatter<<<g, kNT, 0, s>>>(in, out, P->mc_xn, P->mc_xmesh, r, P->W, P->H, P->F, &P->st->status);
-  ctx->launches += 2;
-  return GBN_OK;
+  const McTables* t = P->mc_tab;
+  k_mc_adjoint<<<int((X + kNT - 1) / kNT), kNT, 0, s>>>(in, out, t->off, t->key, t->srcmap, t->wts, r, P->W, P->H,
+                                                       P->F, 0);
+  ctx->launches += 1;
 }
 
 // (sum |v|^2, sum |Re| + |Im|) on the host (synchronises s)
@@ -305,7 +682,7 @@ int sums(gbn_ctx* ctx, gbn_problem* P, const float2* v, double out[2], cudaStrea
   const size_t X = size_t(P->W) * P->H * P->F;
   const int nblk = std::min(1024, grid1(ctx, X));
   k_sums<<<nblk, kNT, 0, s>>>(v, X, P->mc_part);
-  k_sums_final<<<1, 32, 0, s>>>(P->mc_part, nblk, P->mc_part + 2 * 1024);
+  k_sums_final<<<1, kNT, 0, s>>>(P->mc_part, nblk, P->mc_part + 2 * 1024);
   ctx->launches += 2;
   cudaError_t e = cudaMemcpyAsync(out, P->mc_part + 2 * 1024, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
@@ -331,7 +708,7 @@ int mc_normest(gbn_ctx* ctx, gbn_problem* P, cudaStream_t s) {
   int cnt = 0;
   while (std::fabs(e - e0) > tol * e && cnt < 100) {
     e0 = e;
-    if ((rc = mc_apply(ctx, P, x, tmp, s)) != GBN_OK) return rc;
+    mc_apply(ctx, P, x, tmp, s);
     if ((rc = op_ttv(ctx, GBN_TTV_FORWARD, tmp, Sx, W, H, F)) != GBN_OK) return rc;
     if ((rc = sums(ctx, P, Sx, sm, s)) != GBN_OK) return rc;
     if (sm[1] == 0.0) {
@@ -343,7 +720,7 @@ int mc_normest(gbn_ctx* ctx, gbn_problem* P, cudaStream_t s) {
     }
     e = float(std::sqrt(sm[0]));
     if ((rc = op_ttv(ctx, GBN_TTV_ADJOINT, Sx, tmp, W, H, F)) != GBN_OK) return rc;
-    if ((rc = mc_adjoint(ctx, P, tmp, x, s)) != GBN_OK) return rc;
+    mc_adjoint(ctx, P, tmp, x, s);
     if ((rc = sums(ctx, P, x, sm, s)) != GBN_OK) return rc;
     const float nx = float(std::sqrt(sm[0]));
     k_scale2<<<grid1(ctx, X), kNT, 0, s>>>(x, X, 1.0f / nx);
@@ -362,40 +739,48 @@ int mc_normest(gbn_ctx* ctx, gbn_problem* P, cudaStream_t s) {
 int motion_op(gbn_ctx* ctx, int dir, const float2* in, float2* out, const float* xn, const int* xm, const int* bb,
               int W, int H, int F) {
   const McRect r = mc_rect(W, H, bb);
-  if (r.l1 <= 0 || r.l2 <= 0 || r.r1b < 0 || r.r2b < 0 || r.r1b + r.l1 > H || r.r2b + r.l2 > W)
+  if (!rect_ok(r, W, H))
     return set_error(GBN_ERR_INVALID, "motion compensation: bounding box plus margins leaves the image");
+  if (in == out) return set_error(GBN_ERR_INVALID, "motion compensation: input and output must differ");
   void* scr = nullptr;
   int rc = ctx_scratch(ctx, sizeof(int), &scr);
   if (rc != GBN_OK) return rc;
   int* status = static_cast<int*>(scr);
   cudaStream_t s = ctx->stream;
-  const size_t X = size_t(W) * H * F;
+  McTables t;
+  if ((rc = tables_alloc(&t, W, H, F, r.l1 * r.l2)) != GBN_OK) return rc;
   cudaError_t e = cudaMemsetAsync(status, 0, sizeof(int), s);
-  if (e == cudaSuccess) e = cudaMemcpyAsync(out, in, X * sizeof(float2), cudaMemcpyDeviceToDevice, s);
-  if (e != cudaSuccess) return cuda_status(e, "motion compensation");
-  const int g = grid1(ctx, size_t(r.l1) * r.l2 * F);
-  if (dir == GBN_TTV_FORWARD) {
-    k_mc_warp<<<g, kNT, 0, s>>>(in, out, xn, xm, r, W, H, F, status);
+  if (e != cudaSuccess) rc = cuda_status(e, "motion compensation");
+  if (rc == GBN_OK) rc = tables_build(ctx, &t, xn, xm, r, W, H, F, status, s);
+  if (rc == GBN_OK) {
+    const size_t X = size_t(W) * H * F;
+    if (dir == GBN_TTV_FORWARD)
+      k_mc_warp<<<grid1(ctx, X), kNT, 0, s>>>(in, out, xn, t.inv, r, W, H, F, status);
+    else
+      k_mc_adjoint<<<int((X + kNT - 1) / kNT), kNT, 0, s>>>(in, out, t.off, t.key, t.srcmap, t.wts, r, W, H, F, 0);
     ctx->launches += 1;
-  } else {
-    k_mc_zero_rect<<<g, kNT, 0, s>>>(out, r, W, H, F);
-    k_mc_scatter<<<g, kNT, 0, s>>>(in, out, xn, xm, r, W, H, F, status);
-    ctx->launches += 2;
   }
   int h = 0;
-  if ((e = cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, s)) == cudaSuccess)
-    e = cudaStreamSynchronize(s);
-  if (e != cudaSuccess) return cuda_status(e, "motion compensation");
-  if (h) return set_error(GBN_ERR_INVALID, "motion compensation: a mesh point interpolates outside the image");
-  return GBN_OK;
+  if (rc == GBN_OK) {
+    if ((e = cudaMemcpyAsync(&h, status, sizeof(int), cudaMemcpyDeviceToHost, s)) == cudaSuccess)
+      e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = cuda_status(e, "motion compensation");
+  } else {
+    cudaStreamSynchronize(s);
+  }
+  tables_free(&t);
+  if (rc == GBN_OK && h) return set_error(GBN_ERR_INVALID, "motion compensation: a mesh point interpolates outside the image");
+  return rc;
 }
 
 // The motion-compensated solve of problem P; x_out holds the starting image.
 int nesta_run_mc(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, float2* x_out) {
   const SizeKernels* kh = find_size(P->H);
   const SizeKernels* kw = find_size(P->W);
-  const int W = P->W, H = P->H, F = P->F, C = P->C, N = W * H;
+  const int W = P->W, H = P->H, F = P->F, C = P->C;
   cudaStream_t s = ctx->stream;
+  McTables* t = P->mc_tab;
+  const McRect r = mc_rect(W, H, P->mc_bb);
   int cpb, k2;
   tuning_for(ctx, W, H, F, C, &cpb, &k2);
   cpb = std::max(1, std::min(cpb, C));
@@ -403,17 +788,22 @@ int nesta_run_mc(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, floa
   const long long steps = ((long long)F * H * C + kw->rows_per_cta - 1) / kw->rows_per_cta;
   const int g2 = row_grid(ctx, kw, true, steps, k2);
   const dim3 g3(W / kWB, 2, F);
+  const dim3 gtv(t->nbp, (F + kTvFrames - 1) / kTvFrames);
+  const int gadj = int((size_t(W) * H * F + kNT - 1) / kNT);
   FusedArgs a = make_args(P, x_out);
-  a.tv_src = P->mc_xw;
+  a.tv_src = P->mc_xw;  // marks the motion-compensated form: the forward pass skips its tTV sums
   a.grad_ext = P->mc_gm;
+  a.part_tv = t->tvpart;
+  a.ntv = F * t->nbp;
   const FusedArgs* tab = P->d_args;
   const BatchMap bm = single_map(F, P->ctl);
   int rc;
   ctx->launches += launch_pre(P, *prm, s);
+  if ((rc = tables_build(ctx, t, P->mc_xn, P->mc_xmesh, r, W, H, F, &P->st->status, s)) != GBN_OK) return rc;
   ctx->launches += launch_store_args(P->d_args, a, s);
   ctx->launches += launch_group_init(tab, 1, kw->rows_per_cta, P->ctl, s);
   // maxima of x0 and of U x0 = tTV(M x0) (NestaUp.cpp:491, 521-568)
-  if ((rc = mc_apply(ctx, P, x_out, P->mc_xw, s)) != GBN_OK) return rc;
+  mc_apply(ctx, P, x_out, P->mc_xw, s);
   ctx->launches += launch_maxima(ctx, P, x_out, P->mc_xw, s);
   if ((rc = mc_normest(ctx, P, s)) != GBN_OK) return rc;
   ctx->launches += launch_setup(P, s);
@@ -421,13 +811,15 @@ int nesta_run_mc(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, floa
     ctx->launches += launch_outer_begin(ctx, P, int(nl), x_out, s);
     for (unsigned it = 0; it < prm->maxIter; ++it) {
       const float2* xk = (it & 1) ? P->xk1 : P->xk0;
-      if ((rc = mc_apply(ctx, P, xk, P->mc_xw, s)) != GBN_OK) return rc;
-      k_mc_tv<<<dim3(W / kWB, F), 128, 0, s>>>(P->mc_xw, P->st, P->mc_g, P->part_tv, W, H, F);
+      launch_pdl(k_mc_tv, gtv, kNT, 0, s, xk, P->mc_xn, static_cast<const int*>(t->inv), r,
+                 static_cast<const NestaDevState*>(P->st), P->mc_g, t->tvpart, W, H, F, &P->st->status);
       kh->fwd_cols(tab, bm, int(it), cpb, g1, s);
       kw->rows(tab, bm, int(it), true, g2, s);
-      if ((rc = mc_adjoint(ctx, P, P->mc_g, P->mc_gm, s)) != GBN_OK) return rc;
+      launch_pdl(k_mc_adjoint, dim3(gadj), kNT, 0, s, static_cast<const float2*>(P->mc_g), P->mc_gm,
+                 static_cast<const int*>(t->off), static_cast<const int*>(t->key), static_cast<const int*>(t->srcmap),
+                 static_cast<const float2*>(t->wts), r, W, H, F, 1);
       kh->inv_cols(tab, bm, int(it), true, g3, s);
-      ctx->launches += 4;
+      ctx->launches += 5;
     }
     ctx->launches += launch_outer_end(ctx, P, x_out, s);
   }

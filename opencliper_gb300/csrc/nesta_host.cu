@@ -500,13 +500,15 @@ int problem_alloc(gbn_problem* P) {
   return GBN_OK;
 }
 
+void motion_free(gbn_problem* P);
+
 void problem_free(gbn_problem* P) {
   void* ptrs[] = {P->flags, P->full_fh, P->rowmap, P->rowoff,  P->rows_h, P->rows_f,  P->row_full, P->T,
                   P->xk0,   P->xk1,     P->wacc,   P->st,      P->fmean,  P->part_tv, P->part_r,   P->part_ne,
-                  P->ne_b,  P->d_args,  P->ctl,      P->fk,     P->colmax, P->smax,   P->fa,
-                  P->mc_xw, P->mc_g,    P->mc_gm,    P->mc_part};
+                  P->ne_b,  P->d_args,  P->ctl,      P->fk,     P->colmax, P->smax,   P->fa};
   for (void* p : ptrs)
     if (p) cudaFree(p);
+  motion_free(P);
 }
 
 // Kept-row analysis for the current contents of y and mask (device only).
