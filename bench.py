@@ -153,9 +153,10 @@ def measured_peak_hbm() -> tuple[float, str]:
         return 6800.0, "fallback"
 
 
-def algorithmic_bytes(kind: str, G: int) -> int:
-    """Compulsory DRAM bytes of one launch of a fused kernel (complex64 = 8 B)."""
-    W, H, F, C = WL["W"], WL["H"], WL["F"], WL["C"]
+def algorithmic_bytes(kind: str, G: int, shape: tuple | None = None) -> int:
+    """Compulsory DRAM bytes of one launch of a fused kernel (complex64 = 8 B)
+    on a (W, H, F, C) problem with G kept rows (default: the headline workload)."""
+    W, H, F, C = shape if shape is not None else (WL["W"], WL["H"], WL["F"], WL["C"])
     N = W * H
     X, Sb, T = 8 * N * F, 8 * N * C, 8 * G * C * W
     if kind == "fwd_cols":   # x_k, S in; kept rows of DFT_H(S x) out
@@ -518,7 +519,111 @@ def cpu_port_sample(iters: int = 3) -> dict:
             "est_seconds_per_recon": round(est, 3), "sample_wall_s": round(wall, 2)}
 
 
-FORMS = (("mixed", mixed_forms), ("batched", batched_form), ("motion", motion_form))
+STRESS_WL = dict(n=256, sizes=(128, 192, 256, 320, 384, 448), frames=(12, 40), coils=(8, 48), accel=(4, 12),
+                 seed0=5000, device_budget_gb=230)
+
+
+def stress_form(ctx, stream, args=None) -> dict:
+    """The stress batch: 256 reconstructions drawn like the uneven workload but
+    with W=H up to 448 and up to 48 coils (seeds 5000+i), all resident in HBM
+    at once, solved by one captured CUDA graph per precision (one timed replay
+    each after the capturing run).  Host inputs come from a spawn process pool;
+    k-space is formed on the device.  Reports recons/s, the HBM footprint, the
+    algorithmic HBM traffic rate of the fused kernels and the distribution of
+    the mixed form's NRMSE against the plain FP32 images (max, p99).  If the
+    drawn set would exceed device_budget_gb it is cut at that point and the cut
+    is reported."""
+    import multiprocessing as mp
+    from concurrent.futures import ProcessPoolExecutor
+
+    import torch
+
+    import opencliper_gb300 as g
+    from opencliper_gb300 import synth
+    B = STRESS_WL
+    params = []
+    for i in range(B["n"]):
+        r = np.random.default_rng(B["seed0"] + i)
+        Wd = int(r.choice(B["sizes"]))
+        F = int(r.integers(B["frames"][0], B["frames"][1] + 1))
+        Cc = int(r.integers(B["coils"][0], B["coils"][1] + 1))
+        Rr = int(r.integers(B["accel"][0], B["accel"][1] + 1))
+        params.append((Wd, Wd, F, Cc, Rr, B["seed0"] + i))
+    # k-space, maps, masks, output and solver state per instance (bytes, approximate)
+    need = [8 * W * H * F * C + 8 * W * H * C + W * H * F + 8 * W * H * F * 8 + 8 * (H // R + 16) * F * C * W
+            for (W, H, F, C, R, _) in params]  # the row buffer is fitted to the kept rows (gbn_problem_fit_rows)
+    keep, tot = 0, 0
+    for b in need:
+        if (tot + b) / 1e9 > B["device_budget_gb"]:
+            break
+        tot += b
+        keep += 1
+    params = params[:keep]
+    free0, total = torch.cuda.mem_get_info()
+    t0 = time.perf_counter()
+    probs, outs, arrays, shapes = [], [], [], []
+    oom = ""
+    # spawn (the parent already holds a CUDA context); a worker that dies raises here instead of hanging
+    with ProcessPoolExecutor(min(16, os.cpu_count() or 1), mp_context=mp.get_context("spawn")) as pool:
+        for (W, H, F, Cc, Rr, seed), (x, S, rm) in zip(params, pool.map(synth.host_inputs_packed, params)):
+            if oom:
+                continue
+            try:
+                p = synth.device_problem_from(ctx, x, S, rm, seed)
+                arrays += [p.y, p.S, p.mask]
+                xo = ctx.empty((F, H, W), np.complex64)
+                arrays.append(xo)
+                probs.append(g.Problem(ctx, p.y, p.S, p.mask))
+                probs[-1].fit_rows(0)  # row buffer sized to the kept rows instead of the whole k-space
+            except (g.GbnError, torch.cuda.OutOfMemoryError) as e:  # device full: keep what fits
+                oom = str(e)
+                continue
+            outs.append(xo)
+            shapes.append((W, H, F, Cc))
+    gen_s = time.perf_counter() - t0
+    if oom:
+        params = params[:len(probs)]
+    res = {"workload": f"{len(params)} of {B['n']} reconstructions, W=H in {list(B['sizes'])}, F U{{12..40}}, "
+                       f"C U{{8..48}}, R U{{4..12}}, seeds {B['seed0']}+i, one CUDA graph per precision",
+           "unit": UNIT, "instances": len(params), "generation_s": round(gen_s, 1),
+           "pixel_coil_frames": int(sum(W * H * F * C for (W, H, F, C) in shapes))}
+    if oom:
+        res["device_full"] = oom
+    ref = []
+    for name, prec in (("fp32", g.PRECISION_FP32), ("mixed", g.PRECISION_MIXED)):
+        try:
+            b = g.Batch(ctx, probs, g.nesta_params(**NESTA), outs, precision=prec)
+        except g.GbnError as e:
+            res[name] = {"unavailable": str(e)}
+            continue
+        free1, _ = torch.cuda.mem_get_info()
+        rate, ms = _graph_rate(ctx, stream, b, len(probs), 1)
+        G = [int(b.stats(i)["kept_rows"]) for i in range(len(probs))]
+        alg = sum((algorithmic_bytes("fwd_cols", Gi, sh) + algorithmic_bytes("rows", Gi, sh) +
+                   algorithmic_bytes("inv_cols", Gi, sh)) for Gi, sh in zip(G, shapes)) * NESTA["maxIter"]
+        res[name] = {"value": round(rate, 3), "ms_per_batch": round(ms, 1),
+                     "hbm_used_gb": round((total - free1) / 1e9, 1),
+                     "algorithmic_gbs": round(alg / (ms / 1e3) / 1e9, 1),
+                     "status_nonzero": int(sum(b.stats(i)["status"] != 0 for i in range(len(probs))))}
+        dev = torch.device("cuda", ctx.device)
+        imgs = [torch.as_tensor(synth._CudaView(o, "<f4", o.shape + (2,)), device=dev) for o in outs]
+        if name == "fp32":
+            ref = [t.clone() for t in imgs]
+        else:
+            e = torch.stack([(a - r).norm() / r.norm().clamp_min(1e-30) for a, r in zip(imgs, ref)]).cpu().numpy()
+            res["nrmse_mixed_vs_fp32"] = {"max": float(f"{e.max():.3e}"), "p99": float(f"{np.percentile(e, 99):.3e}"),
+                                          "median": float(f"{np.median(e):.3e}")}
+        b.close()
+    del ref
+    for pr in probs:
+        pr.close()
+    for a in arrays:
+        a.free()
+    res["hbm_free_before_gb"] = round(free0 / 1e9, 1)
+    return res
+
+
+FORMS = (("mixed", mixed_forms), ("batched", batched_form), ("motion", motion_form), ("stress", stress_form))
 
 
 def run_reference(args, dist: Dist) -> dict | None:
@@ -552,7 +657,8 @@ def main(argv=None) -> int:
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU restatement timing")
     ap.add_argument("--no-forms", action="store_true", help="skip the mixed, batched and motion form measurements")
     ap.add_argument("--forms", default="mixed,batched,motion",
-                    help="comma-separated forms to measure after the headline (mixed, batched, motion)")
+                    help="comma-separated forms to measure after the headline (mixed, batched, motion; "
+                         "stress, the 256-reconstruction ~150 GB batch, only when named)")
     ap.add_argument("--forms-only", action="store_true",
                     help="measure only the forms named by --forms (no headline line; for profiling)")
     ap.add_argument("--form-reps", type=int, default=3, help="timed repetitions of the motion form")

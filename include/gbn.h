@@ -216,7 +216,10 @@ typedef struct gbn_nesta_stats {
   int inner_iters;    /* inner iterations executed, all outer loops */
   int normest_iters;
   int kept_rows;      /* k-space rows carried by the solver (sampled or nonzero) */
-  int status;         /* 0; nonzero when the device reported a failure of this run */
+  int status;         /* 0; nonzero when the device reported a failure of this run: 3 a tensor-core
+                         wait ran out, 4 kept rows outgrew the mixed form's DFT operand, 5 a
+                         motion-compensation mesh point outside the image, 6 kept rows beyond a
+                         fitted row buffer were dropped */
 } gbn_nesta_stats;
 
 /* Binds the caller's device buffers (not copied, not modified):
@@ -225,6 +228,15 @@ typedef struct gbn_nesta_stats {
 GBN_API int gbn_problem_create(gbn_ctx* ctx, int W, int H, int F, int C, const float* d_y, const float* d_S,
                        const uint8_t* d_mask, gbn_problem** out);
 GBN_API int gbn_problem_destroy(gbn_problem* p);
+/* The row pass keeps one buffer of k-space rows, by default as large as the
+ * k-space (every row of every frame and coil), so that any later contents of
+ * y and mask fit.  This analyses the current y and mask (waiting for the
+ * stream) and resizes it to the rows they keep plus headroom_rows (at most
+ * every row), which roughly halves a problem's device footprint at R >= 4.
+ * A later run whose data keep more rows than that drops the excess and
+ * reports gbn_nesta_stats::status = 6.  *kept_rows (may be NULL) receives the
+ * rows kept now.  Call before the problem joins a batch. */
+GBN_API int gbn_problem_fit_rows(gbn_problem* p, int headroom_rows, int* kept_rows);
 /* MotionCompensation (direction GBN_TTV_FORWARD, MotionCompensation.cpp:57-78)
  * or AdjointMotionCompensation (GBN_TTV_ADJOINT, AdjointMotionCompensation.cpp:
  * 59-86) of XData [F][H][W]; meshes and bounding box as for

@@ -271,6 +271,13 @@ class Problem:
         self._keep = (y, S, mask)
         ctx._children.add(self)
 
+    def fit_rows(self, headroom_rows: int = 0) -> int:
+        """Resize the row buffer to the rows the current y and mask keep plus
+        headroom (gbn_problem_fit_rows); returns the kept rows."""
+        g = C.c_int(0)
+        call("gbn_problem_fit_rows", self.handle, int(headroom_rows), C.byref(g))
+        return g.value
+
     def set_motion(self, xn: DeviceArray | None, xmesh: DeviceArray | None, bound_box=None) -> None:
         """Motion-compensated sparsity operator (gbn_problem_set_motion); the
         run then starts from the image already in its output buffer."""

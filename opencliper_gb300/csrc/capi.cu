@@ -33,6 +33,7 @@ int batch_stats(gbn_batch*, int, gbn_nesta_stats*);
 int batch_destroy(gbn_batch*);
 gbn_ctx* batch_ctx(gbn_batch*);
 int motion_set(gbn_problem*, const float*, const int*, const int*);
+int problem_fit_rows(gbn_problem*, int, int*);
 int motion_op(gbn_ctx*, int, const float2*, float2*, const float*, const int*, const int*, int, int, int);
 int autotune(gbn_ctx*, int, const int*, const char*);
 int autotune_load(gbn_ctx*, const char*);
@@ -561,6 +562,12 @@ int gbn_problem_set_motion(gbn_problem* p, const float* d_xn, const int* d_xmesh
   if (!p) return set_error(GBN_ERR_INVALID, "null problem");
   DeviceGuard guard(p->ctx->device);
   return motion_set(p, d_xn, d_xmesh, bound_box);
+}
+
+int gbn_problem_fit_rows(gbn_problem* p, int headroom_rows, int* kept_rows) {
+  if (!p) return set_error(GBN_ERR_INVALID, "null problem");
+  DeviceGuard guard(p->ctx->device);
+  return problem_fit_rows(p, headroom_rows, kept_rows);
 }
 
 int gbn_problem_destroy(gbn_problem* p) {

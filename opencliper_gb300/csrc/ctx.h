@@ -64,7 +64,8 @@ struct gbn_problem {
   int* rows_h = nullptr;              // [F*H]
   int* rows_f = nullptr;              // [F*H]
   int* row_full = nullptr;            // [F*H]
-  float2* T = nullptr;                // [F*H*C*W] worst case
+  float2* T = nullptr;                // [T_rows][C][W] kept rows of the row pass
+  size_t T_rows = 0;                  // rows T holds (F*H unless fitted with gbn_problem_fit_rows)
   float2* xk0 = nullptr;
   float2* xk1 = nullptr;
   float2* wacc = nullptr;

@@ -74,14 +74,19 @@ __global__ void k_rowflags(const float2* __restrict__ y, const uint8_t* __restri
   }
 }
 
-// one CTA of 512 threads (H <= 512): per-frame prefix numbering of kept rows
+constexpr int kStatusRowsOverflow = 6;  // NestaDevState::status: kept rows beyond the row buffer were dropped
+
+// one CTA of 512 threads (H <= 512): per-frame prefix numbering of kept rows;
+// rows beyond the row buffer's capacity `cap` are dropped (rowmap -1) and
+// reported in *status
 __global__ void __launch_bounds__(512) k_rowscan(const int* __restrict__ flags, const int* __restrict__ full, int H,
                                                  int F, int* __restrict__ rowmap, int* __restrict__ rowoff,
                                                  int* __restrict__ rows_h, int* __restrict__ rows_f,
-                                                 int* __restrict__ row_full) {
+                                                 int* __restrict__ row_full, int cap, int* __restrict__ status) {
   __shared__ int wsum[16];
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
   int base = 0;
+  bool dropped = false;
   for (int f = 0; f < F; ++f) {
     const int fl = (t < H) ? flags[f * H + t] : 0;
     const unsigned bal = __ballot_sync(0xffffffffu, fl);
@@ -93,20 +98,25 @@ __global__ void __launch_bounds__(512) k_rowscan(const int* __restrict__ flags, 
       if (i < wid) woff += wsum[i];
       tot += wsum[i];
     }
+    const int room = max(0, cap - base);
     if (t < H) {
-      const int j = fl ? woff + pre : -1;
+      const int j = (fl && woff + pre < room) ? woff + pre : -1;
       rowmap[f * H + t] = j;
-      if (fl) {
+      if (j >= 0) {
         rows_h[base + j] = t;
         rows_f[base + j] = f;
         row_full[base + j] = full[f * H + t];
       }
     }
     if (t == 0) rowoff[f] = base;
-    base += tot;
+    dropped |= tot > room;
+    base += min(tot, room);
     __syncthreads();
   }
-  if (t == 0) rowoff[F] = base;
+  if (t == 0) {
+    rowoff[F] = base;
+    if (dropped) atomicExch(status, kStatusRowsOverflow);
+  }
 }
 
 // every row kept, in natural order (SimpleMRIRecon: fully sampled data)
@@ -487,6 +497,7 @@ int problem_alloc(gbn_problem* P) {
   A((void**)&P->rows_f, FH * sizeof(int));
   A((void**)&P->row_full, FH * sizeof(int));
   A((void**)&P->T, K * sizeof(float2));
+  P->T_rows = FH;
   A((void**)&P->xk0, X * sizeof(float2));
   A((void**)&P->xk1, X * sizeof(float2));
   A((void**)&P->wacc, X * sizeof(float2));
@@ -498,6 +509,44 @@ int problem_alloc(gbn_problem* P) {
     return set_error(GBN_ERR_NOMEM, std::string("problem workspace allocation failed: ") + cudaGetErrorString(e));
   }
   return GBN_OK;
+}
+
+void launch_row_analysis(gbn_problem* P, cudaStream_t s);
+
+// Shrinks (or grows) the row buffer T to the rows the current y and mask keep
+// plus `headroom` (at most every row); returns the kept rows in *kept.
+int problem_fit_rows(gbn_problem* P, int headroom, int* kept) {
+  if (headroom < 0) return set_error(GBN_ERR_INVALID, "headroom must be >= 0");
+  cudaStream_t s = P->ctx->stream;
+  cudaError_t e = cudaMemsetAsync(&P->st->status, 0, sizeof(int), s);
+  const size_t saved = P->T_rows;
+  P->T_rows = size_t(P->F) * P->H;  // count every kept row
+  if (e == cudaSuccess) {
+    launch_row_analysis(P, s);
+    int g = 0;
+    if ((e = cudaMemcpyAsync(&g, P->rowoff + P->F, sizeof(int), cudaMemcpyDeviceToHost, s)) == cudaSuccess &&
+        (e = cudaStreamSynchronize(s)) == cudaSuccess) {
+      const size_t want = std::min<size_t>(size_t(P->F) * P->H, size_t(g) + size_t(headroom));
+      if (want != saved) {
+        float2* nt = nullptr;
+        if ((e = cudaMalloc(&nt, std::max<size_t>(want, 1) * P->C * P->W * sizeof(float2))) == cudaSuccess) {
+          cudaFree(P->T);
+          P->T = nt;
+          P->T_rows = want;
+          if (kept) *kept = g;
+          return GBN_OK;
+        }
+      } else {
+        P->T_rows = saved;
+        if (kept) *kept = g;
+        return GBN_OK;
+      }
+    }
+  }
+  P->T_rows = saved;
+  cudaGetLastError();
+  return e == cudaErrorMemoryAllocation ? set_error(GBN_ERR_NOMEM, "row buffer allocation failed")
+                                        : cuda_status(e, "fit rows");
 }
 
 void motion_free(gbn_problem* P);
@@ -515,7 +564,7 @@ void problem_free(gbn_problem* P) {
 void launch_row_analysis(gbn_problem* P, cudaStream_t s) {
   k_rowflags<<<dim3(P->H, P->F), 128, 0, s>>>(P->y, P->mask, P->W, P->H, P->F, P->C, P->flags, P->full_fh);
   k_rowscan<<<1, 512, 0, s>>>(P->flags, P->full_fh, P->H, P->F, P->rowmap, P->rowoff, P->rows_h, P->rows_f,
-                              P->row_full);
+                              P->row_full, int(P->T_rows), &P->st->status);
 }
 
 FusedArgs make_args(gbn_problem* P, float2* xref) {

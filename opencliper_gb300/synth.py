@@ -147,20 +147,32 @@ class _CudaView:
                                          "version": 3, "strides": None}
 
 
-def make_problem_device(ctx, W: int, H: int, F: int, C: int, R: float, seed: int,
-                        noise: float = 1e-3) -> DeviceProblem:
-    """The distributions of make_problem with the k-space formed on the device:
-    the library's forward operator (gbn_op_encode, mask * FFT2_ortho(S_c x_f))
-    plus masked complex Gaussian noise drawn by torch from `seed`.  For
-    benchmark workloads too large to generate with numpy FFTs; the noise stream
-    differs from make_problem's."""
-    import torch
-
-    from . import api
+def host_inputs(W: int, H: int, F: int, C: int, R: float, seed: int):
+    """(x [F][H][W], S [C][H][W], row mask [F][H]) of make_problem's
+    distributions, drawn from `seed` (a top-level function, so that process
+    pools can run it)."""
     rng = np.random.default_rng(np.random.PCG64(seed))
     x = phantom_series(W, H, F, rng)
     S = coil_maps(W, H, C)
     rm = row_masks(H, F, R, rng)
+    return x, S, rm
+
+
+def host_inputs_packed(prm: tuple):
+    """host_inputs((W, H, F, C, R, seed)) for Pool.imap."""
+    return host_inputs(*prm)
+
+
+def device_problem_from(ctx, x: np.ndarray, S: np.ndarray, rm: np.ndarray, seed: int,
+                        noise: float = 1e-3) -> DeviceProblem:
+    """k-space formed on the device from host inputs: the library's forward
+    operator (gbn_op_encode, mask * FFT2_ortho(S_c x_f)) plus masked complex
+    Gaussian noise drawn by torch from `seed`."""
+    import torch
+
+    from . import api
+    F, H, W = x.shape
+    C = S.shape[0]
     mask = np.repeat((rm.astype(np.uint8) * 255)[:, :, None], W, axis=2)
     dx, dS, dm = ctx.to_device(x), ctx.to_device(S), ctx.to_device(mask)
     dy = ctx.empty((F, C, H, W), np.complex64)
@@ -178,6 +190,15 @@ def make_problem_device(ctx, W: int, H: int, F: int, C: int, R: float, seed: int
     torch.cuda.synchronize(dev)
     dx.free()
     return DeviceProblem(dy, dS, dm, rm, int(seed))
+
+
+def make_problem_device(ctx, W: int, H: int, F: int, C: int, R: float, seed: int,
+                        noise: float = 1e-3) -> DeviceProblem:
+    """The distributions of make_problem with the k-space formed on the device
+    (device_problem_from).  For benchmark workloads too large to generate with
+    numpy FFTs; the noise stream differs from make_problem's."""
+    x, S, rm = host_inputs(W, H, F, C, R, seed)
+    return device_problem_from(ctx, x, S, rm, seed, noise)
 
 
 def make_motion(W: int, H: int, F: int, seed: int, amplitude: float = 1.2, border: int = 4):

@@ -154,3 +154,31 @@ def test_nesta_full_workload_accuracy(ctx):
     print(f"full workload NRMSE gpu/f64 {e_gpu:.3e}  f32-oracle/f64 {e_32:.3e}  gpu/f32 {R.nrmse(out, r32.x):.3e}")
     assert e_gpu <= 1e-3
     assert e_gpu <= 2.0 * e_32 + 5e-6
+
+
+def test_fit_rows_shrinks_row_buffer(ctx):
+    """gbn_problem_fit_rows: a fitted row buffer gives the same image bit for
+    bit; data that keep more rows than it holds are reported (status 6), and
+    refitting clears that."""
+    p = synth.make_problem(48, 40, 5, 3, 4, seed=12)
+    dy, dS, dm = ctx.to_device(p.y), ctx.to_device(p.S), ctx.to_device(p.mask)
+    prm = g.nesta_params(**FIXED)
+    outs = []
+    for fit in (False, True):
+        prob = g.Problem(ctx, dy, dS, dm)
+        if fit:
+            kept = prob.fit_rows(0)
+            assert kept == int(p.rowmask.astype(bool).sum())
+        x = ctx.empty((5, 40, 48), np.complex64)
+        ctx.seed48(drand48.state_to_seed16v(drand48.DEFAULT_STATE))
+        st = prob.run(prm, x)
+        assert st["status"] == 0 and st["kept_rows"] == int(p.rowmask.astype(bool).sum())
+        outs.append(x.get())
+        if fit:
+            dm.set(np.full(p.mask.shape, 255, np.uint8))  # every row sampled now: more than the buffer holds
+            st = prob.run(prm, x)
+            assert st["status"] == 6
+            assert prob.fit_rows(0) == 5 * 40
+            assert prob.run(prm, x)["status"] == 0
+        prob.close()
+    assert np.array_equal(outs[0], outs[1])
