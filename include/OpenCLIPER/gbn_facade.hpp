@@ -24,8 +24,10 @@
 #include <map>
 #include <memory>
 #include <sstream>
+#include <exception>
 #include <stdexcept>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../gbn.h"
@@ -89,14 +91,33 @@ class Data {
   virtual ~Data() {
     if (dev_ && app_) gbn_free(app_->ctx(), dev_);
   }
-  void* getDevicePtr() const { return dev_; }
-  size_t getBytes() const { return bytes_; }
+  Data(const Data&) = delete;
+  Data& operator=(const Data&) = delete;
+  void* getDevicePtr() const {
+    ensureLoaded();
+    return dev_;
+  }
+  size_t getBytes() const {
+    ensureLoaded();
+    return bytes_;
+  }
   const std::shared_ptr<CLapp>& getApp() const { return app_; }
+  /// Data::waitLoadEnd (Data.cpp:1110-1115): waits for an asynchronous file
+  /// load to finish; a no-op for data that were loaded synchronously.
+  void waitLoadEnd() const { ensureLoaded(); }
 
  protected:
   Data(const std::shared_ptr<CLapp>& app, size_t bytes) : app_(app), bytes_(bytes) {
     gbnCheck(gbn_alloc(app->ctx(), bytes, &dev_), "Data: device allocation");
   }
+  // no device buffer yet (a load that completes later)
+  explicit Data(const std::shared_ptr<CLapp>& app) : app_(app) {}
+  void allocate(size_t bytes) {
+    bytes_ = bytes;
+    gbnCheck(gbn_alloc(app_->ctx(), bytes, &dev_), "Data: device allocation");
+  }
+  // completes a pending load (subclasses with asynchronous loads override it)
+  virtual void ensureLoaded() const {}
   void upload(const void* host) {
     gbnCheck(gbn_upload(app_->ctx(), dev_, host, bytes_), "Data::host2Device");
     app_->finish();
@@ -278,18 +299,53 @@ class KData : public Data {
   /// complex float [F][C][H][W], sensitivity maps <base>_SensitivityMaps.cfl
   /// [C][H][W] and the sampling masks <base>_SamplingMasks.u32 (row mask
   /// [F][H]) or else <base>_SamplingMasks.u8 (pixel mask [F][H][W]), each
-  /// when present.  Only 2-D Cartesian data; the load is synchronous.
-  KData(const std::shared_ptr<CLapp>& app, const std::string& fileName, bool asyncLoad = false)
-      : KData(load(app, fileName)) {
-    (void)asyncLoad;
+  /// when present.  Only 2-D Cartesian data.  With asyncLoad the files are
+  /// read by a host thread (KData.cpp:281-284) while the caller goes on;
+  /// waitLoadEnd() -- or any accessor -- joins it and moves the data to the
+  /// device on the calling thread.  A read error is rethrown there.
+  KData(const std::shared_ptr<CLapp>& app, const std::string& fileName, bool asyncLoad = false) : Data(app) {
+    if (asyncLoad) {
+      loader_.reset(new std::thread([this, fileName] {
+        try {
+          host_ = read_host(fileName);
+        } catch (...) {
+          error_ = std::current_exception();
+        }
+      }));
+    } else {
+      host_ = read_host(fileName);
+      materialize();
+    }
   }
-  std::shared_ptr<SensitivityMapsData> getSensitivityMapsData() const { return sens_; }
-  std::shared_ptr<SamplingMasksData> getSamplingMasksData() const { return masks_; }
-  dimIndexType getNCoils() const { return C_; }
-  dimIndexType getDynDimsTotalSize() const { return F_; }
-  dimIndexType width() const { return W_; }
-  dimIndexType height() const { return H_; }
+  ~KData() override {
+    if (loader_ && loader_->joinable()) loader_->join();  // as Data::~Data (Data.cpp:514)
+  }
+  std::shared_ptr<SensitivityMapsData> getSensitivityMapsData() const {
+    ensureLoaded();
+    return sens_;
+  }
+  std::shared_ptr<SamplingMasksData> getSamplingMasksData() const {
+    ensureLoaded();
+    return masks_;
+  }
+  dimIndexType getNCoils() const {
+    ensureLoaded();
+    return C_;
+  }
+  dimIndexType getDynDimsTotalSize() const {
+    ensureLoaded();
+    return F_;
+  }
+  dimIndexType width() const {
+    ensureLoaded();
+    return W_;
+  }
+  dimIndexType height() const {
+    ensureLoaded();
+    return H_;
+  }
   void device2Host(std::vector<complexType>& out) const {
+    ensureLoaded();
     out.resize(size_t(W_) * H_ * F_ * C_);
     download(out.data());
   }
@@ -297,6 +353,7 @@ class KData : public Data {
   /// SensitivityMaps (H x W x C) when present; the sampling masks are not
   /// saved, as in the reference.  Written uncompressed.
   void matlabSave(const std::string& fileName) const {
+    ensureLoaded();
     std::vector<matfile::Var> vars;
     vars.push_back(matio::dims_var(W_, H_, C_, F_));
     std::vector<complexType> h;
@@ -309,83 +366,115 @@ class KData : public Data {
     matfile::write(fileName, vars);
   }
 
+ protected:
+  void ensureLoaded() const override {
+    if (!loader_) return;
+    loader_->join();
+    loader_.reset();
+    if (error_) {
+      std::exception_ptr e = error_;
+      error_ = nullptr;
+      std::rethrow_exception(e);
+    }
+    const_cast<KData*>(this)->materialize();
+  }
+
  private:
-  struct Loaded {
-    std::shared_ptr<CLapp> app;
-    dimIndexType W, H, F, C;
-    std::vector<complexType> data;
-    std::shared_ptr<SensitivityMapsData> sens;
-    std::shared_ptr<SamplingMasksData> masks;
+  // a file's contents on the host
+  struct HostK {
+    dimIndexType W = 0, H = 0, F = 0, C = 0;
+    std::vector<complexType> data, maps;
+    std::vector<uint32_t> rowmask;
+    std::vector<uint8_t> pixmask;
   };
-  explicit KData(Loaded&& l) : KData(l.app, l.W, l.H, l.F, l.C, l.data, l.sens, l.masks) {}
-  static Loaded load_mat(const std::shared_ptr<CLapp>& app, const std::string& fileName) {
+
+  // the host data to the device (on the calling thread: a context is not shared across threads)
+  void materialize() {
+    HostK h = std::move(host_);
+    if (h.W % 8 != 0) throw std::invalid_argument("NDArray dimension 0 is not multiple of 8");
+    W_ = h.W;
+    H_ = h.H;
+    F_ = h.F;
+    C_ = h.C;
+    allocate(sizeof(complexType) * h.data.size());
+    upload(h.data.data());
+    if (!h.maps.empty()) sens_ = std::make_shared<SensitivityMapsData>(app_, h.W, h.H, h.C, h.maps);
+    if (!h.rowmask.empty())
+      masks_ = SamplingMasksData::fromRowMask(app_, h.W, h.H, h.F, h.rowmask);
+    else if (!h.pixmask.empty())
+      masks_ = std::make_shared<SamplingMasksData>(app_, h.W, h.H, h.F, h.pixmask);
+  }
+
+  static HostK read_mat(const std::string& fileName) {
     const auto vars = matfile::read(fileName);
     const matio::Dims d = matio::parse_dims(vars, "KData::KData");
     const auto it = vars.find("KData");
     if (it == vars.end()) throw std::invalid_argument("Error: no KData variable in matlab file");
-    const dimIndexType C = d.C > 1 ? d.C : 1;
-    matio::check_dims(it->second, d.H, d.W, {C, d.F}, "KData");
-    Loaded l{app, d.W, d.H, d.F, C, matio::complex_rows(it->second, "KData"), nullptr, nullptr};
+    HostK h;
+    h.W = d.W;
+    h.H = d.H;
+    h.F = d.F;
+    h.C = d.C > 1 ? d.C : 1;
+    matio::check_dims(it->second, h.H, h.W, {h.C, h.F}, "KData");
+    h.data = matio::complex_rows(it->second, "KData");
     const auto sm = vars.find("SensitivityMaps");
     if (sm != vars.end()) {
-      matio::check_dims(sm->second, d.H, d.W, {C}, "SensitivityMaps");
-      l.sens = std::make_shared<SensitivityMapsData>(app, d.W, d.H, C, matio::complex_rows(sm->second, "SensitivityMaps"));
+      matio::check_dims(sm->second, h.H, h.W, {h.C}, "SensitivityMaps");
+      h.maps = matio::complex_rows(sm->second, "SensitivityMaps");
     }
     const auto mk = vars.find("SamplingMasks");
     if (mk != vars.end()) {
       const matfile::Var& m = mk->second;
       if (m.complex) throw std::invalid_argument("Invalid mask format (supported: ROWMASK and PIXELMASK");
       if (m.cls == matfile::kUInt32) {  // row mask: MATLAB dims H x F (one 1-D array per frame)
-        if (m.dims[0] != d.H || m.numel() != size_t(d.H) * d.F)
+        if (m.dims[0] != h.H || m.numel() != size_t(h.H) * h.F)
           throw std::out_of_range("Invalid SamplingMasks dimensions");
         const uint32_t* r = m.real<uint32_t>();
-        l.masks = SamplingMasksData::fromRowMask(app, d.W, d.H, d.F, std::vector<uint32_t>(r, r + m.numel()));
+        h.rowmask.assign(r, r + m.numel());
       } else if (m.cls == matfile::kUInt8) {  // pixel mask: H x W x F
-        matio::check_dims(m, d.H, d.W, {d.F}, "SamplingMasks");
-        std::vector<uint8_t> px;
-        matfile::to_row_major<uint8_t>(m, px, nullptr);
-        l.masks = std::make_shared<SamplingMasksData>(app, d.W, d.H, d.F, px);
+        matio::check_dims(m, h.H, h.W, {h.F}, "SamplingMasks");
+        matfile::to_row_major<uint8_t>(m, h.pixmask, nullptr);
       } else {
         throw std::invalid_argument("Invalid mask format (supported: ROWMASK and PIXELMASK");
       }
     }
-    return l;
+    return h;
   }
-  static Loaded load(const std::shared_ptr<CLapp>& app, const std::string& fileName) {
-    if (matfile::is_mat(fileName)) return load_mat(app, fileName);
+
+  static HostK read_host(const std::string& fileName) {
+    if (matfile::is_mat(fileName)) return read_mat(fileName);
     const std::string base = cfl::basename(fileName);
     std::ifstream hdr(base + ".hdr");
     if (!hdr) throw std::invalid_argument("KData: cannot open " + base + ".hdr");
-    Loaded l{app, 0, 0, 0, 0, {}, nullptr, nullptr};
+    HostK h;
     std::string line;
     bool ok = false;
     while (std::getline(hdr, line)) {
       if (line.empty() || line[0] == '#') continue;
       std::istringstream iss(line);
-      if (!(iss >> l.W >> l.H >> l.C >> l.F))
+      if (!(iss >> h.W >> h.H >> h.C >> h.F))
         throw std::invalid_argument("Invalid line format: " + line + " (should be <width> <depth> <numCoils> <numFrames>)");
       ok = true;
       break;
     }
     if (!ok) throw std::invalid_argument("KData: no dimensions in " + base + ".hdr");
-    l.data = cfl::read_raw<complexType>(fileName, size_t(l.W) * l.H * l.F * l.C, "KData");
+    h.data = cfl::read_raw<complexType>(fileName, size_t(h.W) * h.H * h.F * h.C, "KData");
     const std::string sname = base + "_SensitivityMaps.cfl";
-    if (cfl::exists(sname))
-      l.sens = std::make_shared<SensitivityMapsData>(
-          app, l.W, l.H, l.C, cfl::read_raw<complexType>(sname, size_t(l.W) * l.H * l.C, "SensitivityMapsData"));
+    if (cfl::exists(sname)) h.maps = cfl::read_raw<complexType>(sname, size_t(h.W) * h.H * h.C, "SensitivityMapsData");
     const std::string rname = base + "_SamplingMasks.u32", pname = base + "_SamplingMasks.u8";
     if (cfl::exists(rname))
-      l.masks = SamplingMasksData::fromRowMask(app, l.W, l.H, l.F,
-                                               cfl::read_raw<uint32_t>(rname, size_t(l.H) * l.F, "SamplingMasksData"));
+      h.rowmask = cfl::read_raw<uint32_t>(rname, size_t(h.H) * h.F, "SamplingMasksData");
     else if (cfl::exists(pname))
-      l.masks = std::make_shared<SamplingMasksData>(
-          app, l.W, l.H, l.F, cfl::read_raw<uint8_t>(pname, size_t(l.W) * l.H * l.F, "SamplingMasksData"));
-    return l;
+      h.pixmask = cfl::read_raw<uint8_t>(pname, size_t(h.W) * h.H * h.F, "SamplingMasksData");
+    return h;
   }
 
-  dimIndexType W_, H_, F_, C_;
+  dimIndexType W_ = 0, H_ = 0, F_ = 0, C_ = 0;
   std::shared_ptr<SensitivityMapsData> sens_;
   std::shared_ptr<SamplingMasksData> masks_;
+  HostK host_;
+  mutable std::unique_ptr<std::thread> loader_;
+  mutable std::exception_ptr error_;
 };
 
 /// XData: image series [F][H][W]; XData(app, kdata) sizes it like the input

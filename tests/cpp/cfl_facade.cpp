@@ -16,7 +16,7 @@ int main(int argc, char** argv) {
   if (argc < 3) return 2;
   try {
     auto app = CLapp::create();
-    auto k = std::make_shared<KData>(app, std::string(argv[1]));
+    auto k = std::make_shared<KData>(app, std::string(argv[1]), true);  // asynchronous: accessors join the load
     const std::string out = argv[2];
 
     auto simple = Process::create<SimpleMRIRecon>(app);

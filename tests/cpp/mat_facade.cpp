@@ -3,7 +3,8 @@
 // SimpleMRIRecon, XData::matlabSave) plus NestaUp on the same data.
 // Usage: mat_facade <kdata.mat> <outprefix>; writes <outprefix>_simple.mat,
 // <outprefix>_nesta.mat, <outprefix>_k.mat (KData::matlabSave) and
-// <outprefix>_stats.txt ("reload <max abs difference>").
+// <outprefix>_stats.txt ("reload <max abs difference>", "async <error class of
+// a failed asynchronous load>").
 #include <algorithm>
 #include <cmath>
 #include <fstream>
@@ -25,7 +26,9 @@ int main(int argc, char** argv) {
   const std::string in = argv[1], out = argv[2];
   try {
     auto pCLapp = CLapp::create();
-    auto pInputKData = std::make_shared<KData>(pCLapp, in);
+    // asynchronous load joined before use, as tests/MRIRecon.cpp:150-179 does
+    auto pInputKData = std::make_shared<KData>(pCLapp, in, true);
+    pInputKData->waitLoadEnd();
     auto pOutputXData = std::make_shared<XData>(pCLapp, pInputKData);
     auto pProcess = Process::create<SimpleMRIRecon>(pCLapp);
     pProcess->setInput(pInputKData);
@@ -52,7 +55,15 @@ int main(int argc, char** argv) {
     nesta->launch();
     pNestaOut->matlabSave(out + "_nesta.mat");
     pInputKData->matlabSave(out + "_k.mat");
-    std::ofstream(out + "_stats.txt") << "reload " << diff << "\n";
+    // a failed asynchronous load reports its error when joined
+    std::string async_err = "none";
+    try {
+      auto missing = std::make_shared<KData>(pCLapp, out + "_missing.mat", true);
+      missing->waitLoadEnd();
+    } catch (const std::invalid_argument&) {
+      async_err = "invalid_argument";
+    }
+    std::ofstream(out + "_stats.txt") << "reload " << diff << "\nasync " << async_err << "\n";
   } catch (const std::exception& e) {
     std::cerr << "error: " << e.what() << "\n";
     return 1;

@@ -26,7 +26,7 @@ def driver(tmp_path_factory, built_lib):
         pytest.skip("g++ not available")
     exe = tmp_path_factory.mktemp("facade") / "mrirecon_facade"
     libdir = os.path.join(ROOT, "opencliper_gb300")
-    subprocess.run([cxx, "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
+    subprocess.run([cxx, "-std=c++17", "-O2", "-Wall", "-pthread", "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "cpp", "mrirecon_facade.cpp"), "-L", libdir, "-lgbnesta",
                     f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
     return exe
@@ -94,7 +94,7 @@ def test_facade_cfl_files(ctx, tmp_path):
         pytest.skip("g++ not available")
     exe = tmp_path / "cfl_facade"
     libdir = os.path.join(ROOT, "opencliper_gb300")
-    subprocess.run([cxx, "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
+    subprocess.run([cxx, "-std=c++17", "-O2", "-Wall", "-pthread", "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "cpp", "cfl_facade.cpp"), "-L", libdir, "-lgbnesta",
                     f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
     W, H, F, C = 32, 24, 4, 3
@@ -132,7 +132,7 @@ def test_facade_mat_files(ctx, tmp_path):
         pytest.skip("g++ not available")
     exe = tmp_path / "mat_facade"
     libdir = os.path.join(ROOT, "opencliper_gb300")
-    subprocess.run([cxx, "-std=c++17", "-O2", "-Wall", "-I", os.path.join(ROOT, "include"),
+    subprocess.run([cxx, "-std=c++17", "-O2", "-Wall", "-pthread", "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "tests", "cpp", "mat_facade.cpp"), "-L", libdir, "-lgbnesta",
                     f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
     W, H, F, C = 40, 32, 4, 3
@@ -142,7 +142,7 @@ def test_facade_mat_files(ctx, tmp_path):
     out = str(tmp_path / "out")
     r = subprocess.run([str(exe), kfile, out], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
-    assert (tmp_path / "out_stats.txt").read_text().split() == ["reload", "0"]
+    assert (tmp_path / "out_stats.txt").read_text().split() == ["reload", "0", "async", "invalid_argument"]
     simple = matfile.read_xdata(out + "_simple.mat")
     nesta = matfile.read_xdata(out + "_nesta.mat")
     y2, S2 = matfile.read_kdata(out + "_k.mat")
