@@ -60,7 +60,8 @@ FIXED = dict(lambda_i=0.01, mu_f=1e-3, La=1.0, maxIntIter=1, maxIter=50, stoptes
 
 
 @pytest.mark.parametrize("W,H,F,C,Rr", [(32, 32, 6, 4, 4), (48, 40, 5, 3, 4), (64, 64, 8, 4, 6), (24, 56, 2, 2, 2),
-                                         (40, 24, 3, 1, 2), (128, 96, 10, 8, 8)])
+                                         (40, 24, 3, 1, 2), (128, 96, 10, 8, 8), (256, 40, 4, 3, 4),
+                                         (512, 32, 3, 2, 4)])
 def test_nesta_fixed_iterations(ctx, W, H, F, C, Rr):
     _check(ctx, synth.make_problem(W, H, F, C, Rr, seed=W + H), FIXED)
 
