@@ -241,6 +241,11 @@ def run_ours(args, dist: Dist) -> dict | None:
     t_max = dist.max(t_ms)
 
     # ---- end to end through the C ABI with pinned host buffers ------------
+    # Every step copies its inputs from pinned host memory and reads its image
+    # back.  The copies run on the context's copy stream into the other of two
+    # device buffer sets (gbn_copy_upload, double buffering), so step k+1's
+    # inputs travel while step k is solved; one event pair brackets all K steps.
+    # The 133 MB of inputs per step exceed L2, so no flush runs in this loop.
     import ctypes as C
 
     from opencliper_gb300._abi import call
@@ -250,27 +255,52 @@ def run_ours(args, dist: Dist) -> dict | None:
     hx = torch.empty(x.nbytes // 4, dtype=torch.float32).pin_memory()
     bi = hy.numel() * 4 + hS.numel() * 4 + hm.numel()
     bo = x.nbytes
+    y2, S2, m2 = ctx.empty(y.shape, np.complex64), ctx.empty(S.shape, np.complex64), ctx.empty(m.shape, np.uint8)
+    sets = [(y, S, m), (y2, S2, m2)]
+    for d, h in zip(sets[1], (hy, hS, hm)):  # the second set starts with valid data (mixed: operand sizing)
+        ctx.copy_upload(d, h.data_ptr(), d.nbytes)
+    ctx.sync()
+    prob2 = g.Problem(ctx, y2, S2, m2)
+    if mixed:
+        batch2 = g.Batch(ctx, [prob2], prm, [x], precision=g.PRECISION_MIXED)
+        batch2.capture()
+        solvers = [solve, batch2.launch]
+    else:
+        solvers = [solve, lambda: prob2.run(prm, x, stats=False)]
 
-    def e2e_step():
-        call("gbn_upload", ctx.handle, y.ptr, hy.data_ptr(), y.nbytes)
-        call("gbn_upload", ctx.handle, S.ptr, hS.data_ptr(), S.nbytes)
-        call("gbn_upload", ctx.handle, m.ptr, hm.data_ptr(), m.nbytes)
-        solve()
-        call("gbn_download_async", ctx.handle, C.c_void_p(hx.data_ptr()), x.ptr, x.nbytes)
+    def upload(k):
+        for d, h in zip(sets[k % 2], (hy, hS, hm)):
+            ctx.copy_upload(d, h.data_ptr(), d.nbytes)
 
-    e2e_step()
+    def e2e_run(n):
+        ctx.copy_wait_compute()  # the first copy starts inside the timed region
+        upload(0)
+        for k in range(n):
+            ctx.compute_wait_copy()  # step k's inputs are on the device
+            ctx.copy_wait_compute()  # the next copies wait for the solve that last read their buffers
+            if k + 1 < n:
+                upload(k + 1)
+            solvers[k % 2]()
+            call("gbn_download_async", ctx.handle, C.c_void_p(hx.data_ptr()), x.ptr, x.nbytes)
+
+    e2e_run(2)
+    ctx.sync()
     torch.cuda.synchronize()
-    ev2 = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     dist.barrier()
     torch.cuda.synchronize()
-    for k in range(K):
-        flush.fill_(k & 0xFF)
-        ev2[k][0].record(stream)
-        e2e_step()
-        ev2[k][1].record(stream)
+    e0.record(stream)
+    e2e_run(K)
+    ctx.compute_wait_copy()
+    e1.record(stream)
     torch.cuda.synchronize()
     dist.barrier()
-    t2_max = dist.max(sum(a.elapsed_time(b) for a, b in ev2))
+    t2_max = dist.max(e0.elapsed_time(e1))
+    if mixed:
+        batch2.close()
+    prob2.close()
+    for a_ in (y2, S2, m2):
+        a_.free()
 
     # ---- live per-kernel durations for the roofline ----------------------
     ctx.profile(True)
@@ -318,7 +348,8 @@ def run_ours(args, dist: Dist) -> dict | None:
            "data": DATA_DESC,
            "config": workload_config({"kept_rows": G, "precision": args.precision}),
            "e2e": {"value": round(n * K / (t2_max / 1e3), 3), "unit": UNIT, "h2d_bytes_per_step": int(bi),
-                   "d2h_bytes_per_step": int(bo)},
+                   "d2h_bytes_per_step": int(bo),
+                   "pipeline": "inputs of step k+1 copied on the copy stream while step k is solved"},
            "gpu_launches": int(launches), "roofline": roof, "clocks": clk,
            "wall_s_timed_region": round(wall, 3)}
     if forms:

@@ -120,6 +120,20 @@ GBN_API int gbn_upload(gbn_ctx* ctx, void* d_dst, const void* h_src, size_t byte
 GBN_API int gbn_download(gbn_ctx* ctx, void* h_dst, const void* d_src, size_t bytes);
 /* like gbn_download but returns without waiting (h_dst should be page-locked) */
 GBN_API int gbn_download_async(gbn_ctx* ctx, void* h_dst, const void* d_src, size_t bytes);
+/* Prefetch: host->device copies on the context's second (copy) stream, so
+ * that the next reconstruction's inputs travel while the current one is
+ * solved (the reference's asynchronous KData load, KData.cpp:281-284, feeding
+ * the solver queue).  h_src should be pinned for the copy to overlap.
+ * gbn_copy_wait_compute: copies enqueued after it wait for all work enqueued
+ * on the compute stream so far (e.g. the last solve that read the buffer).
+ * gbn_compute_wait_copy: work enqueued on the compute stream after it waits
+ * for all copies enqueued so far.  Double buffering, per step k:
+ *   gbn_compute_wait_copy; gbn_copy_wait_compute;
+ *   gbn_copy_upload(inputs of k+1 -> buffer set (k+1)%2);
+ *   gbn_nesta_run(problem on buffer set k%2); gbn_download_async(result k). */
+GBN_API int gbn_copy_upload(gbn_ctx* ctx, void* d_dst, const void* h_src, size_t bytes);
+GBN_API int gbn_copy_wait_compute(gbn_ctx* ctx);
+GBN_API int gbn_compute_wait_copy(gbn_ctx* ctx);
 GBN_API int gbn_memset(gbn_ctx* ctx, void* d_dst, int value, size_t bytes);
 /* page-locked host buffers for fast transfers */
 GBN_API int gbn_host_alloc(size_t bytes, void** h_ptr);

@@ -97,6 +97,9 @@ SIGNATURES: dict[str, list] = {
     "gbn_problem_destroy": [_vp],
     "gbn_problem_set_motion": [_vp, _vp, _vp, _vp],
     "gbn_problem_fit_rows": [_vp, _i, _vp],
+    "gbn_copy_upload": [_vp, _vp, _vp, _sz],
+    "gbn_copy_wait_compute": [_vp],
+    "gbn_compute_wait_copy": [_vp],
     "gbn_op_motion": [_vp, _i, _vp, _vp, _vp, _vp, _vp, _i, _i, _i],
     "gbn_nesta_run": [_vp, _vp, C.POINTER(NestaParams), _vp, C.POINTER(NestaStats)],
     "gbn_nesta_run_host": [_vp, _i, _i, _i, _i, _vp, _vp, _vp, C.POINTER(NestaParams), _vp,

@@ -110,6 +110,16 @@ class Context:
     def sync(self) -> None:
         call("gbn_ctx_sync", self.handle)
 
+    # prefetch on the context's copy stream (gbn_copy_upload and the two ordering calls)
+    def copy_upload(self, dst: "DeviceArray", host_ptr: int, nbytes: int) -> None:
+        call("gbn_copy_upload", self.handle, dst.ptr, C.c_void_p(int(host_ptr)), int(nbytes))
+
+    def copy_wait_compute(self) -> None:
+        call("gbn_copy_wait_compute", self.handle)
+
+    def compute_wait_copy(self) -> None:
+        call("gbn_compute_wait_copy", self.handle)
+
     @property
     def stream(self) -> int:
         s = C.c_void_p()

@@ -243,6 +243,12 @@ int gbn_ctx_destroy(gbn_ctx* ctx) {
   if (ctx->scratch) cudaFree(ctx->scratch);
   if (ctx->tw_block) cudaFree(ctx->tw_block);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->copy_stream) {
+    cudaStreamSynchronize(ctx->copy_stream);
+    cudaStreamDestroy(ctx->copy_stream);
+  }
+  if (ctx->ev_compute) cudaEventDestroy(ctx->ev_compute);
+  if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
   delete ctx;
   return GBN_OK;
 }
@@ -273,7 +279,9 @@ int gbn_ctx_set_stream(gbn_ctx* ctx, void* stream) {
 
 int gbn_ctx_sync(gbn_ctx* ctx) {
   CHECK_CTX(ctx);
-  return cuda_status(cudaStreamSynchronize(ctx->stream), "stream synchronize");
+  cudaError_t e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess && ctx->copy_stream) e = cudaStreamSynchronize(ctx->copy_stream);
+  return cuda_status(e, "stream synchronize");
 }
 
 int gbn_ctx_seed48(gbn_ctx* ctx, const unsigned short seed16v[3]) {
@@ -379,6 +387,43 @@ int gbn_download_async(gbn_ctx* ctx, void* h_dst, const void* d_src, size_t byte
   CHECK_CTX(ctx);
   if ((!h_dst || !d_src) && bytes) return set_error(GBN_ERR_INVALID, "null buffer");
   return cuda_status(cudaMemcpyAsync(h_dst, d_src, bytes, cudaMemcpyDeviceToHost, ctx->stream), "download");
+}
+
+namespace {
+int copy_stream_ready(gbn_ctx* ctx) {
+  if (ctx->copy_stream) return GBN_OK;
+  DeviceGuard guard(ctx->device);
+  cudaError_t e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_compute, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_copy, cudaEventDisableTiming);
+  return cuda_status(e, "copy stream");
+}
+}  // namespace
+
+int gbn_copy_upload(gbn_ctx* ctx, void* d_dst, const void* h_src, size_t bytes) {
+  CHECK_CTX(ctx);
+  if ((!d_dst || !h_src) && bytes) return set_error(GBN_ERR_INVALID, "null buffer");
+  const int rc = copy_stream_ready(ctx);
+  if (rc != GBN_OK) return rc;
+  return cuda_status(cudaMemcpyAsync(d_dst, h_src, bytes, cudaMemcpyHostToDevice, ctx->copy_stream), "prefetch");
+}
+
+int gbn_copy_wait_compute(gbn_ctx* ctx) {
+  CHECK_CTX(ctx);
+  const int rc = copy_stream_ready(ctx);
+  if (rc != GBN_OK) return rc;
+  cudaError_t e = cudaEventRecord(ctx->ev_compute, ctx->stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_compute, 0);
+  return cuda_status(e, "copy stream wait");
+}
+
+int gbn_compute_wait_copy(gbn_ctx* ctx) {
+  CHECK_CTX(ctx);
+  const int rc = copy_stream_ready(ctx);
+  if (rc != GBN_OK) return rc;
+  cudaError_t e = cudaEventRecord(ctx->ev_copy, ctx->copy_stream);
+  if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->stream, ctx->ev_copy, 0);
+  return cuda_status(e, "compute stream wait");
 }
 
 int gbn_memset(gbn_ctx* ctx, void* d_dst, int value, size_t bytes) {

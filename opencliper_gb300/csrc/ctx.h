@@ -16,6 +16,8 @@
 struct gbn_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // host->device prefetches (created on first use)
+  cudaEvent_t ev_compute = nullptr, ev_copy = nullptr;  // ordering points between the two streams
   bool own_stream = true;
   int nsm = 0;
   std::map<int, float2*> tw;          // device twiddle tables, one per supported length

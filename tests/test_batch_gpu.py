@@ -16,6 +16,7 @@ import opencliper_gb300 as g
 from opencliper_gb300 import synth
 from oracle import drand48
 from oracle import nesta_ref as R
+from tests.conftest import rel_l2
 
 pytestmark = pytest.mark.gpu
 
@@ -153,3 +154,37 @@ def test_batch_rejects_bad_input(ctx):
         g.Batch(ctx, probs, prms, outs[:1])
     for prob in probs:
         prob.close()
+
+
+def test_maximum_sizes(ctx):
+    """The largest supported shape (W = H = 512, 64 frames, the power method's
+    frame limit): finite, no status, batched graph replay equal to the single
+    run bit for bit, the mixed form within FP32-class distance of it, and the
+    kept rows those of the masks."""
+    W = H = 512
+    F, Cc, Rr = 64, 4, 8
+    p = synth.make_problem_device(ctx, W, H, F, Cc, Rr, seed=77)
+    prm = g.nesta_params(lambda_i=0.01, mu_f=1e-3, La=1.0, maxIntIter=1, maxIter=10, stoptest=0, miniter=7,
+                         tolVar=3e-4)
+    prob = g.Problem(ctx, p.y, p.S, p.mask)
+    x1, x2 = ctx.empty((F, H, W), np.complex64), ctx.empty((F, H, W), np.complex64)
+    ctx.seed48(drand48.state_to_seed16v(drand48.DEFAULT_STATE))
+    st = prob.run(prm, x1)
+    assert st["status"] == 0 and st["kept_rows"] == int(p.rowmask.astype(bool).sum())
+    a = x1.get()
+    assert np.isfinite(a).all() and np.abs(a).max() > 0
+    for prec, exact in ((g.PRECISION_FP32, True), (g.PRECISION_MIXED, False)):
+        ctx.seed48(drand48.state_to_seed16v(drand48.DEFAULT_STATE))
+        b = g.Batch(ctx, [prob], prm, [x2], precision=prec)
+        b.capture()
+        b.launch()
+        assert b.stats(0)["status"] == 0
+        c = x2.get()
+        if exact:
+            assert np.array_equal(a, c)
+        else:
+            assert rel_l2(c, a) < 1e-3
+        b.close()
+    prob.close()
+    for d in (p.y, p.S, p.mask, x1, x2):
+        d.free()

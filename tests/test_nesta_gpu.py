@@ -183,3 +183,41 @@ def test_fit_rows_shrinks_row_buffer(ctx):
             assert prob.run(prm, x)["status"] == 0
         prob.close()
     assert np.array_equal(outs[0], outs[1])
+
+
+def test_prefetch_double_buffered_pipeline(ctx):
+    """gbn_copy_upload on the copy stream with the two ordering calls: three
+    reconstructions through two device buffer sets, each step's inputs copied
+    from pinned host memory while the previous one is solved, give the same
+    images as uploading and solving one after another."""
+    torch = pytest.importorskip("torch")
+    W, H, F, C, Rr = 64, 48, 6, 3, 4
+    probs = [synth.make_problem(W, H, F, C, Rr, seed=300 + i) for i in range(3)]
+    prm = g.nesta_params(**FIXED)
+    pin = [[torch.from_numpy(np.ascontiguousarray(a).view(np.uint8).reshape(-1)).pin_memory()
+            for a in (p.y, p.S, p.mask)] for p in probs]
+    sets = [[ctx.empty(p.y.shape, np.complex64), ctx.empty(p.S.shape, np.complex64), ctx.empty(p.mask.shape, np.uint8)]
+            for p in probs[:2]]
+    gp = [g.Problem(ctx, *s) for s in sets]
+    outs = [ctx.empty((F, H, W), np.complex64) for _ in range(3)]
+    ctx.seed48(drand48.state_to_seed16v(drand48.DEFAULT_STATE))
+
+    def upload(k):
+        for d, h in zip(sets[k % 2], pin[k]):
+            ctx.copy_upload(d, h.data_ptr(), h.numel())
+
+    upload(0)
+    for k in range(3):
+        ctx.compute_wait_copy()   # step k's inputs are on the device
+        ctx.copy_wait_compute()   # the next copies wait for the solve that last read their buffers
+        if k + 1 < 3:
+            upload(k + 1)
+        gp[k % 2].run(prm, outs[k], stats=False)
+    ctx.sync()
+    got = [o.get() for o in outs]
+    ctx.seed48(drand48.state_to_seed16v(drand48.DEFAULT_STATE))
+    for k, p in enumerate(probs):
+        ref, _ = g.nesta_run_host(ctx, p.y, p.S, p.mask, prm)
+        assert np.array_equal(got[k], ref), k
+    for pr in gp:
+        pr.close()
