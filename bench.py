@@ -400,8 +400,10 @@ def mixed_forms(ctx, stream, args=None, reps: int = 5) -> dict:
             b.launch()
             imgs[name] = x.get()
             status = b.stats(0)["status"]
+            tc_groups = b.groups()[1]
             rate, ms = _graph_rate(ctx, stream, b, 1, reps)
-            res[name] = {"value": round(rate, 3), "ms_per_recon": round(ms, 3), "status": int(status)}
+            res[name] = {"value": round(rate, 3), "ms_per_recon": round(ms, 3), "status": int(status),
+                         "tensor_core_forward": bool(tc_groups)}
             b.close()
         res["speedup_mixed_over_fp32"] = round(res["mixed"]["value"] / res["fp32"]["value"], 3)
         res["nrmse_mixed_vs_fp32"] = float(f"{_nrmse(imgs['mixed'], imgs['fp32']):.3e}")
@@ -510,6 +512,16 @@ def batched_form(ctx, stream, args=None, reps: int = 2) -> dict:
     res = {"workload": f"{B['n']} uneven reconstructions, W=H in {list(B['sizes'])}, F U{{12..40}}, "
                        f"C U{{8..32}}, R U{{4..12}}, seeds {B['seed0']}+i, one CUDA graph",
            "unit": UNIT, "pixel_coil_frames": int(n_units), "sizes_seen": sorted(set(s[0] for s in shapes))}
+    # autotune one representative shape per matrix size (median frames and coils of
+    # its members): launch shapes and the mixed form's forward choice per group
+    reps_shape = []
+    for Wd in sorted(set(s[0] for s in shapes)):
+        mem = [s for s in shapes if s[0] == Wd]
+        reps_shape.append((Wd, Wd, int(np.median([m[1] for m in mem])), int(np.median([m[2] for m in mem]))))
+    t0 = time.perf_counter()
+    ctx.autotune(reps_shape)
+    res["autotune"] = {"shapes": [list(r) for r in reps_shape], "seconds": round(time.perf_counter() - t0, 1),
+                       "k1_k2": [list(ctx.tuning_for(*r)) for r in reps_shape]}
     for name, prec in (("fp32", g.PRECISION_FP32), ("mixed", g.PRECISION_MIXED)):
         try:
             b = g.Batch(ctx, probs, g.nesta_params(**NESTA), outs, precision=prec)
@@ -517,8 +529,10 @@ def batched_form(ctx, stream, args=None, reps: int = 2) -> dict:
             res[name] = {"unavailable": str(e)}
             continue
         n0 = ctx.launch_count()
+        ng, ntc = b.groups()
         rate, ms = _graph_rate(ctx, stream, b, B["n"], reps)
         res[name] = {"value": round(rate, 3), "ms_per_batch": round(ms, 2), "reps": reps,
+                     "groups": ng, "tensor_core_forward_groups": ntc,
                      "kept_rows_total": int(sum(b.stats(i)["kept_rows"] for i in range(B["n"]))),
                      "status_nonzero": int(sum(b.stats(i)["status"] != 0 for i in range(B["n"]))),
                      "host_launch_calls_per_replay": int((ctx.launch_count() - n0) // (reps + 1))}
@@ -654,7 +668,8 @@ def stress_form(ctx, stream, args=None) -> dict:
     return res
 
 
-FORMS = (("mixed", mixed_forms), ("batched", batched_form), ("motion", motion_form), ("stress", stress_form))
+# the batched form autotunes its shapes into the context: forms that should see the defaults run first
+FORMS = (("mixed", mixed_forms), ("motion", motion_form), ("batched", batched_form), ("stress", stress_form))
 
 
 def run_reference(args, dist: Dist) -> dict | None:

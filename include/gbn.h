@@ -88,9 +88,13 @@ GBN_API int gbn_ctx_sync(gbn_ctx* ctx);
  * (glibc's default state, as if seed48 were never called). */
 GBN_API int gbn_ctx_seed48(gbn_ctx* ctx, const unsigned short seed16v[3]);
 GBN_API int gbn_ctx_get_rand48(gbn_ctx* ctx, unsigned short state16v[3]);
-/* tuning knobs: "k1_coils_per_block", "k2_ctas_per_sm" (>= 1) and
+/* tuning knobs: "k1_coils_per_block", "k2_ctas_per_sm" (>= 1),
  * "mixed_adjoint_tc" (0/1: the mixed form also runs the adjoint column pass on
- * the tensor cores; read when a batch is created) */
+ * the tensor cores) and "mixed_fwd_tc" (1: the mixed form's forward column
+ * pass always on the tensor cores, 0: never -- its groups then run the plain
+ * FP32 kernels --, -1 (default): per (W, H) group, as gbn_autotune measured
+ * for the nearest tuned shape, else on the tensor cores when H >= 320); the
+ * mixed knobs are read when a batch is created */
 GBN_API int gbn_ctx_set_tuning(gbn_ctx* ctx, const char* key, int value);
 /* number of kernels this context has launched so far */
 GBN_API int gbn_ctx_launch_count(gbn_ctx* ctx, unsigned long long* count);
@@ -299,6 +303,9 @@ GBN_API int gbn_batch_launch(gbn_batch* b);
 GBN_API int gbn_batch_capture(gbn_batch* b);
 /* Waits for the context stream, then fills *stats for problem i of the batch. */
 GBN_API int gbn_batch_stats(gbn_batch* b, int i, gbn_nesta_stats* stats);
+/* The batch's (W, H) groups of at most 64 members, and how many of them run
+ * the forward column pass on the tensor cores (mixed form, "mixed_fwd_tc"). */
+GBN_API int gbn_batch_groups(gbn_batch* b, int* groups, int* tensor_core_groups);
 GBN_API int gbn_batch_destroy(gbn_batch* b);
 /* create + launch (+ stats for every problem when stats != NULL, which waits)
  * + destroy */

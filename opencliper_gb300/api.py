@@ -349,6 +349,12 @@ class Batch:
     def launch(self) -> None:
         call("gbn_batch_launch", self.handle)
 
+    def groups(self) -> tuple[int, int]:
+        """(groups, groups whose forward pass runs on the tensor cores)."""
+        ng, ntc = C.c_int(0), C.c_int(0)
+        call("gbn_batch_groups", self.handle, C.byref(ng), C.byref(ntc))
+        return ng.value, ntc.value
+
     def stats(self, i: int) -> dict:
         st = NestaStats()
         call("gbn_batch_stats", self.handle, int(i), C.byref(st))

@@ -8,10 +8,13 @@
 // gbn_autotune measures every candidate pair on a synthetic problem of each
 // requested shape (zero data with a 1/8 row mask: the kernels' cost does not
 // depend on the values) and keeps the fastest in the context; single runs and
-// batch groups look their shape up (tuning_for).  A text cache file keeps the
-// results across processes:
-//   # gbn autotune v1: W H F C k1_coils_per_block k2_ctas_per_sm us_per_iteration
-//   256 256 20 12 4 3 121.5
+// batch groups look their shape up (tuning_for).  It also times the mixed
+// form's tensor-core forward pass against the plain FP32 kernels on the same
+// shape (captured batches of one) and records which is faster
+// (mixed_fwd_tc_for).  A text cache file keeps the results across processes:
+//   # gbn autotune v2: W H F C k1_coils_per_block k2_ctas_per_sm us_per_iteration mixed_fwd_tc
+//   256 256 20 12 4 3 121.5 0
+// (v1 lines without the last column are read with mixed_fwd_tc unknown)
 #include <algorithm>
 #include <cmath>
 #include <cstdio>
@@ -28,27 +31,46 @@ int problem_alloc(gbn_problem*);
 void problem_free(gbn_problem*);
 int validate_problem_dims(int, int, int, int);
 int nesta_run(gbn_ctx*, gbn_problem*, const gbn_nesta_params*, float2*, gbn_nesta_stats*);
+int batch_create(gbn_ctx*, int, gbn_problem* const*, const gbn_nesta_params*, float* const*, int, gbn_batch**);
+int batch_capture(gbn_batch*);
+int batch_launch(gbn_batch*);
+int batch_destroy(gbn_batch*);
 
-void tuning_for(gbn_ctx* ctx, int W, int H, int F, int C, int* cpb, int* k2) {
-  *cpb = ctx->k1_coils_per_block;
-  *k2 = ctx->k2_ctas_per_sm;
-  if (!ctx->use_tuned) return;
+// nearest tuned entry with the same transform lengths (coils first, then frames)
+const gbn_ctx::Tuned* nearest_tuned(gbn_ctx* ctx, int W, int H, int F, int C) {
   const auto it = ctx->tuned.find(std::make_tuple(W, H, F, C));
-  if (it != ctx->tuned.end()) {
-    *cpb = it->second.cpb;
-    *k2 = it->second.k2;
-    return;
-  }
-  // nearest tuned shape with the same transform lengths (coils first, then frames)
+  if (it != ctx->tuned.end()) return &it->second;
+  const gbn_ctx::Tuned* hit = nullptr;
   long best = -1;
   for (const auto& e : ctx->tuned) {
     if (std::get<0>(e.first) != W || std::get<1>(e.first) != H) continue;
     const long d = 1000L * std::abs(std::get<3>(e.first) - C) + std::abs(std::get<2>(e.first) - F);
     if (best < 0 || d < best) {
       best = d;
-      *cpb = e.second.cpb;
-      *k2 = e.second.k2;
+      hit = &e.second;
     }
+  }
+  return hit;
+}
+
+bool mixed_fwd_tc_for(gbn_ctx* ctx, int W, int H, int F, int C) {
+  if (ctx->mixed_fwd_tc >= 0) return ctx->mixed_fwd_tc != 0;
+  if (ctx->use_tuned) {
+    const gbn_ctx::Tuned* t = nearest_tuned(ctx, W, H, F, C);
+    if (t && t->tc >= 0) return t->tc != 0;
+  }
+  (void)W;
+  return H >= 320;  // measured: FP32 faster at 256, tensor cores at 384
+}
+
+void tuning_for(gbn_ctx* ctx, int W, int H, int F, int C, int* cpb, int* k2) {
+  *cpb = ctx->k1_coils_per_block;
+  *k2 = ctx->k2_ctas_per_sm;
+  if (!ctx->use_tuned) return;
+  const gbn_ctx::Tuned* t = nearest_tuned(ctx, W, H, F, C);
+  if (t) {
+    *cpb = t->cpb;
+    *k2 = t->k2;
   }
 }
 
@@ -72,10 +94,11 @@ int load_cache(gbn_ctx* ctx, const char* path, bool must_exist) {
   char line[256];
   while (std::fgets(line, sizeof(line), fp)) {
     if (line[0] == '#' || line[0] == '\n') continue;
-    int W, H, F, C, cpb, k2;
+    int W, H, F, C, cpb, k2, tc = -1;
     float us;
-    if (std::sscanf(line, "%d %d %d %d %d %d %f", &W, &H, &F, &C, &cpb, &k2, &us) == 7 && cpb >= 1 && k2 >= 1)
-      ctx->tuned[std::make_tuple(W, H, F, C)] = gbn_ctx::Tuned{cpb, k2, us};
+    const int got = std::sscanf(line, "%d %d %d %d %d %d %f %d", &W, &H, &F, &C, &cpb, &k2, &us, &tc);
+    if (got >= 7 && cpb >= 1 && k2 >= 1)
+      ctx->tuned[std::make_tuple(W, H, F, C)] = gbn_ctx::Tuned{cpb, k2, us, (got == 8 && tc >= -1 && tc <= 1) ? tc : -1};
   }
   std::fclose(fp);
   return GBN_OK;
@@ -87,8 +110,9 @@ int append_cache(const char* path, int W, int H, int F, int C, const gbn_ctx::Tu
   if (probe) std::fclose(probe);
   FILE* fp = std::fopen(path, "a");
   if (!fp) return set_error(GBN_ERR_INVALID, std::string("cannot write tuning cache ") + path);
-  if (fresh) std::fprintf(fp, "# gbn autotune v1: W H F C k1_coils_per_block k2_ctas_per_sm us_per_iteration\n");
-  std::fprintf(fp, "%d %d %d %d %d %d %.2f\n", W, H, F, C, v.cpb, v.k2, v.us);
+  if (fresh)
+    std::fprintf(fp, "# gbn autotune v2: W H F C k1_coils_per_block k2_ctas_per_sm us_per_iteration mixed_fwd_tc\n");
+  std::fprintf(fp, "%d %d %d %d %d %d %.2f %d\n", W, H, F, C, v.cpb, v.k2, v.us, v.tc);
   std::fclose(fp);
   return GBN_OK;
 }
@@ -162,6 +186,40 @@ int tune_shape(gbn_ctx* ctx, int W, int H, int F, int C, gbn_ctx::Tuned* out) {
       const float us = ms_best * 1e3f / float(prm.maxIter);
       if (rc == GBN_OK && (best.us < 0 || us < best.us)) best = gbn_ctx::Tuned{cpb, k2, us};
     }
+  }
+  // the mixed form's tensor-core forward pass against the plain FP32 kernels:
+  // captured batches of one with the launch shape just found, best of 3 replays
+  if (rc == GBN_OK && best.us > 0.f) {
+    ctx->k1_coils_per_block = best.cpb;
+    ctx->k2_ctas_per_sm = best.k2;
+    const int saved_tc = ctx->mixed_fwd_tc;
+    float ms_mode[2] = {-1.f, -1.f};
+    for (int mode = 0; mode < 2 && rc == GBN_OK; ++mode) {
+      ctx->mixed_fwd_tc = mode;  // 0: FP32 kernels, 1: tensor-core forward
+      gbn_batch* b = nullptr;
+      float* xo = reinterpret_cast<float*>(x);
+      int brc = batch_create(ctx, 1, &P, &prm, &xo, GBN_PRECISION_MIXED, &b);
+      if (brc == GBN_OK) brc = batch_capture(b);
+      for (int rep = 0; rep < 4 && brc == GBN_OK; ++rep) {
+        cudaEventRecord(e0, s);
+        brc = batch_launch(b);
+        cudaEventRecord(e1, s);
+        if (brc != GBN_OK) break;
+        if ((e = cudaEventSynchronize(e1)) != cudaSuccess) {
+          brc = cuda_status(e, "autotune batch");
+          break;
+        }
+        float ms = 0.f;
+        cudaEventElapsedTime(&ms, e0, e1);
+        if (rep > 0 && (ms_mode[mode] < 0 || ms < ms_mode[mode])) ms_mode[mode] = ms;
+      }
+      if (b) batch_destroy(b);
+      // a shape the mixed form cannot take (too many kept rows per frame) stays on FP32
+      if (brc != GBN_OK && mode == 1) ms_mode[1] = -1.f;
+      else if (brc != GBN_OK) rc = brc;
+    }
+    ctx->mixed_fwd_tc = saved_tc;
+    if (rc == GBN_OK && ms_mode[0] > 0.f) best.tc = (ms_mode[1] > 0.f && ms_mode[1] < ms_mode[0]) ? 1 : 0;
   }
   ctx->k1_coils_per_block = saved_cpb;
   ctx->k2_ctas_per_sm = saved_k2;

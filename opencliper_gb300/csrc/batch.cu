@@ -44,6 +44,7 @@ struct gbn_batch {
     int nmax_ac = 0;               // mixed form: widest adjoint B operand of the group
     dim3 g3tc;                     // mixed form: grid of the adjoint tensor-core kernel
     bool adjoint_tc = false;       // mixed form: adjoint column pass on the tensor cores
+    bool tc = false;               // mixed form with the forward pass on the tensor cores (else plain FP32)
     dim3 g1, g3;
     unsigned maxIntIter = 0, maxIter = 0;
     cudaStream_t stream = nullptr;
@@ -56,6 +57,8 @@ struct gbn_batch {
 };
 
 namespace gbn {
+
+bool mixed_fwd_tc_for(gbn_ctx* ctx, int W, int H, int F, int C);  // autotune.cu
 
 // mixed-precision form (mixed.cu)
 int mixed_prepare(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params& prm, const float2* out);
@@ -94,7 +97,7 @@ int batch_enqueue(gbn_batch* b, bool graph_mode) {
     cudaStream_t s = g.stream;
     const SizeKernels* kh = find_size(g.H);
     const SizeKernels* kw = find_size(g.W);
-    const bool mixed = b->precision == GBN_PRECISION_MIXED;
+    const bool mixed = g.tc;
     for (int i : g.idx) {
       n_launch += launch_pre(b->probs[i], b->prm[i], s);
       if (mixed) n_launch += launch_mixed_setup(ctx, b->probs[i], s);
@@ -170,9 +173,6 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
       break;
     }
     if ((rc = run_prepare(ctx, P, &params[i])) != GBN_OK) break;
-    if (precision == GBN_PRECISION_MIXED &&
-        (rc = mixed_prepare(ctx, P, params[i], reinterpret_cast<const float2*>(outputs[i]))) != GBN_OK)
-      break;
     b->probs.push_back(P);
     b->prm.push_back(params[i]);
     b->out.push_back(reinterpret_cast<float2*>(outputs[i]));
@@ -218,6 +218,19 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
     memset(&g.bm, 0, sizeof(g.bm));
     g.bm.n = ng;
     g.bm.ctl = g.ctl;
+    if (precision == GBN_PRECISION_MIXED) {
+      int gF = 2, gC = 1;
+      for (int i : g.idx) {
+        gF = std::max(gF, b->probs[i]->F);
+        gC = std::max(gC, b->probs[i]->C);
+      }
+      g.tc = mixed_fwd_tc_for(ctx, g.W, g.H, gF, gC);
+      for (int i : g.idx) {
+        if (!g.tc || rc != GBN_OK) break;
+        rc = mixed_prepare(ctx, b->probs[i], b->prm[i], b->out[i]);
+      }
+      if (rc != GBN_OK) break;
+    }
     int frames = 0, maxC = 1, maxF = 2;
     long long steps = 0;
     for (int k = 0; k < ng; ++k) {
@@ -231,7 +244,7 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
       g.maxIntIter = std::max(g.maxIntIter, b->prm[i].maxIntIter);
       g.maxIter = std::max(g.maxIter, b->prm[i].maxIter);
       FusedArgs fa = make_args(P, b->out[i]);
-      if (precision == GBN_PRECISION_MIXED) {
+      if (g.tc) {
         mixed_args(P, &fa);
         g.npad_max = std::max(g.npad_max, P->npad);
         g.nmax_ac = std::max(g.nmax_ac, inv_cols_tc_rows(P->C));
@@ -242,13 +255,12 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
     int cpb, k2;
     tuning_for(ctx, g.W, g.H, maxF, maxC, &cpb, &k2);
     g.cpb = std::max(1, std::min(cpb, maxC));
-    g.g1 = (precision == GBN_PRECISION_MIXED) ? fwd_cols_tc_grid(g.W, maxC, frames)
-                                              : dim3(g.W / kWB, (maxC + g.cpb - 1) / g.cpb, frames);
+    g.g1 = g.tc ? fwd_cols_tc_grid(g.W, maxC, frames) : dim3(g.W / kWB, (maxC + g.cpb - 1) / g.cpb, frames);
     g.g2 = row_grid(ctx, kw, true, steps, k2);
     g.g2a = row_grid(ctx, kw, false, steps, k2);
     g.g3 = dim3(g.W / kWB, 2, frames);
     g.g3tc = inv_cols_tc_grid(g.W, g.H, frames);
-    g.adjoint_tc = precision == GBN_PRECISION_MIXED && ctx->mixed_adjoint_tc != 0;
+    g.adjoint_tc = g.tc && ctx->mixed_adjoint_tc != 0;
   }
   if (rc == GBN_OK && (e = cudaGetLastError()) != cudaSuccess) rc = cuda_status(e, "batch tables");
   if (rc != GBN_OK) {
@@ -312,6 +324,15 @@ int batch_stats(gbn_batch* b, int i, gbn_nesta_stats* stats) {
 }
 
 gbn_ctx* batch_ctx(gbn_batch* b) { return b->ctx; }
+
+int batch_groups(gbn_batch* b, int* groups, int* tensor_core_groups) {
+  if (!b) return set_error(GBN_ERR_INVALID, "null batch");
+  int tc = 0;
+  for (const auto& g : b->groups) tc += g.tc ? 1 : 0;
+  if (groups) *groups = int(b->groups.size());
+  if (tensor_core_groups) *tensor_core_groups = tc;
+  return GBN_OK;
+}
 
 int batch_destroy(gbn_batch* b) {
   if (!b) return GBN_OK;

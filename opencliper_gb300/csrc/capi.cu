@@ -32,6 +32,7 @@ int batch_capture(gbn_batch*);
 int batch_stats(gbn_batch*, int, gbn_nesta_stats*);
 int batch_destroy(gbn_batch*);
 gbn_ctx* batch_ctx(gbn_batch*);
+int batch_groups(gbn_batch*, int*, int*);
 int motion_set(gbn_problem*, const float*, const int*, const int*);
 int problem_fit_rows(gbn_problem*, int, int*);
 int motion_op(gbn_ctx*, int, const float2*, float2*, const float*, const int*, const int*, int, int, int);
@@ -306,6 +307,11 @@ int gbn_ctx_set_tuning(gbn_ctx* ctx, const char* key, int value) {
   if (!std::strcmp(key, "mixed_adjoint_tc")) {
     if (value != 0 && value != 1) return set_error(GBN_ERR_INVALID, "mixed_adjoint_tc is 0 or 1");
     ctx->mixed_adjoint_tc = value;
+    return GBN_OK;
+  }
+  if (!std::strcmp(key, "mixed_fwd_tc")) {
+    if (value < -1 || value > 1) return set_error(GBN_ERR_INVALID, "mixed_fwd_tc is -1, 0 or 1");
+    ctx->mixed_fwd_tc = value;
     return GBN_OK;
   }
   if (value < 1) return set_error(GBN_ERR_INVALID, "tuning values must be >= 1");
@@ -696,6 +702,11 @@ int gbn_batch_launch(gbn_batch* b) {
 int gbn_batch_capture(gbn_batch* b) {
   CHECK_BATCH(b);
   return batch_capture(b);
+}
+
+int gbn_batch_groups(gbn_batch* b, int* groups, int* tensor_core_groups) {
+  CHECK_BATCH(b);
+  return batch_groups(b, groups, tensor_core_groups);
 }
 
 int gbn_batch_stats(gbn_batch* b, int i, gbn_nesta_stats* stats) {

@@ -28,10 +28,13 @@ struct gbn_ctx {
   int k1_coils_per_block = 4;         // tuning: coils per CTA in the forward column pass
   int k2_ctas_per_sm = 4;             // tuning: persistent CTAs per SM in the row pass
   int mixed_adjoint_tc = 0;           // tuning: mixed form runs the adjoint column pass on the tensor cores
+  int mixed_fwd_tc = -1;              // tuning: mixed form's forward pass on the tensor cores: 1 always, 0 never,
+                                      // -1 per shape (autotuned where measured, else H >= 320)
   // autotuned launch shapes per problem shape (W, H, F, C) (autotune.cu)
   struct Tuned {
     int cpb, k2;
-    float us;  // measured time per inner iteration
+    float us;     // measured time per inner iteration
+    int tc = -1;  // mixed form: tensor-core forward faster (1) or not (0); -1 not measured
   };
   std::map<std::tuple<int, int, int, int>, Tuned> tuned;
   bool use_tuned = true;

@@ -26,6 +26,7 @@ def test_autotune_cache_roundtrip_and_results(tmp_path):
             assert 1 <= k2 <= 8
         lines = [ln for ln in cache.read_text().splitlines() if not ln.startswith("#")]
         assert len(lines) == len(shapes)
+        assert all(ln.split()[-1] in ("0", "1") and len(ln.split()) == 8 for ln in lines)  # mixed forward measured
         # same image with tuned shapes and with every other candidate pair
         p = synth.make_problem(32, 32, 6, 5, 4, seed=3)
         dy, dS, dm = ctx.to_device(p.y), ctx.to_device(p.S), ctx.to_device(p.mask)
@@ -61,3 +62,13 @@ def test_autotune_rejects_bad_shapes():
             ctx.autotune([(30, 32, 4, 2)])  # width not a multiple of 8
         with pytest.raises(g.GbnError):
             ctx.autotune_load("/nonexistent/tune.txt")
+
+
+def test_autotune_reads_v1_cache(tmp_path):
+    """A cache line without the mixed-forward column (format v1) still loads."""
+    cache = tmp_path / "v1.txt"
+    cache.write_text("# gbn autotune v1: W H F C k1_coils_per_block k2_ctas_per_sm us_per_iteration\n"
+                     "64 64 8 4 2 3 55.0\n")
+    with g.Context(0) as ctx:
+        ctx.autotune_load(str(cache))
+        assert ctx.tuning_for(64, 64, 8, 4) == (2, 3)

@@ -21,6 +21,15 @@ pytestmark = pytest.mark.gpu
 FIXED = dict(lambda_i=0.01, mu_f=1e-3, La=1.0, maxIntIter=1, maxIter=30, stoptest=0, miniter=7, tolVar=3e-4)
 DRIVER = dict(lambda_i=1e-2, mu_f=3e-4, La=1.0, maxIntIter=3, maxIter=40, stoptest=1, miniter=5, tolVar=3e-4)
 
+@pytest.fixture(autouse=True)
+def _tensor_core_forward(ctx):
+    """These shapes are small enough that the automatic choice would run their
+    groups on the FP32 kernels: force the tensor-core forward pass."""
+    ctx.set_tuning("mixed_fwd_tc", 1)
+    yield
+    ctx.set_tuning("mixed_fwd_tc", -1)
+
+
 CASES = [(32, 32, 6, 4, 4, FIXED), (48, 40, 5, 3, 4, FIXED), (64, 64, 8, 5, 2, FIXED), (40, 24, 3, 7, 2, FIXED),
          (96, 64, 6, 6, 4, DRIVER)]
 
@@ -91,3 +100,26 @@ def test_mixed_rejects_too_many_kept_rows(ctx):
     with pytest.raises(g.GbnError):
         g.Batch(ctx, [prob], g.nesta_params(**FIXED), [x], precision=g.PRECISION_MIXED)
     prob.close()
+
+
+def test_mixed_forward_choice_per_group(ctx):
+    """mixed_fwd_tc = 0 runs a mixed batch's groups on the plain FP32 kernels
+    (the same image as an FP32 batch, bit for bit); the automatic choice does
+    the same below H = 320 when nothing was tuned."""
+    p = synth.make_problem(48, 40, 5, 3, 4, seed=91)
+    dy, dS, dm = ctx.to_device(p.y), ctx.to_device(p.S), ctx.to_device(p.mask)
+    prob = g.Problem(ctx, dy, dS, dm)
+    x = ctx.empty((5, 40, 48), np.complex64)
+    prm = g.nesta_params(**FIXED)
+    imgs = []
+    for prec, tc in ((g.PRECISION_FP32, 1), (g.PRECISION_MIXED, 0), (g.PRECISION_MIXED, -1), (g.PRECISION_MIXED, 1)):
+        ctx.set_tuning("mixed_fwd_tc", tc)
+        ctx.seed48(drand48.state_to_seed16v(drand48.DEFAULT_STATE))
+        b = g.Batch(ctx, [prob], prm, [x], precision=prec)
+        b.launch()
+        imgs.append(x.get())
+        b.close()
+    prob.close()
+    assert np.array_equal(imgs[0], imgs[1]) and np.array_equal(imgs[0], imgs[2])
+    assert not np.array_equal(imgs[0], imgs[3])  # the tensor-core forward rounds differently
+    assert R.nrmse(imgs[3], imgs[0]) < 1e-3
