@@ -815,6 +815,9 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT)
       }
     }
   } else {
+    // the epilogue is instantiated twice (MC: the tTV gradient comes from
+    // M^T of the motion-compensated form), so the uniform branch stays out of
+    // the per-element loop
     const float2* __restrict__ xk = (it & 1) ? a.xk1 : a.xk0;
     float2* __restrict__ xn = (it & 1) ? a.xk0 : a.xk1;
     const size_t offm = size_t((f + F - 1) % F) * N, off0 = size_t(f) * N, offp = size_t((f + 1) % F) * N;
@@ -822,6 +825,8 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT)
     const float omt = 1.0f - tauk;
     float cmx = 0.f;  // max |x_{k+1}|^2 of this thread's column (mixed form)
     constexpr int BATCH = 4;  // outputs whose global loads are issued together
+    auto epilogue = [&](auto mc_tag) {
+      constexpr bool MC = decltype(mc_tag)::value;
 #pragma unroll
     for (int ii = 0; ii < NI2; ++ii) {
       const int i = t + ii * kColNT;
@@ -836,7 +841,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT)
             if (k2 < A && k2 >= kb && k2 < ke) {
               const size_t p = size_t(k1p + B * k2) * W + w0 + w;
               xa[b] = xk[off0 + p];
-              if (a.grad_ext) {
+              if constexpr (MC) {
                 xm[b] = a.grad_ext[off0 + p];  // M^T (tTVadj u) of the motion-compensated form
               } else {
                 xm[b] = xk[offm + p];
@@ -854,7 +859,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT)
               // operator_tTVadj gives u_{f+1} - u_f of the normalised temporal
               // differences; NestaUp negates it, scales by lambda, adds A^H r
               float2 adj;
-              if (a.grad_ext) {
+              if constexpr (MC) {
                 adj = xm[b];
               } else {
                 const float2 u0 = tv_normalize(csub(xa[b], xm[b]), inv_mu);
@@ -876,6 +881,11 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT)
         }
       }
     }
+    };
+    if (a.grad_ext)
+      epilogue(std::true_type{});
+    else
+      epilogue(std::false_type{});
     if (a.colmax) {
       // column maxima for the next tensor-core forward pass: lanes l, l^8,
       // l^16, l^24 share a column (i % kWB)
