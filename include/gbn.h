@@ -245,6 +245,7 @@ typedef struct gbn_nesta_stats {
  * Allocates the solver workspace. */
 GBN_API int gbn_problem_create(gbn_ctx* ctx, int W, int H, int F, int C, const float* d_y, const float* d_S,
                        const uint8_t* d_mask, gbn_problem** out);
+/* Refused while a live batch holds the problem (destroy the batch first). */
 GBN_API int gbn_problem_destroy(gbn_problem* p);
 /* The row pass keeps one buffer of k-space rows, by default as large as the
  * k-space (every row of every frame and coil), so that any later contents of

@@ -74,6 +74,8 @@ void launch_fwd_cols_tc(const FusedArgs* tab, const BatchMap& bm, int it, int np
 namespace {
 
 void batch_release(gbn_batch* b) {
+  for (gbn_problem* P : b->probs) P->in_batches -= 1;
+  b->probs.clear();
   if (b->graph) cudaGraphExecDestroy(b->graph);
   for (auto& g : b->groups) {
     if (g.tab) cudaFree(g.tab);
@@ -174,6 +176,7 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
     }
     if ((rc = run_prepare(ctx, P, &params[i])) != GBN_OK) break;
     b->probs.push_back(P);
+    P->in_batches += 1;  // the batch's tables hold pointers into P's buffers
     b->prm.push_back(params[i]);
     b->out.push_back(reinterpret_cast<float2*>(outputs[i]));
     b->rand_off.push_back(b->rand_total);

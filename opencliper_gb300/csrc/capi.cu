@@ -623,6 +623,8 @@ int gbn_problem_fit_rows(gbn_problem* p, int headroom_rows, int* kept_rows) {
 
 int gbn_problem_destroy(gbn_problem* p) {
   if (!p) return GBN_OK;
+  if (p->in_batches > 0)
+    return set_error(GBN_ERR_INVALID, "the problem belongs to a live batch: destroy the batch first");
   DeviceGuard guard(p->ctx->device);
   cudaStreamSynchronize(p->ctx->stream);
   problem_free(p);

@@ -71,6 +71,7 @@ struct gbn_problem {
   int* row_full = nullptr;            // [F*H]
   float2* T = nullptr;                // [T_rows][C][W] kept rows of the row pass
   size_t T_rows = 0;                  // rows T holds (F*H unless fitted with gbn_problem_fit_rows)
+  int in_batches = 0;                 // live batches holding this problem's buffers
   float2* xk0 = nullptr;
   float2* xk1 = nullptr;
   float2* wacc = nullptr;

@@ -306,7 +306,8 @@ __global__ void k_mc_sort(const int* __restrict__ off, int* __restrict__ key, si
 
 // sorted keys entry * 4 + corner -> (the entry's pixel R1*W + R2) * 4 + corner,
 // so that neighbouring targets read neighbouring table entries
-__global__ void k_mc_rekey(int* __restrict__ key, size_t n, McRect r, int W) {
+__global__ void k_mc_rekey(int* __restrict__ key, const int* __restrict__ total, McRect r, int W) {
+  const size_t n = size_t(*total);  // contributions filled (off[F*H*W])
   for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
     const int k = key[i];
     key[i] = entry_offset(r, k >> 2, W) * 4 + (k & 3);
@@ -606,7 +607,7 @@ int tables_build(gbn_ctx* ctx, McTables* t, const float* xn, const int* xm, cons
     return cuda_status(e, "motion compensation tables");
   k_mc_fill<<<grid1(ctx, size_t(E) * F), kNT, 0, s>>>(xn, xm, r, W, H, F, t->off, t->cnt, t->key, t->wts);
   k_mc_sort<<<grid1(ctx, X), kNT, 0, s>>>(t->off, t->key, X);
-  k_mc_rekey<<<grid1(ctx, 4 * size_t(E) * F), kNT, 0, s>>>(t->key, 4 * size_t(E) * F, r, W);
+  k_mc_rekey<<<grid1(ctx, 4 * size_t(E) * F), kNT, 0, s>>>(t->key, t->off + X, r, W);
   ctx->launches += 9;
   return GBN_OK;
 }

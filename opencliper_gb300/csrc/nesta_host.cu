@@ -517,6 +517,8 @@ void launch_row_analysis(gbn_problem* P, cudaStream_t s);
 // plus `headroom` (at most every row); returns the kept rows in *kept.
 int problem_fit_rows(gbn_problem* P, int headroom, int* kept) {
   if (headroom < 0) return set_error(GBN_ERR_INVALID, "headroom must be >= 0");
+  if (P->in_batches > 0)
+    return set_error(GBN_ERR_INVALID, "fit rows: the problem belongs to a live batch (destroy it first)");
   cudaStream_t s = P->ctx->stream;
   cudaError_t e = cudaMemsetAsync(&P->st->status, 0, sizeof(int), s);
   const size_t saved = P->T_rows;

@@ -188,3 +188,21 @@ def test_maximum_sizes(ctx):
     prob.close()
     for d in (p.y, p.S, p.mask, x1, x2):
         d.free()
+
+
+def test_batch_membership_guards(ctx):
+    """While a batch holds a problem, resizing its row buffer and destroying it
+    are refused (the batch's tables point into its buffers)."""
+    p = synth.make_problem(32, 32, 4, 2, 4, seed=5)
+    dy, dS, dm = ctx.to_device(p.y), ctx.to_device(p.S), ctx.to_device(p.mask)
+    prob = g.Problem(ctx, dy, dS, dm)
+    x = ctx.empty((4, 32, 32), np.complex64)
+    b = g.Batch(ctx, [prob], g.nesta_params(maxIter=5, maxIntIter=1, stoptest=0), [x])
+    with pytest.raises(g.GbnError):
+        prob.fit_rows(0)
+    from opencliper_gb300._abi import call
+    with pytest.raises(g.GbnError):
+        call("gbn_problem_destroy", prob.handle)
+    b.close()
+    assert prob.fit_rows(0) == int(p.rowmask.astype(bool).sum())
+    prob.close()
