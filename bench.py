@@ -168,12 +168,13 @@ def algorithmic_bytes(kind: str, G: int, shape: tuple | None = None) -> int:
     raise KeyError(kind)
 
 
-def ncu_traffic(kind: str) -> float | None:
-    """DRAM bytes per launch from the committed ncu summary, when present."""
+def ncu_traffic(kind: str, field: str = "bytes_per_launch") -> float | None:
+    """Per-launch figure (DRAM bytes, or warp instructions) from the committed
+    ncu summary, when present."""
     p = ROOT / "profiles" / "dram_traffic.json"
     try:
         d = json.loads(p.read_text())
-        return float(d[kind]["bytes_per_launch"])
+        return float(d[kind][field])
     except (OSError, KeyError, ValueError):
         return None
 
@@ -325,6 +326,17 @@ def run_ours(args, dist: Dist) -> dict | None:
             "traffic": traffic, "algorithmic_bytes_per_launch": alg, "avg_launch_us": round(avg_s * 1e6, 2),
             "share_of_step": round(ms_dom / max(total_prof, 1e-9), 3),
             "groups_us_per_launch": {k: round(v[1] * 1e3 / max(v[0], 1), 2) for k, v in prof.items()}}
+    # the same kernel against the instruction-issue ceiling it is bound by: warp
+    # instructions per launch (ncu) over the live launch time, against 4
+    # schedulers x SMs x the sampled SM clock
+    inst = ncu_traffic(dom, "warp_instructions_per_launch")
+    sm_mhz = (clk or {}).get("sm_mhz") or 0
+    if inst and sm_mhz:
+        nsm = torch.cuda.get_device_properties(dist.local).multi_processor_count
+        issue_peak = 4.0 * nsm * sm_mhz * 1e6
+        roof["issue"] = {"achieved_ginst_s": round(inst / avg_s / 1e9, 1), "peak_ginst_s": round(issue_peak / 1e9, 1),
+                         "frac": round(inst / avg_s / issue_peak, 4),
+                         "warp_instructions_per_launch": inst, "source": "profiles/dram_traffic.json (ncu)"}
 
     if mixed:
         batch.close()
