@@ -118,7 +118,8 @@ def test_facade_cfl_files(ctx, tmp_path):
     assert hdr == [str(W), str(H), "1", str(F), "1"]
 
 
-def test_facade_mat_files(ctx, tmp_path):
+@pytest.mark.parametrize("mask_form", ["rowmask", "pixelmask"])
+def test_facade_mat_files(ctx, tmp_path, mask_form):
     """KData(app, "x.mat") (compressed MAT-file with Dims, KData,
     SensitivityMaps and a row-mask SamplingMasks, as KData.cpp:276-435 reads
     it), SimpleMRIRecon and NestaUp through the facade, results written by
@@ -138,7 +139,14 @@ def test_facade_mat_files(ctx, tmp_path):
     W, H, F, C = 40, 32, 4, 3
     p = synth.make_problem(W, H, F, C, 2, seed=17)
     kfile = str(tmp_path / "series.mat")
-    matfile.write_kdata(kfile, p.y, p.S, rowmask=p.rowmask)
+    if mask_form == "rowmask":
+        matfile.write_kdata(kfile, p.y, p.S, rowmask=p.rowmask)
+    else:  # uint8 pixel mask H x W x F; every other column of each sampled row left out
+        pm = p.mask.copy()
+        pm[:, :, 1::2] = 0
+        p = synth.Problem(np.where(pm[:, None] != 0, p.y, 0).astype(np.complex64), p.S, pm, p.rowmask, p.x_true,
+                          p.seed)
+        matfile.write_kdata(kfile, p.y, p.S, pixelmask=pm)
     out = str(tmp_path / "out")
     r = subprocess.run([str(exe), kfile, out], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr

@@ -43,15 +43,20 @@ def test_motion_rejects_bad_box(ctx):
         api.op_motion(ctx, 1, x, x, ctx.to_device(xn), ctx.to_device(xm), [1, 1, W + 5, H])
 
 
-@pytest.mark.parametrize("W,H,F,C,Rr", [(48, 40, 6, 3, 4), (64, 64, 8, 4, 4)])
-def test_nesta_motion_compensated(ctx, W, H, F, C, Rr):
+FIXED_MC = dict(lambda_i=0.01, mu_f=1e-3, La=1.0, maxIntIter=1, maxIter=25, stoptest=0, miniter=7, tolVar=3e-4)
+# continuation over three outer loops with the rolling-mean stopping test
+DRIVER_MC = dict(lambda_i=1e-2, mu_f=3e-4, La=1.0, maxIntIter=3, maxIter=30, stoptest=1, miniter=5, tolVar=3e-4)
+
+
+@pytest.mark.parametrize("W,H,F,C,Rr,prm", [(48, 40, 6, 3, 4, FIXED_MC), (64, 64, 8, 4, 4, FIXED_MC),
+                                            (48, 40, 6, 3, 4, DRIVER_MC)])
+def test_nesta_motion_compensated(ctx, W, H, F, C, Rr, prm):
     p = synth.make_problem(W, H, F, C, Rr, seed=W + F)
     xn, xm, bb = synth.make_motion(W, H, F, seed=F)
     dy, dS, dm = ctx.to_device(p.y), ctx.to_device(p.S), ctx.to_device(p.mask)
     prob = g.Problem(ctx, dy, dS, dm)
-    prm = dict(lambda_i=0.01, mu_f=1e-3, La=1.0, maxIntIter=1, maxIter=25, stoptest=0, miniter=7, tolVar=3e-4)
     x = ctx.empty((F, H, W), np.complex64)
-    prob.run(g.nesta_params(**prm), x)            # first reconstruction, without motion
+    prob.run(g.nesta_params(**FIXED_MC), x)       # first reconstruction, without motion
     x0 = x.get()
     dxn, dxm = ctx.to_device(xn), ctx.to_device(xm)
     prob.set_motion(dxn, dxm, bb)
