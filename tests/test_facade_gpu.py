@@ -83,7 +83,8 @@ def test_facade_matches_c_abi(ctx, driver, tmp_path):
     assert np.array_equal(xmc_cpp, xmc.get())
 
 
-def test_facade_cfl_files(ctx, tmp_path):
+@pytest.mark.parametrize("mask_form", ["rowmask", "pixelmask"])
+def test_facade_cfl_files(ctx, tmp_path, mask_form):
     """KData(app, fileName) from the reference's CFL form (row mask file),
     SimpleMRIRecon, SimpleMRIReconSOS and NestaUp through the facade, results
     written by XData::saveCFLData and checked against the oracle."""
@@ -100,7 +101,14 @@ def test_facade_cfl_files(ctx, tmp_path):
     W, H, F, C = 32, 24, 4, 3
     p = synth.make_problem(W, H, F, C, 2, seed=31)
     kfile = str(tmp_path / "series.cfl")
-    cfl.write_kdata(kfile, p.y, p.S, rowmask=p.rowmask)
+    if mask_form == "rowmask":
+        cfl.write_kdata(kfile, p.y, p.S, rowmask=p.rowmask)
+    else:  # <base>_SamplingMasks.u8 with every other column of each sampled row left out
+        pm = p.mask.copy()
+        pm[:, :, 1::2] = 0
+        p = synth.Problem(np.where(pm[:, None] != 0, p.y, 0).astype(np.complex64), p.S, pm, p.rowmask, p.x_true,
+                          p.seed)
+        cfl.write_kdata(kfile, p.y, p.S, pixmask=pm)
     r = subprocess.run([str(exe), kfile, str(tmp_path / "out")], capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
     simple = cfl.read_xdata(str(tmp_path / "out_simple"))
