@@ -10,9 +10,10 @@ from opencliper_gb300 import synth
 from oracle import motion as M
 from oracle import refkernels as K
 
-pytestmark = pytest.mark.skipif(K.build() is None, reason="reference kernel sources not available")
+_needs_ref = pytest.mark.skipif(K.build() is None, reason="reference kernel sources not available")
 
 
+@_needs_ref
 @pytest.mark.parametrize("W,H,F,seed", [(48, 40, 3, 1), (96, 80, 2, 2), (40, 160, 4, 3)])
 def test_motion_oracle_matches_reference_kernels(W, H, F, seed):
     xn, xm, bb = synth.make_motion(W, H, F, seed=seed)
@@ -31,3 +32,20 @@ def test_motion_adjoint_identity():
     lhs = np.vdot(M.warp(x, xn, xm, bb), y)
     rhs = np.vdot(x, M.warp_adjoint(y, xn, xm, bb))
     assert abs(lhs - rhs) <= 1e-12 * abs(lhs)
+
+
+@pytest.mark.parametrize("W,H,F,amp", [(48, 40, 3, 1.2), (256, 256, 4, 1.2), (64, 56, 4, 3.0), (512, 128, 2, 1.2)])
+def test_synthetic_motion_stays_inside_the_image(W, H, F, amp):
+    """synth.make_motion: every rectangle entry's target and interpolation
+    corners are inside the image (so the kernels never report status 5), and
+    the meshes have the reference's layouts and 1-based values."""
+    xn, xm, bb = synth.make_motion(W, H, F, seed=1, amplitude=amp)
+    assert xn.shape == (2, F, H, W) and xn.dtype == np.float32
+    assert xm.shape == (2, W, H) and xm.dtype == np.int32
+    r1, r2 = M.rect(W, H, bb)
+    assert r1.min() >= 0 and r1.max() < H and r2.min() >= 0 and r2.max() < W
+    nh = xn[0][:, r1[:, None], r2[None, :]] - 1
+    nv = xn[1][:, r1[:, None], r2[None, :]] - 1
+    assert np.floor(nh).min() >= 0 and np.floor(nh).max() + 1 < W
+    assert np.floor(nv).min() >= 0 and np.floor(nv).max() + 1 < H
+    assert xm[0].min() == 1 and xm[0].max() == W and xm[1].min() == 1 and xm[1].max() == H
