@@ -313,7 +313,7 @@ __global__ void k_colmax(const float2* __restrict__ in, int R, int H, int W, flo
 //   B[2(8c+w), 2g] = Tr, B[2(8c+w), 2g+1] = -Ti, B[2(8c+w)+1, 2g] = Ti,
 //   B[2(8c+w)+1, 2g+1] = Tr                           (formed from T, scaled)
 // then x = sum_c conj(S_c) Y_c straight from tensor memory.  A CTA takes one
-// frame, 128 rows and 8 columns; coils go through TMEM 16 at a time (N <= 256).
+// frame, 128 rows and 8 columns; coils go through TMEM 8 at a time (N <= 128).
 // Operands are split fp16 hi + lo as in k_fwd_cols_tc; B is scaled by a power
 // of two from the maximum |T| of the coil group (two passes over T), undone in
 // the combination.  K runs in chunks of 32 kept rows (64 real k), one stage.
@@ -322,14 +322,14 @@ namespace {
 constexpr int kAcKC = 64;                  // real k per chunk
 constexpr int kAcRows = kAcKC / 2;         // kept rows per chunk
 constexpr int kAcCols = 8;                 // columns per CTA
-constexpr int kAcCoils = 16;               // coils per TMEM pass
-constexpr int kAcBatch = 4;                // coils combined per TMEM read
+constexpr int kAcCoils = 8;                // coils per TMEM pass
+constexpr int kAcBatch = 2;                // coils combined per TMEM read
 constexpr int kAcAPart = 128 * kAcKC * 2;  // bytes of one A part (hi or lo)
 __host__ __device__ constexpr int ac_b_part(int n) { return n * kAcKC * 2; }
 __host__ __device__ constexpr int ac_smem(int nmax) { return 2 * kAcAPart + 2 * ac_b_part(nmax); }
 }  // namespace
 
-__global__ void __launch_bounds__(128, 2)
+__global__ void __launch_bounds__(128, 3)
     k_inv_cols_tc(const FusedArgs* __restrict__ tab, const __grid_constant__ BatchMap bm, int it) {
   extern __shared__ __align__(1024) unsigned char sm[];
   __shared__ uint64_t mbar;
