@@ -473,33 +473,10 @@ __global__ void __launch_bounds__(kNT) k_mc_tv(const float2* __restrict__ x, con
 __global__ void k_fill(float2* __restrict__ v, size_t n, float2 value) {
   for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) v[i] = value;
 }
-__global__ void k_scale2(float2* __restrict__ v, size_t n, float s) {
-  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
-    const float2 a = v[i];
-    v[i] = make_float2(a.x * s, a.y * s);
-  }
-}
-// complexType(drand48(), 0) in element order (NestaUp.cpp:369-385): draw i+1 after x0
-__global__ void k_fill_drand48(float2* __restrict__ v, size_t n, unsigned long long x0) {
-  for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
-    // jump x0 by i+1 steps: X -> a X + c (mod 2^48)
-    unsigned long long ra = 1, rc = 0, ba = 0x5DEECE66DULL, bc = 0xBULL, k = i + 1;
-    const unsigned long long mask = (1ULL << 48) - 1;
-    while (k) {
-      if (k & 1) {
-        rc = (ba * rc + bc) & mask;
-        ra = (ba * ra) & mask;
-      }
-      bc = (ba * bc + bc) & mask;
-      ba = (ba * ba) & mask;
-      k >>= 1;
-    }
-    const unsigned long long X = (ra * x0 + rc) & mask;
-    v[i] = make_float2(__double2float_rn(double(X) * 0x1p-48), 0.f);
-  }
-}
 // sum of |v|^2 and of |Re| + |Im|: FP32 within a thread's few elements and
 // a warp, FP64 across warps and blocks; per-block partials in fixed slots
+// (blocks stride over the vector in a fixed order, so the sums are
+// deterministic)
 __device__ __forceinline__ void warp_sums_to_block(float s2, float s1, double* sred2, double* sred1, double* part) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
@@ -520,39 +497,210 @@ __device__ __forceinline__ void warp_sums_to_block(float s2, float s1, double* s
     part[2 * blockIdx.x + threadIdx.x] = t;
   }
 }
-__global__ void __launch_bounds__(kNT) k_sums(const float2* __restrict__ v, size_t n, double* __restrict__ part) {
+int grid1(gbn_ctx* ctx, size_t n) { return int(std::min<size_t>((n + kNT - 1) / kNT, size_t(ctx->nsm) * 8)); }
+
+// ---- the power method on the device ------------------------------------------------
+// myNormest's loop (NestaUp.cpp:291-439) with U = tTV M and U^T = M^T tTVadj,
+// driven by a device-side state so that steps are enqueued in chunks without
+// host round trips.  Each step: U x (warp, tTV, partial sums of |Sx|^2 and
+// |Re|+|Im|), a scalar kernel (restart test, e), the drand48 restart (only when
+// U x is exactly zero), U^T Sx (tTVadj and the ordered M^T gather, partial
+// sums), a scalar kernel (||x||, the stopping test).  x is stored unscaled; its
+// scale 1/||x|| is applied as each value is read, which rounds exactly as a
+// separate scaling pass would.
+struct McNe {
+  float e, e0, s;          // current and previous ||U x||, scale of the stored x
+  int cnt, done, restart;  // steps taken, stop flag, restart in the current step
+  int nrestart;            // restarts so far (each consumed F*H*W drand48 draws)
+  int pad;
+  unsigned long long rand;  // drand48 state
+};
+constexpr int kPartDoubles = 2 * 1024 + 2 + 8;  // block partials, two totals, the McNe state
+static_assert(sizeof(McNe) <= 8 * sizeof(double), "McNe fits its slot");
+constexpr float kNeTol = 1e-3f;
+constexpr int kNeMax = 100;
+
+__device__ __forceinline__ McNe* ne_state(double* part) { return reinterpret_cast<McNe*>(part + 2 * 1024 + 2); }
+
+// (M (s x))[k][p] for the stored, unscaled x
+__device__ __forceinline__ float2 warp_scaled(const float2* __restrict__ x, float sc, const float* __restrict__ xn, McRect r,
+                                             int e, int p, int k, int W, int H, int F, int* __restrict__ status) {
+  const float2* xf = x + size_t(k) * H * W;
+  if (e >= 0) {
+    const McPoint q = mc_point(xn, entry_offset(r, e, W), k, W, H, F);
+    if (q.ok) {
+      const float2 i1 = cscale(xf[q.ph + size_t(q.pv) * W], sc), i2 = cscale(xf[q.ph + 1 + size_t(q.pv) * W], sc);
+      const float2 i3 = cscale(xf[q.ph + size_t(q.pv + 1) * W], sc);
+      const float2 i4 = cscale(xf[q.ph + 1 + size_t(q.pv + 1) * W], sc);
+      const float a = float(q.ph + 1) - q.nh, b = q.nh - float(q.ph);
+      const float c = float(q.pv + 1) - q.nv, d = q.nv - float(q.pv);
+      const float2 aux1 = make_float2(lin2(a, i1.x, b, i2.x), lin2(a, i1.y, b, i2.y));
+      const float2 aux2 = make_float2(lin2(a, i3.x, b, i4.x), lin2(a, i3.y, b, i4.y));
+      return make_float2(lin2(c, aux1.x, d, aux2.x), lin2(c, aux1.y, d, aux2.y));
+    }
+    atomicExch(status, kStatusMotionRange);
+  }
+  return cscale(xf[p], sc);
+}
+
+__global__ void k_ne_init(double* part, float e, unsigned long long rand) {
+  McNe* ne = ne_state(part);
+  ne->e = e;
+  ne->e0 = 0.f;
+  ne->s = 1.0f / e;
+  ne->cnt = 0;
+  ne->done = !(fabsf(e - 0.f) > kNeTol * e && 0 < kNeMax);
+  ne->restart = 0;
+  ne->nrestart = 0;
+  ne->rand = rand;
+}
+
+// Sx = tTV(M (s x)), partial sums
+__global__ void __launch_bounds__(kNT) k_ne_u(const float2* __restrict__ x, float2* __restrict__ Sx,
+                                               const float* __restrict__ xn, const int* __restrict__ inv, McRect r,
+                                               int W, int H, int F, double* __restrict__ part, int* __restrict__ status) {
   __shared__ double sred2[kNT / 32], sred1[kNT / 32];
+  const McNe* ne = ne_state(part);
+  if (ne->done) return;
+  const float sc = ne->s;
+  const size_t HW = size_t(H) * W, n = HW * F;
   float s2 = 0.f, s1 = 0.f;
   for (size_t i = blockIdx.x * size_t(kNT) + threadIdx.x; i < n; i += size_t(gridDim.x) * kNT) {
-    const float2 a = v[i];
+    const int p = int(i % HW), k = int(i / HW);
+    const int e = inv[p];
+    const float2 w0 = warp_scaled(x, sc, xn, r, e, p, k, W, H, F, status);
+    const float2 wm = warp_scaled(x, sc, xn, r, e, p, (k + F - 1) % F, W, H, F, status);
+    const float2 a = csub(w0, wm);
+    Sx[i] = a;
     s2 = fmaf(a.x, a.x, fmaf(a.y, a.y, s2));
     s1 += fabsf(a.x) + fabsf(a.y);
   }
   warp_sums_to_block(s2, s1, sred2, sred1, part);
 }
-// the block partials summed by one block: each thread a strided subset in
-// order, then the threads in order
-__global__ void __launch_bounds__(kNT) k_sums_final(const double* __restrict__ part, int nblk, double* __restrict__ out) {
-  __shared__ double sred[kNT / 32];
+
+// sums of the block partials: each thread a strided subset in order, then
+// the threads in order
+__device__ __forceinline__ void ne_totals(const double* __restrict__ part, int nblk, double* sred, double* t2, double* t1) {
   double s2 = 0.0, s1 = 0.0;
   for (int b = threadIdx.x; b < nblk; b += kNT) {
     s2 += part[2 * b];
     s1 += part[2 * b + 1];
   }
-  s2 = block_sum<kNT>(s2, sred);
-  s1 = block_sum<kNT>(s1, sred);
-  if (threadIdx.x == 0) {
-    out[0] = s2;
-    out[1] = s1;
-  }
-}
-__global__ void k_set_normest(NestaDevState* st, float e, int iters) {
-  st->normU = e;
-  st->normest_iters = iters;
-  st->ne_done = 1;
+  *t2 = block_sum<kNT>(s2, sred);
+  *t1 = block_sum<kNT>(s1, sred);
 }
 
-int grid1(gbn_ctx* ctx, size_t n) { return int(std::min<size_t>((n + kNT - 1) / kNT, size_t(ctx->nsm) * 8)); }
+// e0 = e; restart test (Scasum(U x) == 0, NestaUp.cpp:369-385); e = ||U x||
+__global__ void __launch_bounds__(kNT) k_ne_s1(double* part, int nblk) {
+  __shared__ double sred[kNT / 32];
+  McNe* ne = ne_state(part);
+  if (ne->done) return;
+  double t2, t1;
+  ne_totals(part, nblk, sred, &t2, &t1);
+  if (threadIdx.x == 0) {
+    ne->e0 = ne->e;
+    ne->restart = (t1 == 0.0) ? 1 : 0;
+    if (!ne->restart) ne->e = float(sqrt(t2));
+  }
+}
+
+// restart: Sx = (drand48(), 0) in element order, partial sums
+__global__ void __launch_bounds__(kNT) k_ne_restart(float2* __restrict__ Sx, size_t n, double* __restrict__ part) {
+  __shared__ double sred2[kNT / 32], sred1[kNT / 32];
+  const McNe* ne = ne_state(part);
+  if (ne->done || !ne->restart) return;
+  const unsigned long long x0 = ne->rand;
+  float s2 = 0.f, s1 = 0.f;
+  for (size_t i = blockIdx.x * size_t(kNT) + threadIdx.x; i < n; i += size_t(gridDim.x) * kNT) {
+    unsigned long long ra = 1, rc = 0, ba = 0x5DEECE66DULL, bc = 0xBULL, k = i + 1;
+    const unsigned long long mask = (1ULL << 48) - 1;
+    while (k) {
+      if (k & 1) {
+        rc = (ba * rc + bc) & mask;
+        ra = (ba * ra) & mask;
+      }
+      bc = (ba * bc + bc) & mask;
+      ba = (ba * ba) & mask;
+      k >>= 1;
+    }
+    const float2 a = make_float2(__double2float_rn(double((ra * x0 + rc) & mask) * 0x1p-48), 0.f);
+    Sx[i] = a;
+    s2 = fmaf(a.x, a.x, fmaf(a.y, a.y, s2));
+    s1 += fabsf(a.x) + fabsf(a.y);
+  }
+  warp_sums_to_block(s2, s1, sred2, sred1, part);
+}
+
+// after a restart: e = ||Sx||, the generator moved past the n draws
+__global__ void __launch_bounds__(kNT) k_ne_s1b(double* part, int nblk, unsigned long long ja, unsigned long long jc) {
+  __shared__ double sred[kNT / 32];
+  McNe* ne = ne_state(part);
+  if (ne->done || !ne->restart) return;
+  double t2, t1;
+  ne_totals(part, nblk, sred, &t2, &t1);
+  if (threadIdx.x == 0) {
+    ne->e = float(sqrt(t2));
+    ne->rand = (ja * ne->rand + jc) & ((1ULL << 48) - 1);
+    ne->nrestart += 1;
+  }
+}
+
+// x = M^T tTVadj(Sx) (operatorUt without negation), partial sums
+__global__ void __launch_bounds__(kNT) k_ne_ut(const float2* __restrict__ Sx, float2* __restrict__ x,
+                                                const int* __restrict__ off, const int* __restrict__ key,
+                                                const int* __restrict__ srcmap, const float2* __restrict__ wts, McRect r,
+                                                int W, int H, int F, double* __restrict__ part) {
+  __shared__ double sred2[kNT / 32], sred1[kNT / 32];
+  const McNe* ne = ne_state(part);
+  if (ne->done) return;
+  const size_t HW = size_t(H) * W, n = HW * F;
+  float s2 = 0.f, s1 = 0.f;
+  for (size_t q = blockIdx.x * size_t(kNT) + threadIdx.x; q < n; q += size_t(gridDim.x) * kNT) {
+    const int p = int(q % HW), row = p / W, col = p % W;
+    const size_t k = q / HW;
+    const float2* u0 = Sx + k * HW;                   // tTVadj: u_{f+1} - u_f
+    const float2* u1 = Sx + size_t((k + 1) % F) * HW;
+    const bool in_rect = row >= r.r1b && row < r.r1b + r.l1 && col >= r.r2b && col < r.r2b + r.l2;
+    float2 acc = in_rect ? make_float2(0.f, 0.f) : csub(u1[p], u0[p]);
+    const float2* wk = wts + k * HW;
+    for (int c = off[q], ce = off[q + 1]; c < ce; ++c) {
+      const int kc = __ldg(key + c), e = kc >> 2;
+      const float2 w = __ldg(wk + e);
+      const float fa = (kc & 1) ? w.x : __fsub_rn(1.f, w.x);
+      const float fb = (kc & 2) ? w.y : __fsub_rn(1.f, w.y);
+      const int src = __ldg(srcmap + e);
+      const float2 v = csub(u1[src], u0[src]);
+      acc.x = __fadd_rn(acc.x, __fmul_rn(__fmul_rn(v.x, fa), fb));
+      acc.y = __fadd_rn(acc.y, __fmul_rn(__fmul_rn(v.y, fa), fb));
+    }
+    x[q] = acc;
+    s2 = fmaf(acc.x, acc.x, fmaf(acc.y, acc.y, s2));
+    s1 += fabsf(acc.x) + fabsf(acc.y);
+  }
+  warp_sums_to_block(s2, s1, sred2, sred1, part);
+}
+
+// ||x||, the scale of the next step, the stopping test
+__global__ void __launch_bounds__(kNT) k_ne_s2(double* part, int nblk) {
+  __shared__ double sred[kNT / 32];
+  McNe* ne = ne_state(part);
+  if (ne->done) return;
+  double t2, t1;
+  ne_totals(part, nblk, sred, &t2, &t1);
+  if (threadIdx.x == 0) {
+    const float nx = float(sqrt(t2));
+    ne->s = 1.0f / nx;
+    ne->cnt += 1;
+    ne->done = !(fabsf(ne->e - ne->e0) > kNeTol * ne->e && ne->cnt < kNeMax);
+  }
+}
+
+__global__ void k_ne_finish(const double* part, NestaDevState* st) {
+  const McNe* ne = ne_state(const_cast<double*>(part));
+  st->normU = ne->e;
+  st->normest_iters = ne->cnt;
+  st->ne_done = 1;
+}
 
 // ---------------------------------------------------------------------------
 // host side
@@ -641,7 +789,7 @@ int motion_set(gbn_problem* P, const float* xn, const int* xmesh, const int* bb)
     cudaError_t e = cudaMalloc(&P->mc_xw, X * sizeof(float2));
     if (e == cudaSuccess) e = cudaMalloc(&P->mc_g, X * sizeof(float2));
     if (e == cudaSuccess) e = cudaMalloc(&P->mc_gm, X * sizeof(float2));
-    if (e == cudaSuccess) e = cudaMalloc(&P->mc_part, 2 * 1024 * sizeof(double) + 2 * sizeof(double));
+    if (e == cudaSuccess) e = cudaMalloc(&P->mc_part, kPartDoubles * sizeof(double));
     if (e != cudaSuccess) {
       cudaGetLastError();
       motion_free(P);
@@ -668,67 +816,45 @@ void mc_apply(gbn_ctx* ctx, gbn_problem* P, const float2* in, float2* out, cudaS
   ctx->launches += 1;
 }
 
-// out = M^T in
-void mc_adjoint(gbn_ctx* ctx, gbn_problem* P, const float2* in, float2* out, cudaStream_t s) {
-  const size_t X = size_t(P->W) * P->H * P->F;
-  const McRect r = mc_rect(P->W, P->H, P->mc_bb);
-  const McTables* t = P->mc_tab;
-  k_mc_adjoint<<<int((X + kNT - 1) / kNT), kNT, 0, s>>>(in, out, t->off, t->key, t->srcmap, t->wts, r, P->W, P->H,
-                                                       P->F, 0);
-  ctx->launches += 1;
-}
-
-// (sum |v|^2, sum |Re| + |Im|) on the host (synchronises s)
-int sums(gbn_ctx* ctx, gbn_problem* P, const float2* v, double out[2], cudaStream_t s) {
-  const size_t X = size_t(P->W) * P->H * P->F;
-  const int nblk = std::min(1024, grid1(ctx, X));
-  k_sums<<<nblk, kNT, 0, s>>>(v, X, P->mc_part);
-  k_sums_final<<<1, kNT, 0, s>>>(P->mc_part, nblk, P->mc_part + 2 * 1024);
-  ctx->launches += 2;
-  cudaError_t e = cudaMemcpyAsync(out, P->mc_part + 2 * 1024, 2 * sizeof(double), cudaMemcpyDeviceToHost, s);
-  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  return e == cudaSuccess ? GBN_OK : cuda_status(e, "power method norms");
-}
-
-// myNormest (NestaUp.cpp:291-439) with U = tTV M, U^T = M^T tTVadj; float
-// scalars as the reference, norms reduced in FP64
+// myNormest (NestaUp.cpp:291-439) with U = tTV M, U^T = M^T tTVadj: steps on
+// the device (k_ne_*), enqueued kNeChunk at a time; the host reads the stop
+// flag once per chunk
 int mc_normest(gbn_ctx* ctx, gbn_problem* P, cudaStream_t s) {
+  constexpr int kNeChunk = 8;
   const int W = P->W, H = P->H, F = P->F;
   const size_t X = size_t(W) * H * F;
-  float2 *x = P->mc_gm, *Sx = P->mc_g, *tmp = P->mc_xw;
-  const float tol = 1e-3f;
-  double sm[2];
-  int rc;
+  const McTables* t = P->mc_tab;
+  const McRect r = mc_rect(W, H, P->mc_bb);
+  float2 *x = P->mc_gm, *Sx = P->mc_g;
+  const int nblk = std::min(1024, grid1(ctx, X));
+  const float e_init = float(std::sqrt(double(X)));  // ||ones||
+  const Lcg48 jX = lcg48_jump(uint64_t(X));
   k_fill<<<grid1(ctx, X), kNT, 0, s>>>(x, X, make_float2(1.f, 0.f));
-  ctx->launches += 1;
-  if ((rc = sums(ctx, P, x, sm, s)) != GBN_OK) return rc;
-  float e = float(std::sqrt(sm[0]));
-  k_scale2<<<grid1(ctx, X), kNT, 0, s>>>(x, X, 1.0f / e);
-  ctx->launches += 1;
-  float e0 = 0.f;
-  int cnt = 0;
-  while (std::fabs(e - e0) > tol * e && cnt < 100) {
-    e0 = e;
-    mc_apply(ctx, P, x, tmp, s);
-    if ((rc = op_ttv(ctx, GBN_TTV_FORWARD, tmp, Sx, W, H, F)) != GBN_OK) return rc;
-    if ((rc = sums(ctx, P, Sx, sm, s)) != GBN_OK) return rc;
-    if (sm[1] == 0.0) {
-      // restart from (drand48(), 0) in element order, as the reference
-      k_fill_drand48<<<grid1(ctx, X), kNT, 0, s>>>(Sx, X, ctx->rand48);
-      ctx->launches += 1;
-      ctx->rand48 = lcg48_apply(lcg48_jump(uint64_t(X)), ctx->rand48);
-      if ((rc = sums(ctx, P, Sx, sm, s)) != GBN_OK) return rc;
+  k_ne_init<<<1, 1, 0, s>>>(P->mc_part, e_init, (unsigned long long)ctx->rand48);
+  ctx->launches += 2;
+  struct {
+    int done, cnt, nrestart;
+  } h{0, 0, 0};
+  for (int steps = 0; steps < kNeMax;) {
+    for (int k = 0; k < kNeChunk && steps < kNeMax; ++k, ++steps) {
+      k_ne_u<<<nblk, kNT, 0, s>>>(x, Sx, P->mc_xn, t->inv, r, W, H, F, P->mc_part, &P->st->status);
+      k_ne_s1<<<1, kNT, 0, s>>>(P->mc_part, nblk);
+      k_ne_restart<<<nblk, kNT, 0, s>>>(Sx, X, P->mc_part);
+      k_ne_s1b<<<1, kNT, 0, s>>>(P->mc_part, nblk, (unsigned long long)jX.a, (unsigned long long)jX.c);
+      k_ne_ut<<<nblk, kNT, 0, s>>>(Sx, x, t->off, t->key, t->srcmap, t->wts, r, W, H, F, P->mc_part);
+      k_ne_s2<<<1, kNT, 0, s>>>(P->mc_part, nblk);
+      ctx->launches += 6;
     }
-    e = float(std::sqrt(sm[0]));
-    if ((rc = op_ttv(ctx, GBN_TTV_ADJOINT, Sx, tmp, W, H, F)) != GBN_OK) return rc;
-    mc_adjoint(ctx, P, tmp, x, s);
-    if ((rc = sums(ctx, P, x, sm, s)) != GBN_OK) return rc;
-    const float nx = float(std::sqrt(sm[0]));
-    k_scale2<<<grid1(ctx, X), kNT, 0, s>>>(x, X, 1.0f / nx);
-    ctx->launches += 1;
-    ++cnt;
+    const McNe* dne = reinterpret_cast<const McNe*>(P->mc_part + 2 * 1024 + 2);
+    cudaError_t e = cudaMemcpyAsync(&h.done, &dne->done, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h.cnt, &dne->cnt, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&h.nrestart, &dne->nrestart, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_status(e, "power method");
+    if (h.done) break;
   }
-  k_set_normest<<<1, 1, 0, s>>>(P->st, e, cnt);
+  for (int i = 0; i < h.nrestart; ++i) ctx->rand48 = lcg48_apply(jX, ctx->rand48);
+  k_ne_finish<<<1, 1, 0, s>>>(P->mc_part, P->st);
   ctx->launches += 1;
   return GBN_OK;
 }
