@@ -25,7 +25,7 @@ OUT = HERE / "_ref" / "librefkernels.so"
 REF = Path(os.environ.get("REFERENCE_ROOT", "/root/reference"))
 SOURCES = ["hostKernelFunctions.cl", "temporalTV.cl", "vectorNormalization.cl", "complexElementProd.cl",
            "xImageSum.cl", "applyMask.cl", "complexAbsPow2.cl", "complexAbs.cl", "rss.cl", "initialize.cl",
-           "optimizer.cl"]
+           "optimizer.cl", "creabspline.cl", "reductions.cl"]
 
 
 def build(force: bool = False) -> Path | None:
@@ -33,7 +33,7 @@ def build(force: bool = False) -> Path | None:
     if not all((kdir / s).exists() for s in SOURCES):
         return OUT if OUT.exists() else None
     deps = [HERE / "refkernels" / "harness.cpp", HERE / "refkernels" / "shim" / "OpenCLIPER" / "kernels" /
-            "hostKernelFunctions.h"] + [kdir / s for s in SOURCES]
+            "hostKernelFunctions.h", HERE / "refkernels" / "registration_host.hpp"] + [kdir / s for s in SOURCES]
     if OUT.exists() and not force and all(d.stat().st_mtime <= OUT.stat().st_mtime for d in deps):
         return OUT
     cxx = shutil.which("g++") or shutil.which("c++")
@@ -161,3 +161,41 @@ def mc_adjoint(x, xn, xmesh, bb):
     """AdjointMotionCompensation with the reference's kernels (copy, zero rectangle, adjoint interpolator)."""
     return _mc(lib().ref_mc_adjoint, x, xn, xmesh, bb)
 
+
+
+class RegParams(C.Structure):
+    """GroupwiseRegistration::InitParameters (GroupwiseRegistration.hpp:145-158)."""
+    _fields_ = [("W", C.c_float), ("flagW", C.c_int), ("radius", C.c_int), ("E", C.c_int), ("Dp0", C.c_int),
+                ("Dp1", C.c_int), ("nmax", C.c_int), ("et", C.c_float), ("eh", C.c_float),
+                ("lambda_", C.c_float * 4)]
+
+
+def registration(images: np.ndarray, radius: int = 40, E: int = 3, Dp=(4, 4), nmax: int = 100, et: float = 0.01,
+                 eh: float = 0.005, lambda_=(0.0, 0.005, 0.0, 0.5), W: float = 1.0, flagW: bool = True) -> dict:
+    """GroupwiseRegistration (init, creabspline, optimizer) on the host with the
+    reference's kernels; defaults are tests/MRIRecon.cpp:121-129.  images:
+    [F][N][N] complex.  Returns T [C1][C0... as the reference stores it, flat],
+    xn [2][F][N][N], H [iterations + 1], bb, iterations, C0, C1, areaX, Wn."""
+    x = _c64(images)
+    F, N, N2 = x.shape
+    assert N == N2, "square images only (the reference's mask and grid assume it)"
+    L = lib()
+    L.ref_registration.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(RegParams), C.c_void_p, C.c_void_p,
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t]
+    L.ref_registration.restype = C.c_int
+    prm = RegParams(float(W), int(flagW), int(radius), int(E), int(Dp[0]), int(Dp[1]), int(nmax), float(et),
+                    float(eh), (C.c_float * 4)(*[float(v) for v in lambda_]))
+    cap = 4 * N * N * F  # more than any control grid inside the image
+    T = np.zeros(cap, np.float32)
+    xn = np.zeros((2, F, N, N), np.float32)
+    H = np.zeros(nmax + 1, np.float32)
+    bb = np.zeros(4, np.int32)
+    info = np.zeros(4, np.int32)
+    wn = np.zeros(1, np.float32)
+    rc = L.ref_registration(x.ctypes.data, N, F, C.byref(prm), T.ctypes.data, xn.ctypes.data, H.ctypes.data,
+                            bb.ctypes.data, info.ctypes.data, wn.ctypes.data, cap)
+    if rc != 0:
+        raise ValueError("registration: unsupported geometry (grid or supports outside the image, N % 8, F < 3)")
+    it, c0, c1, area = (int(v) for v in info)
+    return dict(T=T[:c1 * c0 * F * 2].reshape(2, F, c0, c1), xn=xn, H=H[:it + 1], bb=bb, iterations=it, C0=c0,
+                C1=c1, areaX=area, Wn=float(wn[0]))

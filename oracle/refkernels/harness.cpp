@@ -22,6 +22,8 @@ thread_local size_t gbnref_gsz[3];
 #include "rss.cl"
 #include "initialize.cl"
 #include "optimizer.cl"
+#include "creabspline.cl"
+#include "reductions.cl"
 
 #include <vector>
 
@@ -183,3 +185,5 @@ void ref_mc_adjoint(const float* in, float* out, const float* xn, const int* x, 
 }
 
 }  // extern "C"
+
+#include "registration_host.hpp"

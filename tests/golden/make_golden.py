@@ -10,6 +10,11 @@ ops_refkernels.npz : outputs of the reference's own operator kernels
                    (src/kernels/*.cl compiled for the host by oracle/refkernels)
                    on seeded inputs; written only where the reference sources
                    are available
+registration_*.npz : GroupwiseRegistration run on the host with the
+                   reference's own kernels (oracle/refkernels/
+                   registration_host.hpp) on seeded cine phantoms: inputs,
+                   parameters, T, xn, the metric per iteration; written only
+                   where the reference sources are available
 
     python tests/golden/make_golden.py
 """
@@ -76,6 +81,36 @@ def refkernel_ops():
          mask_k=K.apply_mask(k, mask), abs2=K.abs2(k), abs=K.cabs(x), rss=K.rss(k))
 
 
+REG_CASES = [
+    # name, N, F, seed, parameters (the rest are tests/MRIRecon.cpp:121-129)
+    ("registration_64x4_circle.npz", 64, 4, 21, dict(radius=12, nmax=6, W=0.05)),
+    # a weight of at least 1 makes sumLambda() non-zero, so the smoothness terms enter the metric
+    ("registration_64x5_lambda.npz", 64, 5, 22, dict(radius=14, nmax=5, W=0.05, lambda_=(0.01, 0.02, 0.1, 1.5))),
+    ("registration_96x6_circle.npz", 96, 6, 23, dict(radius=20, nmax=4, W=0.2, flagW=False)),
+]
+
+
+def registration_inputs(N, F, seed):
+    return synth.phantom_series(N, N, F, np.random.default_rng(seed))
+
+
+def registration_cases():
+    from oracle import refkernels as K
+    if K.build() is None or not K.available():
+        print("reference kernel sources unavailable: registration_*.npz not regenerated")
+        return
+    for name, N, F, seed, kw in REG_CASES:
+        prm = dict(radius=40, E=3, Dp=(4, 4), nmax=100, et=0.01, eh=0.005, lambda_=(0.0, 0.005, 0.0, 0.5), W=1.0,
+                   flagW=True)
+        prm.update(kw)
+        img = registration_inputs(N, F, seed)
+        r = K.registration(img, **prm)
+        save(name, kind="registration", images=img, N=N, F=F, seed=seed,
+             **{"prm_" + k: np.asarray(v) for k, v in prm.items()},
+             **{k: np.asarray(v) for k, v in r.items()})
+
+
 if __name__ == "__main__":
     main()
     refkernel_ops()
+    registration_cases()

@@ -1,0 +1,80 @@
+"""GroupwiseRegistration oracle: the reference's own kernels run on the host
+(oracle/refkernels/registration_host.hpp) against the committed fixtures, and
+the geometry the registration derives from its parameters."""
+import os
+import sys
+
+import numpy as np
+import pytest
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(HERE, "golden"))
+
+import make_golden  # noqa: E402
+from oracle import refkernels as K  # noqa: E402
+
+CASES = [c[0] for c in make_golden.REG_CASES]
+
+
+def _load(name):
+    return dict(np.load(os.path.join(HERE, "golden", name)))
+
+
+def _prm(d):
+    return {k[4:]: (tuple(d[k]) if d[k].ndim else d[k].item()) for k in d if k.startswith("prm_")}
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_fixture_inputs_regenerate(name):
+    d = _load(name)
+    img = make_golden.registration_inputs(int(d["N"]), int(d["F"]), int(d["seed"]))
+    np.testing.assert_array_equal(img, d["images"])
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_reference_kernels_reproduce_fixture(name):
+    if K.build() is None or not K.available():
+        pytest.skip("reference kernel sources unavailable")
+    d = _load(name)
+    r = K.registration(d["images"], **_prm(d))
+    assert r["iterations"] == int(d["iterations"])
+    for k in ("T", "xn", "H", "bb"):
+        np.testing.assert_array_equal(r[k], d[k], err_msg=k)
+    assert r["Wn"] == float(d["Wn"])
+
+
+def _circle_geometry(N, radius):
+    # setMask (GroupwiseRegistration.cpp:486-531): pixels within the radius of
+    # the centre ((N+1)/2, 1-based), their count and 1-based bounding box
+    j = np.arange(N)
+    Cv = (1 - (N + 1) / 2 + j) ** 2
+    inside = (Cv[None, :] + Cv[:, None]) <= radius ** 2
+    rows, cols = np.nonzero(inside)
+    return int(inside.sum()), [cols.min() + 1, rows.min() + 1, cols.max() + 1, rows.max() + 1]
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_geometry_and_descent(name):
+    d = _load(name)
+    prm = _prm(d)
+    N, F = int(d["N"]), int(d["F"])
+    area, bb = _circle_geometry(N, prm["radius"])
+    assert int(d["areaX"]) == area
+    assert list(d["bb"]) == bb
+    # control grid: C = floor((|c - bb| + rp) / Dp) on each side, rp = (E+1) Dp / 2
+    c = (bb[0] + bb[2]) / 2
+    rp = (prm["E"] + 1) * prm["Dp"][0] // 2
+    C = int(np.floor((abs(c - bb[0]) + rp) / prm["Dp"][0]))
+    assert int(d["C0"]) == int(d["C1"]) == 2 * C + 1
+    assert d["T"].shape == (2, F, 2 * C + 1, 2 * C + 1)
+    # outside the bounding box the mesh is the identity
+    xn = d["xn"]
+    rr, cc = np.meshgrid(np.arange(N), np.arange(N), indexing="ij")
+    out = (rr < bb[1] - 1) | (rr > bb[3] - 1) | (cc < bb[0] - 1) | (cc > bb[2] - 1)
+    for f in range(F):
+        np.testing.assert_array_equal(xn[0, f][out], (cc + 1)[out])
+        np.testing.assert_array_equal(xn[1, f][out], (rr + 1)[out])
+    # the step sizes of the fixtures make the metric fall overall
+    H = d["H"]
+    assert H[-1] < H[0]
+    assert len(H) == int(d["iterations"]) + 1
