@@ -273,6 +273,62 @@ GBN_API int gbn_op_motion(gbn_ctx* ctx, int direction, const float* d_in, float*
  * Mesh points whose interpolation leaves the image are skipped and reported
  * in gbn_nesta_stats::status. */
 GBN_API int gbn_problem_set_motion(gbn_problem* p, const float* d_xn, const int* d_xmesh, const int bound_box[4]);
+/* ---- GroupwiseRegistration (motion estimation) ----------------------------
+ * GroupwiseRegistration::InitParameters (GroupwiseRegistration.hpp:145-158);
+ * the reference's defaults are tests/MRIRecon.cpp:121-129: W 1, flagW 1,
+ * radius 40, E 3, Dp {4, 4}, nmax 100, et 0.01, eh 0.005,
+ * lambda {0, 0.005, 0, 0.5}.  This build implements cubic splines (E = 3),
+ * equal control spacing, and the circular region of interest (radius > 0);
+ * the reference's whole-box mode (radius 0) stores a one-pixel bounding box
+ * (GroupwiseRegistration.cpp:113-121) and is refused. */
+typedef struct gbn_registration_params {
+  float W;          /* weight of each displacement step (normalised by the ROI area) */
+  int flagW;        /* adapt the weight: x1.2 after a decrease of the metric, /2 otherwise */
+  int radius;       /* radius of the circular region of interest, pixels */
+  int E;            /* spline order */
+  int Dp[2];        /* control-point spacing, pixels */
+  int nmax;         /* maximum gradient-descent iterations */
+  float et;         /* displacement-norm threshold */
+  float eh;         /* metric-variation threshold (fraction of the initial metric) */
+  float lambda[4];  /* smoothness weights: 1st spatial, 2nd spatial, 1st temporal, 2nd temporal */
+} gbn_registration_params;
+
+/* Sizes the registration derives from (N, F, params) (init(),
+ * GroupwiseRegistration.cpp:92-190): control points per side (the T arrays are
+ * [2][F][cp][cp]), the 1-based bounding box of the region of interest
+ * {first column, first row, last column, last row}, and its pixel count. */
+typedef struct gbn_registration_info {
+  int cp;
+  int bound_box[4];
+  int area;
+} gbn_registration_info;
+
+typedef struct gbn_registration_stats {
+  int iterations;  /* gradient-descent iterations run */
+  float H0;        /* metric of the unregistered frames */
+  float H;         /* metric after the last iteration */
+  float Wn;        /* final step weight */
+  float Tdif;      /* norm of the last displacement update */
+  int status;      /* 0, or 5: an interpolation corner left the image */
+} gbn_registration_stats;
+
+GBN_API int gbn_registration_info_get(int N, int F, const gbn_registration_params* params, gbn_registration_info* info);
+/* GroupwiseRegistration::launch (GroupwiseRegistration.cpp:550-618): modulus
+ * normalised to 500 (DataNormalization), then the gradient descent of
+ * optimizer() (groupwiseRegistration/optimizer.cpp) on the B-spline control
+ * displacements T.  d_images: [F][N][N] complex (the reconstruction to
+ * register).  d_T_init: [2][F][cp][cp] starting displacements, or NULL for
+ * zeros (the reference's TData on its first motion iteration).  Outputs, all
+ * device: d_T [2][F][cp][cp], d_xn the deformed mesh [2][F][N][N] (1-based,
+ * horizontal then vertical), d_xmesh the original mesh [2][N][N] (int,
+ * 1-based, as ArgumentsMotionCompensation::xData); d_xn, d_xmesh and
+ * info.bound_box are the inputs of gbn_problem_set_motion.  h_H (host, may be
+ * NULL): the metric per iteration, params->nmax + 1 floats.  Waits for
+ * completion. */
+GBN_API int gbn_registration_run(gbn_ctx* ctx, const float* d_images, int N, int F,
+                                 const gbn_registration_params* params, const float* d_T_init, float* d_T,
+                                 float* d_xn, int* d_xmesh, float* h_H, gbn_registration_stats* stats);
+
 /* One reconstruction into d_x ([F][H][W], the reference's output XData).
  * Runs asynchronously; when stats != NULL the call waits for completion and
  * fills *stats. */

@@ -50,6 +50,24 @@ class NestaStats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class RegistrationParams(C.Structure):
+    """gbn_registration_params (GroupwiseRegistration::InitParameters)."""
+    _fields_ = [("W", C.c_float), ("flagW", C.c_int), ("radius", C.c_int), ("E", C.c_int), ("Dp", C.c_int * 2),
+                ("nmax", C.c_int), ("et", C.c_float), ("eh", C.c_float), ("lambda_", C.c_float * 4)]
+
+
+class RegistrationInfo(C.Structure):
+    _fields_ = [("cp", C.c_int), ("bound_box", C.c_int * 4), ("area", C.c_int)]
+
+
+class RegistrationStats(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("H0", C.c_float), ("H", C.c_float), ("Wn", C.c_float),
+                ("Tdif", C.c_float), ("status", C.c_int)]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
 _vp = C.c_void_p
 _i = C.c_int
 _sz = C.c_size_t
@@ -101,6 +119,9 @@ SIGNATURES: dict[str, list] = {
     "gbn_copy_wait_compute": [_vp],
     "gbn_compute_wait_copy": [_vp],
     "gbn_op_motion": [_vp, _i, _vp, _vp, _vp, _vp, _vp, _i, _i, _i],
+    "gbn_registration_info_get": [_i, _i, C.POINTER(RegistrationParams), C.POINTER(RegistrationInfo)],
+    "gbn_registration_run": [_vp, _vp, _i, _i, C.POINTER(RegistrationParams), _vp, _vp, _vp, _vp, _vp,
+                             C.POINTER(RegistrationStats)],
     "gbn_nesta_run": [_vp, _vp, C.POINTER(NestaParams), _vp, C.POINTER(NestaStats)],
     "gbn_nesta_run_host": [_vp, _i, _i, _i, _i, _vp, _vp, _vp, C.POINTER(NestaParams), _vp,
                            C.POINTER(NestaStats)],

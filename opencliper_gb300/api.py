@@ -258,6 +258,43 @@ def op_motion(ctx: Context, direction: int, x: DeviceArray, out: DeviceArray, xn
          _ck(xn, np.float32), _ck(xmesh, np.int32), bb, W, H, F)
 
 
+def registration_params(W=1.0, flagW=True, radius=40, E=3, Dp=(4, 4), nmax=100, et=0.01, eh=0.005,
+                        lambda_=(0.0, 0.005, 0.0, 0.5)) -> "_abi.RegistrationParams":
+    """GroupwiseRegistration::InitParameters; defaults are tests/MRIRecon.cpp:121-129."""
+    return _abi.RegistrationParams(float(W), int(bool(flagW)), int(radius), int(E), (C.c_int * 2)(*map(int, Dp)),
+                                   int(nmax), float(et), float(eh), (C.c_float * 4)(*map(float, lambda_)))
+
+
+def registration_info(N: int, F: int, params) -> dict:
+    info = _abi.RegistrationInfo()
+    call("gbn_registration_info_get", int(N), int(F), C.byref(params), C.byref(info))
+    return dict(cp=info.cp, bound_box=list(info.bound_box), area=info.area)
+
+
+def registration(ctx: Context, images: DeviceArray, params, T_init: DeviceArray | None = None) -> dict:
+    """GroupwiseRegistration of images [F][N][N] complex (device).  Returns the
+    control displacements T [2][F][cp][cp], the deformed mesh xn [2][F][N][N],
+    the original mesh xmesh [2][N][N] (device arrays; the inputs of
+    Problem.set_motion with bound_box), the metric per iteration and stats."""
+    F, N, N2 = images.shape
+    if N != N2:
+        raise ValueError("square images only")
+    info = registration_info(N, F, params)
+    cp = info["cp"]
+    T = ctx.empty((2, F, cp, cp), np.float32)
+    xn = ctx.empty((2, F, N, N), np.float32)
+    xmesh = ctx.empty((2, N, N), np.int32)
+    H = np.zeros(params.nmax + 1, np.float32)
+    st = _abi.RegistrationStats()
+    call("gbn_registration_run", ctx.handle, _ck(images, np.complex64), N, F, C.byref(params),
+         None if T_init is None else _ck(T_init, np.float32), T.ptr, xn.ptr, xmesh.ptr,
+         H.ctypes.data, C.byref(st))
+    stats = st.as_dict()
+    stats["H_final"] = stats.pop("H")
+    return dict(T=T, xn=xn, xmesh=xmesh, bound_box=info["bound_box"], H=H[:stats["iterations"] + 1],
+                area=info["area"], cp=cp, **stats)
+
+
 def op_rss(ctx: Context, k: DeviceArray, out: DeviceArray) -> None:
     F, Cc, H, W = k.shape
     call("gbn_op_rss", ctx.handle, _ck(k, np.complex64), _ck(out, np.complex64), W, H, F, Cc)

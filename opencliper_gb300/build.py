@@ -28,6 +28,11 @@ NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "--expt-relaxed-constexpr", "-Xc
               "-Xcompiler", "-fvisibility=hidden", f"-I{INCLUDE}", f"-I{CSRC}"]
 
 
+# per-file flags: the registration rounds each product and sum separately, as
+# the reference's kernels and host code do (no FMA contraction, device or host)
+FILE_FLAGS = {"registration.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"]}
+
+
 def nvcc() -> str:
     for cand in (os.environ.get("NVCC"), shutil.which("nvcc"), "/usr/local/cuda/bin/nvcc"):
         if cand and Path(cand).exists():
@@ -54,7 +59,7 @@ def _compile(src: Path, force: bool, verbose: bool) -> Path:
     obj = BUILD / (src.stem + ".o")
     if not force and not _stale(obj, [src] + _headers()):
         return obj
-    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, "-c", str(src), "-o", str(obj)]
+    cmd = [nvcc(), *ARCH, *NVCC_FLAGS, *FILE_FLAGS.get(src.name, []), "-c", str(src), "-o", str(obj)]
     if verbose:
         print(" ".join(cmd), flush=True)
     r = subprocess.run(cmd, capture_output=True, text=True)

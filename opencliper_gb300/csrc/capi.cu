@@ -36,6 +36,9 @@ int batch_groups(gbn_batch*, int*, int*);
 int motion_set(gbn_problem*, const float*, const int*, const int*);
 int problem_fit_rows(gbn_problem*, int, int*);
 int motion_op(gbn_ctx*, int, const float2*, float2*, const float*, const int*, const int*, int, int, int);
+int registration_info(int, int, const gbn_registration_params*, gbn_registration_info*);
+int registration_run(gbn_ctx*, const float2*, int, int, const gbn_registration_params*, const float*, float*, float*,
+                     int*, float*, gbn_registration_stats*);
 int autotune(gbn_ctx*, int, const int*, const char*);
 int autotune_load(gbn_ctx*, const char*);
 void tuning_for(gbn_ctx*, int, int, int, int, int*, int*);
@@ -607,6 +610,19 @@ int gbn_op_motion(gbn_ctx* ctx, int direction, const float* d_in, float* d_out, 
   const int rc = check_dims(W, H, F, 1);
   if (rc) return rc;
   return motion_op(ctx, direction, CF2(d_in), F2(d_out), d_xn, d_xmesh, bound_box, W, H, F);
+}
+
+int gbn_registration_info_get(int N, int F, const gbn_registration_params* params, gbn_registration_info* info) {
+  return registration_info(N, F, params, info);
+}
+
+int gbn_registration_run(gbn_ctx* ctx, const float* d_images, int N, int F, const gbn_registration_params* params,
+                         const float* d_T_init, float* d_T, float* d_xn, int* d_xmesh, float* h_H,
+                         gbn_registration_stats* stats) {
+  CHECK_CTX(ctx);
+  NONNULL2(d_images, d_T);
+  if (!d_xn) return set_error(GBN_ERR_INVALID, "null deformed-mesh output");
+  return registration_run(ctx, CF2(d_images), N, F, params, d_T_init, d_T, d_xn, d_xmesh, h_H, stats);
 }
 
 int gbn_problem_set_motion(gbn_problem* p, const float* d_xn, const int* d_xmesh, const int bound_box[4]) {

@@ -26,8 +26,8 @@
 // its tTV sums), k_mc_adjoint (M^T g), and the adjoint column pass, which
 // takes M^T g as its tTV gradient; all chained by programmatic dependent
 // launch.  The power method ||U|| cannot use the plain form's per-pixel
-// recurrence (M mixes pixels), so it runs myNormest's loop literally with one
-// host read of the norms per step.
+// recurrence (M mixes pixels), so it runs myNormest's loop step for step on
+// the device (k_ne_*), the host reading the stop flag once per eight steps.
 //
 // Bounds: the reference reads the image at the interpolation corners without
 // checks; here a corner or target outside the image skips that pixel and sets

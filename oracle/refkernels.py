@@ -171,7 +171,8 @@ class RegParams(C.Structure):
 
 
 def registration(images: np.ndarray, radius: int = 40, E: int = 3, Dp=(4, 4), nmax: int = 100, et: float = 0.01,
-                 eh: float = 0.005, lambda_=(0.0, 0.005, 0.0, 0.5), W: float = 1.0, flagW: bool = True) -> dict:
+                 eh: float = 0.005, lambda_=(0.0, 0.005, 0.0, 0.5), W: float = 1.0, flagW: bool = True,
+                 T_init: np.ndarray | None = None) -> dict:
     """GroupwiseRegistration (init, creabspline, optimizer) on the host with the
     reference's kernels; defaults are tests/MRIRecon.cpp:121-129.  images:
     [F][N][N] complex.  Returns T [C1][C0... as the reference stores it, flat],
@@ -181,7 +182,7 @@ def registration(images: np.ndarray, radius: int = 40, E: int = 3, Dp=(4, 4), nm
     assert N == N2, "square images only (the reference's mask and grid assume it)"
     L = lib()
     L.ref_registration.argtypes = [C.c_void_p, C.c_int, C.c_int, C.POINTER(RegParams), C.c_void_p, C.c_void_p,
-                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t]
+                                   C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_size_t, C.c_void_p]
     L.ref_registration.restype = C.c_int
     prm = RegParams(float(W), int(flagW), int(radius), int(E), int(Dp[0]), int(Dp[1]), int(nmax), float(et),
                     float(eh), (C.c_float * 4)(*[float(v) for v in lambda_]))
@@ -192,8 +193,10 @@ def registration(images: np.ndarray, radius: int = 40, E: int = 3, Dp=(4, 4), nm
     bb = np.zeros(4, np.int32)
     info = np.zeros(4, np.int32)
     wn = np.zeros(1, np.float32)
+    Tin = None if T_init is None else np.ascontiguousarray(T_init, np.float32).reshape(-1)
     rc = L.ref_registration(x.ctypes.data, N, F, C.byref(prm), T.ctypes.data, xn.ctypes.data, H.ctypes.data,
-                            bb.ctypes.data, info.ctypes.data, wn.ctypes.data, cap)
+                            bb.ctypes.data, info.ctypes.data, wn.ctypes.data, cap,
+                            None if Tin is None else Tin.ctypes.data)
     if rc != 0:
         raise ValueError("registration: unsupported geometry (grid or supports outside the image, N % 8, F < 3)")
     it, c0, c1, area = (int(v) for v in info)

@@ -146,11 +146,12 @@ extern "C" {
 // column fastest).  Outputs: T [C1 * C0 * F * 2] (the control-point
 // displacements), xn [N * N * F * 2] (the deformed mesh), H [nmax + 1] (the
 // metric per iteration), bb [4] (1-based bounding box), info [4] = {iterations,
-// C0 (= Cp0), C1 (= Cp1), areaX}, wn = the final weight.  Returns 0, or -1
+// C0 (= Cp0), C1 (= Cp1), areaX}, wn = the final weight.  T_init: starting
+// displacements in T's layout, or NULL for zeros.  Returns 0, or -1
 // when the control grid or its supports leave the image (the reference reads
 // outside its buffers there).
 int ref_registration(const float* images, int N, int F, const reg::Params* prm, float* T_out, float* xn_out,
-                     float* H_out, int* bb_out, int* info, float* wn_out, size_t T_cap) {
+                     float* H_out, int* bb_out, int* info, float* wn_out, size_t T_cap, const float* T_init) {
   using namespace reg;
   const cl_uint nROWS = N, nCOLS = N, nFRAMES = F, nt = 2;
   if (N % 8 != 0 || F < 3) return -1;  // frames contiguous at the device alignment; shiftTAux needs 3 frames
@@ -420,7 +421,9 @@ int ref_registration(const float* images, int N, int F, const reg::Params* prm, 
   }
 
   // ---- optimizer() (optimizer.cpp) ----
-  RD TData = make_rd1({Cp1, Cp0, nFRAMES, nt}, 4);  // InitZero: zeros
+  // optimizer(): the given TData (a later motion iteration), else InitZero
+  RD TData = make_rd1({Cp1, Cp0, nFRAMES, nt}, 4);
+  if (T_init) std::memcpy(TData.f(), T_init, TData.count() * 4);
   std::vector<float> Hdif(prm->nmax), Tdif(prm->nmax);
   auto initZero = [&](RD& d) {
     for (size_t i = 0; i < d.nd.size(); ++i) {
@@ -465,7 +468,7 @@ int ref_registration(const float* images, int N, int F, const reg::Params* prm, 
   const float p4 = HData.f()[0] * prm->eh;
   bool stop = false;
   iter = 1;
-  const float factor = 2.0f / nFRAMES;  // GradientMetric: factor = 2 / numFrames
+  const float factor = 2.0 / nFRAMES;  // GradientMetric::launch (GradientMetric.cpp:72)
   while (!stop) {
     initZero(TAuxData);
     transformationAuxL();

@@ -168,5 +168,11 @@ def test_oracle_reproduces_golden(name):
         assert rel_l2(R.coilsum(k), d["coilsum"]) < 1e-6
         assert np.array_equal(R.apply_mask(d["k"], d["mask"]), d["mask_k"])
         assert rel_l2(R.complex_abs2(k), d["abs2"]) < 1e-6 and rel_l2(R.complex_abs(x), d["abs"]) < 1e-6
+    elif kind == "registration":
+        from oracle import registration as RG
+        prm = {k[4:]: (tuple(d[k]) if d[k].ndim else d[k].item()) for k in d.files if k.startswith("prm_")}
+        r = RG.Registration(int(d["N"]), int(d["F"]), **prm).run(d["images"])
+        assert r["iterations"] == int(d["iterations"])
+        assert np.abs(r["T"] - d["T"]).max() <= 2e-6 * np.abs(d["T"]).max() + 1e-6
     else:
         raise AssertionError(kind)

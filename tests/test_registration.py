@@ -78,3 +78,38 @@ def test_geometry_and_descent(name):
     H = d["H"]
     assert H[-1] < H[0]
     assert len(H) == int(d["iterations"]) + 1
+
+
+@pytest.mark.parametrize("name", CASES)
+def test_restatement_matches_reference_kernels(name):
+    """oracle/registration.py (the algorithm per quantity, the reference's
+    regularisation gradient included) against the fixtures of the reference's
+    own kernels: same iterations and weight, T and xn to a few float ulps."""
+    from oracle import registration as RG
+    d = _load(name)
+    prm = _prm(d)
+    r = RG.Registration(int(d["N"]), int(d["F"]), **prm).run(d["images"])
+    assert r["iterations"] == int(d["iterations"])
+    assert r["Wn"] == pytest.approx(float(d["Wn"]), rel=1e-6)
+    scale = np.abs(d["T"]).max()
+    assert np.abs(r["T"] - d["T"]).max() <= 2e-6 * scale + 1e-6
+    assert np.abs(r["xn"] - d["xn"]).max() <= 2e-5
+    np.testing.assert_allclose(r["H"], d["H"], rtol=2e-6)
+
+
+def test_restatement_starting_displacements():
+    """A later motion iteration starts from the previous T (optimizer.cpp:
+    TData given): the restatement against the reference kernels, both
+    continuing from the T of a first run."""
+    if K.build() is None or not K.available():
+        pytest.skip("reference kernel sources unavailable")
+    from oracle import registration as RG
+    d = _load(CASES[0])
+    prm = dict(_prm(d), nmax=3)
+    T0 = d["T"]
+    ref = K.registration(d["images"], T_init=T0, **prm)
+    r = RG.Registration(int(d["N"]), int(d["F"]), **prm).run(d["images"], T_init=T0)
+    assert r["iterations"] == ref["iterations"]
+    assert np.abs(r["T"] - ref["T"]).max() <= 2e-6 * np.abs(ref["T"]).max() + 1e-6
+    np.testing.assert_allclose(r["H"], ref["H"], rtol=2e-6)
+    assert r["H"][0] == ref["H"][0] == d["H"][0]  # the metric restarts from the unregistered frames
