@@ -471,6 +471,74 @@ def motion_form(ctx, stream, args=None) -> dict:
     return res
 
 
+def registration_form(ctx, stream, args=None) -> dict:
+    """GroupwiseRegistration (the motion estimation of MRIRecon's motion loop,
+    MRIRecon.cpp:246-282) on the plain reconstruction of the headline problem,
+    with the reference's defaults (tests/MRIRecon.cpp:121-129: radius-40 region
+    of interest, cubic splines every 4 px, up to 100 iterations); then one
+    motion-compensated solve with the estimated mesh.  Events on the library's
+    stream around each registration.  cpu_port: oracle/registration.py (numpy,
+    one core) on the same frames for two iterations, per iteration."""
+    import time
+
+    import opencliper_gb300 as g
+    from opencliper_gb300 import synth
+    reps = args.form_reps if args is not None else 3
+    W, H, F, Cc, Rr = WL["W"], WL["H"], WL["F"], WL["C"], WL["R"]
+    p = synth.make_problem_device(ctx, W, H, F, Cc, Rr, seed=11)
+    prob = g.Problem(ctx, p.y, p.S, p.mask)
+    x = ctx.empty((F, H, W), np.complex64)
+    prm = g.nesta_params(**NESTA)
+    prob.run(prm, x)
+    x0 = x.get()
+    rp = g.registration_params()
+    times, r = [], None
+    for k in range(reps + 1):
+        if r is not None:
+            for key in ("T", "xn", "xmesh"):
+                r[key].free()
+        a, c = torch_events()
+        a.record(stream)
+        r = g.registration(ctx, x, rp)
+        c.record(stream)
+        stream.synchronize()
+        if k > 0 or reps == 0:
+            times.append(a.elapsed_time(c))
+    ms = sum(times) / len(times)
+    res = {"workload": f"{W}x{H} x {F} frames (the plain reconstruction of the headline problem), radius-40 "
+                       "region of interest, cubic B-splines every 4 px, nmax 100, lambda {0, 0.005, 0, 0.5}",
+           "unit": "registrations/s",
+           "gpu": {"value": round(1e3 / ms, 3), "ms_per_registration": round(ms, 3),
+                   "iterations": int(r["iterations"]), "ms_per_iteration": round(ms / max(1, r["iterations"]), 4),
+                   "kernel_launches_per_iteration": 5, "control_points": int(r["cp"]) ** 2,
+                   "H0": float(r["H0"]), "H": float(r["H_final"]), "status": int(r["status"])}}
+    # the motion-compensated solve with the estimated mesh
+    prob.set_motion(r["xn"], r["xmesh"], r["bound_box"])
+    x.set(x0)
+    a, c = torch_events()
+    a.record(stream)
+    st = prob.run(prm, x, stats=True)
+    c.record(stream)
+    stream.synchronize()
+    mc_ms = a.elapsed_time(c)
+    res["motion_iteration"] = {"registration_plus_mc_solve_ms": round(ms + mc_ms, 3), "mc_solve_ms": round(mc_ms, 3),
+                               "status": int(st["status"])}
+    if args is None or not getattr(args, "no_cpu_baseline", False):
+        from oracle import registration as RG
+        t0 = time.perf_counter()
+        cpu = RG.Registration(W, F, nmax=2).run(x0)
+        dt = time.perf_counter() - t0
+        per_it = dt / max(1, cpu["iterations"])
+        res["cpu_port"] = {"kind": "port", "cores": 1, "sample": f"{cpu['iterations']} iterations, same frames",
+                           "s_per_iteration": round(per_it, 3),
+                           "projected_s_per_registration": round(per_it * max(1, r["iterations"]), 2)}
+        res["speedup_per_iteration_vs_cpu_port"] = round(per_it * 1e3 / (ms / max(1, r["iterations"])), 1)
+    prob.close()
+    for arr in (p.y, p.S, p.mask, x, r["T"], r["xn"], r["xmesh"]):
+        arr.free()
+    return res
+
+
 def run_forms_only(args, dist: Dist) -> dict | None:
     """The forms named by --forms on their own, without the headline timing."""
     import torch
@@ -681,7 +749,8 @@ def stress_form(ctx, stream, args=None) -> dict:
 
 
 # the batched form autotunes its shapes into the context: forms that should see the defaults run first
-FORMS = (("mixed", mixed_forms), ("motion", motion_form), ("batched", batched_form), ("stress", stress_form))
+FORMS = (("mixed", mixed_forms), ("motion", motion_form), ("registration", registration_form),
+         ("batched", batched_form), ("stress", stress_form))
 
 
 def run_reference(args, dist: Dist) -> dict | None:
@@ -714,9 +783,9 @@ def main(argv=None) -> int:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU restatement timing")
     ap.add_argument("--no-forms", action="store_true", help="skip the mixed, batched and motion form measurements")
-    ap.add_argument("--forms", default="mixed,batched,motion",
-                    help="comma-separated forms to measure after the headline (mixed, batched, motion; "
-                         "stress, the 256-reconstruction ~150 GB batch, only when named)")
+    ap.add_argument("--forms", default="mixed,batched,motion,registration",
+                    help="comma-separated forms to measure after the headline (mixed, batched, motion, "
+                         "registration; stress, the 256-reconstruction ~150 GB batch, only when named)")
     ap.add_argument("--forms-only", action="store_true",
                     help="measure only the forms named by --forms (no headline line; for profiling)")
     ap.add_argument("--form-reps", type=int, default=3, help="timed repetitions of the motion form")

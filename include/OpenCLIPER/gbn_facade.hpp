@@ -796,7 +796,15 @@ class ArrayData : public Data {
     if (host.empty()) throw std::invalid_argument("ArrayData: empty array");
     upload(host.data());
   }
+  /// n elements on the device, contents undefined (filled by a process)
+  ArrayData(const std::shared_ptr<CLapp>& app, size_t n) : Data(app, sizeof(T) * n), n_(n) {
+    if (n == 0) throw std::invalid_argument("ArrayData: empty array");
+  }
   size_t size() const { return n_; }
+  void device2Host(std::vector<T>& host) const {
+    host.resize(n_);
+    download(host.data());
+  }
 
  private:
   size_t n_;
@@ -864,6 +872,108 @@ class MotionCompensationProcess : public Process {
 };
 using MotionCompensation = MotionCompensationProcess<GBN_TTV_FORWARD>;
 using AdjointMotionCompensation = MotionCompensationProcess<GBN_TTV_ADJOINT>;
+
+/// GroupwiseRegistration (src/processes/GroupwiseRegistration.cpp:79-618,
+/// groupwiseRegistration/optimizer.cpp; parameters GroupwiseRegistration.hpp:
+/// 145-168): estimates the frames' motion of an XData [F][N][N] and fills
+/// ArgumentsMotionCompensation for MotionCompensation and NestaUp.  As in the
+/// reference, LaunchParameters::TData (the previous motion iteration's
+/// argsMC->TData) starts the descent when given.  Errors are thrown as
+/// std::invalid_argument (bad parameters, unsupported geometry) or CLError.
+class GroupwiseRegistration : public Process {
+ public:
+  struct InitParameters : Process::InitParameters {
+    float W;
+    bool flagW;
+    unsigned int radius;
+    unsigned int E;
+    int* Dp;
+    unsigned int nmax;
+    float et;
+    float eh;
+    std::vector<float> lambda;
+    InitParameters(float W, bool flagW, unsigned int radius, unsigned int E, int* Dp, unsigned int nmax, float et,
+                   float eh, const std::vector<float>& lambda)
+        : W(W), flagW(flagW), radius(radius), E(E), Dp(Dp), nmax(nmax), et(et), eh(eh), lambda(lambda) {}
+  };
+  struct LaunchParameters : Process::LaunchParameters {
+    ArgumentsMotionCompensation* argsMC;
+    std::shared_ptr<Data> TData;
+    int currentMotionIter;
+    LaunchParameters(ArgumentsMotionCompensation* args, const std::shared_ptr<Data>& TData, int iter)
+        : argsMC(args), TData(TData), currentMotionIter(iter) {}
+  };
+  void init() override {
+    Process::init();
+    auto ip = std::dynamic_pointer_cast<InitParameters>(ip_);
+    if (!ip) throw std::invalid_argument("GroupwiseRegistration::init: missing InitParameters");
+    if (!ip->Dp) throw std::invalid_argument("GroupwiseRegistration::init: null Dp");
+    if (ip->lambda.size() != 4) throw std::invalid_argument("GroupwiseRegistration::init: lambda must hold 4 weights");
+    auto in = inputAs<XData>("GroupwiseRegistration::init");
+    if (in->width() != in->height())
+      throw std::invalid_argument("GroupwiseRegistration::init: square frames only (the reference's mask is N x N)");
+    prm_.W = ip->W;
+    prm_.flagW = ip->flagW ? 1 : 0;
+    prm_.radius = int(ip->radius);
+    prm_.E = int(ip->E);
+    prm_.Dp[0] = ip->Dp[0];
+    prm_.Dp[1] = ip->Dp[1];
+    prm_.nmax = int(ip->nmax);
+    prm_.et = ip->et;
+    prm_.eh = ip->eh;
+    for (int i = 0; i < 4; ++i) prm_.lambda[i] = ip->lambda[size_t(i)];
+    N_ = int(in->width());
+    F_ = int(in->getDynDimsTotalSize());
+    const int rc = gbn_registration_info_get(N_, F_, &prm_, &info_);
+    if (rc == GBN_ERR_INVALID || rc == GBN_ERR_UNSUPPORTED)
+      throw std::invalid_argument(std::string("GroupwiseRegistration::init: ") + gbn_last_error_string());
+    gbnCheck(rc, "GroupwiseRegistration::init");
+    bb_.assign(info_.bound_box, info_.bound_box + 4);
+    inited_ = true;
+  }
+  void launch() override {
+    const char* who = "GroupwiseRegistration::launch";
+    if (!inited_) throw std::invalid_argument(std::string(who) + ": init() not called");
+    auto lp = std::dynamic_pointer_cast<LaunchParameters>(lp_);
+    if (!lp || !lp->argsMC) throw std::invalid_argument(std::string(who) + ": missing LaunchParameters or argsMC");
+    auto in = inputAs<XData>(who);
+    ArgumentsMotionCompensation* a = lp->argsMC;
+    const size_t nT = size_t(2) * F_ * info_.cp * info_.cp;
+    const float* Tin = nullptr;
+    if (lp->TData) {
+      if (lp->TData->getBytes() != nT * sizeof(float))
+        throw std::invalid_argument(std::string(who) + ": TData must be float [2][F][cp][cp]");
+      Tin = static_cast<const float*>(lp->TData->getDevicePtr());
+    }
+    // fresh outputs: the motion-compensated solve may still hold the previous ones
+    auto T = std::make_shared<ArrayData<float>>(app_, nT);
+    auto xn = std::make_shared<ArrayData<float>>(app_, size_t(2) * F_ * N_ * N_);
+    auto xm = std::make_shared<ArrayData<int>>(app_, size_t(2) * N_ * N_);
+    H_.assign(size_t(prm_.nmax) + 1, 0.f);
+    gbnCheck(gbn_registration_run(ctx(), static_cast<const float*>(in->getDevicePtr()), N_, F_, &prm_, Tin,
+                                  static_cast<float*>(T->getDevicePtr()), static_cast<float*>(xn->getDevicePtr()),
+                                  static_cast<int*>(xm->getDevicePtr()), H_.data(), &stats_),
+             who);
+    H_.resize(size_t(stats_.iterations) + 1);
+    a->TData = T;
+    a->xnData = xn;
+    a->xData = xm;
+    a->bound_box = &bb_;
+  }
+  const gbn_registration_stats& getStats() const { return stats_; }
+  /// the metric per iteration (HData of the reference)
+  const std::vector<float>& getMetric() const { return H_; }
+  int getControlPoints() const { return info_.cp; }
+
+ private:
+  gbn_registration_params prm_{};
+  gbn_registration_info info_{};
+  gbn_registration_stats stats_{};
+  std::vector<dimIndexType> bb_;
+  std::vector<float> H_;
+  int N_ = 0, F_ = 0;
+  bool inited_ = false;
+};
 
 /// NestaUp (src/processes/nesta/NestaUp.cpp:81-910, NestaUp.hpp:67-83).
 class NestaUp : public Process {

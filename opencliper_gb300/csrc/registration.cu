@@ -23,13 +23,15 @@
 // non-zero, with the reference's pairing of spline factors (optimizer.cl:
 // 746-830) and at the transposed pixel (optimizer.cl:138-187).
 //
-// Here one iteration is four kernels:
-//   k_reg_grad    one thread per (d, frame, control point): the support sum in
-//                 the reference's order (auxiliarCost, cost6DReduction, cost6D)
+// Here one iteration is five kernels:
+//   k_reg_grad    one thread per (d, frame, control point, column offset): the
+//                 support sums in the reference's order (auxiliarCost,
+//                 cost6DReduction, cost6D)
 //   k_reg_update  one thread per (d, control point): the frame mean,
 //                 Dif = Wn (dH - mean), T -= Dif (updateTransformation)
-//   k_reg_pixels  one thread per bounding-box pixel: xn for every frame, the
-//                 warped frames, their mean, V, dy, dx, the smoothness terms
+//   k_reg_warp    one thread per (bounding-box pixel, frame): xn, the warped
+//                 frame, dx, the smoothness terms
+//   k_reg_metric  one thread per bounding-box pixel: the frames' mean, V, dy
 //   k_reg_cost    one CTA: H, |Dif|, evolution() and stopCondition() on the
 //                 device
 // iterations are enqueued eight at a time; the host reads the stop flag once
@@ -165,6 +167,7 @@ int reg_geometry(int N, int F, const gbn_registration_params* p, RegGeom* g) {
     pu[n] = c + float(g->Dp * (n - C0));
     g->sup[n] = int(std::ceil(pu[n] - std::ceil(rp))) - 1;
   }
+  if (g->dp > kRegNT) return set_error(GBN_ERR_UNSUPPORTED, "registration: control spacing too large");
   if (g->sup.front() < 0 || g->sup.back() + g->dp > N)
     return set_error(GBN_ERR_UNSUPPORTED, "registration: the control grid's supports leave the image");
   for (int q = g->box0; q <= g->box1; ++q)
@@ -245,6 +248,7 @@ struct RegArgs {
   float* dx;   // [2][F][N][N] (box pixels)
   float* Vm;   // [N][N] metric (box pixels)
   float* Sm;   // [N][N] smoothness term at the transposed pixel
+  float* sterm;  // [F][2][7][box pixels] weighted squared smoothness terms
   float* H;    // [nmax + 1]
   RegState* st;
 };
@@ -263,14 +267,16 @@ __device__ __forceinline__ bool reg_bilinear(const float* __restrict__ img, int 
   return true;
 }
 
-// xn for bounding-box pixel (row, col), every frame; warped frames, their
-// mean, V, dy, dx; the smoothness terms when enabled
-__global__ void __launch_bounds__(kRegNT) k_reg_pixels(RegArgs a) {
+// one thread per (bounding-box pixel, frame): xn, the warped frame, dx; the
+// smoothness terms of that frame when enabled (7 per direction d, each already
+// weighted and squared as sumLambdaMetric adds it)
+__global__ void __launch_bounds__(kRegNT) k_reg_warp(RegArgs a) {
   if (a.st->done) return;
   const int L = a.box1 - a.box0 + 1;
   const int q = blockIdx.x * kRegNT + threadIdx.x;
-  if (q >= L * L) return;
-  const int row = a.box0 + q / L, col = a.box0 + q % L;
+  if (q >= L * L * a.F) return;
+  const int pix = q % (L * L), f = q / (L * L);
+  const int row = a.box0 + pix / L, col = a.box0 + pix % L;
   const int N = a.N, F = a.F, Cp = a.Cp, E1 = a.E1;
   const size_t NN = size_t(N) * N, p = size_t(row) * N + col;
   const int r0 = a.cr[row], c0 = a.cr[col];
@@ -280,38 +286,93 @@ __global__ void __launch_bounds__(kRegNT) k_reg_pixels(RegArgs a) {
     br[s] = s < E1 ? a.B[size_t(row) * E1 + s] : 0.f;
     bc[s] = s < E1 ? a.B[size_t(col) * E1 + s] : 0.f;
   }
-  float sum = 0.f;
-  bool ok = true;
-  for (int f = 0; f < F; ++f) {
-    float u[2];
+  float u[2];
 #pragma unroll
-    for (int d = 0; d < 2; ++d) {
-      const float* Tf = a.T + (size_t(d) * F + f) * Cp * Cp;
-      float acc = 0.f;
-      for (int aa = 0; aa < E1; ++aa)    // column spline outer, row spline inner (Deformation)
-        for (int b = 0; b < E1; ++b) acc = acc + Tf[(r0 + b) * Cp + c0 + aa] * (br[b] * bc[aa]);
-      u[d] = acc;
-    }
-    const float xh = u[0] + float(col + 1), xv = u[1] + float(row + 1);
-    a.xn[size_t(f) * NN + p] = xh;
-    a.xn[(size_t(F) + f) * NN + p] = xv;
-    float iw, g1, g2;
-    bool okf = reg_bilinear(a.d1 + f * NN, N, xh, xv, &g1) && reg_bilinear(a.d2 + f * NN, N, xh, xv, &g2);
-    if (a.warp)
-      okf = okf && reg_bilinear(a.I + f * NN, N, xh, xv, &iw);
-    else
-      iw = a.I[f * NN + p];
-    if (!okf) {
-      ok = false;
-      iw = a.I[f * NN + p];
-      g1 = g2 = 0.f;
-    }
-    a.dx[size_t(f) * NN + p] = g1;
-    a.dx[(size_t(F) + f) * NN + p] = g2;
-    a.Iw[f * NN + p] = iw;
-    sum = sum + iw;
+  for (int d = 0; d < 2; ++d) {
+    const float* Tf = a.T + (size_t(d) * F + f) * Cp * Cp;
+    float acc = 0.f;
+    for (int aa = 0; aa < E1; ++aa)    // column spline outer, row spline inner (Deformation)
+      for (int b = 0; b < E1; ++b) acc = acc + Tf[(r0 + b) * Cp + c0 + aa] * (br[b] * bc[aa]);
+    u[d] = acc;
   }
-  if (!ok) atomicExch(&a.st->status, kStatusRange);
+  const float xh = u[0] + float(col + 1), xv = u[1] + float(row + 1);
+  a.xn[size_t(f) * NN + p] = xh;
+  a.xn[(size_t(F) + f) * NN + p] = xv;
+  float iw, g1, g2;
+  bool ok = reg_bilinear(a.d1 + f * NN, N, xh, xv, &g1) && reg_bilinear(a.d2 + f * NN, N, xh, xv, &g2);
+  if (a.warp)
+    ok = ok && reg_bilinear(a.I + f * NN, N, xh, xv, &iw);
+  else
+    iw = a.I[f * NN + p];
+  if (!ok) {
+    atomicExch(&a.st->status, kStatusRange);
+    iw = a.I[f * NN + p];
+    g1 = g2 = 0.f;
+  }
+  a.dx[size_t(f) * NN + p] = g1;
+  a.dx[(size_t(F) + f) * NN + p] = g2;
+  a.Iw[f * NN + p] = iw;
+  if (!a.smooth) return;
+  // smoothness terms (Regularization): at the pixel with row `row` and column
+  // `col` the reference pairs the row-direction control offset n with the
+  // column pixel's spline and the column offset m with the row pixel's
+  const float* B0 = a.B;
+  const float* B1 = a.B + size_t(N) * E1;
+  const float* B2 = a.B + 2 * size_t(N) * E1;
+  const float Dp = a.Dp, Dp2 = a.Dp * a.Dp;
+  const float l0 = a.lam[0], l1 = a.lam[1], l2 = a.lam[2], l3 = a.lam[3];
+  for (int d = 0; d < 2; ++d) {
+    const float* T0 = a.T + (size_t(d) * F + f) * Cp * Cp;
+    const float* T1 = a.T + (size_t(d) * F + (f + F - 1) % F) * Cp * Cp;
+    const float* T2 = a.T + (size_t(d) * F + (f + F - 2) % F) * Cp * Cp;
+    float ax0 = 0.f, ax1 = 0.f, bx0 = 0.f, bx1 = 0.f, axy = 0.f, at = 0.f, at2 = 0.f;
+    for (int mm = 0; mm < E1; ++mm)
+      for (int n = 0; n < E1; ++n) {
+        const float t0 = T0[(r0 + n) * Cp + c0 + mm];
+        const float cB = B0[size_t(col) * E1 + n], cB1 = B1[size_t(col) * E1 + n], cB2 = B2[size_t(col) * E1 + n];
+        const float rB = B0[size_t(row) * E1 + mm], rB1 = B1[size_t(row) * E1 + mm], rB2 = B2[size_t(row) * E1 + mm];
+        ax0 = ax0 + t0 * (Dp * (cB * rB1));
+        bx0 = bx0 + t0 * (Dp2 * (cB * rB2));
+        ax1 = ax1 + t0 * (Dp * (cB1 * rB));
+        bx1 = bx1 + t0 * (Dp2 * (cB2 * rB));
+      }
+    for (int mm = 0; mm < E1; ++mm)
+      for (int n = 0; n < E1; ++n)
+        axy = axy + T0[(r0 + n) * Cp + c0 + mm] * (Dp2 * (B1[size_t(col) * E1 + n] * B1[size_t(row) * E1 + mm]));
+    for (int mm = 0; mm < E1; ++mm)
+      for (int n = 0; n < E1; ++n) {
+        const int ti = (r0 + n) * Cp + c0 + mm;
+        const float bb = B0[size_t(col) * E1 + n] * B0[size_t(row) * E1 + mm];
+        at = at + (T0[ti] - T1[ti]) * bb;
+        at2 = float(double(at2) + (double(T0[ti]) - 2.0 * double(T1[ti]) + double(T2[ti])) * double(bb));
+      }
+    if (d == 0) ax0 = ax0 + 1.f;
+    else ax1 = ax1 + 1.f;
+    float* o = a.sterm + (size_t(f) * 2 + d) * 7 * L * L + pix;
+    const size_t st = size_t(L) * L;
+    o[0 * st] = (l1 * 2) * (axy * axy);
+    o[1 * st] = l3 * (at2 * at2);
+    o[2 * st] = l2 * (at * at);
+    o[3 * st] = l0 * (ax0 * ax0);
+    o[4 * st] = l1 * (bx0 * bx0);
+    o[5 * st] = l0 * (ax1 * ax1);
+    o[6 * st] = l1 * (bx1 * bx1);
+  }
+}
+
+// one thread per bounding-box pixel: the frames' mean, V, dy (metric,
+// gradientMetric); the smoothness sum in sumLambdaMetric's order, added at
+// the transposed pixel
+__global__ void __launch_bounds__(kRegNT) k_reg_metric(RegArgs a) {
+  if (a.st->done) return;
+  const int L = a.box1 - a.box0 + 1;
+  const int pix = blockIdx.x * kRegNT + threadIdx.x;
+  if (pix >= L * L) return;
+  const int row = a.box0 + pix / L, col = a.box0 + pix % L;
+  const int N = a.N, F = a.F;
+  const size_t NN = size_t(N) * N, p = size_t(row) * N + col;
+  float sum = 0.f;
+  for (int f = 0; f < F; ++f) sum = sum + a.Iw[f * NN + p];
   const float mean = sum / F;
   float V = 0.f;
   for (int f = 0; f < F; ++f) {
@@ -321,88 +382,57 @@ __global__ void __launch_bounds__(kRegNT) k_reg_pixels(RegArgs a) {
   }
   a.Vm[p] = V / F;
   if (!a.smooth) return;
-  // smoothness terms (Regularization then sumLambdaMetric): at the pixel with
-  // row `row` and column `col` the reference pairs the row-direction control
-  // offset n with the column pixel's spline and the column offset m with the
-  // row pixel's, and adds the sum at the transposed position
-  const float* B0 = a.B;
-  const float* B1 = a.B + size_t(N) * E1;
-  const float* B2 = a.B + 2 * size_t(N) * E1;
-  const float Dp = a.Dp, Dp2 = a.Dp * a.Dp;
-  const float l0 = a.lam[0], l1 = a.lam[1], l2 = a.lam[2], l3 = a.lam[3];
+  const size_t st = size_t(L) * L;
   float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f;
-  for (int f = 0; f < F; ++f) {
+  for (int f = 0; f < F; ++f)
     for (int d = 0; d < 2; ++d) {
-      const float* T0 = a.T + (size_t(d) * F + f) * Cp * Cp;
-      const float* T1 = a.T + (size_t(d) * F + (f + F - 1) % F) * Cp * Cp;
-      const float* T2 = a.T + (size_t(d) * F + (f + F - 2) % F) * Cp * Cp;
-      float ax0 = 0.f, ax1 = 0.f, bx0 = 0.f, bx1 = 0.f, axy = 0.f, at = 0.f, at2 = 0.f;
-      for (int mm = 0; mm < E1; ++mm)
-        for (int n = 0; n < E1; ++n) {
-          const int ti = (r0 + n) * Cp + c0 + mm;
-          const float t0 = T0[ti];
-          const float cB = B0[size_t(col) * E1 + n], cB1 = B1[size_t(col) * E1 + n], cB2 = B2[size_t(col) * E1 + n];
-          const float rB = B0[size_t(row) * E1 + mm], rB1 = B1[size_t(row) * E1 + mm], rB2 = B2[size_t(row) * E1 + mm];
-          ax0 = ax0 + t0 * (Dp * (cB * rB1));
-          bx0 = bx0 + t0 * (Dp2 * (cB * rB2));
-          ax1 = ax1 + t0 * (Dp * (cB1 * rB));
-          bx1 = bx1 + t0 * (Dp2 * (cB2 * rB));
-        }
-      for (int mm = 0; mm < E1; ++mm)
-        for (int n = 0; n < E1; ++n) {
-          const int ti = (r0 + n) * Cp + c0 + mm;
-          axy = axy + T0[ti] * (Dp2 * (B1[size_t(col) * E1 + n] * B1[size_t(row) * E1 + mm]));
-        }
-      for (int mm = 0; mm < E1; ++mm)
-        for (int n = 0; n < E1; ++n) {
-          const int ti = (r0 + n) * Cp + c0 + mm;
-          const float bb = B0[size_t(col) * E1 + n] * B0[size_t(row) * E1 + mm];
-          at = at + (T0[ti] - T1[ti]) * bb;
-          at2 = float(double(at2) + (double(T0[ti]) - 2.0 * double(T1[ti]) + double(T2[ti])) * double(bb));
-        }
-      if (d == 0) ax0 = ax0 + 1.f;
-      else ax1 = ax1 + 1.f;
-      // sumLambdaMetric's order: per frame and d, the xy, t2, t terms, then x and x2 per direction
-      s2 = s2 + (l1 * 2) * (axy * axy);
-      s3 = s3 + l3 * (at2 * at2);
-      s4 = s4 + l2 * (at * at);
-      s0 = s0 + l0 * (ax0 * ax0);
-      s1 = s1 + l1 * (bx0 * bx0);
-      s0 = s0 + l0 * (ax1 * ax1);
-      s1 = s1 + l1 * (bx1 * bx1);
+      const float* o = a.sterm + (size_t(f) * 2 + d) * 7 * st + pix;
+      s2 = s2 + o[0 * st];
+      s3 = s3 + o[1 * st];
+      s4 = s4 + o[2 * st];
+      s0 = s0 + o[3 * st];
+      s1 = s1 + o[4 * st];
+      s0 = s0 + o[5 * st];
+      s1 = s1 + o[6 * st];
     }
-  }
   a.Sm[size_t(col) * N + row] = (((s0 + s1) + s2) + s3) + s4;
 }
 
-// dH for (d, frame, control point): the support sum in the reference's order
-// (auxiliarCost, then cost6DReduction over one offset, cost6D over the other),
-// masked by the region of interest at the transposed pixel
+// dH for (d, frame, control point) in the reference's order (auxiliarCost,
+// then cost6DReduction over the row offsets i of each column offset j, then
+// cost6D over j): one thread per column offset sums its i in order, one
+// thread per group then sums the column sums in order.  The region of interest
+// is read at the pixel itself: the reference reads it at the transposed
+// pixel, and the centred circle is symmetric.
 __global__ void __launch_bounds__(kRegNT) k_reg_grad(RegArgs a) {
   if (a.st->done) return;
+  __shared__ float cs[kRegNT];
   const int Cp = a.Cp, F = a.F, N = a.N, dp = a.dp;
-  const int q = blockIdx.x * kRegNT + threadIdx.x;
-  if (q >= 2 * F * Cp * Cp) return;
-  const int lc = q % Cp, kr = (q / Cp) % Cp, f = (q / (Cp * Cp)) % F, d = q / (Cp * Cp * F);
-  const size_t NN = size_t(N) * N;
-  const int R = a.sup[kr], C = a.sup[lc];
-  const float* dyf = a.dy + f * NN;
-  const float* dxf = a.dx + (size_t(d) * F + f) * NN;
-  const float* S = a.S;
-  float acc = 0.f;
-  for (int j = 0; j < dp; ++j) {
-    float cs = 0.f;
+  const int gpc = kRegNT / dp;  // groups per CTA
+  const int t = threadIdx.x, gl = t / dp, j = t % dp;
+  const int grp = blockIdx.x * gpc + gl;
+  const bool live = gl < gpc && grp < 2 * F * Cp * Cp;
+  if (live) {
+    const int lc = grp % Cp, kr = (grp / Cp) % Cp, f = (grp / (Cp * Cp)) % F, d = grp / (Cp * Cp * F);
+    const size_t NN = size_t(N) * N;
+    const int R = a.sup[kr], C = a.sup[lc];
+    const float* dyf = a.dy + f * NN;
+    const float* dxf = a.dx + (size_t(d) * F + f) * NN;
+    const float Sj = a.S[j];
+    float c = 0.f;
     for (int i = 0; i < dp; ++i) {
-      // terms outside the region of interest add exactly zero: skipped
-      const float m = a.roi[size_t(C + j) * N + R + i];
-      if (m != 0.f) {
-        const size_t p = size_t(R + i) * N + C + j;
-        cs = cs + ((dyf[p] * dxf[p]) * (S[i] * S[j])) * m;
-      }
+      const size_t p = size_t(R + i) * N + C + j;
+      const float m = a.roi[p];
+      if (m != 0.f) c = c + ((dyf[p] * dxf[p]) * (a.S[i] * Sj)) * m;  // terms outside add exactly zero
     }
-    acc = acc + cs;
+    cs[t] = c;
   }
-  a.dH[q] = acc;
+  __syncthreads();
+  if (live && j == 0) {
+    float acc = 0.f;
+    for (int jj = 0; jj < dp; ++jj) acc = acc + cs[gl * dp + jj];
+    a.dH[grp] = acc;
+  }
 }
 
 // updateTransformation (optimizer.cl:519-563): T -= Wn (dH - mean_f dH)
@@ -527,7 +557,7 @@ int registration_run(gbn_ctx* ctx, const float2* images, int N, int F, const gbn
     }
   } free_all{owned};
   RegArgs a{};
-  float *I, *d1, *d2, *roi, *B, *S, *dH, *Dif, *Iw, *dy, *dx, *Vm, *Sm, *H;
+  float *I, *d1, *d2, *roi, *B, *S, *dH, *Dif, *Iw, *dy, *dx, *Vm, *Sm, *H, *sterm = nullptr;
   int *cr, *sup;
   unsigned* maxbits;
   RegState* st;
@@ -536,6 +566,8 @@ int registration_run(gbn_ctx* ctx, const float2* images, int N, int F, const gbn
       (rc = dalloc(&dH, nT, owned)) || (rc = dalloc(&Dif, nT, owned)) || (rc = dalloc(&Iw, X, owned)) ||
       (rc = dalloc(&dy, X, owned)) || (rc = dalloc(&dx, 2 * X, owned)) || (rc = dalloc(&Vm, NN, owned)) ||
       (rc = dalloc(&Sm, NN, owned)) || (rc = dalloc(&H, size_t(prm->nmax) + 1, owned)) ||
+      (g.sum_lambda != 0 &&
+       (rc = dalloc(&sterm, size_t(F) * 14 * (g.box1 - g.box0 + 1) * (g.box1 - g.box0 + 1), owned))) ||
       (rc = dalloc(&cr, size_t(N), owned)) ||
       (rc = dalloc(&sup, size_t(g.Cp), owned)) || (rc = dalloc(&maxbits, 1, owned)) || (rc = dalloc(&st, 1, owned)))
     return rc;
@@ -591,31 +623,58 @@ int registration_run(gbn_ctx* ctx, const float2* images, int N, int F, const gbn
   a.dx = dx;
   a.Vm = Vm;
   a.Sm = Sm;
+  a.sterm = sterm;
   a.H = H;
   a.st = st;
   const int L = g.box1 - g.box0 + 1;
   const int gp = (L * L + kRegNT - 1) / kRegNT;
-  const int gg = (2 * F * g.Cp * g.Cp + kRegNT - 1) / kRegNT;
+  const int gw = (L * L * F + kRegNT - 1) / kRegNT;
+  const int gpc = kRegNT / g.dp;
+  const int gg = (2 * F * g.Cp * g.Cp + gpc - 1) / gpc;
   const int gu = (2 * g.Cp * g.Cp + kRegNT - 1) / kRegNT;
   // the unregistered frames: metric H[0]; dx at the starting mesh (optimizer.cpp: InitIT, Metric, CostReduction)
-  k_reg_pixels<<<gp, kRegNT, 0, s>>>(a);
+  k_reg_warp<<<gw, kRegNT, 0, s>>>(a);
+  k_reg_metric<<<gp, kRegNT, 0, s>>>(a);
   k_reg_cost<<<1, 1024, 0, s>>>(a, 0, prm->et, prm->eh);
-  ctx->launches += 2;
+  ctx->launches += 3;
   a.warp = 1;
   a.smooth = g.sum_lambda != 0;
+  // chunks of iterations with one chunk of lookahead: while the GPU runs chunk
+  // c the host waits for chunk c-1's stop flag (copied to pinned memory behind
+  // it), so the queue never drains; after the stop, the chunk already queued
+  // returns at each kernel's entry
+  struct Pinned {
+    int* flag = nullptr;
+    cudaEvent_t ev[2] = {nullptr, nullptr};
+    ~Pinned() {
+      if (flag) cudaFreeHost(flag);
+      for (cudaEvent_t x : ev)
+        if (x) cudaEventDestroy(x);
+    }
+  } pin;
+  if ((e = cudaHostAlloc(&pin.flag, 2 * sizeof(int), cudaHostAllocDefault)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&pin.ev[0], cudaEventDisableTiming)) != cudaSuccess ||
+      (e = cudaEventCreateWithFlags(&pin.ev[1], cudaEventDisableTiming)) != cudaSuccess)
+    return cuda_status(e, "registration");
   RegState hs{};
-  for (int it = 1; it <= prm->nmax;) {
+  int chunk = 0;
+  for (int it = 1; it <= prm->nmax; ++chunk) {
     for (int k = 0; k < kRegChunk && it <= prm->nmax; ++k, ++it) {
       k_reg_grad<<<gg, kRegNT, 0, s>>>(a);
       k_reg_update<<<gu, kRegNT, 0, s>>>(a);
-      k_reg_pixels<<<gp, kRegNT, 0, s>>>(a);
+      k_reg_warp<<<gw, kRegNT, 0, s>>>(a);
+      k_reg_metric<<<gp, kRegNT, 0, s>>>(a);
       k_reg_cost<<<1, 1024, 0, s>>>(a, it, prm->et, prm->eh);
-      ctx->launches += 4;
+      ctx->launches += 5;
     }
-    if ((e = cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
-        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    if ((e = cudaMemcpyAsync(&pin.flag[chunk & 1], &st->done, sizeof(int), cudaMemcpyDeviceToHost, s)) !=
+            cudaSuccess ||
+        (e = cudaEventRecord(pin.ev[chunk & 1], s)) != cudaSuccess)
       return cuda_status(e, "registration");
-    if (hs.done) break;
+    if (chunk > 0) {
+      if ((e = cudaEventSynchronize(pin.ev[(chunk - 1) & 1])) != cudaSuccess) return cuda_status(e, "registration");
+      if (pin.flag[(chunk - 1) & 1]) break;
+    }
   }
   if ((e = cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_status(e, "registration");
   std::vector<float> hH(size_t(prm->nmax) + 1, 0.f);

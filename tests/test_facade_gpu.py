@@ -170,3 +170,40 @@ def test_facade_mat_files(ctx, tmp_path, mask_form):
     r64 = R.nesta(p.y, p.S, p.mask, prm, "f64")
     r32 = R.nesta(p.y, p.S, p.mask, prm, "f32")
     assert R.nrmse(nesta, r64.x) <= 2.0 * R.nrmse(r32.x, r64.x) + 5e-6
+
+
+def test_facade_registration_motion_loop(ctx, tmp_path, built_lib):
+    """GroupwiseRegistration through the C++ facade in MRIRecon's motion-loop
+    shape (tests/MRIRecon.cpp:204-282): two launches, the second started from
+    the first's TData, then MotionCompensation with the estimate.  Results
+    are the C ABI's bit for bit."""
+    cxx = shutil.which("g++")
+    if not cxx:
+        pytest.skip("g++ not available")
+    exe = tmp_path / "registration_facade"
+    libdir = os.path.join(ROOT, "opencliper_gb300")
+    subprocess.run([cxx, "-std=c++17", "-O2", "-Wall", "-pthread", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "tests", "cpp", "registration_facade.cpp"), "-L", libdir, "-lgbnesta",
+                    f"-Wl,-rpath,{libdir}", "-o", str(exe)], check=True)
+    N, F, radius, nmax = 64, 5, 14, 4
+    img = synth.phantom_series(N, N, F, np.random.default_rng(9)).astype(np.complex64)
+    np.array([N, F, radius, nmax], np.uint32).tofile(tmp_path / "dims.u32")
+    img.tofile(tmp_path / "x.c64")
+    subprocess.run([str(exe), str(tmp_path)], check=True)
+    prm = api.registration_params(W=0.05, radius=radius, nmax=nmax)
+    x = ctx.to_device(img)
+    r1 = api.registration(ctx, x, prm)
+    r2 = api.registration(ctx, x, prm, r1["T"])
+    cp = r1["cp"]
+    for k, r in ((1, r1), (2, r2)):
+        np.testing.assert_array_equal(np.fromfile(tmp_path / f"T{k}.f32", np.float32).reshape(2, F, cp, cp), r["T"].get())
+        np.testing.assert_array_equal(np.fromfile(tmp_path / f"xn{k}.f32", np.float32).reshape(2, F, N, N), r["xn"].get())
+        np.testing.assert_array_equal(np.fromfile(tmp_path / f"H{k}.f32", np.float32), r["H"])
+    np.testing.assert_array_equal(np.fromfile(tmp_path / "xmesh.i32", np.int32).reshape(2, N, N), r2["xmesh"].get())
+    assert np.fromfile(tmp_path / "bb.u32", np.uint32).tolist() == list(r2["bound_box"])
+    mc = ctx.empty((F, N, N), np.complex64)
+    api.op_motion(ctx, 1, x, mc, r2["xn"], r2["xmesh"], r2["bound_box"])  # forward (GBN_TTV_FORWARD)
+    np.testing.assert_array_equal(np.fromfile(tmp_path / "mc.c64", np.complex64).reshape(F, N, N), mc.get())
+    lines = (tmp_path / "stats.txt").read_text().split("\n")
+    assert lines[0].split()[1] == "0" and int(lines[0].split()[2]) == cp
+    assert lines[2] == "refused"

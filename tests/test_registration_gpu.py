@@ -22,13 +22,6 @@ pytestmark = pytest.mark.gpu
 CASES = [c[0] for c in make_golden.REG_CASES]
 
 
-@pytest.fixture(scope="module")
-def ctx():
-    c = api.Context(0)
-    yield c
-    c.close()
-
-
 def _load(name):
     return dict(np.load(os.path.join(HERE, "golden", name)))
 
