@@ -27,13 +27,14 @@
 //   k_reg_grad    one thread per (d, frame, control point, column offset): the
 //                 support sums in the reference's order (auxiliarCost,
 //                 cost6DReduction, cost6D)
-//   k_reg_update  one thread per (d, control point): the frame mean,
+//   k_reg_update  one thread per (d, frame, control point): the frame mean,
 //                 Dif = Wn (dH - mean), T -= Dif (updateTransformation)
 //   k_reg_warp    one thread per (bounding-box pixel, frame): xn, the warped
 //                 frame, dx, the smoothness terms
-//   k_reg_metric  one thread per bounding-box pixel: the frames' mean, V, dy
-//   k_reg_cost    one CTA: H, |Dif|, evolution() and stopCondition() on the
-//                 device
+//   k_reg_metric  one thread per bounding-box pixel: the frames' mean, V, dy,
+//                 per-CTA partial sums of the metric
+//   k_reg_cost    one CTA: H and |Dif| from the partial sums, evolution() and
+//                 stopCondition() on the device
 // iterations are enqueued eight at a time; the host reads the stop flag once
 // per chunk.  This file is compiled without FMA contraction, so products and
 // sums round separately as in the reference's kernels.
@@ -246,10 +247,10 @@ struct RegArgs {
   float* Iw;   // [F][N][N] (box pixels)
   float* dy;   // [F][N][N] (box pixels)
   float* dx;   // [2][F][N][N] (box pixels)
-  float* Vm;   // [N][N] metric (box pixels)
-  float* Sm;   // [N][N] smoothness term at the transposed pixel
   float* sterm;  // [F][2][7][box pixels] weighted squared smoothness terms
   float* H;    // [nmax + 1]
+  float* part_h;  // per-CTA partial sums of the metric (k_reg_metric)
+  float* part_d;  // per-CTA partial sums of Dif^2 (k_reg_update)
   RegState* st;
 };
 
@@ -360,42 +361,65 @@ __global__ void __launch_bounds__(kRegNT) k_reg_warp(RegArgs a) {
   }
 }
 
+// sum of one float per thread of a kRegNT-thread CTA in a fixed order (warp
+// shuffles, then the warps in order); the result in thread 0
+__device__ __forceinline__ float reg_block_sum(float v, float* sw) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if ((threadIdx.x & 31) == 0) sw[threadIdx.x >> 5] = v;
+  __syncthreads();
+  float t = 0.f;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < kRegNT / 32; ++w) t = t + sw[w];
+  return t;
+}
+
 // one thread per bounding-box pixel: the frames' mean, V, dy (metric,
-// gradientMetric); the smoothness sum in sumLambdaMetric's order, added at
-// the transposed pixel
+// gradientMetric); with the smoothness terms, V at this pixel gains the
+// smoothness sum of the transposed pixel in sumLambdaMetric's order (the
+// reference adds each pixel's sum at the transposed position); the CTA's
+// partial sum of V over the region of interest
 __global__ void __launch_bounds__(kRegNT) k_reg_metric(RegArgs a) {
   if (a.st->done) return;
+  __shared__ float sw[kRegNT / 32];
   const int L = a.box1 - a.box0 + 1;
   const int pix = blockIdx.x * kRegNT + threadIdx.x;
-  if (pix >= L * L) return;
-  const int row = a.box0 + pix / L, col = a.box0 + pix % L;
-  const int N = a.N, F = a.F;
-  const size_t NN = size_t(N) * N, p = size_t(row) * N + col;
-  float sum = 0.f;
-  for (int f = 0; f < F; ++f) sum = sum + a.Iw[f * NN + p];
-  const float mean = sum / F;
-  float V = 0.f;
-  for (int f = 0; f < F; ++f) {
-    const float dl = a.Iw[f * NN + p] - mean;
-    V = V + dl * dl;
-    a.dy[f * NN + p] = dl * a.fac;
-  }
-  a.Vm[p] = V / F;
-  if (!a.smooth) return;
-  const size_t st = size_t(L) * L;
-  float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f;
-  for (int f = 0; f < F; ++f)
-    for (int d = 0; d < 2; ++d) {
-      const float* o = a.sterm + (size_t(f) * 2 + d) * 7 * st + pix;
-      s2 = s2 + o[0 * st];
-      s3 = s3 + o[1 * st];
-      s4 = s4 + o[2 * st];
-      s0 = s0 + o[3 * st];
-      s1 = s1 + o[4 * st];
-      s0 = s0 + o[5 * st];
-      s1 = s1 + o[6 * st];
+  float h = 0.f;
+  if (pix < L * L) {
+    const int row = a.box0 + pix / L, col = a.box0 + pix % L;
+    const int N = a.N, F = a.F;
+    const size_t NN = size_t(N) * N, p = size_t(row) * N + col;
+    float sum = 0.f;
+    for (int f = 0; f < F; ++f) sum = sum + a.Iw[f * NN + p];
+    const float mean = sum / F;
+    float V = 0.f;
+    for (int f = 0; f < F; ++f) {
+      const float dl = a.Iw[f * NN + p] - mean;
+      V = V + dl * dl;
+      a.dy[f * NN + p] = dl * a.fac;
     }
-  a.Sm[size_t(col) * N + row] = (((s0 + s1) + s2) + s3) + s4;
+    V = V / F;
+    if (a.smooth) {
+      const size_t st = size_t(L) * L;
+      const int pt = (col - a.box0) * L + (row - a.box0);  // the transposed pixel
+      float s0 = 0.f, s1 = 0.f, s2 = 0.f, s3 = 0.f, s4 = 0.f;
+      for (int f = 0; f < F; ++f)
+        for (int d = 0; d < 2; ++d) {
+          const float* o = a.sterm + (size_t(f) * 2 + d) * 7 * st + pt;
+          s2 = s2 + o[0 * st];
+          s3 = s3 + o[1 * st];
+          s4 = s4 + o[2 * st];
+          s0 = s0 + o[3 * st];
+          s1 = s1 + o[4 * st];
+          s0 = s0 + o[5 * st];
+          s1 = s1 + o[6 * st];
+        }
+      V = V + ((((s0 + s1) + s2) + s3) + s4);
+    }
+    h = V * a.roi[p];
+  }
+  const float t = reg_block_sum(h, sw);
+  if (threadIdx.x == 0) a.part_h[blockIdx.x] = t;
 }
 
 // dH for (d, frame, control point) in the reference's order (auxiliarCost,
@@ -403,11 +427,14 @@ __global__ void __launch_bounds__(kRegNT) k_reg_metric(RegArgs a) {
 // cost6D over j): one thread per column offset sums its i in order, one
 // thread per group then sums the column sums in order.  The region of interest
 // is read at the pixel itself: the reference reads it at the transposed
-// pixel, and the centred circle is symmetric.
+// pixel, and the centred circle is symmetric.  Terms outside it add an exact
+// zero (dy and dx are zero outside the bounding box), so every term is
+// computed, without a branch.  DP > 0: the support width at compile time.
+template <int DP>
 __global__ void __launch_bounds__(kRegNT) k_reg_grad(RegArgs a) {
   if (a.st->done) return;
   __shared__ float cs[kRegNT];
-  const int Cp = a.Cp, F = a.F, N = a.N, dp = a.dp;
+  const int Cp = a.Cp, F = a.F, N = a.N, dp = DP > 0 ? DP : a.dp;
   const int gpc = kRegNT / dp;  // groups per CTA
   const int t = threadIdx.x, gl = t / dp, j = t % dp;
   const int grp = blockIdx.x * gpc + gl;
@@ -416,14 +443,26 @@ __global__ void __launch_bounds__(kRegNT) k_reg_grad(RegArgs a) {
     const int lc = grp % Cp, kr = (grp / Cp) % Cp, f = (grp / (Cp * Cp)) % F, d = grp / (Cp * Cp * F);
     const size_t NN = size_t(N) * N;
     const int R = a.sup[kr], C = a.sup[lc];
-    const float* dyf = a.dy + f * NN;
-    const float* dxf = a.dx + (size_t(d) * F + f) * NN;
+    const float* dyf = a.dy + f * NN + C + j;
+    const float* dxf = a.dx + (size_t(d) * F + f) * NN + C + j;
+    const float* roi = a.roi + C + j;
     const float Sj = a.S[j];
     float c = 0.f;
-    for (int i = 0; i < dp; ++i) {
-      const size_t p = size_t(R + i) * N + C + j;
-      const float m = a.roi[p];
-      if (m != 0.f) c = c + ((dyf[p] * dxf[p]) * (a.S[i] * Sj)) * m;  // terms outside add exactly zero
+    if constexpr (DP > 0) {
+      float v[DP], m[DP];
+#pragma unroll
+      for (int i = 0; i < DP; ++i) {
+        const size_t p = size_t(R + i) * N;
+        v[i] = dyf[p] * dxf[p];
+        m[i] = roi[p];
+      }
+#pragma unroll
+      for (int i = 0; i < DP; ++i) c = c + (v[i] * (a.S[i] * Sj)) * m[i];
+    } else {
+      for (int i = 0; i < dp; ++i) {
+        const size_t p = size_t(R + i) * N;
+        c = c + ((dyf[p] * dxf[p]) * (a.S[i] * Sj)) * roi[p];
+      }
     }
     cs[t] = c;
   }
@@ -435,62 +474,51 @@ __global__ void __launch_bounds__(kRegNT) k_reg_grad(RegArgs a) {
   }
 }
 
-// updateTransformation (optimizer.cl:519-563): T -= Wn (dH - mean_f dH)
+// updateTransformation (optimizer.cl:519-563): T -= Wn (dH - mean_f dH), one
+// thread per (d, frame, control point), each summing its control point's
+// frames in order for the mean; the CTA's partial sum of Dif^2
 __global__ void __launch_bounds__(kRegNT) k_reg_update(RegArgs a) {
   if (a.st->done) return;
-  const int Cp = a.Cp, F = a.F;
+  __shared__ float sw[kRegNT / 32];
+  const int Cp = a.Cp, F = a.F, CC = Cp * Cp;
   const int q = blockIdx.x * kRegNT + threadIdx.x;
-  if (q >= 2 * Cp * Cp) return;
-  const int cp = q % (Cp * Cp), d = q / (Cp * Cp);
-  const float Wn = a.st->Wn;
-  float sum = 0.f;
-  for (int f = 0; f < F; ++f) sum = sum + a.dH[(size_t(d) * F + f) * Cp * Cp + cp];
-  const float mean = sum / F;
-  for (int f = 0; f < F; ++f) {
-    const size_t i = (size_t(d) * F + f) * Cp * Cp + cp;
-    const float dif = Wn * (a.dH[i] - mean);
-    a.Dif[i] = dif;
-    a.T[i] = a.T[i] - dif;
+  float dd = 0.f;
+  if (q < 2 * F * CC) {
+    const int cp = q % CC, d = q / (CC * F);
+    float sum = 0.f;
+    for (int f = 0; f < F; ++f) sum = sum + a.dH[(size_t(d) * F + f) * CC + cp];
+    const float mean = sum / F;
+    const float dif = a.st->Wn * (a.dH[q] - mean);
+    a.Dif[q] = dif;
+    a.T[q] = a.T[q] - dif;
+    dd = dif * dif;
   }
+  const float t = reg_block_sum(dd, sw);
+  if (threadIdx.x == 0) a.part_d[blockIdx.x] = t;
 }
 
-// H over the region of interest (fixed-order: per-thread strided, then a
-// tree), |Dif|, evolution() and stopCondition() (GroupwiseRegistration.cpp:
-// 451-478, 533-545).  it == 0: the unregistered metric and the thresholds.
-__global__ void __launch_bounds__(1024) k_reg_cost(RegArgs a, int it, float et, float eh) {
+// H and |Dif| from the partial sums of k_reg_metric and k_reg_update (fixed
+// order), evolution() and stopCondition() (GroupwiseRegistration.cpp:451-478,
+// 533-545).  it == 0: the unregistered metric and the thresholds.
+__global__ void __launch_bounds__(kRegNT) k_reg_cost(RegArgs a, int it, int nh, int nd, float et, float eh) {
   RegState* st = a.st;
   if (st->done) return;
-  __shared__ float sh[1024], sd[1024];
-  const int N = a.N, L = a.box1 - a.box0 + 1;
+  __shared__ float sw[kRegNT / 32];
   float h = 0.f, dd = 0.f;
-  for (int q = threadIdx.x; q < L * L; q += 1024) {
-    const size_t p = size_t(a.box0 + q / L) * N + a.box0 + q % L;
-    const float V = a.smooth ? a.Vm[p] + a.Sm[p] : a.Vm[p];
-    h = h + V * a.roi[p];
-  }
-  if (it > 0) {
-    const int n = 2 * a.F * a.Cp * a.Cp;
-    for (int q = threadIdx.x; q < n; q += 1024) dd = dd + a.Dif[q] * a.Dif[q];
-  }
-  sh[threadIdx.x] = h;
-  sd[threadIdx.x] = dd;
+  for (int q = threadIdx.x; q < nh; q += kRegNT) h = h + a.part_h[q];
+  if (it > 0)
+    for (int q = threadIdx.x; q < nd; q += kRegNT) dd = dd + a.part_d[q];
+  const float H = reg_block_sum(h, sw);
   __syncthreads();
-  for (int o = 512; o > 0; o >>= 1) {
-    if (threadIdx.x < o) {
-      sh[threadIdx.x] = sh[threadIdx.x] + sh[threadIdx.x + o];
-      sd[threadIdx.x] = sd[threadIdx.x] + sd[threadIdx.x + o];
-    }
-    __syncthreads();
-  }
+  const float D = reg_block_sum(dd, sw);
   if (threadIdx.x != 0) return;
-  const float H = sh[0];
   a.H[it] = H;
   if (it == 0) {
     st->p2 = et * float(a.F * 2);
     st->p4 = H * eh;
     return;
   }
-  const float Tdif = sqrtf(sd[0]);
+  const float Tdif = sqrtf(D);
   const float Hdif = a.H[it - 1] - H;
   if (st->flagW) st->Wn = Hdif > 0 ? float(double(st->Wn) * 1.2) : st->Wn / 2;
   st->Tdif = Tdif;
@@ -557,15 +585,17 @@ int registration_run(gbn_ctx* ctx, const float2* images, int N, int F, const gbn
     }
   } free_all{owned};
   RegArgs a{};
-  float *I, *d1, *d2, *roi, *B, *S, *dH, *Dif, *Iw, *dy, *dx, *Vm, *Sm, *H, *sterm = nullptr;
+  float *I, *d1, *d2, *roi, *B, *S, *dH, *Dif, *Iw, *dy, *dx, *H, *part_h, *part_d, *sterm = nullptr;
   int *cr, *sup;
   unsigned* maxbits;
   RegState* st;
   if ((rc = dalloc(&I, X, owned)) || (rc = dalloc(&d1, X, owned)) || (rc = dalloc(&d2, X, owned)) ||
       (rc = dalloc(&roi, NN, owned)) || (rc = dalloc(&B, g.B.size(), owned)) || (rc = dalloc(&S, g.S.size(), owned)) ||
       (rc = dalloc(&dH, nT, owned)) || (rc = dalloc(&Dif, nT, owned)) || (rc = dalloc(&Iw, X, owned)) ||
-      (rc = dalloc(&dy, X, owned)) || (rc = dalloc(&dx, 2 * X, owned)) || (rc = dalloc(&Vm, NN, owned)) ||
-      (rc = dalloc(&Sm, NN, owned)) || (rc = dalloc(&H, size_t(prm->nmax) + 1, owned)) ||
+      (rc = dalloc(&dy, X, owned)) || (rc = dalloc(&dx, 2 * X, owned)) ||
+      (rc = dalloc(&H, size_t(prm->nmax) + 1, owned)) ||
+      (rc = dalloc(&part_h, size_t(g.box1 - g.box0 + 1) * (g.box1 - g.box0 + 1) / kRegNT + 1, owned)) ||
+      (rc = dalloc(&part_d, nT / kRegNT + 1, owned)) ||
       (g.sum_lambda != 0 &&
        (rc = dalloc(&sterm, size_t(F) * 14 * (g.box1 - g.box0 + 1) * (g.box1 - g.box0 + 1), owned))) ||
       (rc = dalloc(&cr, size_t(N), owned)) ||
@@ -582,7 +612,10 @@ int registration_run(gbn_ctx* ctx, const float2* images, int N, int F, const gbn
   if (e == cudaSuccess) e = cudaMemcpyAsync(sup, g.sup.data(), g.Cp * sizeof(int), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(st, &h0, sizeof(h0), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemsetAsync(maxbits, 0, sizeof(unsigned), s);
-  if (e == cudaSuccess) e = cudaMemsetAsync(Sm, 0, NN * sizeof(float), s);
+  // the gradient reads dy and dx over whole supports, outside the bounding box
+  // times a zero mask: zero there
+  if (e == cudaSuccess) e = cudaMemsetAsync(dy, 0, X * sizeof(float), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(dx, 0, 2 * X * sizeof(float), s);
   if (e == cudaSuccess)
     e = T_init ? cudaMemcpyAsync(T_out, T_init, nT * sizeof(float), cudaMemcpyDeviceToDevice, s)
                : cudaMemsetAsync(T_out, 0, nT * sizeof(float), s);
@@ -621,21 +654,21 @@ int registration_run(gbn_ctx* ctx, const float2* images, int N, int F, const gbn
   a.Iw = Iw;
   a.dy = dy;
   a.dx = dx;
-  a.Vm = Vm;
-  a.Sm = Sm;
   a.sterm = sterm;
   a.H = H;
+  a.part_h = part_h;
+  a.part_d = part_d;
   a.st = st;
   const int L = g.box1 - g.box0 + 1;
   const int gp = (L * L + kRegNT - 1) / kRegNT;
   const int gw = (L * L * F + kRegNT - 1) / kRegNT;
   const int gpc = kRegNT / g.dp;
   const int gg = (2 * F * g.Cp * g.Cp + gpc - 1) / gpc;
-  const int gu = (2 * g.Cp * g.Cp + kRegNT - 1) / kRegNT;
+  const int gu = int((nT + kRegNT - 1) / kRegNT);
   // the unregistered frames: metric H[0]; dx at the starting mesh (optimizer.cpp: InitIT, Metric, CostReduction)
   k_reg_warp<<<gw, kRegNT, 0, s>>>(a);
   k_reg_metric<<<gp, kRegNT, 0, s>>>(a);
-  k_reg_cost<<<1, 1024, 0, s>>>(a, 0, prm->et, prm->eh);
+  k_reg_cost<<<1, kRegNT, 0, s>>>(a, 0, gp, gu, prm->et, prm->eh);
   ctx->launches += 3;
   a.warp = 1;
   a.smooth = g.sum_lambda != 0;
@@ -660,11 +693,14 @@ int registration_run(gbn_ctx* ctx, const float2* images, int N, int F, const gbn
   int chunk = 0;
   for (int it = 1; it <= prm->nmax; ++chunk) {
     for (int k = 0; k < kRegChunk && it <= prm->nmax; ++k, ++it) {
-      k_reg_grad<<<gg, kRegNT, 0, s>>>(a);
+      if (g.dp == 17)
+        k_reg_grad<17><<<gg, kRegNT, 0, s>>>(a);
+      else
+        k_reg_grad<0><<<gg, kRegNT, 0, s>>>(a);
       k_reg_update<<<gu, kRegNT, 0, s>>>(a);
       k_reg_warp<<<gw, kRegNT, 0, s>>>(a);
       k_reg_metric<<<gp, kRegNT, 0, s>>>(a);
-      k_reg_cost<<<1, 1024, 0, s>>>(a, it, prm->et, prm->eh);
+      k_reg_cost<<<1, kRegNT, 0, s>>>(a, it, gp, gu, prm->et, prm->eh);
       ctx->launches += 5;
     }
     if ((e = cudaMemcpyAsync(&pin.flag[chunk & 1], &st->done, sizeof(int), cudaMemcpyDeviceToHost, s)) !=
