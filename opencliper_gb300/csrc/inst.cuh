@@ -15,23 +15,6 @@ inline void allow_smem(K kernel, int bytes, bool& done) {
   }
 }
 
-// launch with programmatic stream serialisation (the kernel may start while
-// its predecessor in the stream drains; it waits in-kernel before reading the
-// predecessor's results)
-template <typename... KArgs, typename... Args>
-inline void launch_pdl(void (*kernel)(KArgs...), dim3 grid, int threads, int smem, cudaStream_t s, Args... args) {
-  cudaLaunchConfig_t cfg = {};
-  cfg.gridDim = grid;
-  cfg.blockDim = dim3(threads);
-  cfg.dynamicSmemBytes = size_t(smem);
-  cfg.stream = s;
-  cudaLaunchAttribute at[1];
-  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-  at[0].val.programmaticStreamSerializationAllowed = 1;
-  cfg.attrs = at;
-  cfg.numAttrs = 1;
-  cudaLaunchKernelEx(&cfg, kernel, args...);
-}
 
 template <int L>
 struct Launchers {

@@ -21,6 +21,7 @@
 #include <cooperative_groups.h>
 
 #include "fft.cuh"
+#include "pdl.cuh"
 #include "types.h"
 
 namespace gbn {
@@ -30,13 +31,6 @@ constexpr int kColNT = 128;  // threads per CTA in the column kernels
 constexpr int kRowNT = 128;  // threads per CTA in the row kernels
 constexpr int kRowWarps = kRowNT / 32;
 
-// Programmatic dependent launch: a kernel launched with programmatic stream
-// serialisation may start while its predecessor drains.  Each fused kernel
-// reads nothing its predecessor writes before grid_dep_wait(), and releases
-// its successor only after that wait, so a successor's early part never runs
-// before the kernel two launches back has completed.
-__device__ __forceinline__ void grid_dep_wait() { asm volatile("griddepcontrol.wait;\n" ::: "memory"); }
-__device__ __forceinline__ void grid_dep_release() { asm volatile("griddepcontrol.launch_dependents;\n" ::: "memory"); }
 
 template <int L>
 struct Split {

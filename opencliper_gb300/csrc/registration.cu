@@ -693,6 +693,8 @@ int registration_run(gbn_ctx* ctx, const float2* images, int N, int F, const gbn
   int chunk = 0;
   for (int it = 1; it <= prm->nmax; ++chunk) {
     for (int k = 0; k < kRegChunk && it <= prm->nmax; ++k, ++it) {
+      // plain launches: chained by programmatic dependent launch these small
+      // grids ran slower (6.3 against 5.1 ms per registration at 256^2 x 20)
       if (g.dp == 17)
         k_reg_grad<17><<<gg, kRegNT, 0, s>>>(a);
       else
