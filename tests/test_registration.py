@@ -113,3 +113,30 @@ def test_restatement_starting_displacements():
     assert np.abs(r["T"] - ref["T"]).max() <= 2e-6 * np.abs(ref["T"]).max() + 1e-6
     np.testing.assert_allclose(r["H"], ref["H"], rtol=2e-6)
     assert r["H"][0] == ref["H"][0] == d["H"][0]  # the metric restarts from the unregistered frames
+
+
+@pytest.mark.parametrize("N,F,radius", [(64, 4, 12), (64, 5, 14), (96, 6, 20), (256, 20, 40), (128, 3, 30)])
+def test_library_geometry_matches_restatement(built_lib, N, F, radius):
+    """gbn_registration_info_get (host code of the library, no GPU needed):
+    control grid, bounding box and region-of-interest area as the restatement
+    derives them from init() and creabspline()."""
+    from opencliper_gb300 import api
+    from oracle import registration as RG
+    info = api.registration_info(N, F, api.registration_params(radius=radius))
+    g = RG.Geometry(N, F, radius)
+    assert info["cp"] == g.Cp
+    assert info["bound_box"] == g.bb
+    assert info["area"] == g.areaX
+
+
+@pytest.mark.parametrize("over,code", [(dict(radius=0), -2), (dict(E=2), -2), (dict(Dp=(4, 3)), -2),
+                                       (dict(nmax=0), -1), (dict(radius=31), -2)])
+def test_library_refuses_geometry(built_lib, over, code):
+    """Refusals, without a GPU: the whole-box region (degenerate in the
+    reference), other spline orders, unequal spacing, nmax 0, and a grid whose
+    supports leave a 64 x 64 image."""
+    from opencliper_gb300 import api
+    from opencliper_gb300._abi import GbnError
+    with pytest.raises(GbnError) as e:
+        api.registration_info(64, 4, api.registration_params(**over))
+    assert e.value.code == code
