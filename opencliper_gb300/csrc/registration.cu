@@ -622,6 +622,17 @@ int registration_run(gbn_ctx* ctx, const float2* images, int N, int F, const gbn
   if (e != cudaSuccess) return cuda_status(e, "registration setup");
   const int gx = int(std::min<size_t>((X + kRegNT - 1) / kRegNT, size_t(ctx->nsm) * 8));
   k_reg_absmax<<<gx, kRegNT, 0, s>>>(images, X, maxbits);
+  {
+    // DataNormalization divides by the largest modulus: frames that are all
+    // zero (or not finite) have no registration
+    unsigned mb = 0;
+    if ((e = cudaMemcpyAsync(&mb, maxbits, sizeof(mb), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+        (e = cudaStreamSynchronize(s)) != cudaSuccess)
+      return cuda_status(e, "registration");
+    float mx;
+    std::memcpy(&mx, &mb, sizeof(mx));
+    if (!(mx > 0.f) || !std::isfinite(mx)) return set_error(GBN_ERR_INVALID, "registration: frames all zero, or an infinite modulus");
+  }
   k_reg_normalize<<<gx, kRegNT, 0, s>>>(images, maxbits, I, X);
   k_reg_imgrad<<<gx, kRegNT, 0, s>>>(I, d1, d2, N, F);
   k_reg_mesh<<<int(std::min<size_t>((NN + kRegNT - 1) / kRegNT, size_t(ctx->nsm) * 8)), kRegNT, 0, s>>>(xmesh_out,

@@ -92,6 +92,12 @@ def test_refused(ctx, over, code):
     assert e.value.code == code
 
 
+def test_refuses_zero_frames(ctx):
+    with pytest.raises(GbnError) as e:
+        _run(ctx, np.zeros((4, 64, 64), np.complex64), api.registration_params(radius=12, nmax=2))
+    assert e.value.code == -1
+
+
 def test_refuses_two_frames(ctx):
     img = synth.phantom_series(64, 64, 2, np.random.default_rng(1))
     with pytest.raises(GbnError):
