@@ -251,6 +251,13 @@ int gbn_ctx_destroy(gbn_ctx* ctx) {
     cudaStreamSynchronize(ctx->copy_stream);
     cudaStreamDestroy(ctx->copy_stream);
   }
+  if (ctx->mc_stream) {
+    cudaStreamSynchronize(ctx->mc_stream);
+    cudaStreamDestroy(ctx->mc_stream);
+  }
+  if (ctx->ev_mc_x) cudaEventDestroy(ctx->ev_mc_x);
+  if (ctx->ev_mc_tv) cudaEventDestroy(ctx->ev_mc_tv);
+  if (ctx->ev_mc_adj) cudaEventDestroy(ctx->ev_mc_adj);
   if (ctx->ev_compute) cudaEventDestroy(ctx->ev_compute);
   if (ctx->ev_copy) cudaEventDestroy(ctx->ev_copy);
   delete ctx;
@@ -285,6 +292,7 @@ int gbn_ctx_sync(gbn_ctx* ctx) {
   CHECK_CTX(ctx);
   cudaError_t e = cudaStreamSynchronize(ctx->stream);
   if (e == cudaSuccess && ctx->copy_stream) e = cudaStreamSynchronize(ctx->copy_stream);
+  if (e == cudaSuccess && ctx->mc_stream) e = cudaStreamSynchronize(ctx->mc_stream);
   return cuda_status(e, "stream synchronize");
 }
 

@@ -18,6 +18,10 @@ struct gbn_ctx {
   cudaStream_t stream = nullptr;
   cudaStream_t copy_stream = nullptr;  // host->device prefetches (created on first use)
   cudaEvent_t ev_compute = nullptr, ev_copy = nullptr;  // ordering points between the two streams
+  // side stream of the motion-compensated solve: M^T runs beside the forward
+  // and row passes (created on first use)
+  cudaStream_t mc_stream = nullptr;
+  cudaEvent_t ev_mc_x = nullptr, ev_mc_tv = nullptr, ev_mc_adj = nullptr;
   bool own_stream = true;
   int nsm = 0;
   std::map<int, float2*> tw;          // device twiddle tables, one per supported length

@@ -24,8 +24,9 @@
 // Huber normalisation, g = D^T u and the objective's partial sums), the fused
 // forward column and row passes as in the plain form (the forward pass skips
 // its tTV sums), k_mc_adjoint (M^T g), and the adjoint column pass, which
-// takes M^T g as its tTV gradient; all chained by programmatic dependent
-// launch.  The power method ||U|| cannot use the plain form's per-pixel
+// takes M^T g as its tTV gradient.  k_mc_tv and k_mc_adjoint run on a side
+// stream beside the forward column pass; events order them after the
+// previous iterate and before the row and adjoint column passes.  The power method ||U|| cannot use the plain form's per-pixel
 // recurrence (M mixes pixels), so it runs myNormest's loop step for step on
 // the device (k_ne_*), the host reading the stop flag once per eight steps.
 //
@@ -934,17 +935,32 @@ int nesta_run_mc(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, floa
   ctx->launches += launch_maxima(ctx, P, x_out, P->mc_xw, s);
   if ((rc = mc_normest(ctx, P, s)) != GBN_OK) return rc;
   ctx->launches += launch_setup(P, s);
+  // k_mc_tv and M^T g run on the side stream beside the forward pass: k_mc_tv
+  // waits for the iterate (the previous adjoint column pass), the row pass
+  // waits for k_mc_tv's objective sums, the adjoint column pass for M^T g
+  cudaError_t se = cudaSuccess;
+  if (!ctx->mc_stream) {
+    se = cudaStreamCreateWithFlags(&ctx->mc_stream, cudaStreamNonBlocking);
+    if (se == cudaSuccess) se = cudaEventCreateWithFlags(&ctx->ev_mc_x, cudaEventDisableTiming);
+    if (se == cudaSuccess) se = cudaEventCreateWithFlags(&ctx->ev_mc_tv, cudaEventDisableTiming);
+    if (se == cudaSuccess) se = cudaEventCreateWithFlags(&ctx->ev_mc_adj, cudaEventDisableTiming);
+    if (se != cudaSuccess) return cuda_status(se, "motion-compensated side stream");
+  }
+  cudaStream_t aux = ctx->mc_stream;
   for (unsigned nl = 1; nl <= prm->maxIntIter; ++nl) {
     ctx->launches += launch_outer_begin(ctx, P, int(nl), x_out, s);
     for (unsigned it = 0; it < prm->maxIter; ++it) {
       const float2* xk = (it & 1) ? P->xk1 : P->xk0;
-      launch_pdl(k_mc_tv, gtv, kNT, 0, s, xk, P->mc_xn, static_cast<const int*>(t->inv), r,
-                 static_cast<const NestaDevState*>(P->st), P->mc_g, t->tvpart, W, H, F, &P->st->status);
+      cudaEventRecord(ctx->ev_mc_x, s);
+      cudaStreamWaitEvent(aux, ctx->ev_mc_x, 0);
+      k_mc_tv<<<gtv, kNT, 0, aux>>>(xk, P->mc_xn, t->inv, r, P->st, P->mc_g, t->tvpart, W, H, F, &P->st->status);
+      cudaEventRecord(ctx->ev_mc_tv, aux);
+      k_mc_adjoint<<<gadj, kNT, 0, aux>>>(P->mc_g, P->mc_gm, t->off, t->key, t->srcmap, t->wts, r, W, H, F, 0);
+      cudaEventRecord(ctx->ev_mc_adj, aux);
       kh->fwd_cols(tab, bm, int(it), cpb, g1, s);
+      cudaStreamWaitEvent(s, ctx->ev_mc_tv, 0);
       kw->rows(tab, bm, int(it), true, g2, s);
-      launch_pdl(k_mc_adjoint, dim3(gadj), kNT, 0, s, static_cast<const float2*>(P->mc_g), P->mc_gm,
-                 static_cast<const int*>(t->off), static_cast<const int*>(t->key), static_cast<const int*>(t->srcmap),
-                 static_cast<const float2*>(t->wts), r, W, H, F, 1);
+      cudaStreamWaitEvent(s, ctx->ev_mc_adj, 0);
       kh->inv_cols(tab, bm, int(it), true, g3, s);
       ctx->launches += 5;
     }
