@@ -87,6 +87,8 @@ REG_CASES = [
     # a weight of at least 1 makes sumLambda() non-zero, so the smoothness terms enter the metric
     ("registration_64x5_lambda.npz", 64, 5, 22, dict(radius=14, nmax=5, W=0.05, lambda_=(0.01, 0.02, 0.1, 1.5))),
     ("registration_96x6_circle.npz", 96, 6, 23, dict(radius=20, nmax=4, W=0.2, flagW=False)),
+    # stopCondition fires before nmax: |Dif| < et 2F and a metric change below eh H0 at iteration 4
+    ("registration_64x4_stop.npz", 64, 4, 24, dict(radius=12, nmax=12, W=0.05, et=0.5, eh=0.05)),
 ]
 
 

@@ -173,6 +173,6 @@ def test_oracle_reproduces_golden(name):
         prm = {k[4:]: (tuple(d[k]) if d[k].ndim else d[k].item()) for k in d.files if k.startswith("prm_")}
         r = RG.Registration(int(d["N"]), int(d["F"]), **prm).run(d["images"])
         assert r["iterations"] == int(d["iterations"])
-        assert np.abs(r["T"] - d["T"]).max() <= 2e-6 * np.abs(d["T"]).max() + 1e-6
+        assert np.abs(r["T"] - d["T"]).max() <= 5e-6 * np.abs(d["T"]).max() + 1e-6
     else:
         raise AssertionError(kind)
