@@ -122,3 +122,22 @@ def test_feeds_motion_compensated_solve(ctx):
     st1 = prob.run(prm, x)
     assert st1["status"] == 0
     assert np.isfinite(x.get()).all()
+
+
+def test_full_size_against_restatement(ctx):
+    """The reference's default configuration at the MRIRecon size (256 x 256,
+    20 frames, radius 40, 23 x 23 control points): two iterations against the
+    restatement (seconds of numpy), then the full 100-iteration run's
+    properties: status 0, the metric falls overall, T and xn finite."""
+    from oracle import registration as RG
+    img = synth.phantom_series(256, 256, 20, np.random.default_rng(41))
+    kw = dict(nmax=2)
+    ref = RG.Registration(256, 20, **kw).run(img)
+    r = _run(ctx, img, api.registration_params(**kw))
+    assert r["iterations"] == ref["iterations"] == 2
+    assert np.abs(r["T"] - ref["T"]).max() <= 1e-5 * np.abs(ref["T"]).max() + 1e-6
+    np.testing.assert_allclose(r["H"], ref["H"], rtol=1e-5)
+    full = _run(ctx, img, api.registration_params())
+    assert full["status"] == 0 and full["cp"] == 23
+    assert full["H"][-1] < full["H"][0]
+    assert np.isfinite(full["T"]).all() and np.isfinite(full["xn"]).all()
