@@ -255,6 +255,9 @@ int gbn_ctx_destroy(gbn_ctx* ctx) {
     cudaStreamSynchronize(ctx->mc_stream);
     cudaStreamDestroy(ctx->mc_stream);
   }
+  if (ctx->host_flags) cudaFreeHost(ctx->host_flags);
+  for (cudaEvent_t x : ctx->ev_flag)
+    if (x) cudaEventDestroy(x);
   if (ctx->ev_mc_x) cudaEventDestroy(ctx->ev_mc_x);
   if (ctx->ev_mc_tv) cudaEventDestroy(ctx->ev_mc_tv);
   if (ctx->ev_mc_adj) cudaEventDestroy(ctx->ev_mc_adj);
@@ -407,6 +410,14 @@ int gbn_download_async(gbn_ctx* ctx, void* h_dst, const void* d_src, size_t byte
 }
 
 namespace {
+int host_flags_ready(gbn_ctx* ctx) {
+  if (ctx->host_flags) return GBN_OK;
+  cudaError_t e = cudaHostAlloc(&ctx->host_flags, 2 * sizeof(int), cudaHostAllocDefault);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_flag[0], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_flag[1], cudaEventDisableTiming);
+  return cuda_status(e, "pinned stop flags");
+}
+
 int copy_stream_ready(gbn_ctx* ctx) {
   if (ctx->copy_stream) return GBN_OK;
   DeviceGuard guard(ctx->device);

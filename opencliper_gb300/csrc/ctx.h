@@ -22,6 +22,9 @@ struct gbn_ctx {
   // and row passes (created on first use)
   cudaStream_t mc_stream = nullptr;
   cudaEvent_t ev_mc_x = nullptr, ev_mc_tv = nullptr, ev_mc_adj = nullptr;
+  // pinned stop flags read one chunk behind the queue (device-driven loops)
+  int* host_flags = nullptr;
+  cudaEvent_t ev_flag[2] = {nullptr, nullptr};
   bool own_stream = true;
   int nsm = 0;
   std::map<int, float2*> tw;          // device twiddle tables, one per supported length
@@ -117,6 +120,8 @@ namespace gbn {
 
 // error helpers (capi.cu)
 int set_error(int code, const std::string& msg);
+// allocates ctx->host_flags (2 pinned ints) and ctx->ev_flag on first use
+int host_flags_ready(gbn_ctx* ctx);
 int cuda_status(cudaError_t e, const char* what);
 
 // twiddle table for length L (nullptr when unsupported)

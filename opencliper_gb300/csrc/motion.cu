@@ -818,8 +818,8 @@ void mc_apply(gbn_ctx* ctx, gbn_problem* P, const float2* in, float2* out, cudaS
 }
 
 // myNormest (NestaUp.cpp:291-439) with U = tTV M, U^T = M^T tTVadj: steps on
-// the device (k_ne_*), enqueued kNeChunk at a time; the host reads the stop
-// flag once per chunk
+// the device (k_ne_*), enqueued kNeChunk at a time; the host reads each
+// chunk's stop flag while the next chunk runs
 int mc_normest(gbn_ctx* ctx, gbn_problem* P, cudaStream_t s) {
   constexpr int kNeChunk = 8;
   const int W = P->W, H = P->H, F = P->F;
@@ -833,10 +833,14 @@ int mc_normest(gbn_ctx* ctx, gbn_problem* P, cudaStream_t s) {
   k_fill<<<grid1(ctx, X), kNT, 0, s>>>(x, X, make_float2(1.f, 0.f));
   k_ne_init<<<1, 1, 0, s>>>(P->mc_part, e_init, (unsigned long long)ctx->rand48);
   ctx->launches += 2;
-  struct {
-    int done, cnt, nrestart;
-  } h{0, 0, 0};
-  for (int steps = 0; steps < kNeMax;) {
+  // chunks of steps with one chunk of lookahead: the host waits for chunk
+  // c-1's stop flag (pinned, copied behind it) while chunk c runs
+  int rc = host_flags_ready(ctx);
+  if (rc != GBN_OK) return rc;
+  const McNe* dne = reinterpret_cast<const McNe*>(P->mc_part + 2 * 1024 + 2);
+  cudaError_t e = cudaSuccess;
+  int chunk = 0;
+  for (int steps = 0; steps < kNeMax; ++chunk) {
     for (int k = 0; k < kNeChunk && steps < kNeMax; ++k, ++steps) {
       k_ne_u<<<nblk, kNT, 0, s>>>(x, Sx, P->mc_xn, t->inv, r, W, H, F, P->mc_part, &P->st->status);
       k_ne_s1<<<1, kNT, 0, s>>>(P->mc_part, nblk);
@@ -846,14 +850,21 @@ int mc_normest(gbn_ctx* ctx, gbn_problem* P, cudaStream_t s) {
       k_ne_s2<<<1, kNT, 0, s>>>(P->mc_part, nblk);
       ctx->launches += 6;
     }
-    const McNe* dne = reinterpret_cast<const McNe*>(P->mc_part + 2 * 1024 + 2);
-    cudaError_t e = cudaMemcpyAsync(&h.done, &dne->done, sizeof(int), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&h.cnt, &dne->cnt, sizeof(int), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(&h.nrestart, &dne->nrestart, sizeof(int), cudaMemcpyDeviceToHost, s);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-    if (e != cudaSuccess) return cuda_status(e, "power method");
-    if (h.done) break;
+    if ((e = cudaMemcpyAsync(&ctx->host_flags[chunk & 1], &dne->done, sizeof(int), cudaMemcpyDeviceToHost, s)) !=
+            cudaSuccess ||
+        (e = cudaEventRecord(ctx->ev_flag[chunk & 1], s)) != cudaSuccess)
+      return cuda_status(e, "power method");
+    if (chunk > 0) {
+      if ((e = cudaEventSynchronize(ctx->ev_flag[(chunk - 1) & 1])) != cudaSuccess) return cuda_status(e, "power method");
+      if (ctx->host_flags[(chunk - 1) & 1]) break;
+    }
   }
+  struct {
+    int nrestart;
+  } h{0};
+  if ((e = cudaMemcpyAsync(&h.nrestart, &dne->nrestart, sizeof(int), cudaMemcpyDeviceToHost, s)) != cudaSuccess ||
+      (e = cudaStreamSynchronize(s)) != cudaSuccess)
+    return cuda_status(e, "power method");
   for (int i = 0; i < h.nrestart; ++i) ctx->rand48 = lcg48_apply(jX, ctx->rand48);
   k_ne_finish<<<1, 1, 0, s>>>(P->mc_part, P->st);
   ctx->launches += 1;

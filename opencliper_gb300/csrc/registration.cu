@@ -687,19 +687,7 @@ int registration_run(gbn_ctx* ctx, const float2* images, int N, int F, const gbn
   // c the host waits for chunk c-1's stop flag (copied to pinned memory behind
   // it), so the queue never drains; after the stop, the chunk already queued
   // returns at each kernel's entry
-  struct Pinned {
-    int* flag = nullptr;
-    cudaEvent_t ev[2] = {nullptr, nullptr};
-    ~Pinned() {
-      if (flag) cudaFreeHost(flag);
-      for (cudaEvent_t x : ev)
-        if (x) cudaEventDestroy(x);
-    }
-  } pin;
-  if ((e = cudaHostAlloc(&pin.flag, 2 * sizeof(int), cudaHostAllocDefault)) != cudaSuccess ||
-      (e = cudaEventCreateWithFlags(&pin.ev[0], cudaEventDisableTiming)) != cudaSuccess ||
-      (e = cudaEventCreateWithFlags(&pin.ev[1], cudaEventDisableTiming)) != cudaSuccess)
-    return cuda_status(e, "registration");
+  if ((rc = host_flags_ready(ctx)) != GBN_OK) return rc;
   RegState hs{};
   int chunk = 0;
   for (int it = 1; it <= prm->nmax; ++chunk) {
@@ -716,13 +704,13 @@ int registration_run(gbn_ctx* ctx, const float2* images, int N, int F, const gbn
       k_reg_cost<<<1, kRegNT, 0, s>>>(a, it, gp, gu, prm->et, prm->eh);
       ctx->launches += 5;
     }
-    if ((e = cudaMemcpyAsync(&pin.flag[chunk & 1], &st->done, sizeof(int), cudaMemcpyDeviceToHost, s)) !=
+    if ((e = cudaMemcpyAsync(&ctx->host_flags[chunk & 1], &st->done, sizeof(int), cudaMemcpyDeviceToHost, s)) !=
             cudaSuccess ||
-        (e = cudaEventRecord(pin.ev[chunk & 1], s)) != cudaSuccess)
+        (e = cudaEventRecord(ctx->ev_flag[chunk & 1], s)) != cudaSuccess)
       return cuda_status(e, "registration");
     if (chunk > 0) {
-      if ((e = cudaEventSynchronize(pin.ev[(chunk - 1) & 1])) != cudaSuccess) return cuda_status(e, "registration");
-      if (pin.flag[(chunk - 1) & 1]) break;
+      if ((e = cudaEventSynchronize(ctx->ev_flag[(chunk - 1) & 1])) != cudaSuccess) return cuda_status(e, "registration");
+      if (ctx->host_flags[(chunk - 1) & 1]) break;
     }
   }
   if ((e = cudaMemcpyAsync(&hs, st, sizeof(hs), cudaMemcpyDeviceToHost, s)) != cudaSuccess) return cuda_status(e, "registration");
