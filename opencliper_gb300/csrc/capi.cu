@@ -178,6 +178,14 @@ int ctx_scratch(gbn_ctx* ctx, size_t bytes, void** out) {
   return GBN_OK;
 }
 
+int host_flags_ready(gbn_ctx* ctx) {
+  if (ctx->host_flags) return GBN_OK;
+  cudaError_t e = cudaHostAlloc(&ctx->host_flags, 2 * sizeof(int), cudaHostAllocDefault);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_flag[0], cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_flag[1], cudaEventDisableTiming);
+  return cuda_status(e, "pinned stop flags");
+}
+
 }  // namespace gbn
 
 using namespace gbn;
@@ -410,14 +418,6 @@ int gbn_download_async(gbn_ctx* ctx, void* h_dst, const void* d_src, size_t byte
 }
 
 namespace {
-int host_flags_ready(gbn_ctx* ctx) {
-  if (ctx->host_flags) return GBN_OK;
-  cudaError_t e = cudaHostAlloc(&ctx->host_flags, 2 * sizeof(int), cudaHostAllocDefault);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_flag[0], cudaEventDisableTiming);
-  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_flag[1], cudaEventDisableTiming);
-  return cuda_status(e, "pinned stop flags");
-}
-
 int copy_stream_ready(gbn_ctx* ctx) {
   if (ctx->copy_stream) return GBN_OK;
   DeviceGuard guard(ctx->device);
