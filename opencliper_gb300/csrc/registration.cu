@@ -50,7 +50,7 @@ namespace gbn {
 namespace {
 
 constexpr int kRegNT = 256;
-constexpr int kRegMaxE1 = 4;  // cubic splines
+constexpr int kRegMaxE1 = 4;  // spline orders up to 3
 constexpr int kStatusRange = 5;
 constexpr int kRegChunk = 8;
 
@@ -63,8 +63,37 @@ struct RegState {
   int flagW;
 };
 
-// ---- groupwiseRegistration/bspline.cpp, order 3 (float results of double arithmetic) ----
-float spline3(int t, float x) {
+// ---- groupwiseRegistration/bspline.cpp: bsplineN / b1splineN / b2splineN
+// (t = 0, 1, 2) of orders 1 to 3, float results of the reference's float and
+// double expressions, its constants included ----
+float spline_e(int t, float x, int E) {
+  if (E == 1) {
+    if (t == 0) {
+      if (x < 0 && x >= -1) return x + 1;
+      if (x < 1 && x >= 0) return 1 - x;
+      return 0;
+    }
+    if (t == 1) return (x < 0 && x >= -1) ? 1.f : ((x < 1 && x >= 0) ? -1.f : 0.f);
+    return 0;
+  }
+  if (E == 2) {
+    if (t == 0) {
+      if (x < -0.5 && x >= -1.5) return float((4 * std::pow(double(x), 2) + double(12 * x) + 9) / 8);
+      if (x < 0.5 && x >= -0.5) return float((-4 * std::pow(double(x), 2) + 3) / 4);
+      if (x < 1.5 && x >= 0.5) return float((4 * std::pow(double(x), 2) - double(12 * x) + 9) / 8);
+      return 0;
+    }
+    if (t == 1) {
+      if (x < -0.5 && x >= -1.5) return (2 * x + 3) / 2;
+      if (x < 0.5 && x >= -0.5) return -2 * x;
+      if (x < 1.5 && x >= 0.5) return (42 * x - 3) / 2;
+      return 0;
+    }
+    if (x < -0.5 && x >= -1.5) return 1;
+    if (x < 0.5 && x >= -0.5) return -2;
+    if (x < 1.5 && x >= 0.5) return 1;
+    return 0;
+  }
   if (t == 0) {
     const float v = std::fabs(x);
     if (v < 1) return float(0.5 * std::pow(double(v), 3) - std::pow(double(v), 2) + 0.6666);
@@ -102,7 +131,7 @@ int reg_geometry(int N, int F, const gbn_registration_params* p, RegGeom* g) {
   if (!p) return set_error(GBN_ERR_INVALID, "null registration parameters");
   if (N < 16 || N % 8 != 0) return set_error(GBN_ERR_UNSUPPORTED, "registration: N must be a multiple of 8, >= 16");
   if (F < 3) return set_error(GBN_ERR_UNSUPPORTED, "registration: at least 3 frames (the temporal terms use f-2)");
-  if (p->E != 3) return set_error(GBN_ERR_UNSUPPORTED, "registration: cubic splines (E = 3) only");
+  if (p->E < 1 || p->E > 3) return set_error(GBN_ERR_UNSUPPORTED, "registration: spline orders 1 to 3");
   if (p->Dp[0] != p->Dp[1] || p->Dp[0] < 1)
     return set_error(GBN_ERR_UNSUPPORTED, "registration: equal positive control spacing in both directions only");
   if (p->radius <= 0)
@@ -152,14 +181,19 @@ int reg_geometry(int N, int F, const gbn_registration_params* p, RegGeom* g) {
   const int E1 = p->E + 1;
   // per-pixel control ranges and spline values (coef, BBAux)
   std::vector<int> kmin(N);
-  for (int q = 0; q < N; ++q) kmin[q] = int(std::floor((float(q + 1) - c) / g->Dp)) - 1;
+  // creabspline.cpp: odd orders floor((x - c) / Dp) - (E - 1) / 2, even orders
+  // round((x - c) / Dp) - E / 2
+  for (int q = 0; q < N; ++q) {
+    const float u = (float(q + 1) - c) / g->Dp;
+    kmin[q] = (p->E % 2) ? int(std::floor(u)) - (p->E - 1) / 2 : int(std::round(u)) - p->E / 2;
+  }
   g->cr.resize(N);
   for (int q = 0; q < N; ++q) g->cr[q] = kmin[q] - kmin[g->bb[0]];
   g->B.assign(size_t(3) * N * E1, 0.f);
   for (int q = 0; q < N; ++q)
     for (int s = 0; s < E1; ++s) {
       const float arg = ((float(q + 1) - c) / float(g->Dp)) - float(kmin[q] + s);
-      for (int t = 0; t < 3; ++t) g->B[(size_t(t) * N + q) * E1 + s] = spline3(t, arg);
+      for (int t = 0; t < 3; ++t) g->B[(size_t(t) * N + q) * E1 + s] = spline_e(t, arg, g->E);
     }
   // control points and supports (ControlPointsLocation, coefg, BBAux1)
   g->sup.resize(g->Cp);
@@ -177,12 +211,12 @@ int reg_geometry(int N, int F, const gbn_registration_params* p, RegGeom* g) {
   g->S.assign(size_t(3) * g->dp, 0.f);
   for (int s = 0; s < g->dp; ++s) {
     const float arg = (float(g->sup[0] + 1 + s) - pu[0]) / float(g->Dp);
-    for (int t = 0; t < 3; ++t) g->S[size_t(t) * g->dp + s] = spline3(t, arg);
+    for (int t = 0; t < 3; ++t) g->S[size_t(t) * g->dp + s] = spline_e(t, arg, g->E);
   }
   for (int n = 1; n < g->Cp; ++n)
     for (int s = 0; s < g->dp; ++s) {
       const float arg = (float(g->sup[n] + 1 + s) - pu[n]) / float(g->Dp);
-      if (spline3(0, arg) != g->S[s])
+      if (spline_e(0, arg, g->E) != g->S[s])
         return set_error(GBN_ERR_UNSUPPORTED, "registration: control supports not uniform");
     }
   if (g->rect0 < 0 || g->rect1 > N - 1) return set_error(GBN_ERR_UNSUPPORTED, "registration: margin leaves the image");

@@ -31,7 +31,44 @@ f32 = np.float32
 
 # ---- groupwiseRegistration/bspline.cpp (float results of double arithmetic) ----
 def _bspline(t: int, x: float, E: int) -> float:
+    """bsplineN / b1splineN / b2splineN (t = 0, 1, 2) of order E = 1, 2, 3,
+    rounded as the reference's float and double expressions round."""
     x = float(np.float32(x))
+    fx = f32(x)
+    if E == 1:
+        if t == 0:
+            if -1 <= x < 0:
+                return float(f32(fx + f32(1)))
+            if 0 <= x < 1:
+                return float(f32(f32(1) - fx))
+            return 0.0
+        if t == 1:
+            return 1.0 if -1 <= x < 0 else (-1.0 if 0 <= x < 1 else 0.0)
+        return 0.0
+    if E == 2:
+        if t == 0:
+            if -1.5 <= x < -0.5:
+                return float(f32((4 * math.pow(x, 2) + float(f32(12 * fx)) + 9) / 8))
+            if -0.5 <= x < 0.5:
+                return float(f32((-4 * math.pow(x, 2) + 3) / 4))
+            if 0.5 <= x < 1.5:
+                return float(f32((4 * math.pow(x, 2) - float(f32(12 * fx)) + 9) / 8))
+            return 0.0
+        if t == 1:
+            if -1.5 <= x < -0.5:
+                return float(f32(f32(f32(2 * fx) + f32(3)) / f32(2)))
+            if -0.5 <= x < 0.5:
+                return float(f32(-2 * fx))
+            if 0.5 <= x < 1.5:
+                return float(f32(f32(f32(42 * fx) - f32(3)) / f32(2)))  # the reference's constant
+            return 0.0
+        if -1.5 <= x < -0.5:
+            return 1.0
+        if -0.5 <= x < 0.5:
+            return -2.0
+        if 0.5 <= x < 1.5:
+            return 1.0
+        return 0.0
     if E == 3:
         if t == 0:
             v = abs(x)
@@ -56,7 +93,12 @@ def _bspline(t: int, x: float, E: int) -> float:
         if 1 <= v < 2:
             return float(f32(-f32(v) + f32(2)))
         return 0.0
-    raise NotImplementedError("spline order 3 only (the reference's default)")
+    raise NotImplementedError("spline orders 1 to 3")
+
+
+def _round_half_away(v: float) -> float:
+    """std::round: halves away from zero."""
+    return float(math.floor(v + 0.5)) if v >= 0 else float(math.ceil(v - 0.5))
 
 
 class Geometry:
@@ -91,7 +133,12 @@ class Geometry:
         self.dp = 2 * int(math.ceil(rp)) + 1
         # per-pixel control ranges and spline values (coef, BBAux)
         p1 = (np.arange(N) + 1).astype(f32)
-        kmin = np.array([math.floor(f32(f32(v - c) / f32(Dp))) - 1 for v in p1], np.float64)
+        # creabspline.cpp: odd orders floor((x - c) / Dp) - (E - 1) / 2, even orders
+        # round((x - c) / Dp) - E / 2
+        if E % 2:
+            kmin = np.array([math.floor(f32(f32(v - c) / f32(Dp))) - (E - 1) // 2 for v in p1], np.float64)
+        else:
+            kmin = np.array([_round_half_away(float(f32(f32(v - c) / f32(Dp)))) - E // 2 for v in p1], np.float64)
         self.kmin = kmin
         ref = kmin[bb[0]]  # coef at index bound_box[d] (creabspline.cpp)
         self.cr = (kmin + 1 - ref - 1).astype(np.int64)  # 0-based first control point of each pixel

@@ -89,7 +89,19 @@ REG_CASES = [
     ("registration_96x6_circle.npz", 96, 6, 23, dict(radius=20, nmax=4, W=0.2, flagW=False)),
     # stopCondition fires before nmax: |Dif| < et 2F and a metric change below eh H0 at iteration 4
     ("registration_64x4_stop.npz", 64, 4, 24, dict(radius=12, nmax=12, W=0.05, et=0.5, eh=0.05)),
+    # linear and quadratic splines (creabspline.cpp's odd and even control ranges)
+    ("registration_64x4_e1.npz", 64, 4, 25, dict(radius=12, nmax=5, W=0.05, E=1)),
+    ("registration_64x4_e2.npz", 64, 4, 25, dict(radius=12, nmax=5, W=0.05, E=2, lambda_=(0.0, 0.0, 0.0, 0.5))),
+    # quadratic splines with the default weights: the order-2 derivative table (b1spline2's
+    # 42 x) makes the frame-broadcast regularisation term large, and its cancellation in the
+    # projected update leaves a rounding residue of ~1e-4 in T (REG_T_TOL)
+    ("registration_64x4_e2_lambda.npz", 64, 4, 25, dict(radius=12, nmax=5, W=0.05, E=2)),
 ]
+# tolerances where they are not a few roundings: T relative to max |T_ref|, xn in
+# pixels, H relative
+REG_T_TOL = {"registration_64x4_e2_lambda.npz": 5e-4}
+REG_XN_TOL = {"registration_64x4_e2_lambda.npz": 1e-3}
+REG_H_TOL = {"registration_64x4_e2_lambda.npz": 2e-5}
 
 
 def registration_inputs(N, F, seed):
