@@ -579,15 +579,20 @@ __global__ void k_reg_mesh(int* __restrict__ xmesh, float* __restrict__ xn, int 
   }
 }
 
-template <typename T>
-int dalloc(T** p, size_t n, std::vector<void*>& owned) {
-  if (cudaMalloc(p, std::max<size_t>(n, 1) * sizeof(T)) != cudaSuccess) {
-    cudaGetLastError();
-    return set_error(GBN_ERR_NOMEM, "registration workspace allocation failed");
+
+// bump allocation of the work arrays in one block (256-byte aligned); a pass
+// with a null base sizes the block
+struct Carve {
+  char* base;
+  size_t off;
+  template <typename T>
+  T* take(size_t n) {
+    off = (off + 255) & ~size_t(255);
+    T* p = reinterpret_cast<T*>(base + off);
+    off += std::max<size_t>(n, 1) * sizeof(T);
+    return p;
   }
-  owned.push_back(*p);
-  return GBN_OK;
-}
+};
 
 }  // namespace
 
@@ -611,30 +616,41 @@ int registration_run(gbn_ctx* ctx, const float2* images, int N, int F, const gbn
   if (rc != GBN_OK) return rc;
   cudaStream_t s = ctx->stream;
   const size_t NN = size_t(N) * N, X = NN * F, nT = size_t(2) * F * g.Cp * g.Cp;
-  std::vector<void*> owned;
-  struct Free {
-    std::vector<void*>& v;
-    ~Free() {
-      for (void* p : v) cudaFree(p);
-    }
-  } free_all{owned};
+  // all work arrays in one grow-only block of the context (no allocation
+  // after the first call of a size)
   RegArgs a{};
   float *I, *d1, *d2, *roi, *B, *S, *dH, *Dif, *Iw, *dy, *dx, *H, *part_h, *part_d, *sterm = nullptr;
   int *cr, *sup;
   unsigned* maxbits;
   RegState* st;
-  if ((rc = dalloc(&I, X, owned)) || (rc = dalloc(&d1, X, owned)) || (rc = dalloc(&d2, X, owned)) ||
-      (rc = dalloc(&roi, NN, owned)) || (rc = dalloc(&B, g.B.size(), owned)) || (rc = dalloc(&S, g.S.size(), owned)) ||
-      (rc = dalloc(&dH, nT, owned)) || (rc = dalloc(&Dif, nT, owned)) || (rc = dalloc(&Iw, X, owned)) ||
-      (rc = dalloc(&dy, X, owned)) || (rc = dalloc(&dx, 2 * X, owned)) ||
-      (rc = dalloc(&H, size_t(prm->nmax) + 1, owned)) ||
-      (rc = dalloc(&part_h, size_t(g.box1 - g.box0 + 1) * (g.box1 - g.box0 + 1) / kRegNT + 1, owned)) ||
-      (rc = dalloc(&part_d, nT / kRegNT + 1, owned)) ||
-      (g.sum_lambda != 0 &&
-       (rc = dalloc(&sterm, size_t(F) * 14 * (g.box1 - g.box0 + 1) * (g.box1 - g.box0 + 1), owned))) ||
-      (rc = dalloc(&cr, size_t(N), owned)) ||
-      (rc = dalloc(&sup, size_t(g.Cp), owned)) || (rc = dalloc(&maxbits, 1, owned)) || (rc = dalloc(&st, 1, owned)))
-    return rc;
+  const size_t L2 = size_t(g.box1 - g.box0 + 1) * (g.box1 - g.box0 + 1);
+  auto plan = [&](Carve& c) {
+    I = c.take<float>(X);
+    d1 = c.take<float>(X);
+    d2 = c.take<float>(X);
+    roi = c.take<float>(NN);
+    B = c.take<float>(g.B.size());
+    S = c.take<float>(g.S.size());
+    dH = c.take<float>(nT);
+    Dif = c.take<float>(nT);
+    Iw = c.take<float>(X);
+    dy = c.take<float>(X);
+    dx = c.take<float>(2 * X);
+    H = c.take<float>(size_t(prm->nmax) + 1);
+    part_h = c.take<float>(L2 / kRegNT + 1);
+    part_d = c.take<float>(nT / kRegNT + 1);
+    sterm = g.sum_lambda != 0 ? c.take<float>(size_t(F) * 14 * L2) : nullptr;
+    cr = c.take<int>(size_t(N));
+    sup = c.take<int>(size_t(g.Cp));
+    maxbits = c.take<unsigned>(1);
+    st = c.take<RegState>(1);
+  };
+  Carve sizer{nullptr, 0};
+  plan(sizer);
+  void* block = nullptr;
+  if ((rc = ctx_scratch(ctx, sizer.off, &block)) != GBN_OK) return rc;
+  Carve carver{static_cast<char*>(block), 0};
+  plan(carver);
   RegState h0{};
   h0.Wn = g.Wn0;
   h0.nmax = prm->nmax;
