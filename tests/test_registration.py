@@ -116,15 +116,16 @@ def test_restatement_starting_displacements():
     assert r["H"][0] == ref["H"][0] == d["H"][0]  # the metric restarts from the unregistered frames
 
 
-@pytest.mark.parametrize("N,F,radius", [(64, 4, 12), (64, 5, 14), (96, 6, 20), (256, 20, 40), (128, 3, 30)])
-def test_library_geometry_matches_restatement(built_lib, N, F, radius):
+@pytest.mark.parametrize("N,F,radius,E", [(64, 4, 12, 3), (64, 5, 14, 3), (96, 6, 20, 3), (256, 20, 40, 3),
+                                          (128, 3, 30, 3), (64, 4, 12, 1), (64, 4, 12, 2), (256, 20, 40, 2)])
+def test_library_geometry_matches_restatement(built_lib, N, F, radius, E):
     """gbn_registration_info_get (host code of the library, no GPU needed):
     control grid, bounding box and region-of-interest area as the restatement
     derives them from init() and creabspline()."""
     from opencliper_gb300 import api
     from oracle import registration as RG
-    info = api.registration_info(N, F, api.registration_params(radius=radius))
-    g = RG.Geometry(N, F, radius)
+    info = api.registration_info(N, F, api.registration_params(radius=radius, E=E))
+    g = RG.Geometry(N, F, radius, E)
     assert info["cp"] == g.Cp
     assert info["bound_box"] == g.bb
     assert info["area"] == g.areaX
