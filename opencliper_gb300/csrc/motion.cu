@@ -58,6 +58,8 @@ struct McTables {
                               // then rewritten to (the entry's pixel R1*W + R2) * 4 + corner
   int* srcmap = nullptr;      // [H*W] pixel each entry (by its R1*W + R2) reads in the adjoint
   float2* wts = nullptr;      // [F][H*W] (Whh, Wvv): each entry's fractional position in frame f
+  int* csrc = nullptr;        // [4 * l1 * l2 * F] per contribution: the pixel the adjoint reads
+  float2* cw = nullptr;       // [4 * l1 * l2 * F] per contribution: its two weights (fa, fb)
   double* tvpart = nullptr;   // [F * pixel blocks][2] partial sums of the fused tTV kernel
   size_t x = 0, entries = 0;  // F*H*W and l1*l2 the buffers were sized for
   int nbp = 0, nscan = 0;
@@ -315,6 +317,23 @@ __global__ void k_mc_rekey(int* __restrict__ key, const int* __restrict__ total,
   }
 }
 
+// per contribution, what the adjoint gathers need: the pixel it reads and its
+// two weights fa = Whh or 1 - Whh (corner bit 0), fb = Wvv or 1 - Wvv (bit 1),
+// rounded as optimizer.cl:880-937 forms them
+__global__ void k_mc_pack(const int* __restrict__ off, const int* __restrict__ key, const int* __restrict__ srcmap,
+                          const float2* __restrict__ wts, int* __restrict__ csrc, float2* __restrict__ cw, size_t X,
+                          size_t HW) {
+  for (size_t q = blockIdx.x * size_t(blockDim.x) + threadIdx.x; q < X; q += size_t(gridDim.x) * blockDim.x) {
+    const float2* wk = wts + (q / HW) * HW;
+    for (int c = off[q], ce = off[q + 1]; c < ce; ++c) {
+      const int kc = key[c], e = kc >> 2;
+      const float2 w = wk[e];
+      csrc[c] = srcmap[e];
+      cw[c] = make_float2((kc & 1) ? w.x : __fsub_rn(1.f, w.x), (kc & 2) ? w.y : __fsub_rn(1.f, w.y));
+    }
+  }
+}
+
 // ---- the operators -------------------------------------------------------------
 // out = M x (MotionCompensation: copy, then the interpolator), one thread per pixel
 __global__ void k_mc_warp(const float2* __restrict__ x, float2* __restrict__ out, const float* __restrict__ xn,
@@ -332,9 +351,9 @@ __global__ void k_mc_warp(const float2* __restrict__ x, float2* __restrict__ out
 // Wvv or 1 - Wvv (c & 2), as optimizer.cl:880-937 rounds them.  Loads of up to
 // four contributions are issued before any of them is accumulated.
 __global__ void __launch_bounds__(kNT) k_mc_adjoint(const float2* __restrict__ g, float2* __restrict__ out,
-                                                     const int* __restrict__ off, const int* __restrict__ key,
-                                                     const int* __restrict__ srcmap, const float2* __restrict__ wts,
-                                                     McRect r, int W, int H, int F, int pdl) {
+                                                     const int* __restrict__ off, const int* __restrict__ csrc,
+                                                     const float2* __restrict__ cw, McRect r, int W, int H, int F,
+                                                     int pdl) {
   if (pdl) {
     grid_dep_wait();  // g comes from the fused tTV kernel two launches back
     grid_dep_release();
@@ -349,27 +368,21 @@ __global__ void __launch_bounds__(kNT) k_mc_adjoint(const float2* __restrict__ g
   float2 acc = in_rect ? make_float2(0.f, 0.f) : g[q];
   const size_t k = q / HW;
   const float2* gk = g + k * HW;
-  const float2* wk = wts + k * HW;
   while (c < ce) {
     const int m = min(4, ce - c);
-    int kc[4];
     float2 w[4], v[4];
-#pragma unroll
-    for (int u = 0; u < 4; ++u) kc[u] = u < m ? __ldg(key + c + u) : 0;
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       if (u < m) {
-        w[u] = __ldg(wk + (kc[u] >> 2));
-        v[u] = gk[__ldg(srcmap + (kc[u] >> 2))];
+        w[u] = __ldg(cw + c + u);
+        v[u] = gk[__ldg(csrc + c + u)];
       }
     }
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       if (u < m) {
-        const float fa = (kc[u] & 1) ? w[u].x : __fsub_rn(1.f, w[u].x);
-        const float fb = (kc[u] & 2) ? w[u].y : __fsub_rn(1.f, w[u].y);
-        acc.x = __fadd_rn(acc.x, __fmul_rn(__fmul_rn(v[u].x, fa), fb));
-        acc.y = __fadd_rn(acc.y, __fmul_rn(__fmul_rn(v[u].y, fa), fb));
+        acc.x = __fadd_rn(acc.x, __fmul_rn(__fmul_rn(v[u].x, w[u].x), w[u].y));
+        acc.y = __fadd_rn(acc.y, __fmul_rn(__fmul_rn(v[u].y, w[u].x), w[u].y));
       }
     }
     c += m;
@@ -648,9 +661,9 @@ __global__ void __launch_bounds__(kNT) k_ne_s1b(double* part, int nblk, unsigned
 
 // x = M^T tTVadj(Sx) (operatorUt without negation), partial sums
 __global__ void __launch_bounds__(kNT) k_ne_ut(const float2* __restrict__ Sx, float2* __restrict__ x,
-                                                const int* __restrict__ off, const int* __restrict__ key,
-                                                const int* __restrict__ srcmap, const float2* __restrict__ wts, McRect r,
-                                                int W, int H, int F, double* __restrict__ part) {
+                                                const int* __restrict__ off, const int* __restrict__ csrc,
+                                                const float2* __restrict__ cw, McRect r, int W, int H, int F,
+                                                double* __restrict__ part) {
   __shared__ double sred2[kNT / 32], sred1[kNT / 32];
   const McNe* ne = ne_state(part);
   if (ne->done) return;
@@ -663,16 +676,12 @@ __global__ void __launch_bounds__(kNT) k_ne_ut(const float2* __restrict__ Sx, fl
     const float2* u1 = Sx + size_t((k + 1) % F) * HW;
     const bool in_rect = row >= r.r1b && row < r.r1b + r.l1 && col >= r.r2b && col < r.r2b + r.l2;
     float2 acc = in_rect ? make_float2(0.f, 0.f) : csub(u1[p], u0[p]);
-    const float2* wk = wts + k * HW;
     for (int c = off[q], ce = off[q + 1]; c < ce; ++c) {
-      const int kc = __ldg(key + c), e = kc >> 2;
-      const float2 w = __ldg(wk + e);
-      const float fa = (kc & 1) ? w.x : __fsub_rn(1.f, w.x);
-      const float fb = (kc & 2) ? w.y : __fsub_rn(1.f, w.y);
-      const int src = __ldg(srcmap + e);
+      const float2 w = __ldg(cw + c);
+      const int src = __ldg(csrc + c);
       const float2 v = csub(u1[src], u0[src]);
-      acc.x = __fadd_rn(acc.x, __fmul_rn(__fmul_rn(v.x, fa), fb));
-      acc.y = __fadd_rn(acc.y, __fmul_rn(__fmul_rn(v.y, fa), fb));
+      acc.x = __fadd_rn(acc.x, __fmul_rn(__fmul_rn(v.x, w.x), w.y));
+      acc.y = __fadd_rn(acc.y, __fmul_rn(__fmul_rn(v.y, w.x), w.y));
     }
     x[q] = acc;
     s2 = fmaf(acc.x, acc.x, fmaf(acc.y, acc.y, s2));
@@ -707,7 +716,7 @@ __global__ void k_ne_finish(const double* part, NestaDevState* st) {
 // host side
 // ---------------------------------------------------------------------------
 void tables_free(McTables* t) {
-  void* ptrs[] = {t->inv, t->cnt, t->off, t->bsum, t->key, t->srcmap, t->wts, t->tvpart};
+  void* ptrs[] = {t->inv, t->cnt, t->off, t->bsum, t->key, t->srcmap, t->wts, t->tvpart, t->csrc, t->cw};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   *t = McTables{};
@@ -731,6 +740,8 @@ int tables_alloc(McTables* t, int W, int H, int F, int E) {
   if (e == cudaSuccess) e = cudaMalloc(&t->srcmap, HW * sizeof(int));
   if (e == cudaSuccess) e = cudaMalloc(&t->wts, X * sizeof(float2));
   if (e == cudaSuccess) e = cudaMalloc(&t->tvpart, 2 * size_t(F) * nbp * sizeof(double));
+  if (e == cudaSuccess) e = cudaMalloc(&t->csrc, 4 * size_t(E) * F * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&t->cw, 4 * size_t(E) * F * sizeof(float2));
   if (e != cudaSuccess) {
     cudaGetLastError();
     tables_free(t);
@@ -757,7 +768,8 @@ int tables_build(gbn_ctx* ctx, McTables* t, const float* xn, const int* xm, cons
   k_mc_fill<<<grid1(ctx, size_t(E) * F), kNT, 0, s>>>(xn, xm, r, W, H, F, t->off, t->cnt, t->key, t->wts);
   k_mc_sort<<<grid1(ctx, X), kNT, 0, s>>>(t->off, t->key, X);
   k_mc_rekey<<<grid1(ctx, 4 * size_t(E) * F), kNT, 0, s>>>(t->key, t->off + X, r, W);
-  ctx->launches += 9;
+  k_mc_pack<<<grid1(ctx, X), kNT, 0, s>>>(t->off, t->key, t->srcmap, t->wts, t->csrc, t->cw, X, HW);
+  ctx->launches += 10;
   return GBN_OK;
 }
 
@@ -846,7 +858,7 @@ int mc_normest(gbn_ctx* ctx, gbn_problem* P, cudaStream_t s) {
       k_ne_s1<<<1, kNT, 0, s>>>(P->mc_part, nblk);
       k_ne_restart<<<nblk, kNT, 0, s>>>(Sx, X, P->mc_part);
       k_ne_s1b<<<1, kNT, 0, s>>>(P->mc_part, nblk, (unsigned long long)jX.a, (unsigned long long)jX.c);
-      k_ne_ut<<<nblk, kNT, 0, s>>>(Sx, x, t->off, t->key, t->srcmap, t->wts, r, W, H, F, P->mc_part);
+      k_ne_ut<<<nblk, kNT, 0, s>>>(Sx, x, t->off, t->csrc, t->cw, r, W, H, F, P->mc_part);
       k_ne_s2<<<1, kNT, 0, s>>>(P->mc_part, nblk);
       ctx->launches += 6;
     }
@@ -896,7 +908,7 @@ int motion_op(gbn_ctx* ctx, int dir, const float2* in, float2* out, const float*
     if (dir == GBN_TTV_FORWARD)
       k_mc_warp<<<grid1(ctx, X), kNT, 0, s>>>(in, out, xn, t.inv, r, W, H, F, status);
     else
-      k_mc_adjoint<<<int((X + kNT - 1) / kNT), kNT, 0, s>>>(in, out, t.off, t.key, t.srcmap, t.wts, r, W, H, F, 0);
+      k_mc_adjoint<<<int((X + kNT - 1) / kNT), kNT, 0, s>>>(in, out, t.off, t.csrc, t.cw, r, W, H, F, 0);
     ctx->launches += 1;
   }
   int h = 0;
@@ -966,7 +978,7 @@ int nesta_run_mc(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, floa
       cudaStreamWaitEvent(aux, ctx->ev_mc_x, 0);
       k_mc_tv<<<gtv, kNT, 0, aux>>>(xk, P->mc_xn, t->inv, r, P->st, P->mc_g, t->tvpart, W, H, F, &P->st->status);
       cudaEventRecord(ctx->ev_mc_tv, aux);
-      k_mc_adjoint<<<gadj, kNT, 0, aux>>>(P->mc_g, P->mc_gm, t->off, t->key, t->srcmap, t->wts, r, W, H, F, 0);
+      k_mc_adjoint<<<gadj, kNT, 0, aux>>>(P->mc_g, P->mc_gm, t->off, t->csrc, t->cw, r, W, H, F, 0);
       cudaEventRecord(ctx->ev_mc_adj, aux);
       kh->fwd_cols(tab, bm, int(it), cpb, g1, s);
       cudaStreamWaitEvent(s, ctx->ev_mc_tv, 0);
