@@ -318,7 +318,8 @@ GBN_API int gbn_registration_info_get(int N, int F, const gbn_registration_param
  * optimizer() (groupwiseRegistration/optimizer.cpp) on the B-spline control
  * displacements T.  d_images: [F][N][N] complex (the reconstruction to
  * register).  d_T_init: [2][F][cp][cp] starting displacements, or NULL for
- * zeros (the reference's TData on its first motion iteration).  Outputs, all
+ * zeros (the reference's TData on its first motion iteration); it may be d_T
+ * itself.  Outputs, all
  * device: d_T [2][F][cp][cp], d_xn the deformed mesh [2][F][N][N] (1-based,
  * horizontal then vertical), d_xmesh the original mesh [2][N][N] (int,
  * 1-based, as ArgumentsMotionCompensation::xData); d_xn, d_xmesh and

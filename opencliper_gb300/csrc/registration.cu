@@ -666,7 +666,8 @@ int registration_run(gbn_ctx* ctx, const float2* images, int N, int F, const gbn
   // times a zero mask: zero there
   if (e == cudaSuccess) e = cudaMemsetAsync(dy, 0, X * sizeof(float), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(dx, 0, 2 * X * sizeof(float), s);
-  if (e == cudaSuccess)
+  // T_init may be T_out itself (a continuation in place)
+  if (e == cudaSuccess && T_init != T_out)
     e = T_init ? cudaMemcpyAsync(T_out, T_init, nT * sizeof(float), cudaMemcpyDeviceToDevice, s)
                : cudaMemsetAsync(T_out, 0, nT * sizeof(float), s);
   if (e != cudaSuccess) return cuda_status(e, "registration setup");
