@@ -142,3 +142,22 @@ def test_full_size_against_restatement(ctx):
     assert full["status"] == 0 and full["cp"] == 23
     assert full["H"][-1] < full["H"][0]
     assert np.isfinite(full["T"]).all() and np.isfinite(full["xn"]).all()
+
+
+def test_continuation_in_place(ctx):
+    """T_init may be the output array itself (the C ABI's d_T_init == d_T)."""
+    import ctypes as C
+    from opencliper_gb300._abi import RegistrationStats, call
+    d = _load(CASES[0])
+    prm = _params(d, nmax=3)
+    x = ctx.to_device(d["images"])
+    ref = api.registration(ctx, x, prm, ctx.to_device(d["T"]))
+    N, F = int(d["N"]), int(d["F"])
+    T = ctx.to_device(np.ascontiguousarray(d["T"], np.float32))
+    xn = ctx.empty((2, F, N, N), np.float32)
+    xm = ctx.empty((2, N, N), np.int32)
+    st = RegistrationStats()
+    call("gbn_registration_run", ctx.handle, x.ptr, N, F, C.byref(prm), T.ptr, T.ptr, xn.ptr, xm.ptr, None,
+         C.byref(st))
+    np.testing.assert_array_equal(T.get(), ref["T"].get())
+    np.testing.assert_array_equal(xn.get(), ref["xn"].get())
