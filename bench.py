@@ -510,7 +510,7 @@ def registration_form(ctx, stream, args=None) -> dict:
            "unit": "registrations/s",
            "gpu": {"value": round(1e3 / ms, 3), "ms_per_registration": round(ms, 3),
                    "iterations": int(r["iterations"]), "ms_per_iteration": round(ms / max(1, r["iterations"]), 4),
-                   "kernel_launches_per_iteration": 5, "control_points": int(r["cp"]) ** 2,
+                   "kernel_launches_per_iteration": 4, "control_points": int(r["cp"]) ** 2,
                    "H0": float(r["H0"]), "H": float(r["H_final"]), "status": int(r["status"])}}
     # the motion-compensated solve with the estimated mesh
     prob.set_motion(r["xn"], r["xmesh"], r["bound_box"])

@@ -23,7 +23,7 @@
 // non-zero, with the reference's pairing of spline factors (optimizer.cl:
 // 746-830) and at the transposed pixel (optimizer.cl:138-187).
 //
-// Here one iteration is five kernels:
+// Here one iteration is four kernels:
 //   k_reg_grad    one thread per (d, frame, control point, column offset): the
 //                 support sums in the reference's order (auxiliarCost,
 //                 cost6DReduction, cost6D)
@@ -32,9 +32,8 @@
 //   k_reg_warp    one thread per (bounding-box pixel, frame): xn, the warped
 //                 frame, dx, the smoothness terms
 //   k_reg_metric  one thread per bounding-box pixel: the frames' mean, V, dy,
-//                 per-CTA partial sums of the metric
-//   k_reg_cost    one CTA: H and |Dif| from the partial sums, evolution() and
-//                 stopCondition() on the device
+//                 per-CTA partial sums of the metric; its last CTA sums the
+//                 partials (H, |Dif|) and runs evolution() and stopCondition()
 // iterations are enqueued eight at a time; the host reads the stop flag once
 // per chunk.  This file is compiled without FMA contraction, so products and
 // sums round separately as in the reference's kernels.
@@ -61,6 +60,7 @@ struct RegState {
   int status;
   int nmax;
   int flagW;
+  unsigned arrived;  // CTAs of k_reg_metric done this iteration (the last one finishes the iteration)
 };
 
 // ---- groupwiseRegistration/bspline.cpp: bsplineN / b1splineN / b2splineN
@@ -413,7 +413,9 @@ __device__ __forceinline__ float reg_block_sum(float v, float* sw) {
 // smoothness sum of the transposed pixel in sumLambdaMetric's order (the
 // reference adds each pixel's sum at the transposed position); the CTA's
 // partial sum of V over the region of interest
-__global__ void __launch_bounds__(kRegNT) k_reg_metric(RegArgs a) {
+__device__ void reg_finish(RegArgs& a, int it, int nh, int nd, float et, float eh, float* sw);
+
+__global__ void __launch_bounds__(kRegNT) k_reg_metric(RegArgs a, int it, int nd, float et, float eh) {
   if (a.st->done) return;
   __shared__ float sw[kRegNT / 32];
   const int L = a.box1 - a.box0 + 1;
@@ -453,7 +455,18 @@ __global__ void __launch_bounds__(kRegNT) k_reg_metric(RegArgs a) {
     h = V * a.roi[p];
   }
   const float t = reg_block_sum(h, sw);
-  if (threadIdx.x == 0) a.part_h[blockIdx.x] = t;
+  // the last CTA to finish reduces every CTA's partial sum (fixed order) and
+  // runs evolution(): no separate launch
+  __shared__ bool last;
+  if (threadIdx.x == 0) {
+    a.part_h[blockIdx.x] = t;
+    __threadfence();
+    last = atomicAdd(&a.st->arrived, 1u) == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  reg_finish(a, it, int(gridDim.x), nd, et, eh, sw);
 }
 
 // dH for (d, frame, control point) in the reference's order (auxiliarCost,
@@ -533,19 +546,20 @@ __global__ void __launch_bounds__(kRegNT) k_reg_update(RegArgs a) {
 
 // H and |Dif| from the partial sums of k_reg_metric and k_reg_update (fixed
 // order), evolution() and stopCondition() (GroupwiseRegistration.cpp:451-478,
-// 533-545).  it == 0: the unregistered metric and the thresholds.
-__global__ void __launch_bounds__(kRegNT) k_reg_cost(RegArgs a, int it, int nh, int nd, float et, float eh) {
+// 533-545); run by the last CTA of k_reg_metric.  it == 0: the unregistered
+// metric and the thresholds.
+__device__ void reg_finish(RegArgs& a, int it, int nh, int nd, float et, float eh, float* sw) {
   RegState* st = a.st;
-  if (st->done) return;
-  __shared__ float sw[kRegNT / 32];
+  __syncthreads();  // sw reuse
   float h = 0.f, dd = 0.f;
-  for (int q = threadIdx.x; q < nh; q += kRegNT) h = h + a.part_h[q];
+  for (int q = threadIdx.x; q < nh; q += kRegNT) h = h + __ldcg(a.part_h + q);
   if (it > 0)
-    for (int q = threadIdx.x; q < nd; q += kRegNT) dd = dd + a.part_d[q];
+    for (int q = threadIdx.x; q < nd; q += kRegNT) dd = dd + __ldcg(a.part_d + q);
   const float H = reg_block_sum(h, sw);
   __syncthreads();
   const float D = reg_block_sum(dd, sw);
   if (threadIdx.x != 0) return;
+  st->arrived = 0;
   a.H[it] = H;
   if (it == 0) {
     st->p2 = et * float(a.F * 2);
@@ -729,9 +743,8 @@ int registration_run(gbn_ctx* ctx, const float2* images, int N, int F, const gbn
   const int gu = int((nT + kRegNT - 1) / kRegNT);
   // the unregistered frames: metric H[0]; dx at the starting mesh (optimizer.cpp: InitIT, Metric, CostReduction)
   k_reg_warp<<<gw, kRegNT, 0, s>>>(a);
-  k_reg_metric<<<gp, kRegNT, 0, s>>>(a);
-  k_reg_cost<<<1, kRegNT, 0, s>>>(a, 0, gp, gu, prm->et, prm->eh);
-  ctx->launches += 3;
+  k_reg_metric<<<gp, kRegNT, 0, s>>>(a, 0, gu, prm->et, prm->eh);
+  ctx->launches += 2;
   a.warp = 1;
   a.smooth = g.sum_lambda != 0;
   // chunks of iterations with one chunk of lookahead: while the GPU runs chunk
@@ -751,9 +764,8 @@ int registration_run(gbn_ctx* ctx, const float2* images, int N, int F, const gbn
         k_reg_grad<0><<<gg, kRegNT, 0, s>>>(a);
       k_reg_update<<<gu, kRegNT, 0, s>>>(a);
       k_reg_warp<<<gw, kRegNT, 0, s>>>(a);
-      k_reg_metric<<<gp, kRegNT, 0, s>>>(a);
-      k_reg_cost<<<1, kRegNT, 0, s>>>(a, it, gp, gu, prm->et, prm->eh);
-      ctx->launches += 5;
+      k_reg_metric<<<gp, kRegNT, 0, s>>>(a, it, gu, prm->et, prm->eh);
+      ctx->launches += 4;
     }
     if ((e = cudaMemcpyAsync(&ctx->host_flags[chunk & 1], &st->done, sizeof(int), cudaMemcpyDeviceToHost, s)) !=
             cudaSuccess ||
