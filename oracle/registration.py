@@ -375,28 +375,27 @@ class Registration:
                (f32(2 * Dp * Dp) * S2[:, None] * S[None, :]).astype(f32)]
         b11g = (f32(2 * Dp * Dp) * S1[:, None] * S1[None, :]).astype(f32)
         # dtheta arrays in the reference's flat layouts: [p][d][l][k][f][i][j]
-        shape6 = (2, Cp, Cp, F, dp, dp)  # [d][l (Cp0 slot)][k (Cp1 slot)][f][i][j]
-        thx = np.zeros((2,) + shape6, f32)
-        thx2 = np.zeros((2,) + shape6, f32)
-        thxy = np.zeros(shape6, f32)
-        tht = np.zeros(shape6, f32)
-        tht2 = np.zeros(shape6, f32)
-        for l in range(Cp):
-            rows = R[l] + i_
-            for k in range(Cp):
-                cols = R[k] + i_
-                for f in range(F):
-                    for d in range(2):
-                        for p in range(2):
-                            thx[p, d, l, k, f] = (dtaux[p, d, f][np.ix_(rows, cols)] * b1g[p]).astype(f32)
-                            thx2[p, d, l, k, f] = (dtaux2[p, d, f][np.ix_(rows, cols)] * b2g[p]).astype(f32)
-                        thxy[d, l, k, f] = (dtauxy[d, f][np.ix_(rows, cols)] * b11g).astype(f32)
-                        a0, a1, a2 = (dtaut[d, f][R[k], R[l]], dtaut[d, (f + 1) % F][R[k], R[l]],
-                                      dtaut[d, (f + 2) % F][R[k], R[l]])
-                        tht[d, l, k, f] = (f32(f32(2) * f32(a0 - a1)) * bbg).astype(f32)
-                        q0, q1, q2 = (dtaut2[d, f][R[k], R[l]], dtaut2[d, (f + 1) % F][R[k], R[l]],
-                                      dtaut2[d, (f + 2) % F][R[k], R[l]])
-                        tht2[d, l, k, f] = (f32(f32(2) * f32(f32(q0 - f32(2) * q1) + q2)) * bbg).astype(f32)
+        # (elementwise products: gathered for every control point at once)
+        RR = R[:, None] + i_[None, :]                                   # [cp][offset]
+        rix, cix = RR[:, None, :, None], RR[None, :, None, :]           # (l, k, i, j)
+
+        def at_support(a):  # a [..., F, N, N] -> [..., Cp(l), Cp(k), F, dp, dp]
+            g_ = a[..., rix, cix]                                       # [..., F, Cp, Cp, dp, dp]
+            nd = g_.ndim
+            order = list(range(nd - 5)) + [nd - 4, nd - 3, nd - 5, nd - 2, nd - 1]
+            return np.ascontiguousarray(g_.transpose(order))
+
+        thx = (at_support(dtaux) * np.stack(b1g)[:, None, None, None, None]).astype(f32)
+        thx2 = (at_support(dtaux2) * np.stack(b2g)[:, None, None, None, None]).astype(f32)
+        thxy = (at_support(dtauxy) * b11g).astype(f32)
+        # temporal terms: dtaut read at the transposed support corner [R[k]][R[l]]
+        corner = lambda a: a[..., R[None, :], R[:, None]]               # [..., F, Cp(l), Cp(k)]
+        c0, c2 = corner(dtaut), corner(dtaut2)                          # [d][f][l][k]
+        c1, c21, c22 = np.roll(c0, -1, axis=1), np.roll(c2, -1, axis=1), np.roll(c2, -2, axis=1)
+        t1 = (f32(2) * (c0 - c1).astype(f32)).astype(f32)
+        t2 = (f32(2) * ((c2 - (f32(2) * c21).astype(f32)).astype(f32) + c22).astype(f32)).astype(f32)
+        tht = (t1.transpose(0, 2, 3, 1)[..., None, None] * bbg).astype(f32)   # [d][l][k][f][i][j]
+        tht2 = (t2.transpose(0, 2, 3, 1)[..., None, None] * bbg).astype(f32)
         n6 = thxy.size
         fx = thx.reshape(-1)
         fx2 = thx2.reshape(-1)
@@ -418,30 +417,29 @@ class Registration:
 
     def gradient(self, dx, dy, aux2):
         """gradientJoint + permutedV + the per-control-point loop of auxiliarMask,
-        auxiliarCost, cost6DReduction, cost6D: dH [d][f][row cp][col cp]."""
+        auxiliarCost, cost6DReduction, cost6D: dH [d][f][row cp][col cp].  The
+        support sum runs in the reference's order (row offsets i summed for each
+        column offset j, then the column sums), for every control point at once."""
         g, F, Cp, dp = self.g, self.F, self.g.Cp, self.g.dp
         S = g.S[0]
         bbg = (S[:, None] * S[None, :]).astype(f32)
         i_ = np.arange(dp)
-        R = g.sup
+        RR = g.sup[:, None] + i_[None, :]
+        rix, cix = RR[:, None, :, None], RR[None, :, None, :]           # (kr, lc, i, j)
+        mask = g.roi.T[rix, cix]                                        # [kr][lc][i][j]
+        dyg = dy[:, rix, cix]                                           # [f][kr][lc][i][j]
         dH = np.zeros((2, F, Cp, Cp), f32)
-        roiT = g.roi.T
-        for kh in range(Cp):
-            rows = R[kh] + i_
-            for lh in range(Cp):
-                cols = R[lh] + i_
-                mask = roiT[np.ix_(rows, cols)]
-                a2 = aux2[kh, lh]
-                for f in range(F):
-                    dyv = dy[f][np.ix_(rows, cols)]
-                    for d in range(2):
-                        dv = (((dyv * dx[d, f][np.ix_(rows, cols)]).astype(f32) * bbg).astype(f32) + a2).astype(f32)
-                        c1 = (dv * mask).astype(f32)
-                        acc = f32(0)
-                        for jj in range(dp):
-                            col_sum = np.cumsum(c1[:, jj], dtype=f32)[-1]
-                            acc = f32(acc + col_sum)
-                        dH[d, f, kh, lh] = acc
+        for d in range(2):
+            dxg = dx[d][:, rix, cix]
+            dv = (((dyg * dxg).astype(f32) * bbg).astype(f32) + aux2[None]).astype(f32)
+            c1 = (dv * mask[None]).astype(f32)
+            acc = np.zeros((F, Cp, Cp), f32)
+            for jj in range(dp):
+                col = np.zeros((F, Cp, Cp), f32)
+                for ii in range(dp):
+                    col = (col + c1[..., ii, jj]).astype(f32)
+                acc = (acc + col).astype(f32)
+            dH[d] = acc
         return dH
 
     def run(self, images, T_init=None):
