@@ -287,49 +287,45 @@ class Registration:
         dtauxy = np.zeros((2,) + shp, f32)
         dtaut = np.zeros((2,) + shp, f32)
         dtaut2 = np.zeros((2,) + shp, f32)
-        for d in range(2):
-            for f in range(F):
-                Tf, T1, T2 = T[d, f], T[d, (f - 1) % F], T[d, (f - 2) % F]
-                ax = [np.zeros(rr.shape, f32) for _ in range(2)]
-                ax2 = [np.zeros(rr.shape, f32) for _ in range(2)]
-                axy = np.zeros(rr.shape, f32)
-                at = np.zeros(rr.shape, f32)
-                at2 = np.zeros(rr.shape, np.float64)
-                for m in range(g.E + 1):
-                    for n in range(g.E + 1):
-                        t0 = Tf[cr + n, ccp + m]
-                        bx = [(f32(Dp) * (B[cc, n] * B1[rr, m]).astype(f32)).astype(f32),
-                              (f32(Dp) * (B1[cc, n] * B[rr, m]).astype(f32)).astype(f32)]
-                        bx2 = [(f32(Dp * Dp) * (B[cc, n] * B2[rr, m]).astype(f32)).astype(f32),
-                               (f32(Dp * Dp) * (B2[cc, n] * B[rr, m]).astype(f32)).astype(f32)]
-                        for p in range(2):
-                            ax[p] = (ax[p] + (t0 * bx[p]).astype(f32)).astype(f32)
-                            ax2[p] = (ax2[p] + (t0 * bx2[p]).astype(f32)).astype(f32)
-                        # the loop over p sits outside m, n in the kernel; per-element
-                        # accumulation order is the same
-                bxy_all = None
+        # every (d, frame) at once; per element the same loop order and roundings
+        T1a, T2a = np.roll(T, 1, axis=1), np.roll(T, 2, axis=1)      # frames f-1, f-2
+        box = (2, F) + rr.shape
+        ax = np.zeros((2,) + box, f32)
+        ax2 = np.zeros((2,) + box, f32)
+        axy = np.zeros(box, f32)
+        at = np.zeros(box, f32)
+        at2 = np.zeros(box, np.float64)
+        E1 = g.E + 1
+        for m in range(E1):
+            for n in range(E1):
+                t0 = T[:, :, cr + n, ccp + m]
+                bx = [(f32(Dp) * (B[cc, n] * B1[rr, m]).astype(f32)).astype(f32),
+                      (f32(Dp) * (B1[cc, n] * B[rr, m]).astype(f32)).astype(f32)]
+                bx2 = [(f32(Dp * Dp) * (B[cc, n] * B2[rr, m]).astype(f32)).astype(f32),
+                       (f32(Dp * Dp) * (B2[cc, n] * B[rr, m]).astype(f32)).astype(f32)]
                 for p in range(2):
-                    v = ax[p]
-                    if p == d:
-                        v = (v + f32(1)).astype(f32)
-                    dtaux[p, d, f][rr, cc] = v
-                    dtaux2[p, d, f][rr, cc] = ax2[p]
-                for m in range(g.E + 1):
-                    for n in range(g.E + 1):
-                        t0 = Tf[cr + n, ccp + m]
-                        bxy = (f32(Dp * Dp) * (B1[cc, n] * B1[rr, m]).astype(f32)).astype(f32)
-                        axy = (axy + (t0 * bxy).astype(f32)).astype(f32)
-                for m in range(g.E + 1):
-                    for n in range(g.E + 1):
-                        t0, t1, t2 = Tf[cr + n, ccp + m], T1[cr + n, ccp + m], T2[cr + n, ccp + m]
-                        bb = (B[cc, n] * B[rr, m]).astype(f32)
-                        at = (at + ((t0 - t1).astype(f32) * bb).astype(f32)).astype(f32)
-                        at2 = (at2.astype(f32).astype(np.float64)
-                               + (t0.astype(np.float64) - 2.0 * t1.astype(np.float64) + t2.astype(np.float64))
-                               * bb.astype(np.float64)).astype(f32).astype(np.float64)
-                dtauxy[d, f][rr, cc] = axy
-                dtaut[d, f][rr, cc] = at
-                dtaut2[d, f][rr, cc] = at2.astype(f32)
+                    ax[p] = (ax[p] + (t0 * bx[p]).astype(f32)).astype(f32)
+                    ax2[p] = (ax2[p] + (t0 * bx2[p]).astype(f32)).astype(f32)
+        for p in range(2):  # + 1 where the derivative direction is the displacement's (p == d)
+            ax[p, p] = (ax[p, p] + f32(1)).astype(f32)
+        for m in range(E1):
+            for n in range(E1):
+                t0 = T[:, :, cr + n, ccp + m]
+                bxy = (f32(Dp * Dp) * (B1[cc, n] * B1[rr, m]).astype(f32)).astype(f32)
+                axy = (axy + (t0 * bxy).astype(f32)).astype(f32)
+        for m in range(E1):
+            for n in range(E1):
+                t0, t1, t2 = T[:, :, cr + n, ccp + m], T1a[:, :, cr + n, ccp + m], T2a[:, :, cr + n, ccp + m]
+                bb = (B[cc, n] * B[rr, m]).astype(f32)
+                at = (at + ((t0 - t1).astype(f32) * bb).astype(f32)).astype(f32)
+                at2 = (at2.astype(f32).astype(np.float64)
+                       + (t0.astype(np.float64) - 2.0 * t1.astype(np.float64) + t2.astype(np.float64))
+                       * bb.astype(np.float64)).astype(f32).astype(np.float64)
+        dtaux[..., rr, cc] = ax
+        dtaux2[..., rr, cc] = ax2
+        dtauxy[..., rr, cc] = axy
+        dtaut[..., rr, cc] = at
+        dtaut2[..., rr, cc] = at2.astype(f32)
         return dtaux, dtaux2, dtauxy, dtaut, dtaut2
 
     # ---- gradient of the metric (Gradient, Initdx, GradientInterpolator, GradientMetric) ----
