@@ -47,17 +47,6 @@ int read_stats(gbn_problem*, cudaStream_t, gbn_nesta_stats*);
 namespace {
 thread_local std::string g_err;
 
-struct DeviceGuard {
-  int prev = -1;
-  explicit DeviceGuard(int dev) {
-    if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
-  }
-  ~DeviceGuard() {
-    int cur = -1;
-    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
-  }
-};
-
 // cached device buffers of gbn_nesta_run_host
 struct HostRunCache {
   int W = 0, H = 0, F = 0, C = 0;
@@ -89,17 +78,6 @@ void free_host_cache(gbn_ctx* ctx) {
   if (!(ctx)) return set_error(GBN_ERR_INVALID, "null context"); \
   DeviceGuard guard_((ctx)->device)
 
-int check_dims(int W, int H, int F, int C) {
-  if (W <= 0 || H <= 0 || F <= 0 || C <= 0) return set_error(GBN_ERR_INVALID, "dimensions must be positive");
-  if (W % 8 != 0) return set_error(GBN_ERR_INVALID, "NDArray dimension 0 (width) is not multiple of 8");
-  return GBN_OK;
-}
-int check_fft(int W, int H) {
-  if (!find_size(W) || !find_size(H))
-    return set_error(GBN_ERR_UNSUPPORTED, "FFT lengths must be 7-smooth multiples of 8 in [8, 512] (got W=" +
-                                              std::to_string(W) + ", H=" + std::to_string(H) + ")");
-  return GBN_OK;
-}
 }  // namespace
 
 int set_error(int code, const std::string& msg) {

@@ -124,6 +124,34 @@ int set_error(int code, const std::string& msg);
 int host_flags_ready(gbn_ctx* ctx);
 int cuda_status(cudaError_t e, const char* what);
 
+// Makes `dev` current for the lifetime of the guard and restores the caller's
+// device on every return path.
+struct DeviceGuard {
+  int prev = -1;
+  explicit DeviceGuard(int dev) {
+    if (cudaGetDevice(&prev) == cudaSuccess && prev != dev) cudaSetDevice(dev);
+  }
+  ~DeviceGuard() {
+    int cur = -1;
+    if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+  }
+  DeviceGuard(const DeviceGuard&) = delete;
+  DeviceGuard& operator=(const DeviceGuard&) = delete;
+};
+
+// argument checks shared by the C ABI entry points
+inline int check_dims(int W, int H, int F, int C) {
+  if (W <= 0 || H <= 0 || F <= 0 || C <= 0) return set_error(GBN_ERR_INVALID, "dimensions must be positive");
+  if (W % 8 != 0) return set_error(GBN_ERR_INVALID, "NDArray dimension 0 (width) is not multiple of 8");
+  return GBN_OK;
+}
+inline int check_fft(int W, int H) {
+  if (!find_size(W) || !find_size(H))
+    return set_error(GBN_ERR_UNSUPPORTED, "FFT lengths must be 7-smooth multiples of 8 in [8, 512] (got W=" +
+                                              std::to_string(W) + ", H=" + std::to_string(H) + ")");
+  return GBN_OK;
+}
+
 // twiddle table for length L (nullptr when unsupported)
 const float2* ctx_twiddles(gbn_ctx* ctx, int L);
 // grow-only scratch of at least `bytes`

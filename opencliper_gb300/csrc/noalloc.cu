@@ -15,7 +15,10 @@
 // Every call reuses it: kernels of the call rewrite the tables and reset the
 // control block before anything reads them.  Calls whose work overlaps on the
 // GPU (different streams, or several host threads) share the one array and
-// race; serialise them.
+// race; serialise them.  The array's device address is resolved on the first
+// call on each device and kept for the life of the process, so the entry point
+// must not be used across cudaDeviceReset (nor may any other object of this
+// library: contexts hold streams of the device's primary context).
 #include <cstdint>
 #include <cstring>
 #include <mutex>
@@ -65,7 +68,6 @@ int static_scratch(int device, void** out) {
 }  // namespace
 
 int simple_recon_static(gbn_ctx* ctx, const float2* y, const float2* S, float2* x, int W, int H, int F, int C) {
-  if (!find_size(H) || !find_size(W)) return set_error(GBN_ERR_UNSUPPORTED, "unsupported FFT length");
   const size_t FH = size_t(F) * H, K = FH * C * W;
   if (K > kStaticMaxT || FH > kStaticMaxRows)
     return set_error(GBN_ERR_UNSUPPORTED,
@@ -88,13 +90,10 @@ extern "C" GBN_API int gbn_simple_recon_static(gbn_ctx* ctx, const float* d_y, c
   if (!ctx) return set_error(GBN_ERR_INVALID, "null context");
   if (!d_y || !d_x) return set_error(GBN_ERR_INVALID, "null buffer");
   if (!d_S) return set_error(GBN_ERR_INVALID, "missing sensitivity maps");
-  if (W <= 0 || H <= 0 || F <= 0 || C <= 0) return set_error(GBN_ERR_INVALID, "dimensions must be positive");
-  if (W % 8 != 0) return set_error(GBN_ERR_INVALID, "NDArray dimension 0 (width) is not multiple of 8");
-  int cur = -1;
-  if (cudaGetDevice(&cur) != cudaSuccess || cur != ctx->device) {
-    const cudaError_t e = cudaSetDevice(ctx->device);
-    if (e != cudaSuccess) return cuda_status(e, "cudaSetDevice");
-  }
+  int rc = check_dims(W, H, F, C);
+  if (rc == GBN_OK) rc = check_fft(W, H);
+  if (rc != GBN_OK) return rc;
+  DeviceGuard guard(ctx->device);  // the caller's current device is restored on return
   return simple_recon_static(ctx, reinterpret_cast<const float2*>(d_y), reinterpret_cast<const float2*>(d_S),
                              reinterpret_cast<float2*>(d_x), W, H, F, C);
 }

@@ -13,3 +13,18 @@ definitions of clFFT and CLBlast, and on libc's drand48 (see drand48.py).
 The per-operator kernels are additionally pinned by compiling the reference's
 own .cl sources on the host (oracle/refkernels, built into oracle/_ref/).
 """
+
+import os as _os
+from pathlib import Path as _Path
+
+
+def reference_root():
+    """Root of the reference source tree, or None when it is not on this machine.
+
+    The location comes from the REFERENCE_ROOT environment variable; without it
+    the recipe looks in the build container's read-only mount.  Tests that need
+    the reference's own files skip when this returns None (the GPU machine has
+    no reference tree)."""
+    root = _Path(_os.environ.get("REFERENCE_ROOT", "/root/reference"))
+    return root if root.is_dir() else None
+

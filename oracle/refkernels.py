@@ -6,8 +6,8 @@ vectorNormalization,complexElementProd,xImageSum,applyMask,complexAbsPow2,
 complexAbs,rss,initialize,optimizer}.cl from the reference tree, with the host shim in
 oracle/refkernels/shim and the harness oracle/refkernels/harness.cpp, into
 oracle/_ref/librefkernels.so.  The reference tree is only read when present
-(REFERENCE_ROOT, default /root/reference); elsewhere the library is simply
-unavailable and the tests that need it skip.  The functions below run the
+(oracle.reference_root()); elsewhere the library is simply unavailable and
+the tests that need it skip.  The functions below run the
 kernels on numpy arrays in the reference layouts.
 """
 from __future__ import annotations
@@ -22,14 +22,18 @@ import numpy as np
 
 HERE = Path(__file__).resolve().parent
 OUT = HERE / "_ref" / "librefkernels.so"
-REF = Path(os.environ.get("REFERENCE_ROOT", "/root/reference"))
+from oracle import reference_root as _reference_root
+
+_ROOT = _reference_root()
 SOURCES = ["hostKernelFunctions.cl", "temporalTV.cl", "vectorNormalization.cl", "complexElementProd.cl",
            "xImageSum.cl", "applyMask.cl", "complexAbsPow2.cl", "complexAbs.cl", "rss.cl", "initialize.cl",
            "optimizer.cl", "creabspline.cl", "reductions.cl"]
 
 
 def build(force: bool = False) -> Path | None:
-    kdir = REF / "src" / "kernels"
+    if _ROOT is None:
+        return OUT if OUT.exists() else None
+    kdir = _ROOT / "src" / "kernels"
     if not all((kdir / s).exists() for s in SOURCES):
         return OUT if OUT.exists() else None
     deps = [HERE / "refkernels" / "harness.cpp", HERE / "refkernels" / "shim" / "OpenCLIPER" / "kernels" /

@@ -17,7 +17,9 @@ from tests.conftest import ROOT
 
 sio = pytest.importorskip("scipy.io")
 
-REF_FILES = ["/root/reference/recon_fullySampled.mat", "/root/reference/recon_halfScan.mat"]
+from oracle import reference_root
+
+REF_FILES = ["recon_fullySampled.mat", "recon_halfScan.mat"]
 CLS = {6: np.float64, 7: np.float32, 8: np.int8, 9: np.uint8, 10: np.int16, 11: np.uint16, 12: np.int32,
        13: np.uint32, 14: np.int64, 15: np.uint64}
 
@@ -53,8 +55,10 @@ def _dump(tool, path, outdir) -> dict:
 
 @pytest.mark.parametrize("path", REF_FILES)
 def test_reads_reference_matio_files(tool, tmp_path, path):
-    if not os.path.exists(path):
+    root = reference_root()
+    if root is None or not (root / path).exists():
         pytest.skip("reference data files not available")
+    path = str(root / path)
     got = _dump(tool, path, tmp_path / "d")
     want = sio.loadmat(path)
     assert set(got) == {"Dims", "XData"}

@@ -10,6 +10,8 @@ gbn_simple_recon, then checks that oversized problems are refused.
 """
 from __future__ import annotations
 
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -39,9 +41,41 @@ def test_static_scratch_matches_allocating_entry_point(ctx, W, H, F, C):
         assert rel_l2(got, want) <= TOL
 
 
-def test_static_scratch_rejects_oversized_problem(ctx):
-    W = H = 512
-    F, C = 1, 8  # F*H*C*W = 2^21 > 2^20
+def _device_free_bytes() -> int:
+    """cudaMemGetInfo's free bytes, from the CUDA runtime the library loaded."""
+    g.lib()
+    with open("/proc/self/maps") as fh:
+        paths = sorted({ln.split()[-1] for ln in fh if "libcudart.so" in ln})
+    assert paths, "libcudart not loaded"
+    rt = ctypes.CDLL(paths[0])
+    free, total = ctypes.c_size_t(0), ctypes.c_size_t(0)
+    assert rt.cudaMemGetInfo(ctypes.byref(free), ctypes.byref(total)) == 0
+    return free.value
+
+
+def test_static_entry_point_allocates_nothing(built_lib):
+    # a context of its own: nothing else grows device memory between the calls
+    W, H, F, C = 64, 64, 2, 4
+    p = synth.make_fully_sampled(W, H, C, seed=5)
+    y = np.ascontiguousarray(np.repeat(p.y, F, axis=0))
+    with g.Context(0) as c:
+        dy, dS = c.to_device(y), c.to_device(p.S)
+        out = c.zeros((F, H, W), np.complex64)
+        _abi.call("gbn_simple_recon_static", c.handle, dy.ptr, dS.ptr, out.ptr, W, H, F, C)  # loads its kernels
+        c.sync()
+        before = _device_free_bytes()
+        for _ in range(3):
+            _abi.call("gbn_simple_recon_static", c.handle, dy.ptr, dS.ptr, out.ptr, W, H, F, C)
+        c.sync()
+        assert _device_free_bytes() == before
+        assert np.isfinite(out.get()).all()
+
+
+@pytest.mark.parametrize("W,H,F,C", [
+    (512, 512, 1, 8),   # F*H*C*W = 2^21 > 2^20
+    (8, 512, 17, 1),    # F*H = 8704 > 8192 with F*H*C*W = 69632 within its limit
+])
+def test_static_scratch_rejects_oversized_problem(ctx, W, H, F, C):
     dy = ctx.zeros((F, C, H, W), np.complex64)
     dS = ctx.zeros((C, H, W), np.complex64)
     out = ctx.zeros((F, H, W), np.complex64)
@@ -49,3 +83,13 @@ def test_static_scratch_rejects_oversized_problem(ctx):
         _abi.call("gbn_simple_recon_static", ctx.handle, dy.ptr, dS.ptr, out.ptr, W, H, F, C)
     assert ei.value.code == _abi.GBN_ERR_UNSUPPORTED
     assert "static scratch" in str(ei.value)
+
+
+def test_static_entry_point_reports_unsupported_length(ctx):
+    dy = ctx.zeros((1, 1, 88, 8), np.complex64)  # 88 = 8 * 11 is not 7-smooth
+    dS = ctx.zeros((1, 88, 8), np.complex64)
+    out = ctx.zeros((1, 88, 8), np.complex64)
+    with pytest.raises(g.GbnError) as ei:
+        _abi.call("gbn_simple_recon_static", ctx.handle, dy.ptr, dS.ptr, out.ptr, 8, 88, 1, 1)
+    assert ei.value.code == _abi.GBN_ERR_UNSUPPORTED
+    assert "W=8, H=88" in str(ei.value)
