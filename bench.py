@@ -358,7 +358,8 @@ def run_ours(args, dist: Dist) -> dict | None:
            "vs_baseline": None,
            "dtype": "c64 (column transforms on tcgen05: split fp16 operands, fp32 accumulation)" if mixed else "c64",
            "data": DATA_DESC,
-           "config": workload_config({"kept_rows": G, "precision": args.precision}),
+           "config": workload_config(),
+           "solver": {"kept_rows": G, "precision": args.precision},
            "e2e": {"value": round(n * K / (t2_max / 1e3), 3), "unit": UNIT, "h2d_bytes_per_step": int(bi),
                    "d2h_bytes_per_step": int(bo),
                    "pipeline": "inputs of step k+1 copied on the copy stream while step k is solved"},
@@ -748,31 +749,132 @@ def stress_form(ctx, stream, args=None) -> dict:
     return res
 
 
+def simple_form(ctx, stream, args=None, reps: int = 50) -> dict:
+    """SimpleMRIRecon (SimpleMRIRecon.cpp:80-101, the fully sampled 256x256
+    single-slice reconstruction with 8 coils): x = sum_c conj(S_c) ifft2(y_c)
+    through gbn_simple_recon on device-resident inputs, events on the library's
+    stream around each call with a 256 MiB L2 flush between calls; algorithmic
+    bytes = y + S read, x written; the FP32 CPU restatement
+    (oracle.nesta_ref.simple_recon, scipy.fft on all host cores) timed beside it."""
+    import torch
+
+    from opencliper_gb300 import api, synth
+    W, H, Cc = 256, 256, 8
+    p = synth.make_fully_sampled(W, H, Cc, seed=0)
+    dy, dS = ctx.to_device(p.y), ctx.to_device(p.S)
+    x = ctx.empty((1, H, W), np.complex64)
+    flush = torch.empty(L2_FLUSH_BYTES, dtype=torch.uint8, device=torch.device("cuda", ctx.device))
+    for _ in range(3):
+        api.simple_recon(ctx, dy, dS, x)
+    stream.synchronize()
+    n0 = ctx.launch_count()
+    times = []
+    for k in range(reps):
+        flush.fill_(k & 0xFF)
+        a, c = torch_events()
+        a.record(stream)
+        api.simple_recon(ctx, dy, dS, x)
+        c.record(stream)
+        times.append((a, c))
+    stream.synchronize()
+    launches = (ctx.launch_count() - n0) // reps
+    ms = float(np.median([a.elapsed_time(c) for a, c in times]))
+    alg = p.y.nbytes + p.S.nbytes + x.nbytes
+    peak, peak_src = measured_peak_hbm()
+    res = {"workload": f"SimpleMRIRecon, {W}x{H}, 1 frame, {Cc} coils, fully sampled, FP32", "unit": UNIT,
+           "value": round(1e3 / ms, 1), "ms_per_recon": round(ms, 4), "launches_per_recon": int(launches),
+           "roofline": {"bound": "hbm", "achieved": round(alg / (ms / 1e3) / 1e9, 1), "peak": peak, "unit": "GB/s",
+                        "frac": round(alg / (ms / 1e3) / 1e9 / peak, 4), "peak_source": f"{peak_src} hbm_gbs",
+                        "algorithmic_bytes": int(alg)}}
+    if args is None or not getattr(args, "no_cpu_baseline", False):
+        from oracle import nesta_ref as R
+        R.simple_recon(p.y, p.S)
+        t0 = time.perf_counter()
+        n = 0
+        while time.perf_counter() - t0 < 3.0:
+            R.simple_recon(p.y, p.S)
+            n += 1
+        cpu_s = (time.perf_counter() - t0) / n
+        res["cpu_baseline"] = {"value": round(1.0 / cpu_s, 2), "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
+                               "sample": f"{n} reconstructions by the FP32 restatement (scipy.fft workers="
+                                         f"{os.cpu_count()})"}
+    for a_ in (dy, dS, x):
+        a_.free()
+    return res
+
+
 # the batched form autotunes its shapes into the context: forms that should see the defaults run first
-FORMS = (("mixed", mixed_forms), ("motion", motion_form), ("registration", registration_form),
+FORMS = (("simple", simple_form), ("mixed", mixed_forms), ("motion", motion_form), ("registration", registration_form),
          ("batched", batched_form), ("stress", stress_form))
 
 
+REF_BUDGET_S = 300.0  # wall-clock budget of the reference arm's measured steps
+
+
+def cpu_port_recon() -> float:
+    """Seconds of one whole reconstruction of the headline workload by the FP32
+    CPU restatement of NestaUp::launch (setup and all 100 inner iterations)."""
+    from oracle import nesta_ref as R
+    p = _ref_problem()
+    t0 = time.perf_counter()
+    R.nesta(p.y, p.S, p.mask, R.NestaParams(**NESTA), "f32")
+    return time.perf_counter() - t0
+
+
+_REF_P = None
+
+
+def _ref_problem():
+    global _REF_P
+    if _REF_P is None:
+        from opencliper_gb300 import synth
+        _REF_P = synth.make_problem(WL["W"], WL["H"], WL["F"], WL["C"], WL["R"], seed=WL["seed"])
+    return _REF_P
+
+
 def run_reference(args, dist: Dist) -> dict | None:
+    """The reference arm: whole reconstructions (setup + 100 iterations) by the
+    FP32 restatement on the host cores, one per step.  One warm-up
+    reconstruction; then up to --steps measured ones while they fit the
+    REF_BUDGET_S wall-clock budget (each takes ~17 s on 16 cores), and the line
+    reports how many ran."""
     if dist.rank != 0:
         return None
-    samples = []
-    for k in range(args.warmup + args.steps):
-        s = cpu_port_sample(iters=2)
-        if k >= args.warmup:
-            samples.append(s["est_seconds_per_recon"])
-    est = float(np.mean(samples))
+    _ref_problem()
+    cpu_port_recon()  # warm-up: FFT plans, page-in
+    times = []
+    t_start = time.perf_counter()
+    for _ in range(args.steps):
+        times.append(cpu_port_recon())
+        elapsed = time.perf_counter() - t_start
+        if elapsed + times[-1] > REF_BUDGET_S:
+            break
+    est = float(np.mean(times))
     v = round(1.0 / est, 6)
     return {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": dist.ws,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(est * 1e3, 2),
+            "steps": len(times), "steps_requested": args.steps, "warmup": 1, "ms_per_step": round(est * 1e3, 2),
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "c64", "data": DATA_DESC,
             "config": workload_config(),
             "cpu_baseline": {"value": v, "unit": UNIT, "cores": os.cpu_count(), "kind": "port",
-                             "sample": "per step: FP32 numpy/scipy restatement of NestaUp::launch, setup + 2 "
-                                       "inner iterations of one reconstruction, extrapolated to 100 iterations "
-                                       "(the reference's OpenCL build is unavailable: no OpenCL ICD, clFFT, "
-                                       "CLBlast)"},
+                             "sample": f"per step one whole reconstruction (setup + {NESTA['maxIter']} inner "
+                                       f"iterations) by the FP32 numpy/scipy restatement of NestaUp::launch "
+                                       f"(scipy.fft workers={os.cpu_count()}); {len(times)} measured steps within a "
+                                       f"{REF_BUDGET_S:.0f} s budget after one warm-up (the reference's OpenCL "
+                                       "build is unavailable: no OpenCL ICD, clFFT, CLBlast)"},
             "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def relaunch_ranks(n: int, argv: list[str], script: str | None = None) -> int:
+    """`--gpus N` without a launcher: start N ranks of `script` (this file by
+    default) with torch.distributed.run on 127.0.0.1 (one process per GPU,
+    LOCAL_RANK = GPU index); rank 0 prints the JSON line."""
+    import socket
+    with socket.socket() as sk:
+        sk.bind(("127.0.0.1", 0))
+        port = sk.getsockname()[1]
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", f"--nproc-per-node={n}",
+           "--master-addr", "127.0.0.1", "--master-port", str(port), script or str(Path(__file__).resolve()), *argv]
+    return subprocess.call(cmd)
 
 
 def main(argv=None) -> int:
@@ -783,8 +885,8 @@ def main(argv=None) -> int:
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-cpu-baseline", action="store_true", help="skip the CPU restatement timing")
     ap.add_argument("--no-forms", action="store_true", help="skip the mixed, batched and motion form measurements")
-    ap.add_argument("--forms", default="mixed,batched,motion,registration",
-                    help="comma-separated forms to measure after the headline (mixed, batched, motion, "
+    ap.add_argument("--forms", default="simple,mixed,batched,motion,registration",
+                    help="comma-separated forms to measure after the headline (simple, mixed, batched, motion, "
                          "registration; stress, the 256-reconstruction ~150 GB batch, only when named)")
     ap.add_argument("--forms-only", action="store_true",
                     help="measure only the forms named by --forms (no headline line; for profiling)")
@@ -796,7 +898,12 @@ def main(argv=None) -> int:
     args = ap.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
+    if args.gpus > 1 and "WORLD_SIZE" not in os.environ:
+        return relaunch_ranks(args.gpus, list(sys.argv[1:] if argv is None else argv))
     dist = Dist()
+    if "WORLD_SIZE" in os.environ and dist.ws != args.gpus:
+        print(f"bench.py: --gpus {args.gpus} but WORLD_SIZE={dist.ws}; reporting the {dist.ws} ranks that run",
+              file=sys.stderr)
     try:
         if args.impl == "reference":
             out = run_reference(args, dist)

@@ -221,14 +221,18 @@ def _nrm2sq(v: np.ndarray) -> float:
 
 def nesta(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams, precision: str = "f32",
           rand_state: int = drand48.DEFAULT_STATE, record: bool = False, timings: dict | None = None,
-          mc=None, x_init: np.ndarray | None = None) -> NestaResult:
+          mc=None, x_init: np.ndarray | None = None, snapshots=None) -> NestaResult:
     """y: KData [F][C][H][W]; S: [C][H][W]; mask: pixel mask [F][H][W] (uint8).
     `timings`, when given, receives wall-clock marks: 'setup' (seconds until the
     first inner iteration) and 'iters' (seconds of each inner iteration).
     `mc` = (xn, xmesh, bb) runs the motion-compensated form (argsMC != nullptr):
     the sparsity operator becomes U = tTV(M x), Ut = M^T tTVadj (NestaUp.cpp:
     201-278), and the solve starts from `x_init` (the output XData's current
-    image) instead of E^H y (NestaUp.cpp:483-486)."""
+    image) instead of E^H y (NestaUp.cpp:483-486).
+    `snapshots`: inner-iteration counts k at which x_k (the iterate after k
+    inner iterations, counted over all outer loops) is copied into
+    stats["snapshots"][k]; with maxIntIter = 1 and stoptest = 0 it equals the
+    output of a run with maxIter = k."""
     import time as _time
     _t0 = _time.perf_counter()
     P = _P(precision)
@@ -280,6 +284,7 @@ def nesta(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams, prec
     qp = s(0)
     iters = 0
     hist = []
+    snaps = {}
     if timings is not None:
         timings["setup"] = _time.perf_counter() - _t0
         timings["iters"] = []
@@ -341,6 +346,8 @@ def nesta(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams, prec
                 timings["iters"].append(_t1 - _t0 - timings["setup"] - sum(timings["iters"]))
             if record:
                 hist.append(float(fx))
+            if snapshots is not None and iters in snapshots:
+                snaps[iters] = xk.copy()
             k += 1
         xref = xk.copy()                            # (889)
     stats = dict(normU=float(normU), normest_iters=ne_iters, maxX=float(maxX), maxUX=float(maxUX),
@@ -349,6 +356,8 @@ def nesta(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams, prec
                  rand_state=new_state)
     if record:
         stats["fx_hist"] = hist
+    if snapshots is not None:
+        stats["snapshots"] = snaps
     return NestaResult(xref, stats)
 
 

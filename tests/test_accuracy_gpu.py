@@ -1,0 +1,32 @@
+"""The metric's accuracy gate, NRMSE <= 1e-3 against FP64, on the large
+workloads, for the plain FP32 and the mixed-precision forms: the 384x384 x 30
+frames x 16 coils reconstruction, and four members of the 64-reconstruction
+uneven batch (largest coil count, largest frame count, largest W*F*C, the
+first) solved as one batch.  The FP64 reference is oracle/nesta_torch.py on the
+same device inputs (tests/accuracy_fp64.py reports the whole batch)."""
+from __future__ import annotations
+
+import pytest
+
+from tests import accuracy_fp64 as A
+
+pytestmark = [pytest.mark.gpu, pytest.mark.slow]
+
+GATE = 1e-3
+
+
+def test_large_workload_within_gate(ctx):
+    pytest.importorskip("torch")
+    (row,) = A.solve(ctx, [A.LARGE])
+    print(row)
+    assert row["fp32"] <= GATE and row["mixed"] <= GATE
+
+
+def test_uneven_batch_members_within_gate(ctx):
+    pytest.importorskip("torch")
+    shapes = A.batch_shapes()
+    rows = A.solve(ctx, [shapes[i] for i in A.sample_members(shapes)])
+    for r in rows:
+        print(r)
+    assert len(rows) >= 3
+    assert all(r["fp32"] <= GATE and r["mixed"] <= GATE for r in rows)

@@ -71,3 +71,36 @@ def test_replica_barrier_and_max_over_gloo_ranks():
     for p in procs:
         p.join(timeout=60)
     assert res == {0: 20.0, 1: 20.0}
+
+
+_RANK_SCRIPT = '''
+import json, os, sys
+sys.path.insert(0, {root!r})
+import bench
+d = bench.Dist()
+d.barrier()
+t = d.max(1.0 + d.rank)
+d.barrier()
+if d.rank == 0:
+    print(json.dumps({{"n_gpus": d.ws, "max": t, "local_ranks": d.ws}}), flush=True)
+d.close()
+'''
+
+
+def test_gpus_flag_launches_one_rank_per_gpu(tmp_path, capfd):
+    """bench.py --gpus N without a launcher starts N ranks through
+    torch.distributed.run; here the ranks run a small script doing the bench's
+    gloo barrier and max instead of the GPU workload."""
+    pytest.importorskip("torch")
+    import json
+
+    import bench
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    script = tmp_path / "ranks.py"
+    script.write_text(_RANK_SCRIPT.format(root=root))
+    rc = bench.relaunch_ranks(2, [], script=str(script))
+    assert rc == 0
+    lines = [ln for ln in capfd.readouterr().out.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    out = json.loads(lines[0])
+    assert out["n_gpus"] == 2 and out["max"] == 2.0

@@ -180,3 +180,25 @@ def test_oracle_reproduces_golden(name):
         assert np.abs(r["T"] - d["T"]).max() <= tol * np.abs(d["T"]).max() + 1e-6
     else:
         raise AssertionError(kind)
+
+
+@pytest.mark.parametrize("prm", [
+    dict(lambda_i=0.01, mu_f=1e-3, La=1.0, maxIntIter=1, maxIter=30, stoptest=0, miniter=7, tolVar=3e-4),
+    dict(lambda_i=1e-2, mu_f=3e-4, La=1.0, maxIntIter=4, maxIter=100, stoptest=1, miniter=7, tolVar=3e-4),
+])
+def test_torch_fp64_restatement_matches_numpy_fp64(prm):
+    """oracle/nesta_torch.py (the FP64 oracle for large workloads, run on the
+    GPU by the accuracy tests) against nesta_ref's FP64 mode on the CPU."""
+    pytest.importorskip("torch")
+    from opencliper_gb300 import synth
+    from oracle import nesta_ref as R
+    from oracle import nesta_torch as RT
+    p = synth.make_problem(40, 32, 5, 3, 4, seed=17)
+    ref = R.nesta(p.y, p.S, p.mask, R.NestaParams(**prm), "f64")
+    x, st = RT.nesta_f64(p.y, p.S, p.mask, R.NestaParams(**prm))
+    assert R.nrmse(x, ref.x) < 1e-11
+    assert st["inner_iters"] == ref.stats["inner_iters"]
+    assert st["normest_iters"] == ref.stats["normest_iters"]
+    assert st["rand_state"] == ref.stats["rand_state"]
+    for k in ("normU", "lambda_", "mu0", "mu_final", "fx_final"):
+        assert abs(st[k] - ref.stats[k]) <= 1e-10 * abs(ref.stats[k]), k
