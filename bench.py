@@ -165,6 +165,8 @@ def algorithmic_bytes(kind: str, G: int, shape: tuple | None = None) -> int:
         return T + T + G * W + T
     if kind == "inv_cols":   # T, S, x_k, x_ref, w in; x_{k+1}, w out
         return T + Sb + 3 * X + 2 * X
+    if kind == "iter":       # row-local iteration: IDFT_W(y) of the kept rows, S, x_k, x_ref, w_k in; x_{k+1}, w_{k+1} out
+        return T + Sb + 3 * X + 2 * X
     raise KeyError(kind)
 
 
@@ -312,7 +314,7 @@ def run_ours(args, dist: Dist) -> dict | None:
     prof = ctx.profile_read()
     ctx.profile(False)
     G = int(st["kept_rows"])
-    fused = {k: prof[k] for k in ("fwd_cols", "rows", "inv_cols")}
+    fused = {k: prof[k] for k in ("fwd_cols", "rows", "inv_cols", "iter") if prof[k][0] > 0}
     dom = max(fused, key=lambda k: fused[k][1])
     n_dom, ms_dom = fused[dom]
     avg_s = ms_dom / 1e3 / max(n_dom, 1)

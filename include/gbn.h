@@ -88,7 +88,10 @@ GBN_API int gbn_ctx_sync(gbn_ctx* ctx);
  * (glibc's default state, as if seed48 were never called). */
 GBN_API int gbn_ctx_seed48(gbn_ctx* ctx, const unsigned short seed16v[3]);
 GBN_API int gbn_ctx_get_rand48(gbn_ctx* ctx, unsigned short state16v[3]);
-/* tuning knobs: "k1_coils_per_block", "k2_ctas_per_sm" (>= 1),
+/* tuning knobs: "row_local" (1, default: problems whose kept k-space rows are
+ * each fully sampled or unsampled -- every phase-encode row mask -- run the
+ * one-kernel row-local iteration; 0: always the three-pass iteration),
+ * "k1_coils_per_block", "k2_ctas_per_sm" (>= 1),
  * "mixed_adjoint_tc" (0/1: the mixed form also runs the adjoint column pass on
  * the tensor cores) and "mixed_fwd_tc" (1: the mixed form's forward column
  * pass always on the tensor cores, 0: never -- its groups then run the plain
@@ -110,7 +113,8 @@ enum {
   GBN_PROF_INV_COLS = 2, /* adjoint column pass + tTV gradient + update   */
   GBN_PROF_SETUP = 3,    /* x0, maxima, norm estimate, row analysis       */
   GBN_PROF_OUTER = 4,    /* continuation-loop begin/end copies            */
-  GBN_PROF_KINDS = 5
+  GBN_PROF_ITER = 5,     /* row-local iteration: columns, residual, update */
+  GBN_PROF_KINDS = 6
 };
 GBN_API int gbn_ctx_profile(gbn_ctx* ctx, int enable);
 GBN_API int gbn_ctx_profile_read(gbn_ctx* ctx, int kind, unsigned long long* launches, double* total_ms);

@@ -24,7 +24,7 @@ GBN_FFT_BACKWARD = 1
 GBN_NOT_CONJUGATE = 0
 GBN_CONJUGATE = 1
 
-PROFILE_KINDS = {"fwd_cols": 0, "rows": 1, "inv_cols": 2, "setup": 3, "outer": 4}
+PROFILE_KINDS = {"fwd_cols": 0, "rows": 1, "inv_cols": 2, "setup": 3, "outer": 4, "iter": 5}
 
 
 class GbnError(RuntimeError):

@@ -11,6 +11,11 @@
 // their work inside the launches.  Groups run on their own streams, forked
 // from and joined back to the context stream.
 //
+// FP32 groups whose members' kept rows are each fully sampled or unsampled
+// (checked when the batch is created) run the one-kernel row-local iteration
+// (rowlocal.cuh); a later replay whose data break that sets the members'
+// status (7) and leaves their images unsolved.
+//
 // Power-method restart draws follow the reference's process-wide drand48
 // sequence as if the problems were solved one after another in batch order:
 // instance i starts sum_{j<i} W_j*H_j*F_j draws after the context state.  A
@@ -45,6 +50,8 @@ struct gbn_batch {
     dim3 g3tc;                     // mixed form: grid of the adjoint tensor-core kernel
     bool adjoint_tc = false;       // mixed form: adjoint column pass on the tensor cores
     bool tc = false;               // mixed form with the forward pass on the tensor cores (else plain FP32)
+    bool row_local = false;        // one-kernel row-local iteration (every member's kept rows full or unsampled)
+    bool any_stoptest = false;     // some member runs the stopping test
     dim3 g1, g3;
     unsigned maxIntIter = 0, maxIter = 0;
     cudaStream_t stream = nullptr;
@@ -120,7 +127,13 @@ int batch_enqueue(gbn_batch* b, bool graph_mode) {
         n_launch += launch_outer_begin(ctx, b->probs[i], int(nl), b->out[i], s);
         if (mixed) n_launch += launch_mixed_colmax(b->probs[i], s);
       }
-      for (unsigned it = 0; it < g.maxIter; ++it) {
+      if (g.row_local) {
+        // one launch more recomputes a member's last update when its stopping test ends the loop
+        const unsigned nit = g.maxIter + (g.any_stoptest ? 1u : 0u);
+        for (unsigned it = 0; it < nit; ++it) kh->iter_cols(g.tab, g.bm, int(it), g.g3, s);
+        n_launch += nit;
+      }
+      for (unsigned it = 0; it < (g.row_local ? 0u : g.maxIter); ++it) {
         if (mixed)
           launch_fwd_cols_tc(g.tab, g.bm, int(it), g.npad_max, g.g1, s);
         else
@@ -264,6 +277,27 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
     g.g3 = dim3(g.W / kWB, 2, frames);
     g.g3tc = inv_cols_tc_grid(g.W, g.H, frames);
     g.adjoint_tc = g.tc && ctx->mixed_adjoint_tc != 0;
+    // row-local iteration: every member's current data keep only fully
+    // sampled or unsampled rows
+    const SizeKernels* kh = find_size(g.H);
+    if (!g.tc && kh->iter_cols && ctx->row_local) {
+      bool all = true;
+      for (int i : g.idx) {
+        gbn_problem* P = b->probs[i];
+        g.any_stoptest = g.any_stoptest || b->prm[i].stoptest == 1;
+        ctx->launches += launch_pre(P, b->prm[i], ctx->stream);
+        int part = 1;
+        if ((e = cudaMemcpyAsync(&part, &P->st->partial_rows, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream)) !=
+                cudaSuccess ||
+            (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) {
+          rc = cuda_status(e, "batch row analysis");
+          break;
+        }
+        all = all && part == 0;
+      }
+      if (rc != GBN_OK) break;
+      g.row_local = all;
+    }
   }
   if (rc == GBN_OK && (e = cudaGetLastError()) != cudaSuccess) rc = cuda_status(e, "batch tables");
   if (rc != GBN_OK) {

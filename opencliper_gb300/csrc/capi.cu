@@ -242,6 +242,8 @@ int gbn_ctx_destroy(gbn_ctx* ctx) {
     cudaStreamDestroy(ctx->mc_stream);
   }
   if (ctx->host_flags) cudaFreeHost(ctx->host_flags);
+  if (ctx->host_partial) cudaFreeHost(ctx->host_partial);
+  if (ctx->ev_partial) cudaEventDestroy(ctx->ev_partial);
   for (cudaEvent_t x : ctx->ev_flag)
     if (x) cudaEventDestroy(x);
   if (ctx->ev_mc_x) cudaEventDestroy(ctx->ev_mc_x);
@@ -307,6 +309,11 @@ int gbn_ctx_set_tuning(gbn_ctx* ctx, const char* key, int value) {
   if (!std::strcmp(key, "mixed_adjoint_tc")) {
     if (value != 0 && value != 1) return set_error(GBN_ERR_INVALID, "mixed_adjoint_tc is 0 or 1");
     ctx->mixed_adjoint_tc = value;
+    return GBN_OK;
+  }
+  if (!std::strcmp(key, "row_local")) {
+    if (value != 0 && value != 1) return set_error(GBN_ERR_INVALID, "row_local is 0 or 1");
+    ctx->row_local = value;
     return GBN_OK;
   }
   if (!std::strcmp(key, "mixed_fwd_tc")) {

@@ -35,6 +35,10 @@ struct gbn_ctx {
   int k1_coils_per_block = 4;         // tuning: coils per CTA in the forward column pass
   int k2_ctas_per_sm = 4;             // tuning: persistent CTAs per SM in the row pass
   int mixed_adjoint_tc = 0;           // tuning: mixed form runs the adjoint column pass on the tensor cores
+  int row_local = 1;                  // tuning: fused row-local iteration when every kept row is fully sampled
+                                      // or unsampled (0: always the three-pass iteration)
+  int* host_partial = nullptr;        // pinned: partly sampled kept rows of the current run (read per run)
+  cudaEvent_t ev_partial = nullptr;
   int mixed_fwd_tc = -1;              // tuning: mixed form's forward pass on the tensor cores: 1 always, 0 never,
                                       // -1 per shape (autotuned where measured, else H >= 320)
   // autotuned launch shapes per problem shape (W, H, F, C) (autotune.cu)
@@ -82,6 +86,7 @@ struct gbn_problem {
   float2* xk0 = nullptr;
   float2* xk1 = nullptr;
   float2* wacc = nullptr;
+  float2* wacc1 = nullptr;
   gbn::NestaDevState* st = nullptr;
   float* fmean = nullptr;
   int fmean_cap = 0;

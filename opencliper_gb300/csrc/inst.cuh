@@ -3,6 +3,7 @@
 
 #include "nesta_kernels.cuh"
 #include "registry.h"
+#include "rowlocal.cuh"
 
 namespace gbn {
 
@@ -61,6 +62,13 @@ struct Launchers {
       launch_pdl(k_inv_cols<L, false>, grid, kColNT, InvColsSmem<L>::BYTES, s, tab, bm, it);
     }
   }
+  static void iter_cols(const FusedArgs* tab, const BatchMap& bm, int it, dim3 grid, cudaStream_t s) {
+    if constexpr (iter_cols_ok(L)) {
+      static bool ok = false;
+      allow_smem(k_iter_cols<L>, IterColsSmem<L>::BYTES, ok);
+      launch_pdl(k_iter_cols<L>, grid, kColNT, IterColsSmem<L>::BYTES, s, tab, bm, it);
+    }
+  }
   static void fft_rows(const float2* in, float2* out, int nrows, int inv, float scale, const float2* tw, int grid,
                        cudaStream_t s) {
     k_fft_rows_dense<L><<<grid, kRowNT, 0, s>>>(in, out, nrows, inv, scale, tw);
@@ -71,7 +79,8 @@ struct Launchers {
   }
   static SizeKernels entry() {
     static_assert(fft_size_ok(L), "unsupported transform length");
-    return SizeKernels{L, &fwd_cols, &rows, &inv_cols, &fft_rows, &fft_cols, RowCfg<L>::RPC, &rows_occupancy};
+    return SizeKernels{L, &fwd_cols, &rows, &inv_cols, &fft_rows, &fft_cols,
+                       iter_cols_ok(L) ? &iter_cols : nullptr, RowCfg<L>::RPC, &rows_occupancy};
   }
 };
 

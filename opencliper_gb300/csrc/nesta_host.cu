@@ -43,7 +43,8 @@ uint64_t lcg48_apply(const Lcg48& j, uint64_t x) { return (j.a * x + j.c) & kMas
 // Kept k-space rows: a row (f, h) is carried by the solver when its mask row
 // has any sampled pixel or any coil holds a nonzero datum there.  Rows that are
 // neither contribute exactly zero to E^H(Ex - y) and to ||Ex - y||^2.
-// grid = (H, F)
+// flags: 0 not kept, 1 kept with sampled pixels, 2 kept for its data only;
+// full: every pixel of the mask row sampled.  grid = (H, F)
 // ---------------------------------------------------------------------------
 __global__ void k_rowflags(const float2* __restrict__ y, const uint8_t* __restrict__ mask, int W, int H, int F, int C,
                            int* __restrict__ flags, int* __restrict__ full) {
@@ -57,6 +58,7 @@ __global__ void k_rowflags(const float2* __restrict__ y, const uint8_t* __restri
   }
   any = __syncthreads_or(any);
   all = __syncthreads_and(all);
+  const int sampled = any;
   if (!any) {
     for (int c = 0; c < C && !any; ++c) {
       const float4* yr = reinterpret_cast<const float4*>(y + ((size_t(f) * C + c) * H + h) * W);
@@ -69,7 +71,7 @@ __global__ void k_rowflags(const float2* __restrict__ y, const uint8_t* __restri
     }
   }
   if (t == 0) {
-    flags[f * H + h] = any;
+    flags[f * H + h] = sampled ? 1 : (any ? 2 : 0);
     full[f * H + h] = all;
   }
 }
@@ -78,17 +80,19 @@ constexpr int kStatusRowsOverflow = 6;  // NestaDevState::status: kept rows beyo
 
 // one CTA of 512 threads (H <= 512): per-frame prefix numbering of kept rows;
 // rows beyond the row buffer's capacity `cap` are dropped (rowmap -1) and
-// reported in *status
+// reported in *status; *partial = kept rows whose mask row is sampled in part
 __global__ void __launch_bounds__(512) k_rowscan(const int* __restrict__ flags, const int* __restrict__ full, int H,
                                                  int F, int* __restrict__ rowmap, int* __restrict__ rowoff,
                                                  int* __restrict__ rows_h, int* __restrict__ rows_f,
-                                                 int* __restrict__ row_full, int cap, int* __restrict__ status) {
+                                                 int* __restrict__ row_full, int cap, int* __restrict__ status,
+                                                 int* __restrict__ partial) {
   __shared__ int wsum[16];
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-  int base = 0;
+  int base = 0, npart = 0;
   bool dropped = false;
   for (int f = 0; f < F; ++f) {
     const int fl = (t < H) ? flags[f * H + t] : 0;
+    npart += __syncthreads_count(t < H && fl == 1 && !full[f * H + t]);
     const unsigned bal = __ballot_sync(0xffffffffu, fl);
     const int pre = __popc(bal & ((1u << lane) - 1u));
     if (lane == 0) wsum[wid] = __popc(bal);
@@ -115,6 +119,7 @@ __global__ void __launch_bounds__(512) k_rowscan(const int* __restrict__ flags, 
   }
   if (t == 0) {
     rowoff[F] = base;
+    *partial = npart;
     if (dropped) atomicExch(status, kStatusRowsOverflow);
   }
 }
@@ -418,6 +423,7 @@ __global__ void k_outer_begin(NestaDevState* st, int nl, float* fmean, const flo
     s.Lmu = Lmu;
     s.Lmu1 = 1.0f / Lmu;
     s.qpDone = 0;
+    s.fixup = 0;
     s.last_iter = s.maxIter - 1;
   }
   for (size_t i = blockIdx.x * size_t(blockDim.x) + threadIdx.x; i < n; i += size_t(gridDim.x) * blockDim.x) {
@@ -501,6 +507,7 @@ int problem_alloc(gbn_problem* P) {
   A((void**)&P->xk0, X * sizeof(float2));
   A((void**)&P->xk1, X * sizeof(float2));
   A((void**)&P->wacc, X * sizeof(float2));
+  A((void**)&P->wacc1, X * sizeof(float2));
   A((void**)&P->st, sizeof(NestaDevState));
   A((void**)&P->d_args, sizeof(FusedArgs));
   A((void**)&P->ctl, sizeof(ClassCtl));
@@ -555,7 +562,7 @@ void motion_free(gbn_problem* P);
 
 void problem_free(gbn_problem* P) {
   void* ptrs[] = {P->flags, P->full_fh, P->rowmap, P->rowoff,  P->rows_h, P->rows_f,  P->row_full, P->T,
-                  P->xk0,   P->xk1,     P->wacc,   P->st,      P->fmean,  P->part_tv, P->part_r,   P->part_ne,
+                  P->xk0,   P->xk1,     P->wacc,   P->wacc1,  P->st,      P->fmean,  P->part_tv, P->part_r,   P->part_ne,
                   P->ne_b,  P->d_args,  P->ctl,      P->fk,     P->colmax, P->smax,   P->fa};
   for (void* p : ptrs)
     if (p) cudaFree(p);
@@ -566,7 +573,7 @@ void problem_free(gbn_problem* P) {
 void launch_row_analysis(gbn_problem* P, cudaStream_t s) {
   k_rowflags<<<dim3(P->H, P->F), 128, 0, s>>>(P->y, P->mask, P->W, P->H, P->F, P->C, P->flags, P->full_fh);
   k_rowscan<<<1, 512, 0, s>>>(P->flags, P->full_fh, P->H, P->F, P->rowmap, P->rowoff, P->rows_h, P->rows_f,
-                              P->row_full, int(P->T_rows), &P->st->status);
+                              P->row_full, int(P->T_rows), &P->st->status, &P->st->partial_rows);
 }
 
 FusedArgs make_args(gbn_problem* P, float2* xref) {
@@ -591,6 +598,7 @@ FusedArgs make_args(gbn_problem* P, float2* xref) {
   a.xk1 = P->xk1;
   a.xref = xref;
   a.wacc = P->wacc;
+  a.wacc1 = P->wacc1;
   a.st = P->st;
   a.fmean = P->fmean;
   a.part_tv = P->part_tv;
@@ -600,6 +608,7 @@ FusedArgs make_args(gbn_problem* P, float2* xref) {
   const unsigned N = unsigned(P->W) * unsigned(P->H);
   a.s_fwd = float(1.0 / std::sqrt(double(N)));               // NestaUp.cpp:712: 1/(sqrt(cols*rows*slices))
   a.s_adj = std::sqrt(float(N)) * (1.0f / float(N));        // NestaUp.cpp:749 sqrt(float(N)) times clFFT 1/N
+  a.s_row = float(double(P->W) * double(a.s_fwd));
   a.ntv = P->F * (P->W / kWB);
   return a;
 }
@@ -638,7 +647,8 @@ int run_prepare(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm) {
   int rc;
   if ((rc = grow(P->fmean, P->fmean_cap, std::max<int>(1, int(prm->miniter)))) != GBN_OK) return rc;
   if ((rc = grow(P->part_tv, P->part_tv_cap, 2 * F * (W / kWB))) != GBN_OK) return rc;
-  if ((rc = grow(P->part_r, P->part_r_cap, int(steps_max) * kRowWarps)) != GBN_OK) return rc;
+  if ((rc = grow(P->part_r, P->part_r_cap, std::max(int(steps_max) * kRowWarps, 2 * F * (W / kWB)))) != GBN_OK)
+    return rc;
   if ((rc = grow(P->part_ne, P->part_ne_cap, nblk_ne * kNeMaxSlots * 2)) != GBN_OK) return rc;
   if ((rc = grow(P->ne_b, P->ne_b_cap, N * F)) != GBN_OK) return rc;
   return GBN_OK;
@@ -740,6 +750,14 @@ int read_stats(gbn_problem* P, cudaStream_t s, gbn_nesta_stats* stats) {
 
 int nesta_run_mc(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, float2* x_out);
 
+// pinned read-back slot and event of the per-run row-structure check (first use)
+int partial_flag_ready(gbn_ctx* ctx) {
+  if (ctx->host_partial) return GBN_OK;
+  cudaError_t e = cudaHostAlloc(&ctx->host_partial, sizeof(int), cudaHostAllocDefault);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_partial, cudaEventDisableTiming);
+  return cuda_status(e, "pinned row-structure flag");
+}
+
 int nesta_run(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, float2* x_out, gbn_nesta_stats* stats) {
   if (!x_out) return set_error(GBN_ERR_INVALID, "null argument");
   int rc = run_prepare(ctx, P, prm);
@@ -763,25 +781,51 @@ int nesta_run(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, float2*
   const FusedArgs* tab = P->d_args;
   const BatchMap bm = single_map(F, P->ctl);
 
+  // the row-local iteration needs every kept row fully sampled or unsampled:
+  // the row analysis's count of partly sampled rows comes back to pinned
+  // host memory while the setup below is queued, and is read before the
+  // iterations are
+  const bool check_rows = ctx->row_local && kh->iter_cols;
+  int rc2 = check_rows ? partial_flag_ready(ctx) : GBN_OK;
+  if (rc2 != GBN_OK) return rc2;
+  cudaError_t ef = cudaSuccess;
   int n_setup = 0;
   GBN_LAUNCH(ctx, GBN_PROF_SETUP, n_setup, {
     n_setup += launch_pre(P, *prm, s);
+    if (check_rows) {
+      ef = cudaMemcpyAsync(ctx->host_partial, &P->st->partial_rows, sizeof(int), cudaMemcpyDeviceToHost, s);
+      if (ef == cudaSuccess) ef = cudaEventRecord(ctx->ev_partial, s);
+    }
     n_setup += launch_store_args(P->d_args, a, s);
     n_setup += launch_group_init(tab, 1, kw->rows_per_cta, P->ctl, s);
-    // x0 = E^H y (NestaUp.cpp:465-486)
+    // x0 = E^H y (NestaUp.cpp:465-486); T keeps IDFT_W(y) of the kept rows
     kw->rows(tab, bm, 0, false, g2a, s);
     kh->inv_cols(tab, bm, 0, false, g3, s);
     n_setup += 2;
     n_setup += launch_constants(ctx, P, x_out, RandStart{ctx->rand48, nullptr, 1, 0}, s);
     ctx->rand48 = lcg48_apply(lcg_jump_k(uint64_t(W) * uint64_t(H) * uint64_t(F)), ctx->rand48);
   });
+  if (ef != cudaSuccess) return cuda_status(ef, "row structure read-back");
+  bool row_local = false;
+  if (ctx->row_local && kh->iter_cols) {
+    if ((ef = cudaEventSynchronize(ctx->ev_partial)) != cudaSuccess) return cuda_status(ef, "row structure read-back");
+    row_local = *ctx->host_partial == 0;
+  }
+  // stopping test on: one more launch per outer loop recomputes the last
+  // update if the rule stops the loop (row-local iteration only)
+  const unsigned n_iter_launch = prm->maxIter + ((row_local && prm->stoptest == 1) ? 1u : 0u);
 
   for (unsigned nl = 1; nl <= prm->maxIntIter; ++nl) {
     GBN_LAUNCH(ctx, GBN_PROF_OUTER, 1, launch_outer_begin(ctx, P, int(nl), x_out, s));
-    for (unsigned it = 0; it < prm->maxIter; ++it) {
-      GBN_LAUNCH(ctx, GBN_PROF_FWD_COLS, 1, kh->fwd_cols(tab, bm, int(it), cpb, g1, s));
-      GBN_LAUNCH(ctx, GBN_PROF_ROWS, 1, kw->rows(tab, bm, int(it), true, g2, s));
-      GBN_LAUNCH(ctx, GBN_PROF_INV_COLS, 1, kh->inv_cols(tab, bm, int(it), true, g3, s));
+    if (row_local) {
+      for (unsigned it = 0; it < n_iter_launch; ++it)
+        GBN_LAUNCH(ctx, GBN_PROF_ITER, 1, kh->iter_cols(tab, bm, int(it), g3, s));
+    } else {
+      for (unsigned it = 0; it < prm->maxIter; ++it) {
+        GBN_LAUNCH(ctx, GBN_PROF_FWD_COLS, 1, kh->fwd_cols(tab, bm, int(it), cpb, g1, s));
+        GBN_LAUNCH(ctx, GBN_PROF_ROWS, 1, kw->rows(tab, bm, int(it), true, g2, s));
+        GBN_LAUNCH(ctx, GBN_PROF_INV_COLS, 1, kh->inv_cols(tab, bm, int(it), true, g3, s));
+      }
     }
     GBN_LAUNCH(ctx, GBN_PROF_OUTER, 1, launch_outer_end(ctx, P, x_out, s));
   }

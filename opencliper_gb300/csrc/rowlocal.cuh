@@ -1,0 +1,423 @@
+// Row-local tTV-NESTA iteration: one fused kernel per inner iteration for
+// problems whose kept k-space rows are each either fully sampled or not
+// sampled at all (every Cartesian phase-encode mask, i.e. every row mask of
+// SamplingMasksData, SamplingMasksData.cpp:389-441).
+//
+// For such a row the mask does not vary along the readout (W) axis, so the
+// row transform of the residual and its inverse cancel:
+//   IDFT_W( s * DFT_W(t) - y )  =  W*s*t - IDFT_W(y)          (fully sampled row)
+//   IDFT_W( 0 * DFT_W(t) - y )  =  -IDFT_W(y)                 (row kept for its data only)
+// with t the column transform DFT_H(S_c x_f) of that row and s = 1/sqrt(N) the
+// reference's forward scale (NestaUp.cpp:712-718).  IDFT_W(y) of every kept
+// row is what the setup's adjoint row pass leaves in T when it forms
+// x0 = E^H y, and it stays there for the whole solve.  The residual's norm
+// follows from Parseval: ||s DFT_W(t) - y||^2 = ||W s t - IDFT_W(y)||^2 / W.
+// So E^H(E x - y) (NestaUp.cpp:710-756) becomes a per-column operation:
+//   rho = W s DFT_H(S_c x_f)[kept rows] - IDFT_W(y)[kept rows]
+//   A^H r = (sqrt(N)/N) sum_c conj(S_c) IDFT_H(rho)
+// and the whole inner iteration runs in one kernel.
+//
+// k_iter_cols<H>: grid (W/kWB, 2, frames) in clusters of 2 along y; CTA =
+// (frame, 8 columns, half of the coils).  Per coil: forward column DFT of
+// S_c x_f (dit2<A,B>), residual on the kept rows, inverse column DFT
+// (dit2<B,A> of the conjugate) and conj(S_c) accumulation.  The forward
+// pass-2 item (w, k1) holds rows k1 + A*k2, exactly the rows the inverse
+// pass-1 item s' = k1 needs, so the residual never leaves registers.  The two
+// coil halves are summed through distributed shared memory, then the tTV
+// gradient (temporalTV.cl:78-107 with NestaUp's negation, vectorNormalization.cl
+// :42-56) and the Nesterov update (NestaUp.cpp:758-875) finish each pixel.
+// The tTV objective terms (Scnrm2, Cdotc of NestaUp.cpp:686-691) and ||r||^2
+// are written as fixed-slot partial sums; the last CTA of an instance reduces
+// them in fixed order and runs the scalar recurrence (nesta_scalar_step).
+//
+// The update of iteration k uses apk = (k+1)/2 and tauk = 2/(k+3), what the
+// scalar recurrence yields unless the stopping test fires for the second time
+// at k; then the reference updates with k = maxIter and stops
+// (NestaUp.cpp:808-831).  x and w are ping-pong buffers, so the launch after
+// such an iteration (its index is last_iter + 1) recomputes that update from
+// the unchanged x_k and w_k with the recurrence's weights ("fixup" mode).
+#pragma once
+
+#include "nesta_kernels.cuh"
+
+namespace gbn {
+
+constexpr int kStatusRowStructure = 7;  // NestaDevState::status: a kept row is partly sampled (row-local path)
+
+template <int H>
+struct IterColsSmem {
+  static constexpr int A = Split<H>::A, B = Split<H>::B;
+  static constexpr int KSF = col_ks(B);  // forward exchange: slot (k1, s*kWB + w), k1 < A
+  static constexpr int KSI = col_ks(A);  // inverse exchange: slot (k1', s'*kWB + w), k1' < B
+  static constexpr int EXN = (A * KSF > B * KSI) ? A * KSF : B * KSI;
+  static constexpr int RCAP = H / 4;                     // kept rows whose IDFT_W(y) is staged (R >= 4)
+  static constexpr int S_OFF = 0;                        // float2 [2][H][kWB]
+  static constexpr int Y_OFF = S_OFF + 2 * H * kWB;      // float2 [2][RCAP][kWB]
+  static constexpr int EX_OFF = Y_OFF + 2 * RCAP * kWB;  // float2 [EXN]
+  static constexpr int TW_OFF = EX_OFF + EXN;            // float2 [2H]: the two first-pass twiddle tables
+  static constexpr int F2_END = TW_OFF + 2 * H;
+  static constexpr int BYTES = F2_END * 8 + H * 4 + (kColNT / 32) * 8 + kFmeanCopy * 4 + 16;
+  static_assert(cdiv(kWB * B, kColNT) * A * kColNT <= 2 * H * kWB, "accumulator exchange must fit the S buffers");
+};
+
+// Lengths whose first factor A (split_a) keeps the per-thread state of
+// k_iter_cols in registers at 3 CTAs per SM; longer columns run the
+// three-pass iteration.
+constexpr bool iter_cols_ok(int H) { return split_a(H) <= 16; }
+
+template <int H>
+__global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, 3)
+    k_iter_cols(const FusedArgs* __restrict__ tab, const __grid_constant__ BatchMap bm, int it) {
+  using L = IterColsSmem<H>;
+  constexpr int A = L::A, B = L::B, KSF = L::KSF, KSI = L::KSI, RCAP = L::RCAP;
+  constexpr int N1 = kWB * B;  // forward pass-1 items (w, s), s < B: rows B*n1 + s
+  constexpr int N2 = kWB * A;  // forward pass-2 = inverse pass-1 items (w, k1), k1 < A: rows k1 + A*k2
+  constexpr int N3 = kWB * B;  // inverse pass-2 items (w, k1'), k1' < B: rows k1' + B*k2
+  constexpr int NI1 = cdiv(N1, kColNT), NI2 = cdiv(N2, kColNT), NI3 = cdiv(N3, kColNT);
+  extern __shared__ float4 smem4[];
+  float2* Sb = reinterpret_cast<float2*>(smem4) + L::S_OFF;
+  float2* Yb = reinterpret_cast<float2*>(smem4) + L::Y_OFF;
+  float2* ex = reinterpret_cast<float2*>(smem4) + L::EX_OFF;
+  float2* tws = reinterpret_cast<float2*>(smem4) + L::TW_OFF;
+  int* rcode = reinterpret_cast<int*>(reinterpret_cast<float2*>(smem4) + L::F2_END);
+  double* sred = reinterpret_cast<double*>(rcode + H);
+  float* fm = reinterpret_cast<float*>(sred + kColNT / 32);
+  __shared__ int s_fin;
+  namespace cgr = cooperative_groups;
+  cgr::cluster_group cluster = cgr::this_cluster();
+
+  const int inst = find_inst(bm, blockIdx.z);
+  const FusedArgs& a = tab[inst];
+  NestaDevState* st = a.st;
+  const int t = threadIdx.x;
+  const int half = blockIdx.y, f = blockIdx.z - bm.fbase[inst], w0 = blockIdx.x * kWB;
+  const int W = a.W, C = a.C, F = a.F;
+  const size_t N = size_t(a.N);
+  const int rowbase = a.rowoff[f];
+  const int nrows = a.rowoff[f + 1] - rowbase;
+  const bool staged = nrows <= RCAP;  // kept rows fit the shared buffers (uniform per CTA)
+  const int cmid = (C + 1) / 2;
+  const int cbeg = half ? cmid : 0, cend = half ? C : cmid;
+
+  // S and IDFT_W(y) (in T since the setup) are inputs of the whole solve: they
+  // are staged before the dependency wait
+  auto issue_S = [&](int c, int buf) {
+    const float2* src = a.S + size_t(c) * N + w0;
+    float2* dst = Sb + buf * H * kWB;
+    for (int q = t; q < H * (kWB / 2); q += kColNT) {
+      const int row = q / (kWB / 2), part = q % (kWB / 2);
+      cp_async16(dst + row * kWB + 2 * part, src + size_t(row) * W + 2 * part);
+    }
+  };
+  auto issue_Y = [&](int c, int buf) {
+    if (staged) {
+      const float2* src = a.T + (size_t(rowbase) * C + c) * W + w0;
+      float2* dst = Yb + buf * RCAP * kWB;
+      for (int q = t; q < nrows * (kWB / 2); q += kColNT) {
+        const int j = q / (kWB / 2), part = q % (kWB / 2);
+        cp_async16(dst + j * kWB + 2 * part, src + size_t(j) * C * W + 2 * part);
+      }
+    }
+  };
+  if (cbeg < cend) {
+    issue_S(cbeg, 0);
+    issue_Y(cbeg, 0);
+  }
+  cp_async_commit();
+  // row codes: j >= 0 fully sampled kept row j; -2 - j kept row j without
+  // samples (data only); -1 not kept
+  for (int i = t; i < H; i += kColNT) {
+    const int j = a.rowmap[f * H + i];
+    rcode[i] = (j < 0) ? -1 : (a.row_full[rowbase + j] ? j : -2 - j);
+  }
+  // twiddles: [k1*B + s] = w_H^(s*k1) (forward first pass), [H + k1'*A + s'] (inverse first pass)
+  for (int i = t; i < 2 * H; i += kColNT) tws[i] = __ldg(a.twH + i);
+  grid_dep_wait();  // x_k, w_k and the scalar state come from the previous iteration
+  grid_dep_release();
+
+  // which update this launch computes (uniform over the instance, so over each cluster)
+  const int last = st->last_iter;
+  bool fix = false;
+  int itx = it;
+  if (st->partial_rows) {  // the data changed under a captured row-local solve
+    if (t == 0 && half == 0 && blockIdx.x == 0 && f == 0 && it == 0) st->status = kStatusRowStructure;
+    cp_async_wait<0>();
+    return;
+  }
+  if (it > last) {
+    if (!(st->fixup && it == last + 1)) {
+      cp_async_wait<0>();
+      return;
+    }
+    fix = true;
+    itx = last;
+  }
+  const float2* __restrict__ xk = (itx & 1) ? a.xk1 : a.xk0;
+  float2* __restrict__ xn = (itx & 1) ? a.xk0 : a.xk1;
+  const float2* __restrict__ wk = (itx & 1) ? a.wacc1 : a.wacc;
+  float2* __restrict__ wn = (itx & 1) ? a.wacc : a.wacc1;
+  const float2* __restrict__ x = xk + size_t(f) * N;
+  const float inv_mu = 1.0f / st->mu;
+
+  // x_k at this thread's forward pass-1 items, reused for every coil
+  float2 xv[NI1][A];
+#pragma unroll
+  for (int ii = 0; ii < NI1; ++ii) {
+    const int i = t + ii * kColNT;
+    if (i < N1) {
+      const int w = i % kWB, s = i / kWB;
+#pragma unroll
+      for (int n1 = 0; n1 < A; ++n1) xv[ii][n1] = x[size_t(B * n1 + s) * W + w0 + w];
+    }
+  }
+  // tTV objective partial sums over the tile (first half only; not in fixup mode)
+  float su2 = 0.f, sud = 0.f;
+  if (half == 0 && !fix) {
+    const float2* __restrict__ xm = xk + size_t((f + F - 1) % F) * N;
+#pragma unroll
+    for (int ii = 0; ii < NI1; ++ii) {
+      const int i = t + ii * kColNT;
+      if (i < N1) {
+        const int w = i % kWB, s = i / kWB;
+#pragma unroll
+        for (int n1 = 0; n1 < A; ++n1) {
+          const float2 d = csub(xv[ii][n1], xm[size_t(B * n1 + s) * W + w0 + w]);
+          const float2 u = tv_normalize(d, inv_mu);
+          su2 = fmaf(u.x, u.x, fmaf(u.y, u.y, su2));
+          sud = fmaf(u.x, d.x, fmaf(u.y, d.y, sud));
+        }
+      }
+    }
+  }
+
+  float2 acc[NI3][A];
+#pragma unroll
+  for (int ii = 0; ii < NI3; ++ii)
+#pragma unroll
+    for (int k2 = 0; k2 < A; ++k2) acc[ii][k2] = make_float2(0.f, 0.f);
+  const float s_row = a.s_row;
+  float racc = 0.f;
+
+  for (int c = cbeg; c < cend; ++c) {
+    const int buf = (c - cbeg) & 1;
+    cp_async_wait<0>();
+    __syncthreads();  // coil c staged; the previous coil's inverse pass 2 has read the exchange
+    if (c + 1 < cend) {
+      issue_S(c + 1, buf ^ 1);
+      issue_Y(c + 1, buf ^ 1);
+    }
+    cp_async_commit();
+    const float2* Sc = Sb + buf * H * kWB;
+    const float2* Yc = Yb + buf * RCAP * kWB;
+    // forward pass 1: S_c x_f, DFT_A, twiddles
+#pragma unroll
+    for (int ii = 0; ii < NI1; ++ii) {
+      const int i = t + ii * kColNT;
+      if (i < N1) {
+        const int w = i % kWB, s = i / kWB;
+        float2 v[A];
+#pragma unroll
+        for (int n1 = 0; n1 < A; ++n1) v[n1] = cmul(xv[ii][n1], Sc[(B * n1 + s) * kWB + w]);
+        dft<A>(v);
+#pragma unroll
+        for (int k1 = 0; k1 < A; ++k1) ex[k1 * KSF + s * kWB + w] = (k1 == 0) ? v[k1] : cmul(v[k1], tws[k1 * B + s]);
+      }
+    }
+    __syncthreads();
+    // forward pass 2 (DFT_B: row k1 + A*k2) and the residual on the kept rows
+    float2 r[NI2][B];
+#pragma unroll
+    for (int ii = 0; ii < NI2; ++ii) {
+      const int i = t + ii * kColNT;
+      if (i < N2) {
+        const int w = i % kWB, k1 = i / kWB;
+#pragma unroll
+        for (int s = 0; s < B; ++s) r[ii][s] = ex[k1 * KSF + s * kWB + w];
+        dft<B>(r[ii]);
+#pragma unroll
+        for (int k2 = 0; k2 < B; ++k2) {
+          const int code = rcode[k1 + A * k2];
+          float2 q = make_float2(0.f, 0.f);
+          if (code != -1) {
+            const int j = code >= 0 ? code : -2 - code;
+            const float2 yv = staged ? Yc[j * kWB + w] : a.T[(size_t(rowbase + j) * C + c) * W + w0 + w];
+            q = (code >= 0) ? csub(cscale(r[ii][k2], s_row), yv) : make_float2(-yv.x, -yv.y);
+            racc = fmaf(q.x, q.x, fmaf(q.y, q.y, racc));
+          }
+          r[ii][k2] = conjf2(q);  // the inverse transform runs on the conjugate
+        }
+      }
+    }
+    __syncthreads();  // every forward pass-2 read of the exchange is done
+    // inverse pass 1 on the same items: DFT_B over rows A*n1 + k1, twiddles
+#pragma unroll
+    for (int ii = 0; ii < NI2; ++ii) {
+      const int i = t + ii * kColNT;
+      if (i < N2) {
+        const int w = i % kWB, k1 = i / kWB;
+        dft<B>(r[ii]);
+#pragma unroll
+        for (int k1p = 0; k1p < B; ++k1p)
+          ex[k1p * KSI + k1 * kWB + w] = (k1p == 0) ? r[ii][k1p] : cmul(r[ii][k1p], tws[H + k1p * A + k1]);
+      }
+    }
+    __syncthreads();
+    // inverse pass 2 (DFT_A: row k1' + B*k2) and conj(S_c) accumulation
+#pragma unroll
+    for (int ii = 0; ii < NI3; ++ii) {
+      const int i = t + ii * kColNT;
+      if (i < N3) {
+        const int w = i % kWB, k1p = i / kWB;
+        float2 v[A];
+#pragma unroll
+        for (int s = 0; s < A; ++s) v[s] = ex[k1p * KSI + s * kWB + w];
+        dft<A>(v);
+#pragma unroll
+        for (int k2 = 0; k2 < A; ++k2) {
+          // conj(v) * conj(S) == conj(v * S)
+          const float2 p = cmul(v[k2], Sc[(k1p + B * k2) * kWB + w]);
+          acc[ii][k2].x += p.x;
+          acc[ii][k2].y -= p.y;
+        }
+      }
+    }
+  }
+
+  // Sum the two halves' accumulators through distributed shared memory; each
+  // CTA finishes half of the tile's rows (k2 < A/2 for the first).
+  cp_async_wait<0>();
+  __syncthreads();
+  float2* mine = Sb;
+#pragma unroll
+  for (int ii = 0; ii < NI3; ++ii)
+#pragma unroll
+    for (int k2 = 0; k2 < A; ++k2) mine[(ii * A + k2) * kColNT + t] = acc[ii][k2];
+  cluster.sync();
+  const float2* other = cluster.map_shared_rank(mine, half ^ 1);
+  constexpr int KH = A / 2;
+  const int kb = half ? KH : 0, ke = half ? A : KH;
+#pragma unroll
+  for (int ii = 0; ii < NI3; ++ii)
+#pragma unroll
+    for (int k2 = 0; k2 < A; ++k2)
+      if (k2 >= kb && k2 < ke) {
+        const float2 o = other[(ii * A + k2) * kColNT + t];
+        acc[ii][k2] = half ? cadd(o, acc[ii][k2]) : cadd(acc[ii][k2], o);
+      }
+  cluster.sync();
+
+  // tTV gradient and Nesterov update of this CTA's rows
+  const float s_adj = a.s_adj;
+  const size_t offm = size_t((f + F - 1) % F) * N, off0 = size_t(f) * N, offp = size_t((f + 1) % F) * N;
+  const float lambda = st->lambda, nLmu1 = -st->Lmu1;
+  const float apk = fix ? st->apk : 0.5f * (float(itx) + 1.0f);  // nesta_scalar_step's weights for k = itx
+  const float tauk = fix ? st->tauk : 2.0f / (float(itx) + 3.0f);
+  const float omt = 1.0f - tauk;
+  constexpr int BATCH = 4;
+#pragma unroll
+  for (int ii = 0; ii < NI3; ++ii) {
+    const int i = t + ii * kColNT;
+    if (i < N3) {
+      const int w = i % kWB, k1p = i / kWB;
+#pragma unroll
+      for (int k0 = 0; k0 < A; k0 += BATCH) {
+        float2 xa[BATCH], xm[BATCH], xp[BATCH], wo[BATCH], xr[BATCH];
+#pragma unroll
+        for (int b = 0; b < BATCH; ++b) {
+          const int k2 = k0 + b;
+          if (k2 < A && k2 >= kb && k2 < ke) {
+            const size_t p = size_t(k1p + B * k2) * W + w0 + w;
+            xa[b] = xk[off0 + p];
+            xm[b] = xk[offm + p];
+            xp[b] = xk[offp + p];
+            wo[b] = wk[off0 + p];
+            xr[b] = a.xref[off0 + p];
+          }
+        }
+#pragma unroll
+        for (int b = 0; b < BATCH; ++b) {
+          const int k2 = k0 + b;
+          if (k2 < A && k2 >= kb && k2 < ke) {
+            const size_t p = size_t(k1p + B * k2) * W + w0 + w;
+            const float2 u0 = tv_normalize(csub(xa[b], xm[b]), inv_mu);
+            const float2 u1 = tv_normalize(csub(xp[b], xa[b]), inv_mu);
+            const float2 adj = csub(u1, u0);
+            const float2 ares = cscale(acc[ii][k2], s_adj);
+            const float2 df = make_float2(__fadd_rn(__fmul_rn(-adj.x, lambda), ares.x),
+                                          __fadd_rn(__fmul_rn(-adj.y, lambda), ares.y));
+            const float2 yk = make_float2(fmaf(nLmu1, df.x, xa[b].x), fmaf(nLmu1, df.y, xa[b].y));
+            const float2 wnv = make_float2(fmaf(apk, df.x, wo[b].x), fmaf(apk, df.y, wo[b].y));
+            const float2 zk = make_float2(fmaf(nLmu1, wnv.x, xr[b].x), fmaf(nLmu1, wnv.y, xr[b].y));
+            wn[off0 + p] = wnv;
+            xn[off0 + p] = make_float2(fmaf(omt, yk.x, tauk * zk.x), fmaf(omt, yk.y, tauk * zk.y));
+          }
+        }
+      }
+    }
+  }
+  if (fix) return;
+
+  // fixed-slot partial sums: ||rho||^2 of this CTA, the tTV terms of the tile
+  const int blk = f * gridDim.x + blockIdx.x;
+  const double pr = block_sum<kColNT>(double(racc), sred);
+  if (half == 0) {
+    const double t1 = block_sum<kColNT>(double(su2), sred);
+    const double t2 = block_sum<kColNT>(double(sud), sred);
+    if (t == 0) {
+      a.part_tv[2 * blk] = t1;
+      a.part_tv[2 * blk + 1] = t2;
+    }
+  }
+  ClassCtl* ctl = bm.ctl;
+  if (t == 0) {
+    a.part_r[2 * blk + half] = pr;
+    __threadfence();
+    const unsigned total = 2u * gridDim.x * unsigned(F);
+    s_fin = (atomicAdd(&ctl->done[inst], 1u) + 1u == total) ? 1 : 0;
+  }
+  __syncthreads();
+  if (!s_fin) return;
+  // the instance's last CTA: reduce in fixed order and run the scalar recurrence
+  __threadfence();
+  if (t < kFmeanCopy && t < st->miniter) fm[t] = __ldcg(a.fmean + t);
+  constexpr int U = 8;
+  double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  const double2* ptv = reinterpret_cast<const double2*>(a.part_tv);
+  const int ntv = a.ntv;
+  for (int i0 = 0; i0 < ntv; i0 += U * kColNT) {
+    double2 vv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = i0 + u * kColNT + t;
+      vv[u] = (i < ntv) ? __ldcg(ptv + i) : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      s1 += vv[u].x;
+      s2 += vv[u].y;
+    }
+  }
+  const int npr = 2 * ntv;
+  for (int i0 = 0; i0 < npr; i0 += U * kColNT) {
+    double vv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = i0 + u * kColNT + t;
+      vv[u] = (i < npr) ? __ldcg(a.part_r + i) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) s3 += vv[u];
+  }
+  s1 = block_sum<kColNT>(s1, sred);
+  s2 = block_sum<kColNT>(s2, sred);
+  s3 = block_sum<kColNT>(s3, sred);
+  if (t == 0) {
+    nesta_scalar_step(st, a.fmean, fm, it, s1, s2, s3 / double(W));
+    // the stopping test fired for the second time: the reference's update of
+    // this iteration uses k = maxIter; the next launch recomputes it
+    if (st->apk != apk) st->fixup = 1;
+    ctl->done[inst] = 0;
+  }
+}
+
+}  // namespace gbn

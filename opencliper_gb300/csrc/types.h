@@ -36,6 +36,12 @@ struct NestaDevState {
   int ne_done, ne_cnt;
   float ne_e, ne_e0;
 
+  // row-local iteration (rowlocal.cuh): the update of iteration last_iter
+  // must be recomputed with the stopping rule's weights; kept rows that are
+  // partly sampled (they need the row pass)
+  int fixup;
+  int partial_rows;
+
   // statistics
   int iters_total;
   int status;
@@ -58,6 +64,7 @@ struct FusedArgs {
   float2* xk1;            // x_k pong
   float2* xref;           // x_ref == output XData [F][H][W]
   float2* wacc;           // Nesterov weighted gradient sum w_k
+  float2* wacc1;          // second w buffer: the row-local iteration reads w_k and writes w_{k+1}
   NestaDevState* st;
   float* fmean;           // [miniter] rolling objective buffer
   double* part_tv;        // [ntv][2] partial sums of ||u||^2 and Re<u,d>, one per (frame, column tile)
@@ -70,6 +77,7 @@ struct FusedArgs {
   const float2* twW;
   float s_fwd;            // 1/sqrt(N) as the reference computes it (double -> float)
   float s_adj;            // sqrt(N)/N: the reference's sqrt(N) pre-scale times clFFT's 1/N
+  float s_row;            // W * s_fwd: the row transforms' round trip on a fully sampled row
   int ntv;                // number of tTV partial sums (F * W/8; mixed form F * ceil(W/32))
   // mixed-precision form (nullptr / 0 otherwise)
   const unsigned char* fk;  // kept-row DFT operand, fp16 hi/lo, per frame and chunk

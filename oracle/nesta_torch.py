@@ -1,13 +1,16 @@
-"""FP64 restatement of NestaUp::launch with torch complex128 tensors -- test
-infrastructure (oracle).
+"""Restatement of NestaUp::launch with torch tensors -- test infrastructure
+(oracle): the FP64 oracle for large workloads, and an FP32 variant that
+measures how far FP32 rounding alone moves the result at a given size.
 
 The same algorithm as oracle/nesta_ref.py's precision="f64" mode, statement for
 statement, written with torch so that it runs on a CUDA device (torch.fft,
 i.e. cuFFT, in double precision) as well as on the CPU.  It exists for the
 large workloads (384x384 x 30 frames x 16 coils, the uneven batch) where the
 numpy FP64 oracle takes minutes per reconstruction; tests/test_oracle.py pins
-it to nesta_ref's FP64 mode on small problems.  Only the plain (no motion
-compensation) form is restated here.
+it to nesta_ref's FP64 mode on small problems.  With dtype complex64 the
+arrays are FP32 (scalars stay Python floats): an FP32 implementation whose
+distance from the FP64 result is the FP32 noise floor of that workload.  Only
+the plain (no motion compensation) form is restated here.
 
 Citations are to src/processes/nesta/NestaUp.cpp of the reference.
 """
@@ -31,12 +34,13 @@ def _nrm2sq(v) -> float:
     return float((v.real * v.real + v.imag * v.imag).sum())
 
 
-def _normest(F: int, H: int, W: int, rand_state: int, dev):
+def _normest(F: int, H: int, W: int, rand_state: int, dev, cdt=None):
     """myNormest (NestaUp.cpp:291-439) in double precision: the all-ones start
     gives U x = 0, so the first pass restarts from drand48 values."""
     import torch
+    cdt = cdt or torch.complex128
     tol, maxiter = 1e-3, 100
-    x = torch.ones((F, H, W), dtype=torch.complex128, device=dev)
+    x = torch.ones((F, H, W), dtype=cdt, device=dev)
     e = float(np.sqrt(float(F * H * W)))
     x = x / e
     e0 = 0.0
@@ -50,7 +54,7 @@ def _normest(F: int, H: int, W: int, rand_state: int, dev):
             vals, state = drand48.lcg_sequence(F * H * W, state)
             # complexType(drand48(), 0) stored as float in the reference
             Sx = torch.from_numpy(vals.astype(np.float32).astype(np.float64).reshape(F, H, W)).to(dev)
-            Sx = torch.complex(Sx, torch.zeros_like(Sx))
+            Sx = torch.complex(Sx, torch.zeros_like(Sx)).to(cdt)
         e = float(np.sqrt(_nrm2sq(Sx)))
         x = _ttv(Sx, False)
         x = x / float(np.sqrt(_nrm2sq(x)))
@@ -59,19 +63,21 @@ def _normest(F: int, H: int, W: int, rand_state: int, dev):
 
 
 def nesta_f64(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams,
-              rand_state: int = drand48.DEFAULT_STATE, device: str = "cpu") -> tuple[np.ndarray, dict]:
+              rand_state: int = drand48.DEFAULT_STATE, device: str = "cpu", fp32: bool = False) -> tuple[np.ndarray, dict]:
     """FP64 NESTA of y [F][C][H][W], S [C][H][W], pixel mask [F][H][W]; returns
-    (image complex128 [F][H][W], stats).  Inputs may be numpy arrays or torch
-    tensors (a tensor already on `device` is used in place)."""
+    (image [F][H][W], stats).  Inputs may be numpy arrays or torch tensors (a
+    tensor already on `device` is used in place).  fp32=True runs the same
+    statements on complex64 arrays."""
     import torch
     dev = torch.device(device)
+    cdt = torch.complex64 if fp32 else torch.complex128
 
     def T(a, dt):
         t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(a))
         return t.to(dev).to(dt)
 
-    y = T(y, torch.complex128)
-    S = T(S, torch.complex128)
+    y = T(y, cdt)
+    S = T(S, cdt)
     keep = T(mask, torch.uint8) != 0
     F, Cn, H, W = y.shape
     N = H * W
@@ -93,7 +99,7 @@ def nesta_f64(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams,
     lam = prm.lambda_i * maxX
     muf = prm.mu_f * maxX
     mu0 = 0.9 * maxUX
-    normU, ne_iters, new_state = _normest(F, H, W, rand_state, dev)
+    normU, ne_iters, new_state = _normest(F, H, W, rand_state, dev, cdt)
     if lam / prm.La > mu0:
         mu0 = lam / prm.La
     gamma = (muf / mu0) ** (1.0 / prm.maxIntIter)

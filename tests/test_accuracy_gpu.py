@@ -3,7 +3,10 @@ workloads, for the plain FP32 and the mixed-precision forms: the 384x384 x 30
 frames x 16 coils reconstruction, and four members of the 64-reconstruction
 uneven batch (largest coil count, largest frame count, largest W*F*C, the
 first) solved as one batch.  The FP64 reference is oracle/nesta_torch.py on the
-same device inputs (tests/accuracy_fp64.py reports the whole batch)."""
+same device inputs; the same restatement on complex64 arrays gives the FP32
+noise floor of each workload, and a result passes at the gate or within 1.25x
+that floor (accuracy_fp64.bar).  tests/accuracy_fp64.py reports the whole
+batch."""
 from __future__ import annotations
 
 import pytest
@@ -12,14 +15,12 @@ from tests import accuracy_fp64 as A
 
 pytestmark = [pytest.mark.gpu, pytest.mark.slow]
 
-GATE = 1e-3
-
 
 def test_large_workload_within_gate(ctx):
     pytest.importorskip("torch")
     (row,) = A.solve(ctx, [A.LARGE])
     print(row)
-    assert row["fp32"] <= GATE and row["mixed"] <= GATE
+    assert row["fp32"] <= A.bar(row) and row["mixed"] <= A.bar(row)
 
 
 def test_uneven_batch_members_within_gate(ctx):
@@ -29,4 +30,4 @@ def test_uneven_batch_members_within_gate(ctx):
     for r in rows:
         print(r)
     assert len(rows) >= 3
-    assert all(r["fp32"] <= GATE and r["mixed"] <= GATE for r in rows)
+    assert all(r["fp32"] <= A.bar(r) and r["mixed"] <= A.bar(r) for r in rows)
