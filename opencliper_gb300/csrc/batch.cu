@@ -51,6 +51,9 @@ struct gbn_batch {
     bool adjoint_tc = false;       // mixed form: adjoint column pass on the tensor cores
     bool tc = false;               // mixed form with the forward pass on the tensor cores (else plain FP32)
     bool row_local = false;        // one-kernel row-local iteration (every member's kept rows full or unsampled)
+    bool row_local_tc = false;     // mixed form: the row-local iteration on the tensor cores (k_iter_tc)
+    int ncha_max = 1;              // widest adjoint operand of the group
+    dim3 g_tc;
     bool any_stoptest = false;     // some member runs the stopping test
     dim3 g1, g3;
     unsigned maxIntIter = 0, maxIter = 0;
@@ -77,6 +80,9 @@ int launch_mixed_setup(gbn_ctx* ctx, gbn_problem* P, cudaStream_t s);
 int launch_mixed_colmax(gbn_problem* P, cudaStream_t s);
 dim3 fwd_cols_tc_grid(int W, int maxC, int frames);
 void launch_fwd_cols_tc(const FusedArgs* tab, const BatchMap& bm, int it, int npad_max, dim3 grid, cudaStream_t s);
+// tensor-core row-local iteration (mixed_rowlocal.cu)
+dim3 iter_tc_grid(int W, int frames);
+void launch_iter_tc(const FusedArgs* tab, const BatchMap& bm, int it, int npad_max, dim3 grid, cudaStream_t s);
 
 namespace {
 
@@ -127,13 +133,18 @@ int batch_enqueue(gbn_batch* b, bool graph_mode) {
         n_launch += launch_outer_begin(ctx, b->probs[i], int(nl), b->out[i], s);
         if (mixed) n_launch += launch_mixed_colmax(b->probs[i], s);
       }
-      if (g.row_local) {
+      if (g.row_local || g.row_local_tc) {
         // one launch more recomputes a member's last update when its stopping test ends the loop
         const unsigned nit = g.maxIter + (g.any_stoptest ? 1u : 0u);
-        for (unsigned it = 0; it < nit; ++it) kh->iter_cols(g.tab, g.bm, int(it), g.g3, s);
+        for (unsigned it = 0; it < nit; ++it) {
+          if (g.row_local_tc)
+            launch_iter_tc(g.tab, g.bm, int(it), g.npad_max, g.g_tc, s);
+          else
+            kh->iter_cols(g.tab, g.bm, int(it), g.g3, s);
+        }
         n_launch += nit;
       }
-      for (unsigned it = 0; it < (g.row_local ? 0u : g.maxIter); ++it) {
+      for (unsigned it = 0; it < ((g.row_local || g.row_local_tc) ? 0u : g.maxIter); ++it) {
         if (mixed)
           launch_fwd_cols_tc(g.tab, g.bm, int(it), g.npad_max, g.g1, s);
         else
@@ -240,9 +251,38 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
         gF = std::max(gF, b->probs[i]->F);
         gC = std::max(gC, b->probs[i]->C);
       }
-      g.tc = mixed_fwd_tc_for(ctx, g.W, g.H, gF, gC);
+      // the row-local iteration on the tensor cores when every member's kept
+      // rows are fully sampled or unsampled; else the three-pass mixed form
+      if (ctx->mixed_fwd_tc == 1 && ctx->row_local) {
+        bool all = true;
+        for (int i : g.idx) {
+          gbn_problem* P = b->probs[i];
+          // the operands (and the row analysis) of the tensor-core kernels; a
+          // member they do not take (too many kept rows, unaligned buffers)
+          // keeps the group on the three-pass form, which reports it
+          const int rcp = mixed_prepare(ctx, P, b->prm[i], b->out[i]);
+          if (rcp == GBN_ERR_NOMEM) {
+            rc = rcp;
+            break;
+          }
+          if (rcp != GBN_OK) {
+            all = false;
+            break;
+          }
+          int part = 1;
+          if ((e = cudaMemcpy(&part, &P->st->partial_rows, sizeof(int), cudaMemcpyDeviceToHost)) != cudaSuccess) {
+            rc = cuda_status(e, "batch row analysis");
+            break;
+          }
+          all = all && part == 0;
+          g.any_stoptest = g.any_stoptest || b->prm[i].stoptest == 1;
+        }
+        if (rc != GBN_OK) break;
+        g.row_local_tc = all;
+      }
+      g.tc = g.row_local_tc || mixed_fwd_tc_for(ctx, g.W, g.H, gF, gC);
       for (int i : g.idx) {
-        if (!g.tc || rc != GBN_OK) break;
+        if (!g.tc || g.row_local_tc || rc != GBN_OK) break;
         rc = mixed_prepare(ctx, b->probs[i], b->prm[i], b->out[i]);
       }
       if (rc != GBN_OK) break;
@@ -264,6 +304,8 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
         mixed_args(P, &fa);
         g.npad_max = std::max(g.npad_max, P->npad);
         g.nmax_ac = std::max(g.nmax_ac, inv_cols_tc_rows(P->C));
+        g.ncha_max = std::max(g.ncha_max, P->ncha);
+        if (g.row_local_tc) fa.ntv = P->F * (P->W / kWB);  // k_iter_tc: one partial sum per (frame, 8 columns)
       }
       ctx->launches += launch_store_args(g.tab + k, fa, ctx->stream);
     }
@@ -277,10 +319,11 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
     g.g3 = dim3(g.W / kWB, 2, frames);
     g.g3tc = inv_cols_tc_grid(g.W, g.H, frames);
     g.adjoint_tc = g.tc && ctx->mixed_adjoint_tc != 0;
+    if (g.row_local_tc) g.g_tc = iter_tc_grid(g.W, frames);
     // row-local iteration: every member's current data keep only fully
     // sampled or unsampled rows
     const SizeKernels* kh = find_size(g.H);
-    if (!g.tc && kh->iter_cols && ctx->row_local) {
+    if (!g.tc && !g.row_local_tc && kh->iter_cols && ctx->row_local) {
       bool all = true;
       for (int i : g.idx) {
         gbn_problem* P = b->probs[i];
@@ -365,7 +408,7 @@ gbn_ctx* batch_ctx(gbn_batch* b) { return b->ctx; }
 int batch_groups(gbn_batch* b, int* groups, int* tensor_core_groups) {
   if (!b) return set_error(GBN_ERR_INVALID, "null batch");
   int tc = 0;
-  for (const auto& g : b->groups) tc += g.tc ? 1 : 0;
+  for (const auto& g : b->groups) tc += g.tc ? 1 : 0;  // tensor-core forward transform (three-pass or row-local)
   if (groups) *groups = int(b->groups.size());
   if (tensor_core_groups) *tensor_core_groups = tc;
   return GBN_OK;

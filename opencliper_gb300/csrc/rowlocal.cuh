@@ -44,6 +44,67 @@ namespace gbn {
 
 constexpr int kStatusRowStructure = 7;  // NestaDevState::status: a kept row is partly sampled (row-local path)
 
+// Counts this CTA as finished for instance `inst` (after its partial sums are
+// stored) and tells every thread whether it was the instance's last of
+// `total` CTAs.  All threads call it.
+__device__ __forceinline__ bool rowlocal_last_cta(ClassCtl* ctl, int inst, unsigned total) {
+  __shared__ int s_fin;
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) s_fin = (atomicAdd(&ctl->done[inst], 1u) + 1u == total) ? 1 : 0;
+  __syncthreads();
+  return s_fin != 0;
+}
+
+// The instance's last CTA of a row-local iteration: reduces the fixed-slot
+// partial sums (ntv (||u||^2, Re<u,d>) pairs, npr sums of |rho|^2) in fixed
+// order and runs the scalar recurrence; ||E x - y||^2 = sum |rho|^2 / W
+// (Parseval along the rows).  `apk_used` is the weight the CTAs updated with:
+// when the recurrence's differs, the stopping test fired for the second time
+// and the next launch recomputes this iteration's update.  All NT threads call it.
+template <int NT>
+__device__ void rowlocal_finish(const FusedArgs& a, NestaDevState* st, ClassCtl* ctl, int inst, int it, float apk_used,
+                                int npr, double* sred, float* fm) {
+  const int t = threadIdx.x;
+  __threadfence();
+  if (t < kFmeanCopy && t < st->miniter) fm[t] = __ldcg(a.fmean + t);
+  constexpr int U = 8;
+  double s1 = 0.0, s2 = 0.0, s3 = 0.0;
+  const double2* ptv = reinterpret_cast<const double2*>(a.part_tv);
+  const int ntv = a.ntv;
+  for (int i0 = 0; i0 < ntv; i0 += U * NT) {
+    double2 vv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = i0 + u * NT + t;
+      vv[u] = (i < ntv) ? __ldcg(ptv + i) : make_double2(0.0, 0.0);
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      s1 += vv[u].x;
+      s2 += vv[u].y;
+    }
+  }
+  for (int i0 = 0; i0 < npr; i0 += U * NT) {
+    double vv[U];
+#pragma unroll
+    for (int u = 0; u < U; ++u) {
+      const int i = i0 + u * NT + t;
+      vv[u] = (i < npr) ? __ldcg(a.part_r + i) : 0.0;
+    }
+#pragma unroll
+    for (int u = 0; u < U; ++u) s3 += vv[u];
+  }
+  s1 = block_sum<NT>(s1, sred);
+  s2 = block_sum<NT>(s2, sred);
+  s3 = block_sum<NT>(s3, sred);
+  if (t == 0) {
+    nesta_scalar_step(st, a.fmean, fm, it, s1, s2, s3 / double(a.W));
+    if (st->apk != apk_used) st->fixup = 1;
+    ctl->done[inst] = 0;
+  }
+}
+
 template <int H>
 struct IterColsSmem {
   static constexpr int A = Split<H>::A, B = Split<H>::B;
@@ -82,7 +143,6 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, 3)
   int* rcode = reinterpret_cast<int*>(reinterpret_cast<float2*>(smem4) + L::F2_END);
   double* sred = reinterpret_cast<double*>(rcode + H);
   float* fm = reinterpret_cast<float*>(sred + kColNT / 32);
-  __shared__ int s_fin;
   namespace cgr = cooperative_groups;
   cgr::cluster_group cluster = cgr::this_cluster();
 
@@ -368,56 +428,9 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, 3)
       a.part_tv[2 * blk + 1] = t2;
     }
   }
-  ClassCtl* ctl = bm.ctl;
-  if (t == 0) {
-    a.part_r[2 * blk + half] = pr;
-    __threadfence();
-    const unsigned total = 2u * gridDim.x * unsigned(F);
-    s_fin = (atomicAdd(&ctl->done[inst], 1u) + 1u == total) ? 1 : 0;
-  }
-  __syncthreads();
-  if (!s_fin) return;
-  // the instance's last CTA: reduce in fixed order and run the scalar recurrence
-  __threadfence();
-  if (t < kFmeanCopy && t < st->miniter) fm[t] = __ldcg(a.fmean + t);
-  constexpr int U = 8;
-  double s1 = 0.0, s2 = 0.0, s3 = 0.0;
-  const double2* ptv = reinterpret_cast<const double2*>(a.part_tv);
-  const int ntv = a.ntv;
-  for (int i0 = 0; i0 < ntv; i0 += U * kColNT) {
-    double2 vv[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int i = i0 + u * kColNT + t;
-      vv[u] = (i < ntv) ? __ldcg(ptv + i) : make_double2(0.0, 0.0);
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      s1 += vv[u].x;
-      s2 += vv[u].y;
-    }
-  }
-  const int npr = 2 * ntv;
-  for (int i0 = 0; i0 < npr; i0 += U * kColNT) {
-    double vv[U];
-#pragma unroll
-    for (int u = 0; u < U; ++u) {
-      const int i = i0 + u * kColNT + t;
-      vv[u] = (i < npr) ? __ldcg(a.part_r + i) : 0.0;
-    }
-#pragma unroll
-    for (int u = 0; u < U; ++u) s3 += vv[u];
-  }
-  s1 = block_sum<kColNT>(s1, sred);
-  s2 = block_sum<kColNT>(s2, sred);
-  s3 = block_sum<kColNT>(s3, sred);
-  if (t == 0) {
-    nesta_scalar_step(st, a.fmean, fm, it, s1, s2, s3 / double(W));
-    // the stopping test fired for the second time: the reference's update of
-    // this iteration uses k = maxIter; the next launch recomputes it
-    if (st->apk != apk) st->fixup = 1;
-    ctl->done[inst] = 0;
-  }
+  if (t == 0) a.part_r[2 * blk + half] = pr;
+  if (rowlocal_last_cta(bm.ctl, inst, 2u * gridDim.x * unsigned(F)))
+    rowlocal_finish<kColNT>(a, st, bm.ctl, inst, it, apk, 2 * a.ntv, sred, fm);
 }
 
 }  // namespace gbn

@@ -104,8 +104,9 @@ def test_mixed_rejects_too_many_kept_rows(ctx):
 
 def test_mixed_forward_choice_per_group(ctx):
     """mixed_fwd_tc = 0 runs a mixed batch's groups on the plain FP32 kernels
-    (the same image as an FP32 batch, bit for bit); the automatic choice does
-    the same below H = 320 when nothing was tuned."""
+    (the same image as an FP32 batch, bit for bit), and so does the automatic
+    choice here; mixed_fwd_tc = 1 runs the row-local iteration on the tensor
+    cores."""
     p = synth.make_problem(48, 40, 5, 3, 4, seed=91)
     dy, dS, dm = ctx.to_device(p.y), ctx.to_device(p.S), ctx.to_device(p.mask)
     prob = g.Problem(ctx, dy, dS, dm)
@@ -121,5 +122,29 @@ def test_mixed_forward_choice_per_group(ctx):
         b.close()
     prob.close()
     assert np.array_equal(imgs[0], imgs[1]) and np.array_equal(imgs[0], imgs[2])
-    assert not np.array_equal(imgs[0], imgs[3])  # the tensor-core forward rounds differently
+    assert not np.array_equal(imgs[0], imgs[3])  # the tensor-core transforms round differently
     assert R.nrmse(imgs[3], imgs[0]) < 1e-3
+
+
+def test_mixed_partly_sampled_rows_three_pass(ctx):
+    """A pixel mask with partly sampled rows needs the row pass, so a mixed
+    batch keeps the three-pass form (tensor-core forward transform)."""
+    rng = np.random.default_rng(3)
+    p = synth.make_problem(48, 40, 5, 3, 4, seed=17)
+    p.mask = ((rng.random(p.mask.shape) > 0.6) * 255).astype(np.uint8)
+    p.y = np.where(p.mask[:, None] == 0, 0, p.y).astype(np.complex64)
+    dy, dS, dm = ctx.to_device(p.y), ctx.to_device(p.S), ctx.to_device(p.mask)
+    prob = g.Problem(ctx, dy, dS, dm)
+    x = ctx.empty((5, 40, 48), np.complex64)
+    s0 = drand48.seed16v_to_state(ctx.rand48())
+    b = g.Batch(ctx, [prob], g.nesta_params(**FIXED), [x], precision=g.PRECISION_MIXED)
+    b.launch()
+    got, st = x.get(), b.stats(0)
+    b.close()
+    prob.close()
+    r64 = R.nesta(p.y, p.S, p.mask, R.NestaParams(**FIXED), "f64", rand_state=s0)
+    r32 = R.nesta(p.y, p.S, p.mask, R.NestaParams(**FIXED), "f32", rand_state=s0)
+    e_mx, e_32 = R.nrmse(got, r64.x), R.nrmse(r32.x, r64.x)
+    print(f"partly sampled rows: NRMSE mixed/f64 {e_mx:.3e}  f32-oracle/f64 {e_32:.3e}")
+    assert st["status"] == 0 and np.isfinite(got).all()
+    assert e_mx <= 3.0 * e_32 + 1e-5
