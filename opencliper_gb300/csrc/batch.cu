@@ -53,6 +53,7 @@ struct gbn_batch {
     bool row_local = false;        // one-kernel row-local iteration (every member's kept rows full or unsampled)
     bool row_local_tc = false;     // mixed form: the row-local iteration on the tensor cores (k_iter_tc)
     int ncha_max = 1;              // widest adjoint operand of the group
+    int cnmax_tc = 1;              // widest coil group of the tensor-core row-local iteration
     dim3 g_tc;
     bool any_stoptest = false;     // some member runs the stopping test
     dim3 g1, g3;
@@ -81,8 +82,12 @@ int launch_mixed_colmax(gbn_problem* P, cudaStream_t s);
 dim3 fwd_cols_tc_grid(int W, int maxC, int frames);
 void launch_fwd_cols_tc(const FusedArgs* tab, const BatchMap& bm, int it, int npad_max, dim3 grid, cudaStream_t s);
 // tensor-core row-local iteration (mixed_rowlocal.cu)
+int iter_tc_coils(int C, int ncha);
+bool iter_tc_prepare(gbn_problem* P);
+void iter_tc_args(gbn_problem* P, FusedArgs* a);
 dim3 iter_tc_grid(int W, int frames);
-void launch_iter_tc(const FusedArgs* tab, const BatchMap& bm, int it, int npad_max, dim3 grid, cudaStream_t s);
+void launch_iter_tc(const FusedArgs* tab, const BatchMap& bm, int it, int npad_max, int cnmax, dim3 grid,
+                    cudaStream_t s);
 
 namespace {
 
@@ -138,7 +143,7 @@ int batch_enqueue(gbn_batch* b, bool graph_mode) {
         const unsigned nit = g.maxIter + (g.any_stoptest ? 1u : 0u);
         for (unsigned it = 0; it < nit; ++it) {
           if (g.row_local_tc)
-            launch_iter_tc(g.tab, g.bm, int(it), g.npad_max, g.g_tc, s);
+            launch_iter_tc(g.tab, g.bm, int(it), g.npad_max, g.cnmax_tc, g.g_tc, s);
           else
             kh->iter_cols(g.tab, g.bm, int(it), g.g3, s);
         }
@@ -274,7 +279,8 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
             rc = cuda_status(e, "batch row analysis");
             break;
           }
-          all = all && part == 0;
+          // and the tensor maps of the tensor-core row-local iteration
+          all = all && part == 0 && iter_tc_prepare(P);
           g.any_stoptest = g.any_stoptest || b->prm[i].stoptest == 1;
         }
         if (rc != GBN_OK) break;
@@ -305,7 +311,10 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
         g.npad_max = std::max(g.npad_max, P->npad);
         g.nmax_ac = std::max(g.nmax_ac, inv_cols_tc_rows(P->C));
         g.ncha_max = std::max(g.ncha_max, P->ncha);
-        if (g.row_local_tc) fa.ntv = P->F * (P->W / kWB);  // k_iter_tc: one partial sum per (frame, 8 columns)
+        if (g.row_local_tc) {
+          iter_tc_args(P, &fa);
+          g.cnmax_tc = std::max(g.cnmax_tc, iter_tc_coils(P->C, P->ncha));
+        }
       }
       ctx->launches += launch_store_args(g.tab + k, fa, ctx->stream);
     }

@@ -107,6 +107,9 @@ struct gbn_problem {
   unsigned char* fa = nullptr;        // adjoint kept-row DFT operand
   size_t fa_bytes = 0;
   int ncha = 0;
+  int gmax = 0;                       // most kept rows of a frame (fixed when the mixed operands are built)
+  bool tmaps_ok = false;              // tensor maps of the tensor-core row-local iteration encoded
+  CUtensorMap tm_x[2], tm_s, tm_se, tm_y;
   // motion-compensated form (motion.cu): caller's meshes, not owned
   bool mc_on = false;
   const float* mc_xn = nullptr;       // deformed mesh [2][F][H][W], 1-based

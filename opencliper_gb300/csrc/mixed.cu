@@ -626,6 +626,7 @@ int mixed_prepare(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params& prm, con
   P->npad = npad;
   P->nch = nch;
   P->ncha = ncha;
+  P->gmax = gmax;
   return GBN_OK;
 }
 

@@ -32,6 +32,8 @@
 // columns, so two CTAs share an SM.  Every mbarrier wait is bounded; a wait
 // that runs out sets the instance's status and the CTA still completes its
 // barriers.
+#include <cudaTypedefs.h>
+
 #include <algorithm>
 
 #include "ctx.h"
@@ -48,19 +50,32 @@ namespace {
 constexpr int kRtCols = 8;                       // image columns per CTA
 constexpr int kRtNT = 128;                       // threads per CTA (one TMEM lane each)
 constexpr int kRtA1Part = 128 * kTcKC * 2;       // bytes of one part of a forward A chunk (8 KB)
+constexpr int kRtA1Stage = 2 * kRtA1Part;        // hi + lo
 constexpr int kRtA3Bytes = 2 * kAcAPart;         // adjoint A chunk, hi + lo (32 KB)
+constexpr int kRtB3Max = 64 * 1024;              // adjoint B operand: all its chunks of one coil group
+constexpr int kRtR2 = kRtB3Max;                  // second region: IDFT_W(y) tile, adjoint A chunk, S ring
+constexpr int kRtR2Bytes = 32 * 1024;
+constexpr int kRtSlots = 4;                      // S ring of the coil combination: one coil per slot
+constexpr int kRtSlotBytes = 128 * 64;           // 128 image rows x 8 complex columns
+constexpr uint32_t kRtWaitPolls = 4096;          // suspending polls of one wait (~1 ms each at most)
 
-constexpr int kRtB3Max = 64 * 1024;             // adjoint B operand: all its chunks of one coil group
-
-// dynamic shared memory: two forward stages, aliased by the adjoint B operand
-// once the forward GEMM is done, then one adjoint A chunk
-__host__ __device__ constexpr int rt_stage_bytes(int npad) { return 2 * kRtA1Part + 2 * npad * kTcKC * 2; }
-__host__ __device__ constexpr int rt_b3_chunk(int pairs) { return 2 * ac_b_part(2 * pairs); }
-__host__ __device__ constexpr int rt_a3_offset(int npad_max) {
-  const int r0 = 2 * rt_stage_bytes(npad_max) > kRtB3Max ? 2 * rt_stage_bytes(npad_max) : kRtB3Max;
-  return (r0 + 1023) / 1024 * 1024;
+// Shared memory (1024-aligned base):
+//   forward GEMM: [0, 2 A1 stages) then a ring of nst stages, each
+//     [x tile: 16 rows x 8 columns][S tile: cnmax coils x 16 rows x 8 columns]
+//     [the frame's forward DFT operand chunk, npad rows hi | lo];
+//   afterwards: [0, 64 KB) the adjoint B operand, [64 KB, 96 KB) the kept rows'
+//   IDFT_W(y) tile, then one adjoint A chunk at a time, then the S ring.
+__host__ __device__ constexpr int rt_ring_stage(int npad_max, int cnmax) {
+  return 1024 + cnmax * 1024 + npad_max * kTcKC * 4;
 }
-__host__ __device__ constexpr int rt_smem(int npad_max) { return rt_a3_offset(npad_max) + kRtA3Bytes; }
+__host__ __device__ constexpr int rt_nst(int npad_max, int cnmax) {
+  return 2 * kRtA1Stage + 3 * rt_ring_stage(npad_max, cnmax) <= 100 * 1024 ? 3 : 2;
+}
+__host__ __device__ constexpr int rt_smem(int npad_max, int cnmax) {
+  const int fwd = 2 * kRtA1Stage + rt_nst(npad_max, cnmax) * rt_ring_stage(npad_max, cnmax);
+  return fwd > kRtR2 + kRtR2Bytes ? fwd : kRtR2 + kRtR2Bytes;
+}
+__host__ __device__ constexpr int rt_b3_chunk(int pairs) { return 2 * ac_b_part(2 * pairs); }
 
 // Coils per group of an instance with C coils and ncha adjoint chunks: 8 * cg
 // pairs <= 128 TMEM lanes and the group's adjoint B operand within kRtB3Max,
@@ -87,12 +102,16 @@ __device__ __forceinline__ float pow2_scale(float mx, float* inv) {
 
 }  // namespace
 
-// grid (W/8, 1, total frames), 128 threads; the launch's widest forward
-// operand npad_max fixes the shared-memory layout
-__global__ void __launch_bounds__(kRtNT, 2)
-    k_iter_tc(const FusedArgs* __restrict__ tab, const __grid_constant__ BatchMap bm, int it, int npad_max) {
+// grid (W/8, 1, total frames), 128 threads; npad_max and cnmax (the launch's
+// widest forward operand and coil group) fix the shared-memory layout.  The
+// register cap keeps two CTAs per SM (two CTAs of 255 registers a thread
+// would need the whole register file, and the SM then keeps one).
+__global__ void __maxnreg__(224)
+    k_iter_tc(const FusedArgs* __restrict__ tab, const __grid_constant__ BatchMap bm, int it, int npad_max, int cnmax) {
   extern __shared__ __align__(1024) unsigned char sm[];
-  __shared__ uint64_t mbar[3];  // 0, 1: forward stages; 2: adjoint GEMM
+  // mbarriers: ring stages, forward MMAs (per A1 stage), adjoint A chunk,
+  // adjoint MMAs, IDFT_W(y) tile, S ring slots
+  __shared__ uint64_t bar_full[3], bar_mma[2], bar_a3, bar_mma3, bar_y, bar_s[kRtSlots];
   __shared__ uint32_t tslot;
   __shared__ float s_isig3[128];  // per-pair scale of the adjoint B operand
   __shared__ float s_cmx[kRtNT / 32][kRtCols];
@@ -109,22 +128,12 @@ __global__ void __launch_bounds__(kRtNT, 2)
   const int npad = a.npad, nch = a.nch, ncha = a.ncha;
   const int rowbase = a.rowoff[f], G = a.rowoff[f + 1] - rowbase;
   const int nht = (H + 127) / 128;
-  const int stg = rt_stage_bytes(npad);
-  unsigned char* a3s = sm + rt_a3_offset(npad_max);
-  const int cgmax = rt_coils(C, ncha);
+  const int cgmax = rt_coils(C, ncha);  // this instance's coils per group (the S and IDFT_W(y) boxes)
+  const int rs = rt_ring_stage(npad_max, cnmax), nst = rt_nst(npad_max, cnmax);
+  unsigned char* ring = sm + 2 * kRtA1Stage;
+  unsigned char* r2 = sm + kRtR2;
   const unsigned char* fk = a.fk + size_t(f) * nch * (2 * npad * kTcKC * 2);
   const unsigned char* fa = a.fa + size_t(f) * nht * ncha * kRtA3Bytes;
-  auto issue_B1 = [&](int j, int s) {
-    const unsigned char* src = fk + size_t(j) * (2 * npad * kTcKC * 2);
-    unsigned char* dst = sm + s * stg + 2 * kRtA1Part;
-    for (int q = t; q < npad * kTcKC * 4 / 16; q += kRtNT) cp_async16(dst + 16 * q, src + 16 * q);
-  };
-  auto issue_A3 = [&](int ht, int j) {
-    const unsigned char* src = fa + (size_t(ht) * ncha + j) * kRtA3Bytes;
-    for (int q = t; q < kRtA3Bytes / 16; q += kRtNT) cp_async16(a3s + 16 * q, src + 16 * q);
-  };
-  issue_B1(0, 0);  // the DFT operand is an input of the whole solve
-  cp_async_commit();
   grid_dep_wait();  // x_k, w_k, the column maxima and the scalar state come from the previous iteration
   grid_dep_release();
 
@@ -134,14 +143,10 @@ __global__ void __launch_bounds__(kRtNT, 2)
   int itx = it;
   if (st->partial_rows) {
     if (t == 0 && blockIdx.x == 0 && f == 0 && it == 0) st->status = kStatusRowStructure;
-    cp_async_wait<0>();
     return;
   }
   if (it > last) {
-    if (!(st->fixup && it == last + 1)) {
-      cp_async_wait<0>();
-      return;
-    }
+    if (!(st->fixup && it == last + 1)) return;
     fix = true;
     itx = last;
   }
@@ -153,8 +158,17 @@ __global__ void __launch_bounds__(kRtNT, 2)
     tc::tmem_relinquish();
   }
   if (t == 0) {
-    for (int i = 0; i < 3; ++i) tc::mbar_init(&mbar[i], 1);
+    for (int i = 0; i < 3; ++i) tc::mbar_init(&bar_full[i], 1);
+    for (int i = 0; i < 2; ++i) tc::mbar_init(&bar_mma[i], 1);
+    tc::mbar_init(&bar_a3, 1);
+    tc::mbar_init(&bar_mma3, 1);
+    tc::mbar_init(&bar_y, 1);
+    for (int i = 0; i < kRtSlots; ++i) tc::mbar_init(&bar_s[i], 1);
     tc::fence_mbar_init();
+    tc::tmap_acquire(&a.tm_x[itx & 1]);
+    tc::tmap_acquire(&a.tm_s);
+    tc::tmap_acquire(&a.tm_se);
+    tc::tmap_acquire(&a.tm_y);
   }
   tc::fence_before_sync();
   __syncthreads();
@@ -167,7 +181,17 @@ __global__ void __launch_bounds__(kRtNT, 2)
   const float2* __restrict__ wk = (itx & 1) ? a.wacc1 : a.wacc;
   float2* __restrict__ wn = (itx & 1) ? a.wacc : a.wacc1;
   const float* colmax_k = a.colmax + size_t(itx & 1) * F * W + size_t(f) * W;
+  const CUtensorMap* tmx = &a.tm_x[itx & 1];
   const float s_row = a.s_row;
+
+  // barrier phases: bits 0-2 ring stages, 3-4 forward MMAs, 5 adjoint A, 6
+  // adjoint MMAs, 7 IDFT_W(y), 8-11 S slots
+  uint32_t ph = 0u;
+  bool ok = true;
+  auto waitb = [&](uint64_t* b, int bit) {
+    ok = tc::mbar_wait_sleep(b, (ph >> bit) & 1u, kRtWaitPolls) && ok;
+    ph ^= 1u << bit;
+  };
 
   float2 acc[4][kRtCols];  // x_grad of rows h = 128 ht + t (H <= 512)
 #pragma unroll
@@ -175,67 +199,56 @@ __global__ void __launch_bounds__(kRtNT, 2)
 #pragma unroll
     for (int w = 0; w < kRtCols; ++w) acc[ht][w] = make_float2(0.f, 0.f);
   float racc = 0.f;
-  bool ok = true;
-  uint32_t ph = 0u;  // bit s: the phase parity next awaited on mbar[s]
-  int q0 = 0;  // forward chunks issued so far (stage of chunk q is q & 1)
+  int q0 = 0;  // forward chunks so far: ring stage q % nst, A1 stage q & 1
 
   for (int cg0 = 0; cg0 < C; cg0 += cgmax) {
     const int cn = min(cgmax, C - cg0), pairs = kRtCols * cn;
     const int cl = t / kRtCols, wl = t % kRtCols;
     const bool valid = t < pairs;
     const int c = cg0 + (valid ? cl : 0), w = w0 + wl;
-    if (cg0 > 0) {  // the stages held the previous group's adjoint operand until its GEMMs finished
-      issue_B1(0, q0 & 1);
-      cp_async_commit();
-    }
+    const uint32_t chunk_bytes = 1024u + uint32_t(cgmax) * 1024u + uint32_t(npad) * kTcKC * 4u;
+    // the forward operands of chunk j (x, S of the group, DFT rows) into ring stage sidx (thread 0)
+    auto load_chunk = [&](int j, int sidx) {
+      unsigned char* sp = ring + sidx * rs;
+      tc::mbar_arrive_expect_tx(&bar_full[sidx], chunk_bytes);
+      tc::tma_load_3d(sp, tmx, 2 * w0, kTcHC * j, f, &bar_full[sidx]);
+      tc::tma_load_3d(sp + 1024, &a.tm_s, 2 * w0, kTcHC * j, cg0, &bar_full[sidx]);
+      tc::bulk_g2s(sp + 1024 + cnmax * 1024, fk + size_t(j) * (2 * npad * kTcKC * 2), uint32_t(npad) * kTcKC * 4u,
+                   &bar_full[sidx]);
+    };
+    if (t == 0)
+      for (int i = 0; i < nst && i < nch; ++i) load_chunk(i, (q0 + i) % nst);
+
     // ---- 1. forward GEMM ------------------------------------------------
     float isig = 1.f;
     const float sig = valid ? pow2_scale(colmax_k[w] * a.smax[size_t(c) * W + w], &isig) : 1.f;
-    const float2* __restrict__ xcol = xk + size_t(f) * N + w;
-    const float2* __restrict__ scol = a.S + size_t(c) * N + w;
-    float2 px[kTcHC], ps[kTcHC];
-    auto prefetch = [&](int j) {
-      const int h0 = j * kTcHC;
-#pragma unroll
-      for (int q = 0; q < kTcHC; ++q) {
-        const bool in = valid && (h0 + q < H);
-        px[q] = in ? xcol[size_t(h0 + q) * W] : make_float2(0.f, 0.f);
-        ps[q] = in ? scol[size_t(h0 + q) * W] : make_float2(0.f, 0.f);
-      }
-    };
-    prefetch(0);
     const uint32_t idesc1 = tc::idesc_f16_f32(128, npad);
     for (int j = 0; j < nch; ++j) {
-      const int q = q0 + j, s = q & 1;
-      unsigned char* stgp = sm + s * stg;
-      // A1 chunk j (this thread's row): 4 core-matrix K groups of 4 complex values
+      const int q = q0 + j, sidx = q % nst, a1 = q & 1;
+      waitb(&bar_full[sidx], sidx);
+      const unsigned char* sp = ring + sidx * rs;
+      const float2* xs = reinterpret_cast<const float2*>(sp);                          // [16 rows][8]
+      const float2* ss = reinterpret_cast<const float2*>(sp + 1024) + cl * kTcHC * 8;  // [coil][16 rows][8]
+      unsigned char* a1p = sm + a1 * kRtA1Stage;
 #pragma unroll
       for (int gi = 0; gi < kTcKC / 8; ++gi) {
         uint32_t hw[4], lw[4];
 #pragma unroll
         for (int e = 0; e < 4; ++e) {
-          const float2 v = cmul(px[4 * gi + e], ps[4 * gi + e]);
+          const int r = 4 * gi + e;
+          const float2 v = valid ? cmul(xs[r * 8 + wl], ss[r * 8 + wl]) : make_float2(0.f, 0.f);
           split_pair(v.x * sig, v.y * sig, hw[e], lw[e]);
         }
         const uint32_t off = tc::kmajor_offset(t, 8 * gi, kTcKC);
-        *reinterpret_cast<uint4*>(stgp + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
-        *reinterpret_cast<uint4*>(stgp + kRtA1Part + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
+        *reinterpret_cast<uint4*>(a1p + off) = make_uint4(hw[0], hw[1], hw[2], hw[3]);
+        *reinterpret_cast<uint4*>(a1p + kRtA1Part + off) = make_uint4(lw[0], lw[1], lw[2], lw[3]);
       }
-      if (j + 1 < nch) prefetch(j + 1);
-      if (j >= 1) {  // the MMAs of chunk q-1 are done: its stage takes B1 of chunk q+1
-        const int sp = (q - 1) & 1;
-        ok = tc::mbar_wait(&mbar[sp], (ph >> sp) & 1u, kWaitLimit) && ok;
-        ph ^= 1u << sp;
-      }
-      if (j + 1 < nch) issue_B1(j + 1, (q + 1) & 1);
-      cp_async_commit();
-      cp_async_wait<1>();  // B1 of chunk q has landed
       tc::fence_proxy_async();
       tc::fence_before_sync();
-      __syncthreads();
+      __syncthreads();  // A1 chunk complete; the ring stage's x and S are consumed
       if (t == 0) {
         tc::fence_after_sync();
-        const uint32_t sa = tc::smem_u32(stgp), sb = sa + 2 * kRtA1Part;
+        const uint32_t sa = tc::smem_u32(a1p), sb = tc::smem_u32(sp + 1024 + cnmax * 1024);
         const uint32_t bpart = uint32_t(npad) * kTcKC * 2;
 #pragma unroll
         for (int ks = 0; ks < kTcKC / 16; ++ks) {
@@ -247,24 +260,28 @@ __global__ void __launch_bounds__(kRtNT, 2)
           tc::mma_f16(tbase, alo, bhi, idesc1, true);
           tc::mma_f16(tbase, ahi, blo, idesc1, true);
         }
-        tc::mma_commit(&mbar[s]);
+        tc::mma_commit(&bar_mma[a1]);
+      }
+      if (j >= 1) {  // the MMAs of chunk q-1: their A1 stage and ring stage are free again
+        waitb(&bar_mma[(q - 1) & 1], 3 + ((q - 1) & 1));
+        if (t == 0 && j - 1 + nst < nch) load_chunk(j - 1 + nst, (q - 1) % nst);
       }
     }
-    {
-      const int sl = (q0 + nch - 1) & 1;
-      ok = tc::mbar_wait(&mbar[sl], (ph >> sl) & 1u, kWaitLimit) && ok;
-      ph ^= 1u << sl;
-    }
+    waitb(&bar_mma[(q0 + nch - 1) & 1], 3 + ((q0 + nch - 1) & 1));
     q0 += nch;
-    cp_async_wait<0>();
     tc::fence_after_sync();
+    // the kept rows' IDFT_W(y) of this group's coils: [G rows][cgmax coils][8 columns]
+    if (t == 0) {
+      tc::mbar_arrive_expect_tx(&bar_y, uint32_t(a.gmax_box) * uint32_t(cgmax) * 64u);
+      tc::tma_load_3d(r2, &a.tm_y, 2 * w0, cg0, rowbase, &bar_y);
+    }
+    waitb(&bar_y, 7);
 
     // ---- 2. residual -> adjoint B operand (this thread's pair) ------------
-    const float2* __restrict__ yhat = a.T + (size_t(rowbase) * C + c) * W + w;  // IDFT_W(y) of kept row 0
-    const size_t ystride = size_t(C) * W;
+    const float2* ys = reinterpret_cast<const float2*>(r2) + cl * 8 + wl;  // + j * cgmax * 8
     auto rho_of = [&](const float* v, int i, int jrow) -> float2 {
       const float2 tv = make_float2(v[2 * i] * isig, v[2 * i + 1] * isig);
-      const float2 yv = yhat[size_t(jrow) * ystride];
+      const float2 yv = ys[jrow * cgmax * 8];
       return __ldg(a.row_full + rowbase + jrow) ? csub(cscale(tv, s_row), yv) : make_float2(-yv.x, -yv.y);
     };
     float mx = 0.f;
@@ -283,16 +300,13 @@ __global__ void __launch_bounds__(kRtNT, 2)
     }
     float isig3 = 1.f;
     const float sig3 = pow2_scale(mx, &isig3);
-    if (t < 128) s_isig3[t] = valid ? isig3 : 0.f;
-    tc::fence_before_sync();
-    __syncthreads();  // every forward stage is free: the adjoint B operand takes their place
-    tc::fence_after_sync();
+    s_isig3[t] = valid ? isig3 : 0.f;
     const int n0 = 2 * t;  // B3 rows of this pair
     for (int col0 = 0; col0 < 2 * kAcRows * ncha; col0 += 16) {
       float v[16];
       tc::tmem_ld16(taddr + uint32_t(col0 < npad ? col0 : 0), v);
       if (valid) {
-        const int jc = col0 / (2 * kAcRows);        // adjoint K chunk
+        const int jc = col0 / (2 * kAcRows);  // adjoint K chunk
         unsigned char* b3 = sm + jc * rt_b3_chunk(pairs);
         const int bpart3 = ac_b_part(2 * pairs);
 #pragma unroll
@@ -317,6 +331,10 @@ __global__ void __launch_bounds__(kRtNT, 2)
         }
       }
     }
+    tc::fence_proxy_async();
+    tc::fence_before_sync();
+    __syncthreads();  // B3 complete; the IDFT_W(y) tile and D1 are no longer read
+    tc::fence_after_sync();
 
     // ---- 3./4. adjoint GEMM per row tile and the coil combination ----------
     const uint32_t idesc3 = tc::idesc_f16_f32(128, 2 * pairs);
@@ -324,15 +342,13 @@ __global__ void __launch_bounds__(kRtNT, 2)
     for (int ht = 0; ht < 4; ++ht) {  // unrolled: acc[ht] stays in registers
       if (ht >= nht) break;           // uniform over the CTA
       for (int jc = 0; jc < ncha; ++jc) {
-        issue_A3(ht, jc);
-        cp_async_commit();
-        cp_async_wait<0>();
-        tc::fence_proxy_async();
-        tc::fence_before_sync();
-        __syncthreads();  // A3 chunk and B3 visible; the previous TMEM reads are done
         if (t == 0) {
-          tc::fence_after_sync();
-          const uint32_t sa = tc::smem_u32(a3s), sb = tc::smem_u32(sm + jc * rt_b3_chunk(pairs));
+          tc::mbar_arrive_expect_tx(&bar_a3, kRtA3Bytes);
+          tc::bulk_g2s(r2, fa + (size_t(ht) * ncha + jc) * kRtA3Bytes, kRtA3Bytes, &bar_a3);
+        }
+        waitb(&bar_a3, 5);
+        if (t == 0) {
+          const uint32_t sa = tc::smem_u32(r2), sb = tc::smem_u32(sm + jc * rt_b3_chunk(pairs));
 #pragma unroll
           for (int ks = 0; ks < kAcKC / 16; ++ks) {
             const uint64_t ahi = tc::smem_desc(sa + ks * 256, 128, kAcKC * 16);
@@ -343,39 +359,48 @@ __global__ void __launch_bounds__(kRtNT, 2)
             tc::mma_f16(tbase, alo, bhi, idesc3, true);
             tc::mma_f16(tbase, ahi, blo, idesc3, true);
           }
-          tc::mma_commit(&mbar[2]);
+          tc::mma_commit(&bar_mma3);
         }
-        ok = tc::mbar_wait(&mbar[2], (ph >> 2) & 1u, kWaitLimit) && ok;
-        ph ^= 4u;
+        waitb(&bar_mma3, 6);  // the MMAs read the A chunk: the region is free again
         tc::fence_after_sync();
       }
+      // S of this row tile, one coil per ring slot (thread 0 issues, all wait)
+      auto load_s = [&](int k) {
+        tc::mbar_arrive_expect_tx(&bar_s[k % kRtSlots], kRtSlotBytes);
+        tc::tma_load_3d(r2 + (k % kRtSlots) * kRtSlotBytes, &a.tm_se, 2 * w0, 128 * ht, cg0 + k, &bar_s[k % kRtSlots]);
+      };
+      if (t == 0)
+        for (int k = 0; k < kRtSlots && k < cn; ++k) load_s(k);
       // x_grad[h, w] += sum_c conj(S_c[h, w]) Y_c[h, w] for this thread's row
       const int h = ht * 128 + t;
       const bool hrow = h < H;
-      const float4* srow = reinterpret_cast<const float4*>(a.S + size_t(hrow ? h : 0) * W + w0);
       for (int k = 0; k < cn; ++k) {
         float v[16];
         tc::tmem_ld16(taddr + uint32_t(16 * k), v);
+        waitb(&bar_s[k % kRtSlots], 8 + (k % kRtSlots));
+        const float4* srow = reinterpret_cast<const float4*>(r2 + (k % kRtSlots) * kRtSlotBytes) + t * 4;
         if (hrow) {
-          float4 s4[kRtCols / 2];
-#pragma unroll
-          for (int qq = 0; qq < kRtCols / 2; ++qq) s4[qq] = __ldg(srow + size_t(cg0 + k) * (N / 2) + qq);
 #pragma unroll
           for (int qq = 0; qq < kRtCols / 2; ++qq) {
+            const float4 s4 = srow[qq];
             const float i0 = s_isig3[k * kRtCols + 2 * qq], i1 = s_isig3[k * kRtCols + 2 * qq + 1];
             const float yr0 = v[4 * qq] * i0, yi0 = v[4 * qq + 1] * i0;
             const float yr1 = v[4 * qq + 2] * i1, yi1 = v[4 * qq + 3] * i1;
             float2& a0 = acc[ht][2 * qq];
             float2& a1 = acc[ht][2 * qq + 1];
-            a0.x = fmaf(s4[qq].x, yr0, fmaf(s4[qq].y, yi0, a0.x));
-            a0.y = fmaf(s4[qq].x, yi0, fmaf(-s4[qq].y, yr0, a0.y));
-            a1.x = fmaf(s4[qq].z, yr1, fmaf(s4[qq].w, yi1, a1.x));
-            a1.y = fmaf(s4[qq].z, yi1, fmaf(-s4[qq].w, yr1, a1.y));
+            a0.x = fmaf(s4.x, yr0, fmaf(s4.y, yi0, a0.x));
+            a0.y = fmaf(s4.x, yi0, fmaf(-s4.y, yr0, a0.y));
+            a1.x = fmaf(s4.z, yr1, fmaf(s4.w, yi1, a1.x));
+            a1.y = fmaf(s4.z, yi1, fmaf(-s4.w, yr1, a1.y));
           }
+        }
+        if (k + kRtSlots < cn) {
+          __syncthreads();  // every thread read this slot
+          if (t == 0) load_s(k + kRtSlots);
         }
       }
       tc::fence_before_sync();
-      __syncthreads();  // TMEM read before the next tile's (or group's) MMAs
+      __syncthreads();  // TMEM and the S slots read before the next tile's (or group's) loads and MMAs
       tc::fence_after_sync();
     }
   }
@@ -474,15 +499,78 @@ __global__ void __launch_bounds__(kRtNT, 2)
 // ---------------------------------------------------------------------------
 // host side
 // ---------------------------------------------------------------------------
+namespace {
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// float32 tensor of dims (d0 innermost, d1, d2), dense, box (b0, b1, b2);
+// elements outside the tensor read as zero
+bool encode3d(CUtensorMap* m, const void* base, uint64_t d0, uint64_t d1, uint64_t d2, uint32_t b0, uint32_t b1,
+              uint32_t b2) {
+  PFN_cuTensorMapEncodeTiled_v12000 fn = encode_fn();
+  if (!fn) return false;
+  const cuuint64_t dims[3] = {d0, d1, d2};
+  const cuuint64_t strides[2] = {d0 * 4, d0 * d1 * 4};
+  const cuuint32_t box[3] = {b0, b1, b2};
+  const cuuint32_t es[3] = {1, 1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, const_cast<void*>(base), dims, strides, box, es,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+}  // namespace
+
+// Coils per group of an instance (the S and IDFT_W(y) boxes of its tensor maps).
+int iter_tc_coils(int C, int ncha) { return rt_coils(C, ncha); }
+
+// Whether the tensor-core row-local iteration takes a prepared problem (its
+// IDFT_W(y) tile must fit the 32 KB region); encodes its tensor maps.
+bool iter_tc_prepare(gbn_problem* P) {
+  const int cg = rt_coils(P->C, P->ncha);
+  P->tmaps_ok = false;
+  if (P->gmax < 1 || P->gmax > 256 || P->gmax * cg * 64 > kRtR2Bytes) return false;
+  const uint64_t W2 = uint64_t(2) * P->W;
+  bool ok = encode3d(&P->tm_x[0], P->xk0, W2, P->H, P->F, 2 * kRtCols, kTcHC, 1) &&
+            encode3d(&P->tm_x[1], P->xk1, W2, P->H, P->F, 2 * kRtCols, kTcHC, 1) &&
+            encode3d(&P->tm_s, P->S, W2, P->H, P->C, 2 * kRtCols, kTcHC, cg) &&
+            encode3d(&P->tm_se, P->S, W2, P->H, P->C, 2 * kRtCols, 128, 1) &&
+            encode3d(&P->tm_y, P->T, W2, P->C, P->T_rows, 2 * kRtCols, cg, P->gmax);
+  P->tmaps_ok = ok;
+  return ok;
+}
+
+void iter_tc_args(gbn_problem* P, FusedArgs* a) {
+  a->tm_x[0] = P->tm_x[0];
+  a->tm_x[1] = P->tm_x[1];
+  a->tm_s = P->tm_s;
+  a->tm_se = P->tm_se;
+  a->tm_y = P->tm_y;
+  a->gmax_box = P->gmax;
+  a->ntv = P->F * (P->W / kRtCols);  // one partial sum per (frame, 8 columns)
+}
+
 dim3 iter_tc_grid(int W, int frames) { return dim3(W / kRtCols, 1, frames); }
 
-void launch_iter_tc(const FusedArgs* tab, const BatchMap& bm, int it, int npad_max, dim3 grid, cudaStream_t s) {
+void launch_iter_tc(const FusedArgs* tab, const BatchMap& bm, int it, int npad_max, int cnmax, dim3 grid,
+                    cudaStream_t s) {
   static bool ok = false;
   if (!ok) {
-    cudaFuncSetAttribute(k_iter_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, rt_smem(256));
+    cudaFuncSetAttribute(k_iter_tc, cudaFuncAttributeMaxDynamicSharedMemorySize, rt_smem(256, 16));
+    // the whole unified memory as shared memory: two CTAs of ~100 KB per SM
+    cudaFuncSetAttribute(k_iter_tc, cudaFuncAttributePreferredSharedMemoryCarveout, cudaSharedmemCarveoutMaxShared);
     ok = true;
   }
-  launch_pdl(k_iter_tc, grid, kRtNT, rt_smem(npad_max), s, tab, bm, it, npad_max);
+  launch_pdl(k_iter_tc, grid, kRtNT, rt_smem(npad_max, cnmax), s, tab, bm, it, npad_max, cnmax);
 }
 
 }  // namespace gbn

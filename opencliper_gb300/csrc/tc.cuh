@@ -103,6 +103,51 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint3
   return false;
 }
 
+// Waits like mbar_wait, letting the hardware suspend the thread between polls
+// (suspend-time hint in ns) instead of spinning on the issue slots.
+__device__ __forceinline__ bool mbar_wait_sleep(uint64_t* mbar, uint32_t parity, uint32_t limit) {
+  const uint32_t a = smem_u32(mbar);
+  for (uint32_t i = 0; i < limit; ++i) {
+    uint32_t done = 0;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(done)
+        : "r"(a), "r"(parity), "r"(1000000u)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+// one arrival on mbar that also expects `bytes` of asynchronous copies
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(mbar)), "r"(bytes) : "memory");
+}
+
+// ---- bulk copies (TMA) ----------------------------------------------------------
+// contiguous global -> shared copy; both addresses 16-byte aligned, bytes a
+// multiple of 16; completion counted on mbar
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, uint64_t* mbar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(mbar))
+      : "memory");
+}
+// tiled 3-D tensor copy of the box at (c0, c1, c2) (c0 innermost, elements)
+// into shared memory (128-byte aligned); completion counted on mbar.  The
+// caller keeps c0 * element size a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_3d(void* dst, const void* tmap, int c0, int c1, int c2, uint64_t* mbar) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], [%5];\n" ::"r"(
+          smem_u32(dst)),
+      "l"(tmap), "r"(c0), "r"(c1), "r"(c2), "r"(smem_u32(mbar))
+      : "memory");
+}
+// orders this thread's later tensor copies after generic-proxy writes of the
+// tensor map at tmap (written by an earlier kernel)
+__device__ __forceinline__ void tmap_acquire(const void* tmap) {
+  asm volatile("fence.proxy.tensormap::generic.acquire.gpu [%0], 128;\n" ::"l"(tmap) : "memory");
+}
+
 // ---- TMEM -> registers -----------------------------------------------------------
 // 16 consecutive FP32 columns of this thread's lane, without waiting: the
 // registers are valid after tmem_wait_ld()

@@ -2,6 +2,7 @@
 #pragma once
 
 #include <cstdint>
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 namespace gbn {
@@ -92,6 +93,14 @@ struct FusedArgs {
   // pass takes instead of forming it from x_k
   const float2* tv_src;
   const float2* grad_ext;
+  // tensor-core row-local iteration (mixed_rowlocal.cu): tensor maps of x_k
+  // (ping, pong), of S for the forward chunks and for the adjoint row tiles,
+  // and of the kept rows' IDFT_W(y) in T; zero when unused
+  CUtensorMap tm_x[2];
+  CUtensorMap tm_s;
+  CUtensorMap tm_se;
+  CUtensorMap tm_y;
+  int gmax_box;           // kept rows per box of tm_y (the most kept rows of a frame)
 };
 
 // Instances covered by one launch of the fused kernels.  All of them share the
