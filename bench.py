@@ -552,6 +552,9 @@ def run_forms_only(args, dist: Dist) -> dict | None:
     torch.cuda.set_stream(stream)
     ctx = g.Context(dist.local)
     ctx.set_stream(stream.cuda_stream)
+    for kv in args.tuning:
+        key, val = kv.split("=", 1)
+        ctx.set_tuning(key, int(val))
     wanted = {f.strip() for f in args.forms.split(",") if f.strip()}
     forms = {name: fn(ctx, stream, args) for name, fn in FORMS if name in wanted}
     ctx.set_stream(None)
