@@ -170,6 +170,14 @@ def algorithmic_bytes(kind: str, G: int, shape: tuple | None = None) -> int:
     raise KeyError(kind)
 
 
+def dense_iteration_bytes() -> int:
+    """Bytes one inner iteration of the reference's algorithm moves at the headline
+    workload: y, S once, x_k, x_ref, w_k read, x_{k+1}, w_{k+1} written, the pixel mask."""
+    W, H, F, C = WL["W"], WL["H"], WL["F"], WL["C"]
+    N = W * H
+    return 8 * (N * F * C + N * C + 5 * N * F) + N * F
+
+
 def ncu_traffic(kind: str, field: str = "bytes_per_launch") -> float | None:
     """Per-launch figure (DRAM bytes, or warp instructions) from the committed
     ncu summary, when present."""
@@ -325,6 +333,9 @@ def run_ours(args, dist: Dist) -> dict | None:
     total_prof = sum(v[1] for v in prof.values())
     roof = {"bound": "hbm", "kernel": dom, "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
             "frac": round(achieved / peak, 4), "peak_source": f"{peak_src} hbm_gbs",
+            # the same launch against the dense per-iteration bytes of the reference's
+            # algorithm (all of y read each iteration, pixel mask): what the reference moves
+            "frac_dense_bytes": round(dense_iteration_bytes() / avg_s / 1e9 / peak, 4) if dom == "iter" else None,
             "traffic": traffic, "algorithmic_bytes_per_launch": alg, "avg_launch_us": round(avg_s * 1e6, 2),
             "share_of_step": round(ms_dom / max(total_prof, 1e-9), 3),
             "groups_us_per_launch": {k: round(v[1] * 1e3 / max(v[0], 1), 2) for k, v in prof.items()}}
