@@ -5,13 +5,16 @@
 // number of coils each forward-column CTA transforms (k1_coils_per_block:
 // fewer coils, more CTAs and more re-reads of x; more coils, fewer and longer
 // CTAs) and how many persistent row-pass CTAs run per SM (k2_ctas_per_sm).
+// Both shape the three-pass iteration only (the one-kernel row-local
+// iteration has a fixed launch), so the tuner times that iteration:
 // gbn_autotune measures every candidate pair on a synthetic problem of each
 // requested shape (zero data with a 1/8 row mask: the kernels' cost does not
 // depend on the values) and keeps the fastest in the context; single runs and
 // batch groups look their shape up (tuning_for).  It also times the mixed
-// form's tensor-core forward pass against the plain FP32 kernels on the same
-// shape (captured batches of one) and records which is faster
-// (mixed_fwd_tc_for).  A text cache file keeps the results across processes:
+// form's three-pass iteration with the tensor-core forward pass against the
+// plain FP32 kernels on the same shape (captured batches of one) and records
+// which is faster (mixed_fwd_tc_for; mixed groups that the row-local
+// iteration takes run it in FP32 and do not ask).  A text cache file keeps the results across processes:
 //   # gbn autotune v2: W H F C k1_coils_per_block k2_ctas_per_sm us_per_iteration mixed_fwd_tc
 //   256 256 20 12 4 3 121.5 0
 // (v1 lines without the last column are read with mixed_fwd_tc unknown)
@@ -60,7 +63,7 @@ bool mixed_fwd_tc_for(gbn_ctx* ctx, int W, int H, int F, int C) {
     if (t && t->tc >= 0) return t->tc != 0;
   }
   (void)W;
-  return H >= 320;  // measured: FP32 faster at 256, tensor cores at 384
+  return H >= 320;  // three-pass iteration, measured: FP32 faster at 256, tensor cores at 384
 }
 
 void tuning_for(gbn_ctx* ctx, int W, int H, int F, int C, int* cpb, int* k2) {
@@ -157,9 +160,13 @@ int tune_shape(gbn_ctx* ctx, int W, int H, int F, int C, gbn_ctx::Tuned* out) {
   gbn_nesta_params prm{0.01f, 1e-3f, 1.0f, 1u, 3e-4f, 0, 40u, 0u, 7u};
   const int saved_cpb = ctx->k1_coils_per_block, saved_k2 = ctx->k2_ctas_per_sm;
   const bool saved_use = ctx->use_tuned, saved_prof = ctx->profile;
+  const int saved_rl = ctx->row_local;
   const uint64_t saved_rand = ctx->rand48;
   ctx->use_tuned = false;
   ctx->profile = false;
+  // the launch shapes and the tensor-core choice shape the three-pass
+  // iteration (the row-local iteration has neither), so it is what is timed
+  ctx->row_local = 0;
   gbn_ctx::Tuned best{saved_cpb, saved_k2, -1.f};
   std::vector<int> cpbs;
   for (int c : {1, 2, 3, 4, 6, 8})
@@ -225,6 +232,7 @@ int tune_shape(gbn_ctx* ctx, int W, int H, int F, int C, gbn_ctx::Tuned* out) {
   ctx->k2_ctas_per_sm = saved_k2;
   ctx->use_tuned = saved_use;
   ctx->profile = saved_prof;
+  ctx->row_local = saved_rl;
   ctx->rand48 = saved_rand;  // tuning runs do not consume the caller's drand48 sequence
   if (e0) cudaEventDestroy(e0);
   if (e1) cudaEventDestroy(e1);

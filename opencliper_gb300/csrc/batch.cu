@@ -250,7 +250,37 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
     memset(&g.bm, 0, sizeof(g.bm));
     g.bm.n = ng;
     g.bm.ctl = g.ctl;
-    if (precision == GBN_PRECISION_MIXED) {
+    const SizeKernels* kh = find_size(g.H);
+    // row analysis of every member (the setup's row kernels): whether all of
+    // them keep only fully sampled or unsampled rows, within what the
+    // row-local iteration stages
+    auto rows_all_local = [&](bool* all) -> int {
+      *all = true;
+      for (int i : g.idx) {
+        gbn_problem* P = b->probs[i];
+        g.any_stoptest = g.any_stoptest || b->prm[i].stoptest == 1;
+        ctx->launches += launch_pre(P, b->prm[i], ctx->stream);
+        int part = 1;
+        if ((e = cudaMemcpyAsync(&part, &P->st->partial_rows, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream)) !=
+                cudaSuccess ||
+            (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess)
+          return cuda_status(e, "batch row analysis");
+        *all = *all && part == 0;
+      }
+      return GBN_OK;
+    };
+    // FP32 groups, and mixed groups left to the automatic choice, run the FP32
+    // row-local iteration where it applies: faster than every tensor-core form
+    // measured (the tensor-core row-local iteration, and the three-pass
+    // iteration with the tensor-core forward pass, at 256 and 384)
+    bool analysed = false;
+    if (kh->iter_cols && ctx->row_local && (precision == GBN_PRECISION_FP32 || ctx->mixed_fwd_tc < 0)) {
+      bool all = false;
+      if ((rc = rows_all_local(&all)) != GBN_OK) break;
+      g.row_local = all;
+      analysed = true;
+    }
+    if (precision == GBN_PRECISION_MIXED && !g.row_local) {
       int gF = 2, gC = 1;
       for (int i : g.idx) {
         gF = std::max(gF, b->probs[i]->F);
@@ -329,25 +359,12 @@ int batch_create(gbn_ctx* ctx, int n, gbn_problem* const* problems, const gbn_ne
     g.g3tc = inv_cols_tc_grid(g.W, g.H, frames);
     g.adjoint_tc = g.tc && ctx->mixed_adjoint_tc != 0;
     if (g.row_local_tc) g.g_tc = iter_tc_grid(g.W, frames);
-    // row-local iteration: every member's current data keep only fully
-    // sampled or unsampled rows
-    const SizeKernels* kh = find_size(g.H);
-    if (!g.tc && !g.row_local_tc && kh->iter_cols && ctx->row_local) {
-      bool all = true;
-      for (int i : g.idx) {
-        gbn_problem* P = b->probs[i];
-        g.any_stoptest = g.any_stoptest || b->prm[i].stoptest == 1;
-        ctx->launches += launch_pre(P, b->prm[i], ctx->stream);
-        int part = 1;
-        if ((e = cudaMemcpyAsync(&part, &P->st->partial_rows, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream)) !=
-                cudaSuccess ||
-            (e = cudaStreamSynchronize(ctx->stream)) != cudaSuccess) {
-          rc = cuda_status(e, "batch row analysis");
-          break;
-        }
-        all = all && part == 0;
-      }
-      if (rc != GBN_OK) break;
+    // a mixed group with the FP32 kernels forced (mixed_fwd_tc = 0) runs them
+    // as an FP32 group does
+    if (precision == GBN_PRECISION_MIXED && !analysed && !g.tc && !g.row_local_tc && kh->iter_cols &&
+        ctx->row_local) {
+      bool all = false;
+      if ((rc = rows_all_local(&all)) != GBN_OK) break;
       g.row_local = all;
     }
   }

@@ -10,6 +10,7 @@
 
 #include "ctx.h"
 #include "nesta_kernels.cuh"
+#include "rowlocal.cuh"
 #include "solver.h"
 
 namespace gbn {
@@ -80,7 +81,9 @@ constexpr int kStatusRowsOverflow = 6;  // NestaDevState::status: kept rows beyo
 
 // one CTA of 512 threads (H <= 512): per-frame prefix numbering of kept rows;
 // rows beyond the row buffer's capacity `cap` are dropped (rowmap -1) and
-// reported in *status; *partial = kept rows whose mask row is sampled in part
+// reported in *status; *partial counts what keeps a problem off the
+// row-local iteration: kept rows whose mask row is sampled in part, and
+// frames with more kept rows than that iteration stages (iter_cols_rcap)
 __global__ void __launch_bounds__(512) k_rowscan(const int* __restrict__ flags, const int* __restrict__ full, int H,
                                                  int F, int* __restrict__ rowmap, int* __restrict__ rowoff,
                                                  int* __restrict__ rows_h, int* __restrict__ rows_f,
@@ -88,7 +91,7 @@ __global__ void __launch_bounds__(512) k_rowscan(const int* __restrict__ flags, 
                                                  int* __restrict__ partial) {
   __shared__ int wsum[16];
   const int t = threadIdx.x, lane = t & 31, wid = t >> 5;
-  int base = 0, npart = 0;
+  int base = 0, npart = 0, nwide = 0;
   bool dropped = false;
   for (int f = 0; f < F; ++f) {
     const int fl = (t < H) ? flags[f * H + t] : 0;
@@ -114,12 +117,13 @@ __global__ void __launch_bounds__(512) k_rowscan(const int* __restrict__ flags, 
     }
     if (t == 0) rowoff[f] = base;
     dropped |= tot > room;
+    nwide += tot > iter_cols_rcap(H);
     base += min(tot, room);
     __syncthreads();
   }
   if (t == 0) {
     rowoff[F] = base;
-    *partial = npart;
+    *partial = npart + nwide;
     if (dropped) atomicExch(status, kStatusRowsOverflow);
   }
 }

@@ -105,13 +105,25 @@ __device__ void rowlocal_finish(const FusedArgs& a, NestaDevState* st, ClassCtl*
   }
 }
 
+// Kept rows per frame whose IDFT_W(y) k_iter_cols<L> stages: a quarter of the
+// rows (every Cartesian mask at R >= 4), at least 32 for short columns.
+constexpr int iter_cols_rcap(int L) { return L / 4 > (L < 32 ? L : 32) ? L / 4 : (L < 32 ? L : 32); }
+
+// Shared-memory bytes of k_iter_cols<L> (the layout of IterColsSmem<L>).
+constexpr int iter_cols_bytes(int L) {
+  const int a = split_a(L), b = split_b(L);
+  const int ex = (a * col_ks(b) > b * col_ks(a)) ? a * col_ks(b) : b * col_ks(a);
+  return (2 * L * kWB + 2 * iter_cols_rcap(L) * kWB + ex + 2 * L) * 8 + L * 4 + (kColNT / 32) * 8 +
+         kFmeanCopy * 4 + 16;
+}
+
 template <int H>
 struct IterColsSmem {
   static constexpr int A = Split<H>::A, B = Split<H>::B;
   static constexpr int KSF = col_ks(B);  // forward exchange: slot (k1, s*kWB + w), k1 < A
   static constexpr int KSI = col_ks(A);  // inverse exchange: slot (k1', s'*kWB + w), k1' < B
   static constexpr int EXN = (A * KSF > B * KSI) ? A * KSF : B * KSI;
-  static constexpr int RCAP = H / 4;                     // kept rows whose IDFT_W(y) is staged (R >= 4)
+  static constexpr int RCAP = iter_cols_rcap(H);         // kept rows whose IDFT_W(y) is staged
   static constexpr int S_OFF = 0;                        // float2 [2][H][kWB]
   static constexpr int Y_OFF = S_OFF + 2 * H * kWB;      // float2 [2][RCAP][kWB]
   static constexpr int EX_OFF = Y_OFF + 2 * RCAP * kWB;  // float2 [EXN]
@@ -119,15 +131,27 @@ struct IterColsSmem {
   static constexpr int F2_END = TW_OFF + 2 * H;
   static constexpr int BYTES = F2_END * 8 + H * 4 + (kColNT / 32) * 8 + kFmeanCopy * 4 + 16;
   static_assert(cdiv(kWB * B, kColNT) * A * kColNT <= 2 * H * kWB, "accumulator exchange must fit the S buffers");
+  static_assert(BYTES == iter_cols_bytes(H), "layout and byte count agree");
 };
 
-// Lengths whose first factor A (split_a) keeps the per-thread state of
-// k_iter_cols in registers at 3 CTAs per SM; longer columns run the
-// three-pass iteration.
-constexpr bool iter_cols_ok(int H) { return split_a(H) <= 16; }
+
+// CTAs per SM the launch bounds ask for.  A first factor A <= 16 keeps the
+// per-thread state (x at the pass-1 items, the accumulators, one pass-2 item)
+// within 168 registers at three CTAs per SM; longer first factors hold more
+// per thread, and their shared memory allows two CTAs per SM (one past 448),
+// which leaves each thread up to 255 registers.
+constexpr int iter_cols_min_blocks(int H) {
+  return split_a(H) <= 16 ? 3 : (iter_cols_bytes(H) + 1024 <= 114 * 1024 ? 2 : 1);
+}
+
+// Lengths that run the row-local iteration; the others (whose per-thread
+// state would spill) run the three-pass iteration.
+constexpr bool iter_cols_ok(int H) {
+  return split_a(H) != 0 && (split_a(H) <= 16 || (split_b(H) >= 8 && split_b(H) <= 16 && split_a(H) <= 24));
+}
 
 template <int H>
-__global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, 3)
+__global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_min_blocks(H))
     k_iter_cols(const FusedArgs* __restrict__ tab, const __grid_constant__ BatchMap bm, int it) {
   using L = IterColsSmem<H>;
   constexpr int A = L::A, B = L::B, KSF = L::KSF, KSI = L::KSI, RCAP = L::RCAP;
@@ -155,7 +179,9 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, 3)
   const size_t N = size_t(a.N);
   const int rowbase = a.rowoff[f];
   const int nrows = a.rowoff[f + 1] - rowbase;
-  const bool staged = nrows <= RCAP;  // kept rows fit the shared buffers (uniform per CTA)
+  // kept rows fit the shared buffers: a frame with more runs the three-pass
+  // iteration (the row analysis counts it in partial_rows, checked below)
+  const bool staged = nrows <= RCAP;
   const int cmid = (C + 1) / 2;
   const int cbeg = half ? cmid : 0, cend = half ? C : cmid;
 
@@ -230,25 +256,6 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, 3)
       for (int n1 = 0; n1 < A; ++n1) xv[ii][n1] = x[size_t(B * n1 + s) * W + w0 + w];
     }
   }
-  // tTV objective partial sums over the tile (first half only; not in fixup mode)
-  float su2 = 0.f, sud = 0.f;
-  if (half == 0 && !fix) {
-    const float2* __restrict__ xm = xk + size_t((f + F - 1) % F) * N;
-#pragma unroll
-    for (int ii = 0; ii < NI1; ++ii) {
-      const int i = t + ii * kColNT;
-      if (i < N1) {
-        const int w = i % kWB, s = i / kWB;
-#pragma unroll
-        for (int n1 = 0; n1 < A; ++n1) {
-          const float2 d = csub(xv[ii][n1], xm[size_t(B * n1 + s) * W + w0 + w]);
-          const float2 u = tv_normalize(d, inv_mu);
-          su2 = fmaf(u.x, u.x, fmaf(u.y, u.y, su2));
-          sud = fmaf(u.x, d.x, fmaf(u.y, d.y, sud));
-        }
-      }
-    }
-  }
 
   float2 acc[NI3][A];
 #pragma unroll
@@ -300,7 +307,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, 3)
           float2 q = make_float2(0.f, 0.f);
           if (code != -1) {
             const int j = code >= 0 ? code : -2 - code;
-            const float2 yv = staged ? Yc[j * kWB + w] : a.T[(size_t(rowbase + j) * C + c) * W + w0 + w];
+            const float2 yv = Yc[j * kWB + w];
             q = (code >= 0) ? csub(cscale(r[ii][k2], s_row), yv) : make_float2(-yv.x, -yv.y);
             racc = fmaf(q.x, q.x, fmaf(q.y, q.y, racc));
           }
@@ -338,6 +345,26 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, 3)
           const float2 p = cmul(v[k2], Sc[(k1p + B * k2) * kWB + w]);
           acc[ii][k2].x += p.x;
           acc[ii][k2].y -= p.y;
+        }
+      }
+    }
+  }
+
+  // tTV objective partial sums over the tile (first half only; not in fixup mode)
+  float su2 = 0.f, sud = 0.f;
+  if (half == 0 && !fix) {
+    const float2* __restrict__ xm = xk + size_t((f + F - 1) % F) * N;
+#pragma unroll
+    for (int ii = 0; ii < NI1; ++ii) {
+      const int i = t + ii * kColNT;
+      if (i < N1) {
+        const int w = i % kWB, s = i / kWB;
+#pragma unroll
+        for (int n1 = 0; n1 < A; ++n1) {
+          const float2 d = csub(xv[ii][n1], xm[size_t(B * n1 + s) * W + w0 + w]);
+          const float2 u = tv_normalize(d, inv_mu);
+          su2 = fmaf(u.x, u.x, fmaf(u.y, u.y, su2));
+          sud = fmaf(u.x, d.x, fmaf(u.y, d.y, sud));
         }
       }
     }

@@ -102,15 +102,17 @@ def test_mixed_rejects_too_many_kept_rows(ctx):
     prob.close()
 
 
-def test_mixed_forward_choice_per_group(ctx):
+@pytest.mark.parametrize("W,H,F,C,Rr", [(48, 40, 5, 3, 4), (32, 384, 3, 3, 8)])
+def test_mixed_forward_choice_per_group(ctx, W, H, F, C, Rr):
     """mixed_fwd_tc = 0 runs a mixed batch's groups on the plain FP32 kernels
     (the same image as an FP32 batch, bit for bit), and so does the automatic
-    choice here; mixed_fwd_tc = 1 runs the row-local iteration on the tensor
-    cores."""
-    p = synth.make_problem(48, 40, 5, 3, 4, seed=91)
+    choice for row masks at any H (the FP32 row-local iteration beats the
+    tensor-core forms); mixed_fwd_tc = 1 runs the row-local iteration on the
+    tensor cores."""
+    p = synth.make_problem(W, H, F, C, Rr, seed=91)
     dy, dS, dm = ctx.to_device(p.y), ctx.to_device(p.S), ctx.to_device(p.mask)
     prob = g.Problem(ctx, dy, dS, dm)
-    x = ctx.empty((5, 40, 48), np.complex64)
+    x = ctx.empty((F, H, W), np.complex64)
     prm = g.nesta_params(**FIXED)
     imgs = []
     for prec, tc in ((g.PRECISION_FP32, 1), (g.PRECISION_MIXED, 0), (g.PRECISION_MIXED, -1), (g.PRECISION_MIXED, 1)):

@@ -98,6 +98,9 @@ def test_nesta_general_mask_and_data_outside_mask(ctx):
 @pytest.mark.parametrize("W,H,F,C,Rr,prm", [
     (64, 64, 8, 4, 6, {**FIXED, "maxIter": 20}),
     (128, 96, 10, 8, 8, {**FIXED, "maxIter": 20}),
+    (64, 384, 4, 5, 8, {**FIXED, "maxIter": 20}),   # first factor 24: two CTAs per SM
+    (40, 320, 3, 4, 8, {**FIXED, "maxIter": 20}),   # first factor 20
+    (48, 168, 4, 3, 6, {**FIXED, "maxIter": 20}),   # 21 x 8
     (48, 48, 6, 3, 4, dict(lambda_i=1e-2, mu_f=3e-4, La=1.0, maxIntIter=4, maxIter=100, stoptest=1, miniter=7,
                            tolVar=3e-4)),
     (32, 32, 4, 2, 4, dict(lambda_i=1e-2, mu_f=3e-4, La=1.0, maxIntIter=3, maxIter=100, stoptest=1, miniter=4,
@@ -115,12 +118,10 @@ def test_row_local_iteration_matches_three_pass(ctx, W, H, F, C, Rr, prm):
     p = synth.make_problem(W, H, F, C, Rr, seed=W * 3 + F)
     outs, sts = [], []
     for rl in (1, 0):
-        ctx.set_tuning("row_local", rl)
-        ctx.seed48(drand48.state_to_seed16v(drand48.DEFAULT_STATE))
-        o, st, _ = _run(ctx, p.y, p.S, p.mask, prm)
+        o, st, n_iter = _run_counting_iter(ctx, p, prm, rl)
+        assert (n_iter > 0) == (rl == 1), (rl, n_iter)
         outs.append(o)
         sts.append(st)
-    ctx.set_tuning("row_local", 1)
     assert sts[0]["inner_iters"] == sts[1]["inner_iters"]
     assert sts[0]["status"] == 0 and sts[1]["status"] == 0
     # ||Ex - y||^2 is the square of a residual ~1e-3 of the data, so its FP32
@@ -129,6 +130,35 @@ def test_row_local_iteration_matches_three_pass(ctx, W, H, F, C, Rr, prm):
     err = R.nrmse(outs[0], outs[1])
     print(f"row-local vs three-pass: NRMSE {err:.3e}, fx {sts[0]['fx_final']:.6f} / {sts[1]['fx_final']:.6f}")
     assert err <= 1e-4
+
+
+def _run_counting_iter(ctx, p, prm, row_local: int):
+    """Runs with the tuning knob row_local set; returns the image, the stats
+    and how many row-local iteration kernels ran (event profile)."""
+    ctx.set_tuning("row_local", row_local)
+    ctx.seed48(drand48.state_to_seed16v(drand48.DEFAULT_STATE))
+    ctx.profile(True)
+    ctx.profile_reset()
+    try:
+        o, st, _ = _run(ctx, p.y, p.S, p.mask, prm)
+        n_iter = ctx.profile_read().get("iter", (0, 0.0))[0]
+    finally:
+        ctx.profile(False)
+        ctx.set_tuning("row_local", 1)
+    return o, st, n_iter
+
+
+def test_wide_frames_run_three_pass(ctx):
+    """Frames keeping more rows than the row-local iteration stages (a quarter
+    of H, at least 32; R = 2 here) make the row analysis send the problem to
+    the three-pass iteration, which then gives exactly the result it gives
+    with the knob off."""
+    p = synth.make_problem(32, 256, 4, 3, 2, seed=21)
+    assert max(int(np.any(p.mask[f] != 0, axis=1).sum()) for f in range(4)) > 256 // 4
+    o1, st1, n1 = _run_counting_iter(ctx, p, FIXED, 1)
+    o0, st0, n0 = _run_counting_iter(ctx, p, FIXED, 0)
+    assert n1 == 0 and n0 == 0
+    assert st1["status"] == 0 and np.array_equal(o1, o0)
 
 
 def test_nesta_deterministic_with_same_seed(ctx):
