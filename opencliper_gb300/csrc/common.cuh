@@ -72,6 +72,23 @@ GBN_HD __forceinline__ void sfor(F&& f) {
 GBN_HD __forceinline__ float2 cadd(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
 GBN_HD __forceinline__ float2 csub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
 GBN_HD __forceinline__ float2 cscale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+// Packed forms of cadd and csub: one FP32x2 instruction on sm_100 and later.
+// Each lane rounds as the scalar operation does (a - b is a + (-b) in IEEE
+// arithmetic), so the results are identical.
+GBN_HD __forceinline__ float2 padd(float2 a, float2 b) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+  return __fadd2_rn(a, b);
+#else
+  return cadd(a, b);
+#endif
+}
+GBN_HD __forceinline__ float2 psub(float2 a, float2 b) {
+#if defined(__CUDA_ARCH__) && __CUDA_ARCH__ >= 1000
+  return __fadd2_rn(a, make_float2(-b.x, -b.y));
+#else
+  return csub(a, b);
+#endif
+}
 // a * b
 GBN_HD __forceinline__ float2 cmul(float2 a, float2 b) {
   return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));

@@ -85,14 +85,16 @@ GBN_HD __forceinline__ void dft(float2* a) {
   if constexpr (N == 1) {
   } else if constexpr (N == 2) {
     const float2 t = a[1];
-    a[1] = csub(a[0], t);
-    a[0] = cadd(a[0], t);
+    a[1] = psub(a[0], t);
+    a[0] = padd(a[0], t);
   } else if constexpr (N == 4) {
-    const float2 s02 = cadd(a[0], a[2]), d02 = csub(a[0], a[2]);
-    const float2 s13 = cadd(a[1], a[3]), d13 = csub(a[1], a[3]);
+    // packed adds where both operands are whole complex values; the -i turn
+    // swaps components, so those two outputs stay scalar
+    const float2 s02 = padd(a[0], a[2]), d02 = psub(a[0], a[2]);
+    const float2 s13 = padd(a[1], a[3]), d13 = psub(a[1], a[3]);
     const float2 r = cmul_negi(d13);
-    a[0] = cadd(s02, s13);
-    a[2] = csub(s02, s13);
+    a[0] = padd(s02, s13);
+    a[2] = psub(s02, s13);
     a[1] = cadd(d02, r);
     a[3] = csub(d02, r);
   } else if constexpr (N == 3 || N == 5 || N == 7) {

@@ -109,6 +109,18 @@ __device__ void rowlocal_finish(const FusedArgs& a, NestaDevState* st, ClassCtl*
 // rows (every Cartesian mask at R >= 4), at least 32 for short columns.
 constexpr int iter_cols_rcap(int L) { return L / 4 > (L < 32 ? L : 32) ? L / 4 : (L < 32 ? L : 32); }
 
+// Twiddle m of a thread's item from its row of M consecutive values (16-byte
+// aligned when M is even): pairs come from one 16-byte shared load.
+template <int M>
+__device__ __forceinline__ float2 twiddle(const float2* row, int m) {
+  if constexpr (M % 2 == 0) {
+    const float4 q = reinterpret_cast<const float4*>(row)[m >> 1];
+    return (m & 1) ? make_float2(q.z, q.w) : make_float2(q.x, q.y);
+  } else {
+    return row[m];
+  }
+}
+
 // Shared-memory bytes of k_iter_cols<L> (the layout of IterColsSmem<L>).
 constexpr int iter_cols_bytes(int L) {
   const int a = split_a(L), b = split_b(L);
@@ -132,6 +144,7 @@ struct IterColsSmem {
   static constexpr int BYTES = F2_END * 8 + H * 4 + (kColNT / 32) * 8 + kFmeanCopy * 4 + 16;
   static_assert(cdiv(kWB * B, kColNT) * A * kColNT <= 2 * H * kWB, "accumulator exchange must fit the S buffers");
   static_assert(BYTES == iter_cols_bytes(H), "layout and byte count agree");
+  static_assert(TW_OFF % 2 == 0, "twiddle rows start on 16-byte boundaries");
 };
 
 
@@ -216,8 +229,14 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
     const int j = a.rowmap[f * H + i];
     rcode[i] = (j < 0) ? -1 : (a.row_full[rowbase + j] ? j : -2 - j);
   }
-  // twiddles: [k1*B + s] = w_H^(s*k1) (forward first pass), [H + k1'*A + s'] (inverse first pass)
-  for (int i = t; i < 2 * H; i += kColNT) tws[i] = __ldg(a.twH + i);
+  // twiddles, stored per item so that a thread reads its own as consecutive
+  // pairs: [s*A + k1] = w_H^(s*k1) (forward first pass, item s) and
+  // [H + k1*B + k1'] = w_H^(k1*k1') (inverse first pass, item k1); the global
+  // table holds them as [k1*B + s] and [H + k1'*A + k1]
+  for (int i = t; i < 2 * H; i += kColNT) {
+    const int d = i < H ? (i % B) * A + i / B : H + ((i - H) % A) * B + (i - H) / A;
+    tws[d] = __ldg(a.twH + i);
+  }
   grid_dep_wait();  // x_k, w_k and the scalar state come from the previous iteration
   grid_dep_release();
 
@@ -264,6 +283,18 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
     for (int k2 = 0; k2 < A; ++k2) acc[ii][k2] = make_float2(0.f, 0.f);
   const float s_row = a.s_row;
   float racc = 0.f;
+  // kept rows of each pass-2 item (w, k1): bit k2 for row k1 + A*k2
+  __syncthreads();  // row codes written
+  unsigned kept[NI2];
+#pragma unroll
+  for (int ii = 0; ii < NI2; ++ii) {
+    kept[ii] = 0u;
+    const int k1 = (t + ii * kColNT) / kWB;
+    if (t + ii * kColNT < N2) {
+#pragma unroll
+      for (int k2 = 0; k2 < B; ++k2) kept[ii] |= (rcode[k1 + A * k2] != -1 ? 1u : 0u) << k2;
+    }
+  }
 
   for (int c = cbeg; c < cend; ++c) {
     const int buf = (c - cbeg) & 1;
@@ -287,7 +318,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
         for (int n1 = 0; n1 < A; ++n1) v[n1] = cmul(xv[ii][n1], Sc[(B * n1 + s) * kWB + w]);
         dft<A>(v);
 #pragma unroll
-        for (int k1 = 0; k1 < A; ++k1) ex[k1 * KSF + s * kWB + w] = (k1 == 0) ? v[k1] : cmul(v[k1], tws[k1 * B + s]);
+        for (int k1 = 0; k1 < A; ++k1) ex[k1 * KSF + s * kWB + w] = (k1 == 0) ? v[k1] : cmul(v[k1], twiddle<A>(tws + s * A, k1));
       }
     }
     __syncthreads();
@@ -303,9 +334,9 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
         dft<B>(r[ii]);
 #pragma unroll
         for (int k2 = 0; k2 < B; ++k2) {
-          const int code = rcode[k1 + A * k2];
           float2 q = make_float2(0.f, 0.f);
-          if (code != -1) {
+          if (kept[ii] & (1u << k2)) {
+            const int code = rcode[k1 + A * k2];
             const int j = code >= 0 ? code : -2 - code;
             const float2 yv = Yc[j * kWB + w];
             q = (code >= 0) ? csub(cscale(r[ii][k2], s_row), yv) : make_float2(-yv.x, -yv.y);
@@ -325,7 +356,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
         dft<B>(r[ii]);
 #pragma unroll
         for (int k1p = 0; k1p < B; ++k1p)
-          ex[k1p * KSI + k1 * kWB + w] = (k1p == 0) ? r[ii][k1p] : cmul(r[ii][k1p], tws[H + k1p * A + k1]);
+          ex[k1p * KSI + k1 * kWB + w] = (k1p == 0) ? r[ii][k1p] : cmul(r[ii][k1p], twiddle<B>(tws + H + k1 * B, k1p));
       }
     }
     __syncthreads();
@@ -341,10 +372,10 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
         dft<A>(v);
 #pragma unroll
         for (int k2 = 0; k2 < A; ++k2) {
-          // conj(v) * conj(S) == conj(v * S)
-          const float2 p = cmul(v[k2], Sc[(k1p + B * k2) * kWB + w]);
-          acc[ii][k2].x += p.x;
-          acc[ii][k2].y -= p.y;
+          // conj(v) * conj(S) == conj(v * S), formed as cmul's negated imaginary part
+          const float2 sv = Sc[(k1p + B * k2) * kWB + w];
+          const float2 p = make_float2(fmaf(v[k2].x, sv.x, -v[k2].y * sv.y), fmaf(-v[k2].x, sv.y, -(v[k2].y * sv.x)));
+          acc[ii][k2] = padd(acc[ii][k2], p);
         }
       }
     }
