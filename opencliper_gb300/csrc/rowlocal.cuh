@@ -39,6 +39,7 @@
 #pragma once
 
 #include "nesta_kernels.cuh"
+#include "tc.cuh"
 
 namespace gbn {
 
@@ -121,11 +122,44 @@ __device__ __forceinline__ float2 twiddle(const float2* row, int m) {
   }
 }
 
+// Lengths whose x values and coil accumulators live in tensor memory instead
+// of registers: first factors above 16 with one pass-1 and one inverse pass-2
+// item per thread (H = 288, 320, 336, 384).  With the registers this frees and
+// a single S buffer, three CTAs share an SM at H = 320 and 384 instead of two
+// (measured: 1.28x at 384 x 384).  At H = 256 the register form is faster.
+constexpr bool iter_cols_tmem(int L) { return split_a(L) > 16 && kWB * split_b(L) == kColNT; }
+
+// Calls fn(offset, count) for consecutive pieces of F TMEM columns: pieces of
+// 16, then one each of 8, 4 and 2 as F requires (F even); every piece starts
+// at a multiple of its size.
+template <int F, typename Fn>
+__device__ __forceinline__ void tmem_pieces(Fn&& fn) {
+  static_assert(F % 2 == 0, "whole complex values");
+  sfor<0, F / 16>([&](auto qc) {
+    fn(std::integral_constant<int, 16 * decltype(qc)::value>{}, std::integral_constant<int, 16>{});
+  });
+  constexpr int o8 = F / 16 * 16, o4 = o8 + ((F - o8) & 8), o2 = o4 + ((F - o4) & 4);
+  if constexpr ((F - o8) & 8) fn(std::integral_constant<int, o8>{}, std::integral_constant<int, 8>{});
+  if constexpr ((F - o4) & 4) fn(std::integral_constant<int, o4>{}, std::integral_constant<int, 4>{});
+  if constexpr ((F - o2) & 2) fn(std::integral_constant<int, o2>{}, std::integral_constant<int, 2>{});
+}
+template <int N>
+__device__ __forceinline__ void tmem_ld_n(uint32_t taddr, float* v) {
+  if constexpr (N == 16) tc::tmem_ld16(taddr, v);
+  else tc::tmem_ld_small<N>(taddr, v);
+}
+template <int N>
+__device__ __forceinline__ void tmem_st_n(uint32_t taddr, const float* v) {
+  if constexpr (N == 16) tc::tmem_st16(taddr, v);
+  else tc::tmem_st_small<N>(taddr, v);
+}
+constexpr int iter_cols_sbufs(int L) { return iter_cols_tmem(L) ? 1 : 2; }
+
 // Shared-memory bytes of k_iter_cols<L> (the layout of IterColsSmem<L>).
 constexpr int iter_cols_bytes(int L) {
   const int a = split_a(L), b = split_b(L);
   const int ex = (a * col_ks(b) > b * col_ks(a)) ? a * col_ks(b) : b * col_ks(a);
-  return (2 * L * kWB + 2 * iter_cols_rcap(L) * kWB + ex + 2 * L) * 8 + L * 4 + (kColNT / 32) * 8 +
+  return (iter_cols_sbufs(L) * L * kWB + 2 * iter_cols_rcap(L) * kWB + ex + 2 * L) * 8 + L * 4 + (kColNT / 32) * 8 +
          kFmeanCopy * 4 + 16;
 }
 
@@ -136,25 +170,28 @@ struct IterColsSmem {
   static constexpr int KSI = col_ks(A);  // inverse exchange: slot (k1', s'*kWB + w), k1' < B
   static constexpr int EXN = (A * KSF > B * KSI) ? A * KSF : B * KSI;
   static constexpr int RCAP = iter_cols_rcap(H);         // kept rows whose IDFT_W(y) is staged
-  static constexpr int S_OFF = 0;                        // float2 [2][H][kWB]
-  static constexpr int Y_OFF = S_OFF + 2 * H * kWB;      // float2 [2][RCAP][kWB]
+  static constexpr int SB = iter_cols_sbufs(H);          // S buffers: 2 (next coil copied during this one) or 1
+  static constexpr int S_OFF = 0;                        // float2 [SB][H][kWB]
+  static constexpr int Y_OFF = S_OFF + SB * H * kWB;     // float2 [2][RCAP][kWB]
   static constexpr int EX_OFF = Y_OFF + 2 * RCAP * kWB;  // float2 [EXN]
   static constexpr int TW_OFF = EX_OFF + EXN;            // float2 [2H]: the two first-pass twiddle tables
   static constexpr int F2_END = TW_OFF + 2 * H;
   static constexpr int BYTES = F2_END * 8 + H * 4 + (kColNT / 32) * 8 + kFmeanCopy * 4 + 16;
-  static_assert(cdiv(kWB * B, kColNT) * A * kColNT <= 2 * H * kWB, "accumulator exchange must fit the S buffers");
+  static_assert(cdiv(kWB * B, kColNT) * A * kColNT <= SB * H * kWB, "accumulator exchange must fit the S buffers");
   static_assert(BYTES == iter_cols_bytes(H), "layout and byte count agree");
   static_assert(TW_OFF % 2 == 0, "twiddle rows start on 16-byte boundaries");
 };
 
 
-// CTAs per SM the launch bounds ask for.  A first factor A <= 16 keeps the
-// per-thread state (x at the pass-1 items, the accumulators, one pass-2 item)
-// within 168 registers at three CTAs per SM; longer first factors hold more
-// per thread, and their shared memory allows two CTAs per SM (one past 448),
-// which leaves each thread up to 255 registers.
+// CTAs per SM the launch bounds ask for.  With x and the accumulators in
+// tensor memory, as many as shared memory allows (at most three); otherwise a
+// first factor A <= 16 keeps the per-thread state (x at the pass-1 items, the
+// accumulators, one pass-2 item) within 168 registers at three CTAs per SM,
+// and longer first factors hold more per thread at the two CTAs per SM (one
+// past 448) their shared memory allows, with up to 255 registers a thread.
 constexpr int iter_cols_min_blocks(int H) {
-  return split_a(H) <= 16 ? 3 : (iter_cols_bytes(H) + 1024 <= 114 * 1024 ? 2 : 1);
+  return iter_cols_tmem(H) ? ((228 * 1024) / (iter_cols_bytes(H) + 1024) < 3 ? (228 * 1024) / (iter_cols_bytes(H) + 1024) : 3)
+         : split_a(H) <= 16 ? 3 : (iter_cols_bytes(H) + 1024 <= 114 * 1024 ? 2 : 1);
 }
 
 // Lengths that run the row-local iteration; the others (whose per-thread
@@ -172,6 +209,12 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   constexpr int N2 = kWB * A;  // forward pass-2 = inverse pass-1 items (w, k1), k1 < A: rows k1 + A*k2
   constexpr int N3 = kWB * B;  // inverse pass-2 items (w, k1'), k1' < B: rows k1' + B*k2
   constexpr int NI1 = cdiv(N1, kColNT), NI2 = cdiv(N2, kColNT), NI3 = cdiv(N3, kColNT);
+  // tensor memory: columns [0, 2A) x at the pass-1 item, [ACC0, ACC0 + 2A) the accumulators
+  constexpr bool TM = iter_cols_tmem(H);
+  constexpr int ACC0 = (2 * A + 15) / 16 * 16;
+  constexpr uint32_t TCOLS = (ACC0 + 2 * A <= 32) ? 32u : (ACC0 + 2 * A <= 64) ? 64u : 128u;
+  static_assert(!TM || (N1 == kColNT && N3 == kColNT && ACC0 + 2 * A <= 128), "one whole item per thread");
+  __shared__ uint32_t tslot;
   extern __shared__ float4 smem4[];
   float2* Sb = reinterpret_cast<float2*>(smem4) + L::S_OFF;
   float2* Yb = reinterpret_cast<float2*>(smem4) + L::Y_OFF;
@@ -202,7 +245,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   // are staged before the dependency wait
   auto issue_S = [&](int c, int buf) {
     const float2* src = a.S + size_t(c) * N + w0;
-    float2* dst = Sb + buf * H * kWB;
+    float2* dst = Sb + (L::SB == 2 ? buf : 0) * H * kWB;
     for (int q = t; q < H * (kWB / 2); q += kColNT) {
       const int row = q / (kWB / 2), part = q % (kWB / 2);
       cp_async16(dst + row * kWB + 2 * part, src + size_t(row) * W + 2 * part);
@@ -264,6 +307,17 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   const float2* __restrict__ x = xk + size_t(f) * N;
   const float inv_mu = 1.0f / st->mu;
 
+  uint32_t tl = 0;  // this thread's TMEM lane
+  if constexpr (TM) {
+    if (t < 32) {
+      tc::tmem_alloc(&tslot, TCOLS);
+      tc::tmem_relinquish();
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    tl = tslot + (uint32_t(32 * (t >> 5)) << 16);
+  }
   // x_k at this thread's forward pass-1 items, reused for every coil
   float2 xv[NI1][A];
 #pragma unroll
@@ -281,6 +335,21 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   for (int ii = 0; ii < NI3; ++ii)
 #pragma unroll
     for (int k2 = 0; k2 < A; ++k2) acc[ii][k2] = make_float2(0.f, 0.f);
+  if constexpr (TM) {  // x and the zeroed accumulators move to tensor memory for the coil loop
+    tmem_pieces<2 * A>([&](auto oc, auto nc) {
+      constexpr int o = decltype(oc)::value, n = decltype(nc)::value;
+      float xf[n], zf[n];
+#pragma unroll
+      for (int e = 0; e < n / 2; ++e) {
+        xf[2 * e] = xv[0][o / 2 + e].x;
+        xf[2 * e + 1] = xv[0][o / 2 + e].y;
+        zf[2 * e] = zf[2 * e + 1] = 0.f;
+      }
+      tmem_st_n<n>(tl + o, xf);
+      tmem_st_n<n>(tl + ACC0 + o, zf);
+    });
+    tc::tmem_wait_st();
+  }
   const float s_row = a.s_row;
   float racc = 0.f;
   // kept rows of each pass-2 item (w, k1): bit k2 for row k1 + A*k2
@@ -301,11 +370,11 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
     cp_async_wait<0>();
     __syncthreads();  // coil c staged; the previous coil's inverse pass 2 has read the exchange
     if (c + 1 < cend) {
-      issue_S(c + 1, buf ^ 1);
+      if constexpr (L::SB == 2) issue_S(c + 1, buf ^ 1);  // one buffer: copied once this coil's pass 2 read S
       issue_Y(c + 1, buf ^ 1);
     }
     cp_async_commit();
-    const float2* Sc = Sb + buf * H * kWB;
+    const float2* Sc = Sb + (L::SB == 2 ? buf : 0) * H * kWB;
     const float2* Yc = Yb + buf * RCAP * kWB;
     // forward pass 1: S_c x_f, DFT_A, twiddles
 #pragma unroll
@@ -314,8 +383,19 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
       if (i < N1) {
         const int w = i % kWB, s = i / kWB;
         float2 v[A];
+        if constexpr (TM) {
+          tmem_pieces<2 * A>([&](auto oc, auto nc) {
+            constexpr int o = decltype(oc)::value, n = decltype(nc)::value;
+            float xf[n];
+            tmem_ld_n<n>(tl + o, xf);
 #pragma unroll
-        for (int n1 = 0; n1 < A; ++n1) v[n1] = cmul(xv[ii][n1], Sc[(B * n1 + s) * kWB + w]);
+            for (int e = 0; e < n / 2; ++e)
+              v[o / 2 + e] = cmul(make_float2(xf[2 * e], xf[2 * e + 1]), Sc[(B * (o / 2 + e) + s) * kWB + w]);
+          });
+        } else {
+#pragma unroll
+          for (int n1 = 0; n1 < A; ++n1) v[n1] = cmul(xv[ii][n1], Sc[(B * n1 + s) * kWB + w]);
+        }
         dft<A>(v);
 #pragma unroll
         for (int k1 = 0; k1 < A; ++k1) ex[k1 * KSF + s * kWB + w] = (k1 == 0) ? v[k1] : cmul(v[k1], twiddle<A>(tws + s * A, k1));
@@ -370,15 +450,55 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
 #pragma unroll
         for (int s = 0; s < A; ++s) v[s] = ex[k1p * KSI + s * kWB + w];
         dft<A>(v);
-#pragma unroll
-        for (int k2 = 0; k2 < A; ++k2) {
-          // conj(v) * conj(S) == conj(v * S), formed as cmul's negated imaginary part
+        // conj(v) * conj(S) == conj(v * S), formed as cmul's negated imaginary part
+        auto term = [&](int k2) {
           const float2 sv = Sc[(k1p + B * k2) * kWB + w];
-          const float2 p = make_float2(fmaf(v[k2].x, sv.x, -v[k2].y * sv.y), fmaf(-v[k2].x, sv.y, -(v[k2].y * sv.x)));
-          acc[ii][k2] = padd(acc[ii][k2], p);
+          return make_float2(fmaf(v[k2].x, sv.x, -v[k2].y * sv.y), fmaf(-v[k2].x, sv.y, -(v[k2].y * sv.x)));
+        };
+        if constexpr (TM) {
+          tc::tmem_wait_st();  // the previous coil's accumulator stores
+          tmem_pieces<2 * A>([&](auto oc, auto nc) {
+            constexpr int o = decltype(oc)::value, n = decltype(nc)::value;
+            float af[n];
+            tmem_ld_n<n>(tl + ACC0 + o, af);
+#pragma unroll
+            for (int e = 0; e < n / 2; ++e) {
+              const float2 sum = padd(make_float2(af[2 * e], af[2 * e + 1]), term(o / 2 + e));
+              af[2 * e] = sum.x;
+              af[2 * e + 1] = sum.y;
+            }
+            tmem_st_n<n>(tl + ACC0 + o, af);
+          });
+        } else {
+#pragma unroll
+          for (int k2 = 0; k2 < A; ++k2) acc[ii][k2] = padd(acc[ii][k2], term(k2));
         }
       }
     }
+    if constexpr (L::SB == 1) {  // one S buffer: the next coil's copy starts once every thread has read this one
+      if (c + 1 < cend) {
+        __syncthreads();
+        issue_S(c + 1, 0);
+        cp_async_commit();
+      }
+    }
+  }
+  if constexpr (TM) {  // x and the accumulators back to registers; the tensor memory is released
+    tc::tmem_wait_st();
+    tmem_pieces<2 * A>([&](auto oc, auto nc) {
+      constexpr int o = decltype(oc)::value, n = decltype(nc)::value;
+      float xf[n], af[n];
+      tmem_ld_n<n>(tl + o, xf);
+      tmem_ld_n<n>(tl + ACC0 + o, af);
+#pragma unroll
+      for (int e = 0; e < n / 2; ++e) {
+        xv[0][o / 2 + e] = make_float2(xf[2 * e], xf[2 * e + 1]);
+        acc[0][o / 2 + e] = make_float2(af[2 * e], af[2 * e + 1]);
+      }
+    });
+    tc::fence_before_sync();
+    __syncthreads();
+    if (t < 32) tc::tmem_dealloc(tslot, TCOLS);
   }
 
   // tTV objective partial sums over the tile (first half only; not in fixup mode)
