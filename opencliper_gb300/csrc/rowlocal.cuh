@@ -197,7 +197,8 @@ constexpr int iter_cols_min_blocks(int H) {
 // Lengths that run the row-local iteration; the others (whose per-thread
 // state would spill) run the three-pass iteration.
 constexpr bool iter_cols_ok(int H) {
-  return split_a(H) != 0 && (split_a(H) <= 16 || (split_b(H) >= 8 && split_b(H) <= 16 && split_a(H) <= 24));
+  return split_a(H) != 0 && (split_a(H) <= 16 || (split_b(H) >= 8 && split_b(H) <= 16 && split_a(H) <= 24) ||
+                             (iter_cols_tmem(H) && split_a(H) <= 32));
 }
 
 template <int H>

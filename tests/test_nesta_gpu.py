@@ -98,9 +98,11 @@ def test_nesta_general_mask_and_data_outside_mask(ctx):
 @pytest.mark.parametrize("W,H,F,C,Rr,prm", [
     (64, 64, 8, 4, 6, {**FIXED, "maxIter": 20}),
     (128, 96, 10, 8, 8, {**FIXED, "maxIter": 20}),
-    (64, 384, 4, 5, 8, {**FIXED, "maxIter": 20}),   # first factor 24: two CTAs per SM
+    (64, 384, 4, 5, 8, {**FIXED, "maxIter": 20}),   # 24 x 16: x and accumulators in tensor memory
     (40, 320, 3, 4, 8, {**FIXED, "maxIter": 20}),   # first factor 20
     (48, 168, 4, 3, 6, {**FIXED, "maxIter": 20}),   # 21 x 8
+    (32, 448, 3, 3, 8, {**FIXED, "maxIter": 20}),   # 28 x 16: x and accumulators in tensor memory
+    (24, 512, 2, 3, 8, {**FIXED, "maxIter": 20}),   # 32 x 16
     (48, 48, 6, 3, 4, dict(lambda_i=1e-2, mu_f=3e-4, La=1.0, maxIntIter=4, maxIter=100, stoptest=1, miniter=7,
                            tolVar=3e-4)),
     (32, 32, 4, 2, 4, dict(lambda_i=1e-2, mu_f=3e-4, La=1.0, maxIntIter=3, maxIter=100, stoptest=1, miniter=4,
