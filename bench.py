@@ -170,6 +170,25 @@ def algorithmic_bytes(kind: str, G: int, shape: tuple | None = None) -> int:
     raise KeyError(kind)
 
 
+def iteration_bytes(path: str, G: int, shape: tuple) -> int:
+    """Algorithmic bytes of one inner iteration of a (W, H, F, C) problem with G
+    kept rows on the given path of gbn_batch_group_info."""
+    if path.startswith("row_local"):
+        return algorithmic_bytes("iter", G, shape)
+    return sum(algorithmic_bytes(k, G, shape) for k in ("fwd_cols", "rows", "inv_cols"))
+
+
+def batch_paths(b) -> list:
+    """The inner-iteration path of every member of a batch."""
+    ng, _ = b.groups()
+    out: dict = {}
+    for gi in range(ng):
+        info = b.group_info(gi)
+        for i in info["members"]:
+            out[i] = info["path"]
+    return [out[i] for i in range(len(out))]
+
+
 def dense_iteration_bytes() -> int:
     """Bytes one inner iteration of the reference's algorithm moves at the headline
     workload: y, S once, x_k, x_ref, w_k read, x_{k+1}, w_{k+1} written, the pixel mask."""
@@ -381,9 +400,6 @@ def run_ours(args, dist: Dist) -> dict | None:
     if forms:
         out["forms"] = forms
     return out
-
-
-BATCH_WL = dict(n=64, sizes=(128, 192, 256, 320, 384), frames=(12, 40), coils=(8, 32), accel=(4, 12), seed0=1000)
 
 
 def _graph_rate(ctx, stream, batch, n: int, reps: int) -> tuple[float, float]:
@@ -628,8 +644,10 @@ def batched_form(ctx, stream, args=None, reps: int = 2) -> dict:
         n0 = ctx.launch_count()
         ng, ntc = b.groups()
         rate, ms = _graph_rate(ctx, stream, b, B["n"], reps)
+        paths = batch_paths(b)
         res[name] = {"value": round(rate, 3), "ms_per_batch": round(ms, 2), "reps": reps,
                      "groups": ng, "tensor_core_forward_groups": ntc,
+                     "members_by_path": {k: paths.count(k) for k in sorted(set(paths))},
                      "kept_rows_total": int(sum(b.stats(i)["kept_rows"] for i in range(B["n"]))),
                      "status_nonzero": int(sum(b.stats(i)["status"] != 0 for i in range(B["n"]))),
                      "host_launch_calls_per_replay": int((ctx.launch_count() - n0) // (reps + 1))}
@@ -733,6 +751,7 @@ def stress_form(ctx, stream, args=None) -> dict:
         res["device_full"] = oom
     ref = []
     for name, prec in (("fp32", g.PRECISION_FP32), ("mixed", g.PRECISION_MIXED)):
+        ctx.seed48((0x330E, 0xABCD, 0x1234))  # both precisions replay the same drand48 sequence
         try:
             b = g.Batch(ctx, probs, g.nesta_params(**NESTA), outs, precision=prec)
         except g.GbnError as e:
@@ -740,12 +759,13 @@ def stress_form(ctx, stream, args=None) -> dict:
             continue
         free1, _ = torch.cuda.mem_get_info()
         rate, ms = _graph_rate(ctx, stream, b, len(probs), 1)
+        paths = batch_paths(b)
         G = [int(b.stats(i)["kept_rows"]) for i in range(len(probs))]
-        alg = sum((algorithmic_bytes("fwd_cols", Gi, sh) + algorithmic_bytes("rows", Gi, sh) +
-                   algorithmic_bytes("inv_cols", Gi, sh)) for Gi, sh in zip(G, shapes)) * NESTA["maxIter"]
+        alg = sum(iteration_bytes(paths[i], Gi, sh) for i, (Gi, sh) in enumerate(zip(G, shapes))) * NESTA["maxIter"]
         res[name] = {"value": round(rate, 3), "ms_per_batch": round(ms, 1),
                      "hbm_used_gb": round((total - free1) / 1e9, 1),
                      "algorithmic_gbs": round(alg / (ms / 1e3) / 1e9, 1),
+                     "members_by_path": {k: paths.count(k) for k in sorted(set(paths))},
                      "status_nonzero": int(sum(b.stats(i)["status"] != 0 for i in range(len(probs))))}
         dev = torch.device("cuda", ctx.device)
         imgs = [torch.as_tensor(synth._CudaView(o, "<f4", o.shape + (2,)), device=dev) for o in outs]

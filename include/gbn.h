@@ -368,6 +368,15 @@ GBN_API int gbn_batch_stats(gbn_batch* b, int i, gbn_nesta_stats* stats);
 /* The batch's (W, H) groups of at most 64 members, and how many of them run
  * the forward column pass on the tensor cores (mixed form, "mixed_fwd_tc"). */
 GBN_API int gbn_batch_groups(gbn_batch* b, int* groups, int* tensor_core_groups);
+/* Group g (0 <= g < groups) of a batch: its W, H, member count, the members'
+ * batch indices (member_idx: room for 64, or NULL) and the inner iteration it
+ * runs (path: one of GBN_PATH_*).  No reference counterpart (batches are the
+ * the benchmark spec's form). */
+#define GBN_PATH_THREE_PASS 0       /* forward column, row and adjoint column passes, FP32 */
+#define GBN_PATH_THREE_PASS_TC 1    /* the same with the forward column pass on the tensor cores */
+#define GBN_PATH_ROW_LOCAL 2        /* one fused kernel per iteration (row masks), FP32 */
+#define GBN_PATH_ROW_LOCAL_TC 3     /* the row-local iteration on the tensor cores */
+GBN_API int gbn_batch_group_info(gbn_batch* b, int g, int* W, int* H, int* members, int* member_idx, int* path);
 GBN_API int gbn_batch_destroy(gbn_batch* b);
 /* create + launch (+ stats for every problem when stats != NULL, which waits)
  * + destroy */

@@ -132,6 +132,7 @@ SIGNATURES: dict[str, list] = {
     "gbn_batch_capture": [_vp],
     "gbn_batch_stats": [_vp, _i, C.POINTER(NestaStats)],
     "gbn_batch_groups": [_vp, _vp, _vp],
+    "gbn_batch_group_info": [_vp, _i, _vp, _vp, _vp, _vp, _vp],
     "gbn_batch_destroy": [_vp],
     "gbn_batch_run": [_vp, _i, C.POINTER(_vp), C.POINTER(NestaParams), C.POINTER(_vp), _i, C.POINTER(NestaStats)],
     "gbn_graph_capture": [_vp],

@@ -392,6 +392,16 @@ class Batch:
         call("gbn_batch_groups", self.handle, C.byref(ng), C.byref(ntc))
         return ng.value, ntc.value
 
+    PATHS = {0: "three_pass", 1: "three_pass_tc", 2: "row_local", 3: "row_local_tc"}
+
+    def group_info(self, g: int) -> dict:
+        """W, H, member indices and the inner iteration ("three_pass",
+        "three_pass_tc", "row_local", "row_local_tc") of group g."""
+        W, H, n, path = C.c_int(0), C.c_int(0), C.c_int(0), C.c_int(0)
+        idx = (C.c_int * 64)()
+        call("gbn_batch_group_info", self.handle, int(g), C.byref(W), C.byref(H), C.byref(n), idx, C.byref(path))
+        return {"W": W.value, "H": H.value, "members": list(idx[:n.value]), "path": self.PATHS[path.value]}
+
     def stats(self, i: int) -> dict:
         st = NestaStats()
         call("gbn_batch_stats", self.handle, int(i), C.byref(st))

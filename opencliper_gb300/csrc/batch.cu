@@ -440,6 +440,23 @@ int batch_groups(gbn_batch* b, int* groups, int* tensor_core_groups) {
   return GBN_OK;
 }
 
+int batch_group_info(gbn_batch* b, int g, int* W, int* H, int* members, int* member_idx, int* path) {
+  if (!b) return set_error(GBN_ERR_INVALID, "null batch");
+  if (g < 0 || g >= int(b->groups.size())) return set_error(GBN_ERR_INVALID, "group index out of range");
+  const auto& G = b->groups[size_t(g)];
+  if (W) *W = G.W;
+  if (H) *H = G.H;
+  if (members) *members = int(G.idx.size());
+  if (member_idx)
+    for (size_t k = 0; k < G.idx.size(); ++k) member_idx[k] = G.idx[k];
+  if (path)
+    *path = G.row_local_tc ? GBN_PATH_ROW_LOCAL_TC
+            : G.row_local  ? GBN_PATH_ROW_LOCAL
+            : G.tc         ? GBN_PATH_THREE_PASS_TC
+                           : GBN_PATH_THREE_PASS;
+  return GBN_OK;
+}
+
 int batch_destroy(gbn_batch* b) {
   if (!b) return GBN_OK;
   cudaStreamSynchronize(b->ctx->stream);  // work of this batch may still be queued

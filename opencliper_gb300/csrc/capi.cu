@@ -33,6 +33,7 @@ int batch_stats(gbn_batch*, int, gbn_nesta_stats*);
 int batch_destroy(gbn_batch*);
 gbn_ctx* batch_ctx(gbn_batch*);
 int batch_groups(gbn_batch*, int*, int*);
+int batch_group_info(gbn_batch*, int, int*, int*, int*, int*, int*);
 int motion_set(gbn_problem*, const float*, const int*, const int*);
 int problem_fit_rows(gbn_problem*, int, int*);
 int motion_op(gbn_ctx*, int, const float2*, float2*, const float*, const int*, const int*, int, int, int);
@@ -729,6 +730,11 @@ int gbn_batch_capture(gbn_batch* b) {
 int gbn_batch_groups(gbn_batch* b, int* groups, int* tensor_core_groups) {
   CHECK_BATCH(b);
   return batch_groups(b, groups, tensor_core_groups);
+}
+
+int gbn_batch_group_info(gbn_batch* b, int g, int* W, int* H, int* members, int* member_idx, int* path) {
+  CHECK_BATCH(b);
+  return batch_group_info(b, g, W, H, members, member_idx, path);
 }
 
 int gbn_batch_stats(gbn_batch* b, int i, gbn_nesta_stats* stats) {

@@ -45,14 +45,18 @@ namespace gbn {
 
 constexpr int kStatusRowStructure = 7;  // NestaDevState::status: a kept row is partly sampled (row-local path)
 
-// Counts this CTA as finished for instance `inst` (after its partial sums are
-// stored) and tells every thread whether it was the instance's last of
-// `total` CTAs.  All threads call it.
+// Counts this CTA as finished for instance `inst` (after thread 0 stored its
+// partial sums) and tells every thread whether it was the instance's last of
+// `total` CTAs.  All threads call it.  Only thread 0's stores need to be
+// visible before the count (the other threads' image stores are read by the
+// next launch), so only thread 0 fences.
 __device__ __forceinline__ bool rowlocal_last_cta(ClassCtl* ctl, int inst, unsigned total) {
   __shared__ int s_fin;
-  __threadfence();
   __syncthreads();
-  if (threadIdx.x == 0) s_fin = (atomicAdd(&ctl->done[inst], 1u) + 1u == total) ? 1 : 0;
+  if (threadIdx.x == 0) {
+    __threadfence();
+    s_fin = (atomicAdd(&ctl->done[inst], 1u) + 1u == total) ? 1 : 0;
+  }
   __syncthreads();
   return s_fin != 0;
 }
@@ -159,8 +163,8 @@ constexpr int iter_cols_sbufs(int L) { return iter_cols_tmem(L) ? 1 : 2; }
 constexpr int iter_cols_bytes(int L) {
   const int a = split_a(L), b = split_b(L);
   const int ex = (a * col_ks(b) > b * col_ks(a)) ? a * col_ks(b) : b * col_ks(a);
-  return (iter_cols_sbufs(L) * L * kWB + 2 * iter_cols_rcap(L) * kWB + ex + 2 * L) * 8 + L * 4 + (kColNT / 32) * 8 +
-         kFmeanCopy * 4 + 16;
+  return (iter_cols_sbufs(L) * L * kWB + 2 * iter_cols_rcap(L) * kWB + ex + b * (a + 2) + a * (b + 2)) * 8 + L * 4 +
+         (kColNT / 32) * 8 + kFmeanCopy * 4 + 16;
 }
 
 template <int H>
@@ -174,8 +178,13 @@ struct IterColsSmem {
   static constexpr int S_OFF = 0;                        // float2 [SB][H][kWB]
   static constexpr int Y_OFF = S_OFF + SB * H * kWB;     // float2 [2][RCAP][kWB]
   static constexpr int EX_OFF = Y_OFF + 2 * RCAP * kWB;  // float2 [EXN]
-  static constexpr int TW_OFF = EX_OFF + EXN;            // float2 [2H]: the two first-pass twiddle tables
-  static constexpr int F2_END = TW_OFF + 2 * H;
+  // twiddles: B rows of A (forward first pass, one row per item s) and A rows
+  // of B (inverse first pass, one per item k1), each row padded by one 16-byte
+  // pair so that the rows a warp reads at once sit in different banks
+  static constexpr int TWF = A + 2, TWI = B + 2;
+  static constexpr int TW_OFF = EX_OFF + EXN;
+  static constexpr int TWI_OFF = B * TWF;                // inverse rows, from TW_OFF
+  static constexpr int F2_END = TW_OFF + TWI_OFF + A * TWI;
   static constexpr int BYTES = F2_END * 8 + H * 4 + (kColNT / 32) * 8 + kFmeanCopy * 4 + 16;
   static_assert(cdiv(kWB * B, kColNT) * A * kColNT <= SB * H * kWB, "accumulator exchange must fit the S buffers");
   static_assert(BYTES == iter_cols_bytes(H), "layout and byte count agree");
@@ -274,12 +283,17 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
     rcode[i] = (j < 0) ? -1 : (a.row_full[rowbase + j] ? j : -2 - j);
   }
   // twiddles, stored per item so that a thread reads its own as consecutive
-  // pairs: [s*A + k1] = w_H^(s*k1) (forward first pass, item s) and
-  // [H + k1*B + k1'] = w_H^(k1*k1') (inverse first pass, item k1); the global
-  // table holds them as [k1*B + s] and [H + k1'*A + k1]
-  for (int i = t; i < 2 * H; i += kColNT) {
-    const int d = i < H ? (i % B) * A + i / B : H + ((i - H) % A) * B + (i - H) / A;
-    tws[d] = __ldg(a.twH + i);
+  // pairs: row s, entry k1 = w_H^(s*k1) (forward first pass) and row k1,
+  // entry k1' = w_H^(k1*k1') (inverse first pass); the global table holds them
+  // as [k1*B + s] and [H + k1'*A + k1]
+  for (int d = t; d < L::TWI_OFF + A * L::TWI; d += kColNT) {
+    if (d < L::TWI_OFF) {
+      const int s = d / L::TWF, k1 = d % L::TWF;
+      if (k1 < A) tws[d] = __ldg(a.twH + k1 * B + s);
+    } else {
+      const int k1 = (d - L::TWI_OFF) / L::TWI, k1p = (d - L::TWI_OFF) % L::TWI;
+      if (k1p < B) tws[d] = __ldg(a.twH + H + k1p * A + k1);
+    }
   }
   grid_dep_wait();  // x_k, w_k and the scalar state come from the previous iteration
   grid_dep_release();
@@ -399,7 +413,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
         }
         dft<A>(v);
 #pragma unroll
-        for (int k1 = 0; k1 < A; ++k1) ex[k1 * KSF + s * kWB + w] = (k1 == 0) ? v[k1] : cmul(v[k1], twiddle<A>(tws + s * A, k1));
+        for (int k1 = 0; k1 < A; ++k1) ex[k1 * KSF + s * kWB + w] = (k1 == 0) ? v[k1] : cmul(v[k1], twiddle<A>(tws + s * L::TWF, k1));
       }
     }
     __syncthreads();
@@ -437,7 +451,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
         dft<B>(r[ii]);
 #pragma unroll
         for (int k1p = 0; k1p < B; ++k1p)
-          ex[k1p * KSI + k1 * kWB + w] = (k1p == 0) ? r[ii][k1p] : cmul(r[ii][k1p], twiddle<B>(tws + H + k1 * B, k1p));
+          ex[k1p * KSI + k1 * kWB + w] = (k1p == 0) ? r[ii][k1p] : cmul(r[ii][k1p], twiddle<B>(tws + L::TWI_OFF + k1 * L::TWI, k1p));
       }
     }
     __syncthreads();

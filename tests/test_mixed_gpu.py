@@ -114,14 +114,18 @@ def test_mixed_forward_choice_per_group(ctx, W, H, F, C, Rr):
     prob = g.Problem(ctx, dy, dS, dm)
     x = ctx.empty((F, H, W), np.complex64)
     prm = g.nesta_params(**FIXED)
-    imgs = []
+    imgs, paths = [], []
     for prec, tc in ((g.PRECISION_FP32, 1), (g.PRECISION_MIXED, 0), (g.PRECISION_MIXED, -1), (g.PRECISION_MIXED, 1)):
         ctx.set_tuning("mixed_fwd_tc", tc)
         ctx.seed48(drand48.state_to_seed16v(drand48.DEFAULT_STATE))
         b = g.Batch(ctx, [prob], prm, [x], precision=prec)
         b.launch()
         imgs.append(x.get())
+        info = b.group_info(0)
+        assert (info["W"], info["H"], info["members"]) == (W, H, [0])
+        paths.append(info["path"])
         b.close()
+    assert paths == ["row_local", "row_local", "row_local", "row_local_tc"]
     prob.close()
     assert np.array_equal(imgs[0], imgs[1]) and np.array_equal(imgs[0], imgs[2])
     assert not np.array_equal(imgs[0], imgs[3])  # the tensor-core transforms round differently
@@ -142,6 +146,9 @@ def test_mixed_partly_sampled_rows_three_pass(ctx):
     b = g.Batch(ctx, [prob], g.nesta_params(**FIXED), [x], precision=g.PRECISION_MIXED)
     b.launch()
     got, st = x.get(), b.stats(0)
+    assert b.group_info(0)["path"] == "three_pass_tc"
+    with pytest.raises(g.GbnError):
+        b.group_info(1)
     b.close()
     prob.close()
     r64 = R.nesta(p.y, p.S, p.mask, R.NestaParams(**FIXED), "f64", rand_state=s0)
