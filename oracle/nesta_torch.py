@@ -63,14 +63,19 @@ def _normest(F: int, H: int, W: int, rand_state: int, dev, cdt=None):
 
 
 def nesta_f64(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams,
-              rand_state: int = drand48.DEFAULT_STATE, device: str = "cpu", fp32: bool = False) -> tuple[np.ndarray, dict]:
+              rand_state: int = drand48.DEFAULT_STATE, device: str = "cpu", fp32: bool = False,
+              fp64_state: tuple = ()) -> tuple[np.ndarray, dict]:
     """FP64 NESTA of y [F][C][H][W], S [C][H][W], pixel mask [F][H][W]; returns
     (image [F][H][W], stats).  Inputs may be numpy arrays or torch tensors (a
     tensor already on `device` is used in place).  fp32=True runs the same
-    statements on complex64 arrays."""
+    statements on complex64 arrays; with it, fp64_state may name iteration
+    state kept in complex128 all the same: "w" (the weighted gradient sum of
+    NestaUp.cpp:837-840) and "x" (x_k, y_k, z_k and x_ref)."""
     import torch
     dev = torch.device(device)
     cdt = torch.complex64 if fp32 else torch.complex128
+    wdt = torch.complex128 if "w" in fp64_state else cdt
+    xdt = torch.complex128 if "x" in fp64_state else cdt
 
     def T(a, dt):
         t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(a))
@@ -110,10 +115,11 @@ def nesta_f64(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams,
     inv_sqrtN = 1.0 / np.sqrt(float(N))
     fx = qp = 0.0
     iters = 0
+    xref = xref.to(xdt)
     for nl in range(1, prm.maxIntIter + 1):
         mu *= gamma
         tolVar *= gammat
-        w = torch.zeros_like(xref)
+        w = torch.zeros(xref.shape, dtype=wdt, device=dev)
         xk = xref.clone()
         Lmu = normU / mu
         if miniter > 0:
@@ -123,15 +129,16 @@ def nesta_f64(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams,
         qpDone = False
         k = 0
         while k < prm.maxIter:
-            d = _ttv(xk, True)                                   # operatorU (669)
+            xc = xk.to(cdt)
+            d = _ttv(xc, True)                                   # operatorU (669)
             u = d / torch.clamp(d.abs(), min=mu)                 # VectorNormalization (680-683)
             normUk = np.sqrt(_nrm2sq(u))                         # Scnrm2 (686)
             fxdot = float((u.conj() * d).real.sum())             # Cdotc real part (691)
             Df = -_ttv(u, False)                                 # operatorUt + Cscal(-1) (696-704)
-            res = A(xk) * inv_sqrtN - y                          # (710-727)
+            res = A(xc) * inv_sqrtN - y                          # (710-727)
             l2 = _nrm2sq(res)                                    # (738-746)
             Df = Df * lam + At(res * sqrtN)                      # (749-772)
-            yk = xk - Lmu1 * Df                                  # (777-786)
+            yk = xk - Lmu1 * Df.to(xdt)                          # (777-786)
             l1term = fxdot - mu / 2.0 * normUk ** 2              # (797-798)
             fx = 0.5 * l2 + lam * l1term
             if prm.stoptest == 1:                                # (799-824)
@@ -150,12 +157,12 @@ def nesta_f64(y: np.ndarray, S: np.ndarray, mask: np.ndarray, prm: NestaParams,
                     fmean[(miniter - 1) - ((k + 1) % miniter)] = fx
             apk = 0.5 * (k + 1.0)                                # (829-831)
             tauk = 2.0 / (k + 3.0)
-            w = w + apk * Df                                     # (837-840)
-            zk = xref - Lmu1 * w                                 # (843-852)
+            w = w + apk * Df.to(wdt)                             # (837-840)
+            zk = xref - (Lmu1 * w).to(xdt)                       # (843-852)
             xk = tauk * zk + (1.0 - tauk) * yk                   # (858-875)
             iters += 1
             k += 1
         xref = xk                                                # (889)
     stats = dict(normU=normU, normest_iters=ne_iters, maxX=maxX, maxUX=maxUX, lambda_=lam, muf=muf, mu0=mu0,
                  mu_final=mu, tolVar_final=tolVar, fx_final=fx, qp_final=qp, inner_iters=iters, rand_state=new_state)
-    return xref.cpu().numpy(), stats
+    return xref.to(cdt).cpu().numpy(), stats

@@ -13,7 +13,10 @@ arrays).  The rounding schemes:
 
 A scheme whose error stays under the gate with room beside the FP32 floor
 could store that operand in 16 bits; each solve runs the FP64 restatement
-oracle/nesta_torch.py (torch; a CUDA device when available).
+oracle/nesta_torch.py (torch; a CUDA device when available).  A second table
+keeps iteration state in FP64 inside the FP32 solve (the weighted gradient
+sum w, the iterate x, both): if the FP32 floor came from accumulating w or x
+it would drop there.
 
     python tests/precision_study.py [--size 256,256,20,12,8] [--iters 100] [--device cuda]
 """
@@ -79,6 +82,10 @@ def main(argv=None) -> int:
             S = _round16(p.S, kind, axes)
         x, _ = RT.nesta_f64(y, S, p.mask, prm, device=dev)
         print(f"| {name} | {R.nrmse(x, ref):.2e} |")
+    print("\n| FP32 solve with FP64 state | NRMSE vs FP64 |\n|---|---|")
+    for state in ((), ("w",), ("x",), ("w", "x")):
+        x, _ = RT.nesta_f64(p.y, p.S, p.mask, prm, device=dev, fp32=True, fp64_state=state)
+        print(f"| {', '.join(state) or 'none'} | {R.nrmse(x, ref):.2e} |")
     return 0
 
 
