@@ -21,12 +21,15 @@
 // the reference's atomic scatter depends on the order of its atomics.
 //
 // Per inner iteration: k_mc_tv (M x_k for three frames on the fly, D, the
-// Huber normalisation, g = D^T u and the objective's partial sums), the fused
-// forward column and row passes as in the plain form (the forward pass skips
-// its tTV sums), k_mc_adjoint (M^T g), and the adjoint column pass, which
-// takes M^T g as its tTV gradient.  k_mc_tv and k_mc_adjoint run on a side
-// stream beside the forward column pass; events order them after the
-// previous iterate and before the row and adjoint column passes.  The power method ||U|| cannot use the plain form's per-pixel
+// Huber normalisation, g = D^T u and the objective's partial sums),
+// k_mc_adjoint (M^T g), and the data term with the update.  For row masks the
+// last is the one-kernel row-local iteration (rowlocal.cuh), launched after
+// the two on one stream: its coil loop overlaps them and its update waits for
+// M^T g, its tTV gradient.  Otherwise it is the fused forward column and row
+// passes as in the plain form (the forward pass skips its tTV sums) and the
+// adjoint column pass, which takes M^T g; k_mc_tv and k_mc_adjoint then run on
+// a side stream beside the forward column pass, events ordering them after
+// the previous iterate and before the row and adjoint column passes.  The power method ||U|| cannot use the plain form's per-pixel
 // recurrence (M mixes pixels), so it runs myNormest's loop step for step on
 // the device (k_ne_*), the host reading the stop flag once per eight steps.
 //
@@ -394,9 +397,13 @@ __global__ void __launch_bounds__(kNT) k_mc_adjoint(const float2* __restrict__ g
 // the objective's partial sums of |u|^2 and Re<u, d> per (frame, block of 256
 // pixels).  grid (ceil(H*W/256), ceil(F/kTvFrames)); each thread warps its
 // pixel for kTvFrames+2 consecutive frames (periodic in f) and slides over them.
-__global__ void __launch_bounds__(kNT) k_mc_tv(const float2* __restrict__ x, const float* __restrict__ xn,
-                                                const int* __restrict__ inv, McRect r, const NestaDevState* __restrict__ st,
-                                                float2* __restrict__ g, double* __restrict__ part, int W, int H, int F,
+// Inner iteration `it` reads x_it from the ping-pong pair (x0, x1); past the
+// outer loop's last iteration it does nothing, except in the launch that
+// recomputes the last update (row-local iteration, fixup), which reads x_last.
+__global__ void __launch_bounds__(kNT) k_mc_tv(const float2* __restrict__ x0, const float2* __restrict__ x1, int it,
+                                                const float* __restrict__ xn, const int* __restrict__ inv, McRect r,
+                                                const NestaDevState* __restrict__ st, float2* __restrict__ g,
+                                                double* __restrict__ part, int W, int H, int F,
                                                 int* __restrict__ status) {
   __shared__ double sred[2 * kTvFrames][kNT / 32];
   const int HW = H * W;
@@ -404,8 +411,15 @@ __global__ void __launch_bounds__(kNT) k_mc_tv(const float2* __restrict__ x, con
   const bool live = p < HW;
   const int e = live ? __ldg(inv + p) : -1;
   const int f0 = blockIdx.y * kTvFrames, f1 = min(F, f0 + kTvFrames);
-  grid_dep_wait();  // x_k comes from the previous adjoint column pass
+  grid_dep_wait();  // x_k comes from the previous iteration's update
   grid_dep_release();
+  const int last = st->last_iter;
+  int itx = it;
+  if (it > last) {  // uniform over the grid
+    if (!(st->fixup && it == last + 1)) return;
+    itx = last;
+  }
+  const float2* __restrict__ x = (itx & 1) ? x1 : x0;
   const float inv_mu = 1.0f / st->mu;
   float su2[kTvFrames], sud[kTvFrames];
 #pragma unroll
@@ -949,10 +963,25 @@ int nesta_run_mc(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, floa
   const FusedArgs* tab = P->d_args;
   const BatchMap bm = single_map(F, P->ctl);
   int rc;
+  // the row-local iteration (rowlocal.cuh) takes problems whose kept rows are
+  // fully sampled or unsampled; the row analysis's verdict comes back to
+  // pinned host memory while the setup is queued
+  const bool check_rows = ctx->row_local && kh->iter_cols;
+  if (check_rows && (rc = partial_flag_ready(ctx)) != GBN_OK) return rc;
   ctx->launches += launch_pre(P, *prm, s);
+  cudaError_t ef = cudaSuccess;
+  if (check_rows) {
+    ef = cudaMemcpyAsync(ctx->host_partial, &P->st->partial_rows, sizeof(int), cudaMemcpyDeviceToHost, s);
+    if (ef == cudaSuccess) ef = cudaEventRecord(ctx->ev_partial, s);
+    if (ef != cudaSuccess) return cuda_status(ef, "row structure read-back");
+  }
   if ((rc = tables_build(ctx, t, P->mc_xn, P->mc_xmesh, r, W, H, F, &P->st->status, s)) != GBN_OK) return rc;
   ctx->launches += launch_store_args(P->d_args, a, s);
   ctx->launches += launch_group_init(tab, 1, kw->rows_per_cta, P->ctl, s);
+  if (check_rows) {  // T = IDFT_W(y) of the kept rows, the row-local iteration's data term
+    kw->rows(tab, bm, 0, false, row_grid(ctx, kw, false, steps, k2), s);
+    ctx->launches += 1;
+  }
   // maxima of x0 and of U x0 = tTV(M x0) (NestaUp.cpp:491, 521-568)
   mc_apply(ctx, P, x_out, P->mc_xw, s);
   ctx->launches += launch_maxima(ctx, P, x_out, P->mc_xw, s);
@@ -969,14 +998,42 @@ int nesta_run_mc(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, floa
     if (se == cudaSuccess) se = cudaEventCreateWithFlags(&ctx->ev_mc_adj, cudaEventDisableTiming);
     if (se != cudaSuccess) return cuda_status(se, "motion-compensated side stream");
   }
+  bool row_local = false;
+  if (check_rows) {
+    if ((ef = cudaEventSynchronize(ctx->ev_partial)) != cudaSuccess) return cuda_status(ef, "row structure read-back");
+    row_local = *ctx->host_partial == 0;
+  }
+  if (row_local) {
+    // per inner iteration, on one stream with programmatic dependent launch:
+    // k_mc_tv (M x_k, D, normalisation, tTVadj, objective sums), M^T g, and the
+    // one-kernel iteration, whose coil loop overlaps the two and whose update
+    // waits for M^T g; one more launch per outer loop recomputes the last
+    // update if the stopping rule ends the loop
+    const unsigned n_iter_launch = prm->maxIter + (prm->stoptest == 1 ? 1u : 0u);
+    for (unsigned nl = 1; nl <= prm->maxIntIter; ++nl) {
+      ctx->launches += launch_outer_begin(ctx, P, int(nl), x_out, s);
+      for (unsigned it = 0; it < n_iter_launch; ++it) {
+        launch_pdl(k_mc_tv, gtv, kNT, 0, s, (const float2*)P->xk0, (const float2*)P->xk1, int(it),
+                   (const float*)P->mc_xn, (const int*)t->inv, r, (const NestaDevState*)P->st, P->mc_g, t->tvpart, W,
+                   H, F, &P->st->status);
+        launch_pdl(k_mc_adjoint, dim3(gadj), kNT, 0, s, (const float2*)P->mc_g, P->mc_gm, (const int*)t->off,
+                   (const int*)t->csrc, (const float2*)t->cw, r, W, H, F, 1);
+        GBN_LAUNCH(ctx, GBN_PROF_ITER, 1, kh->iter_cols(tab, bm, int(it), g3, s));
+        ctx->launches += 2;
+      }
+      ctx->launches += launch_outer_end(ctx, P, x_out, s);
+    }
+    const cudaError_t e = cudaGetLastError();
+    return e == cudaSuccess ? GBN_OK : cuda_status(e, "motion-compensated nesta launch");
+  }
   cudaStream_t aux = ctx->mc_stream;
   for (unsigned nl = 1; nl <= prm->maxIntIter; ++nl) {
     ctx->launches += launch_outer_begin(ctx, P, int(nl), x_out, s);
     for (unsigned it = 0; it < prm->maxIter; ++it) {
-      const float2* xk = (it & 1) ? P->xk1 : P->xk0;
       cudaEventRecord(ctx->ev_mc_x, s);
       cudaStreamWaitEvent(aux, ctx->ev_mc_x, 0);
-      k_mc_tv<<<gtv, kNT, 0, aux>>>(xk, P->mc_xn, t->inv, r, P->st, P->mc_g, t->tvpart, W, H, F, &P->st->status);
+      k_mc_tv<<<gtv, kNT, 0, aux>>>(P->xk0, P->xk1, int(it), P->mc_xn, t->inv, r, P->st, P->mc_g, t->tvpart, W, H, F,
+                                    &P->st->status);
       cudaEventRecord(ctx->ev_mc_tv, aux);
       k_mc_adjoint<<<gadj, kNT, 0, aux>>>(P->mc_g, P->mc_gm, t->off, t->csrc, t->cw, r, W, H, F, 0);
       cudaEventRecord(ctx->ev_mc_adj, aux);

@@ -295,7 +295,14 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
       if (k1p < B) tws[d] = __ldg(a.twH + H + k1p * A + k1);
     }
   }
-  grid_dep_wait();  // x_k, w_k and the scalar state come from the previous iteration
+  // Plain form: x_k, w_k and the scalar state come from the previous launch,
+  // the previous iteration.  Motion-compensated form: the launch before this
+  // one is M^T(tTVadj u) (k_mc_adjoint), which is read only by the update
+  // below, after a later wait; the previous iteration is three launches back
+  // and complete when this kernel starts (k_mc_adjoint and k_mc_tv release
+  // their successors only after their own waits).
+  const bool motion = a.grad_ext != nullptr;
+  if (!motion) grid_dep_wait();
   grid_dep_release();
 
   // which update this launch computes (uniform over the instance, so over each cluster)
@@ -518,7 +525,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
 
   // tTV objective partial sums over the tile (first half only; not in fixup mode)
   float su2 = 0.f, sud = 0.f;
-  if (half == 0 && !fix) {
+  if (half == 0 && !fix && !motion) {  // the motion-compensated form has them from k_mc_tv
     const float2* __restrict__ xm = xk + size_t((f + F - 1) % F) * N;
 #pragma unroll
     for (int ii = 0; ii < NI1; ++ii) {
@@ -560,6 +567,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   cluster.sync();
 
   // tTV gradient and Nesterov update of this CTA's rows
+  if (motion) grid_dep_wait();  // M^T(tTVadj u) of x_k
   const float s_adj = a.s_adj;
   const size_t offm = size_t((f + F - 1) % F) * N, off0 = size_t(f) * N, offp = size_t((f + 1) % F) * N;
   const float lambda = st->lambda, nLmu1 = -st->Lmu1;
@@ -581,8 +589,12 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
           if (k2 < A && k2 >= kb && k2 < ke) {
             const size_t p = size_t(k1p + B * k2) * W + w0 + w;
             xa[b] = xk[off0 + p];
-            xm[b] = xk[offm + p];
-            xp[b] = xk[offp + p];
+            if (motion) {
+              xm[b] = a.grad_ext[off0 + p];  // M^T (tTVadj u) of the motion-compensated form
+            } else {
+              xm[b] = xk[offm + p];
+              xp[b] = xk[offp + p];
+            }
             wo[b] = wk[off0 + p];
             xr[b] = a.xref[off0 + p];
           }
@@ -592,9 +604,16 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
           const int k2 = k0 + b;
           if (k2 < A && k2 >= kb && k2 < ke) {
             const size_t p = size_t(k1p + B * k2) * W + w0 + w;
-            const float2 u0 = tv_normalize(csub(xa[b], xm[b]), inv_mu);
-            const float2 u1 = tv_normalize(csub(xp[b], xa[b]), inv_mu);
-            const float2 adj = csub(u1, u0);
+            // operator_tTVadj gives u_{f+1} - u_f of the normalised temporal
+            // differences; NestaUp negates it, scales by lambda, adds A^H r
+            float2 adj;
+            if (motion) {
+              adj = xm[b];
+            } else {
+              const float2 u0 = tv_normalize(csub(xa[b], xm[b]), inv_mu);
+              const float2 u1 = tv_normalize(csub(xp[b], xa[b]), inv_mu);
+              adj = csub(u1, u0);
+            }
             const float2 ares = cscale(acc[ii][k2], s_adj);
             const float2 df = make_float2(__fadd_rn(__fmul_rn(-adj.x, lambda), ares.x),
                                           __fadd_rn(__fmul_rn(-adj.y, lambda), ares.y));
@@ -613,7 +632,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   // fixed-slot partial sums: ||rho||^2 of this CTA, the tTV terms of the tile
   const int blk = f * gridDim.x + blockIdx.x;
   const double pr = block_sum<kColNT>(double(racc), sred);
-  if (half == 0) {
+  if (half == 0 && !motion) {  // the motion-compensated form's come from k_mc_tv, in the same buffer
     const double t1 = block_sum<kColNT>(double(su2), sred);
     const double t2 = block_sum<kColNT>(double(sud), sred);
     if (t == 0) {
@@ -623,7 +642,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   }
   if (t == 0) a.part_r[2 * blk + half] = pr;
   if (rowlocal_last_cta(bm.ctl, inst, 2u * gridDim.x * unsigned(F)))
-    rowlocal_finish<kColNT>(a, st, bm.ctl, inst, it, apk, 2 * a.ntv, sred, fm);
+    rowlocal_finish<kColNT>(a, st, bm.ctl, inst, it, apk, 2 * F * int(gridDim.x), sred, fm);
 }
 
 }  // namespace gbn

@@ -55,6 +55,8 @@ int launch_setup(gbn_problem* P, cudaStream_t s);
 // start (w = 0, x_k = x_ref, mu/tolVar/Lmu) and end (x_ref = x_k) of outer loop nl
 int launch_outer_begin(gbn_ctx* ctx, gbn_problem* P, int nl, const float2* xref, cudaStream_t s);
 int launch_outer_end(gbn_ctx* ctx, gbn_problem* P, float2* xref, cudaStream_t s);
+// pinned host slot and event for the per-run row-structure read-back (created on first use)
+int partial_flag_ready(gbn_ctx* ctx);
 // 1-thread kernel storing a 48-bit generator state (outside captured graphs)
 int launch_set_rand(unsigned long long* dst, unsigned long long v, cudaStream_t s);
 
