@@ -145,7 +145,7 @@ int batch_enqueue(gbn_batch* b, bool graph_mode) {
           if (g.row_local_tc)
             launch_iter_tc(g.tab, g.bm, int(it), g.npad_max, g.cnmax_tc, g.g_tc, s);
           else
-            kh->iter_cols(g.tab, g.bm, int(it), g.g3, s);
+            kh->iter_cols(g.tab, g.bm, int(it), false, g.g3, s);
         }
         n_launch += nit;
       }

@@ -62,11 +62,16 @@ struct Launchers {
       launch_pdl(k_inv_cols<L, false>, grid, kColNT, InvColsSmem<L>::BYTES, s, tab, bm, it);
     }
   }
-  static void iter_cols(const FusedArgs* tab, const BatchMap& bm, int it, dim3 grid, cudaStream_t s) {
+  static void iter_cols(const FusedArgs* tab, const BatchMap& bm, int it, bool motion, dim3 grid, cudaStream_t s) {
     if constexpr (iter_cols_ok(L)) {
-      static bool ok = false;
-      allow_smem(k_iter_cols<L>, IterColsSmem<L>::BYTES, ok);
-      launch_pdl(k_iter_cols<L>, grid, kColNT, IterColsSmem<L>::BYTES, s, tab, bm, it);
+      static bool ok0 = false, ok1 = false;
+      if (motion) {
+        allow_smem(k_iter_cols<L, true>, IterColsSmem<L>::BYTES, ok1);
+        launch_pdl(k_iter_cols<L, true>, grid, kColNT, IterColsSmem<L>::BYTES, s, tab, bm, it);
+      } else {
+        allow_smem(k_iter_cols<L, false>, IterColsSmem<L>::BYTES, ok0);
+        launch_pdl(k_iter_cols<L, false>, grid, kColNT, IterColsSmem<L>::BYTES, s, tab, bm, it);
+      }
     }
   }
   static void fft_rows(const float2* in, float2* out, int nrows, int inv, float scale, const float2* tw, int grid,

@@ -823,7 +823,7 @@ int nesta_run(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, float2*
     GBN_LAUNCH(ctx, GBN_PROF_OUTER, 1, launch_outer_begin(ctx, P, int(nl), x_out, s));
     if (row_local) {
       for (unsigned it = 0; it < n_iter_launch; ++it)
-        GBN_LAUNCH(ctx, GBN_PROF_ITER, 1, kh->iter_cols(tab, bm, int(it), g3, s));
+        GBN_LAUNCH(ctx, GBN_PROF_ITER, 1, kh->iter_cols(tab, bm, int(it), false, g3, s));
     } else {
       for (unsigned it = 0; it < prm->maxIter; ++it) {
         GBN_LAUNCH(ctx, GBN_PROF_FWD_COLS, 1, kh->fwd_cols(tab, bm, int(it), cpb, g1, s));

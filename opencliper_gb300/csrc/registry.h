@@ -22,9 +22,10 @@ struct SizeKernels {
                    cudaStream_t s);
   void (*fft_cols)(const float2* in, float2* out, int W, int nimg, int inv, float scale, const float2* tw,
                    cudaStream_t s);
-  // row-local inner iteration (k_iter_cols<L>), grid (W/8, 2, total frames) in
-  // clusters of 2; nullptr for lengths that run only the three-pass iteration
-  void (*iter_cols)(const FusedArgs* tab, const BatchMap& bm, int it, dim3 grid, cudaStream_t s);
+  // row-local inner iteration (k_iter_cols<L, motion>), grid (W/8, 2, total
+  // frames) in clusters of 2; nullptr for lengths that run only the three-pass
+  // iteration
+  void (*iter_cols)(const FusedArgs* tab, const BatchMap& bm, int it, bool motion, dim3 grid, cudaStream_t s);
   int rows_per_cta;  // rows processed per CTA step by the row kernels
   int (*rows_occupancy)(bool resid);  // resident row-kernel CTAs per SM
 };

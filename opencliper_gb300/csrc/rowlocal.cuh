@@ -210,7 +210,9 @@ constexpr bool iter_cols_ok(int H) {
                              (iter_cols_tmem(H) && split_a(H) <= 32));
 }
 
-template <int H>
+// MOTION: the motion-compensated form (tTV gradient M^T(tTVadj u) and the
+// tTV sums from the motion kernels launched before it).
+template <int H, bool MOTION>
 __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_min_blocks(H))
     k_iter_cols(const FusedArgs* __restrict__ tab, const __grid_constant__ BatchMap bm, int it) {
   using L = IterColsSmem<H>;
@@ -297,12 +299,13 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   }
   // Plain form: x_k, w_k and the scalar state come from the previous launch,
   // the previous iteration.  Motion-compensated form: the launch before this
-  // one is M^T(tTVadj u) (k_mc_adjoint), which is read only by the update
-  // below, after a later wait; the previous iteration is three launches back
-  // and complete when this kernel starts (k_mc_adjoint and k_mc_tv release
-  // their successors only after their own waits).
-  const bool motion = a.grad_ext != nullptr;
-  if (!motion) grid_dep_wait();
+  // one is M^T(tTVadj u) (k_mc_adjoint, after the fused tTV kernel that also
+  // writes the objective's tTV sums), which only the update below reads, after
+  // a later wait; the previous iteration is three launches back and complete
+  // when this kernel starts (both motion kernels release their successors only
+  // after their own waits).
+  constexpr bool motion = MOTION;
+  if constexpr (!motion) grid_dep_wait();
   grid_dep_release();
 
   // which update this launch computes (uniform over the instance, so over each cluster)
@@ -567,7 +570,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   cluster.sync();
 
   // tTV gradient and Nesterov update of this CTA's rows
-  if (motion) grid_dep_wait();  // M^T(tTVadj u) of x_k
+  if constexpr (motion) grid_dep_wait();  // M^T(tTVadj u) of x_k
   const float s_adj = a.s_adj;
   const size_t offm = size_t((f + F - 1) % F) * N, off0 = size_t(f) * N, offp = size_t((f + 1) % F) * N;
   const float lambda = st->lambda, nLmu1 = -st->Lmu1;
@@ -589,7 +592,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
           if (k2 < A && k2 >= kb && k2 < ke) {
             const size_t p = size_t(k1p + B * k2) * W + w0 + w;
             xa[b] = xk[off0 + p];
-            if (motion) {
+            if constexpr (motion) {
               xm[b] = a.grad_ext[off0 + p];  // M^T (tTVadj u) of the motion-compensated form
             } else {
               xm[b] = xk[offm + p];
@@ -607,7 +610,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
             // operator_tTVadj gives u_{f+1} - u_f of the normalised temporal
             // differences; NestaUp negates it, scales by lambda, adds A^H r
             float2 adj;
-            if (motion) {
+            if constexpr (motion) {
               adj = xm[b];
             } else {
               const float2 u0 = tv_normalize(csub(xa[b], xm[b]), inv_mu);
