@@ -141,7 +141,8 @@ int prof_collect(gbn_ctx* ctx) {
   return GBN_OK;
 }
 
-int ctx_scratch(gbn_ctx* ctx, size_t bytes, void** out) {
+int ctx_scratch(gbn_ctx* ctx, size_t bytes, void** out, int user) {
+  ctx->scratch_user = user;
   if (bytes > ctx->scratch_bytes) {
     if (ctx->scratch) {
       cudaStreamSynchronize(ctx->stream);

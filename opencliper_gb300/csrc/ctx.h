@@ -32,6 +32,17 @@ struct gbn_ctx {
   uint64_t rand48 = 0x1234ABCD330EULL;  // drand48 state (glibc default before any seeding)
   void* scratch = nullptr;            // grow-only scratch for per-operator entry points
   size_t scratch_bytes = 0;
+  int scratch_user = 0;               // entry point that used the scratch last (kScratch*)
+  // SimpleMRIRecon keeps its tables (identity row map, instance entry, control
+  // block) in the scratch: a call with the same shape, buffers and scratch,
+  // with no other user of the scratch in between, launches only the two passes
+  struct SimpleKey {
+    const void* y = nullptr;
+    const void* S = nullptr;
+    const void* x = nullptr;
+    const void* ws = nullptr;
+    int W = 0, H = 0, F = 0, C = 0;
+  } simple_key;
   int k1_coils_per_block = 4;         // tuning: coils per CTA in the forward column pass
   int k2_ctas_per_sm = 4;             // tuning: persistent CTAs per SM in the row pass
   int mixed_adjoint_tc = 0;           // tuning: mixed form runs the adjoint column pass on the tensor cores
@@ -162,8 +173,9 @@ inline int check_fft(int W, int H) {
 
 // twiddle table for length L (nullptr when unsupported)
 const float2* ctx_twiddles(gbn_ctx* ctx, int L);
-// grow-only scratch of at least `bytes`
-int ctx_scratch(gbn_ctx* ctx, size_t bytes, void** out);
+// grow-only scratch of at least `bytes`, recorded as used by `user`
+constexpr int kScratchOther = 0, kScratchSimple = 1;
+int ctx_scratch(gbn_ctx* ctx, size_t bytes, void** out, int user = kScratchOther);
 
 // event-profiling helpers: bracket one launch of kernel group `kind`
 void prof_begin(gbn_ctx* ctx, int kind, cudaEvent_t* ev);

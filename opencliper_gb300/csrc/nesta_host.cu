@@ -849,7 +849,8 @@ size_t simple_recon_bytes(int W, int H, int F, int C) {
          up(sizeof(FusedArgs)) + up(sizeof(ClassCtl));
 }
 
-int simple_recon_in(gbn_ctx* ctx, void* ws, const float2* y, const float2* S, float2* x, int W, int H, int F, int C) {
+int simple_recon_in(gbn_ctx* ctx, void* ws, const float2* y, const float2* S, float2* x, int W, int H, int F, int C,
+                    bool tables_valid) {
   const SizeKernels* kh = find_size(H);
   const SizeKernels* kw = find_size(W);
   if (!kh || !kw) return set_error(GBN_ERR_UNSUPPORTED, "unsupported FFT length");
@@ -894,11 +895,16 @@ int simple_recon_in(gbn_ctx* ctx, void* ws, const float2* y, const float2* S, fl
   const long long steps = ((long long)FH * C + kw->rows_per_cta - 1) / kw->rows_per_cta;
   const int g2 = row_grid(ctx, kw, false, steps, ctx->k2_ctas_per_sm);
   const BatchMap bm = single_map(F, ctl);
-  GBN_LAUNCH(ctx, GBN_PROF_SETUP, 5, {
-    k_rows_identity<<<int(std::min<size_t>((FH + 255) / 256, 1024)), 256, 0, s>>>(H, F, rowmap, rowoff, rows_h, rows_f,
-                                                                                  row_full);
-    k_store_args<<<1, 1, 0, s>>>(tab, a);
-    k_group_init<<<1, 64, 0, s>>>(tab, 1, kw->rows_per_cta, ctl);
+  // the tables persist in `ws`, and the row pass leaves its control block
+  // ready for the next launch
+  const int n_tables = tables_valid ? 0 : 3;
+  GBN_LAUNCH(ctx, GBN_PROF_SETUP, n_tables + 2, {
+    if (!tables_valid) {
+      k_rows_identity<<<int(std::min<size_t>((FH + 255) / 256, 1024)), 256, 0, s>>>(H, F, rowmap, rowoff, rows_h,
+                                                                                    rows_f, row_full);
+      k_store_args<<<1, 1, 0, s>>>(tab, a);
+      k_group_init<<<1, 64, 0, s>>>(tab, 1, kw->rows_per_cta, ctl);
+    }
     kw->rows(tab, bm, 0, false, g2, s);
     kh->inv_cols(tab, bm, 0, false, dim3(W / kWB, 2, F), s);
   });
@@ -912,9 +918,26 @@ int simple_recon_in(gbn_ctx* ctx, void* ws, const float2* y, const float2* S, fl
 int simple_recon(gbn_ctx* ctx, const float2* y, const float2* S, float2* x, int W, int H, int F, int C) {
   if (!find_size(H) || !find_size(W)) return set_error(GBN_ERR_UNSUPPORTED, "unsupported FFT length");
   void* scr = nullptr;
-  const int rc = ctx_scratch(ctx, simple_recon_bytes(W, H, F, C), &scr);
+  const bool mine = ctx->scratch_user == kScratchSimple;
+  const int rc = ctx_scratch(ctx, simple_recon_bytes(W, H, F, C), &scr, kScratchSimple);
   if (rc != GBN_OK) return rc;
-  return simple_recon_in(ctx, scr, y, S, x, W, H, F, C);
+  gbn_ctx::SimpleKey& k = ctx->simple_key;
+  const bool same = mine && k.y == y && k.S == S && k.x == x && k.ws == scr && k.W == W && k.H == H && k.F == F &&
+                    k.C == C;
+  const int rc2 = simple_recon_in(ctx, scr, y, S, x, W, H, F, C, same);
+  if (rc2 == GBN_OK) {
+    k.y = y;
+    k.S = S;
+    k.x = x;
+    k.ws = scr;
+    k.W = W;
+    k.H = H;
+    k.F = F;
+    k.C = C;
+  } else {
+    k = gbn_ctx::SimpleKey{};
+  }
+  return rc2;
 }
 
 }  // namespace gbn

@@ -30,7 +30,8 @@
 namespace gbn {
 
 size_t simple_recon_bytes(int W, int H, int F, int C);
-int simple_recon_in(gbn_ctx* ctx, void* ws, const float2* y, const float2* S, float2* x, int W, int H, int F, int C);
+int simple_recon_in(gbn_ctx* ctx, void* ws, const float2* y, const float2* S, float2* x, int W, int H, int F, int C,
+                    bool tables_valid);
 
 namespace {
 
@@ -79,7 +80,7 @@ int simple_recon_static(gbn_ctx* ctx, const float2* y, const float2* S, float2* 
   if (rc != GBN_OK) return rc;
   if (simple_recon_bytes(W, H, F, C) > kStaticScratchBytes)
     return set_error(GBN_ERR_UNSUPPORTED, "gbn_simple_recon_static: problem exceeds the static scratch");
-  return simple_recon_in(ctx, base, y, S, x, W, H, F, C);
+  return simple_recon_in(ctx, base, y, S, x, W, H, F, C, false);  // the array is shared between contexts
 }
 
 }  // namespace gbn

@@ -48,6 +48,35 @@ def test_fft2_and_encode_operators(ctx, W, H, F, C):
     assert rel_l2(ox.get(), R.simple_recon(_c128(k), _c128(S))) < TOL
 
 
+def test_simple_recon_repeated_calls(ctx):
+    """A repeated call with the same shape and buffers reuses the tables the
+    first call left in the context's scratch (2 launches instead of 5); new
+    data in the same buffers, another operator using the scratch in between,
+    and another shape all give the oracle's result."""
+    rng = np.random.default_rng(11)
+    W, H, F, C = 64, 48, 2, 3
+    k1, k2, S = _rand(rng, (F, C, H, W)), _rand(rng, (F, C, H, W)), _rand(rng, (C, H, W))
+    dk, dS = ctx.to_device(k1), ctx.to_device(S)
+    ox = ctx.empty((F, H, W), np.complex64)
+    counts = []
+    for k in (k1, k2, k2):
+        dk.set(k)
+        n0 = ctx.launch_count()
+        api.simple_recon(ctx, dk, dS, ox)
+        counts.append(ctx.launch_count() - n0)
+        assert rel_l2(ox.get(), R.simple_recon(_c128(k), _c128(S))) < TOL
+    assert counts[1] < counts[0] and counts[2] == counts[1]
+    api.op_encode_adjoint(ctx, dk, dS, ox)  # another user of the scratch
+    n0 = ctx.launch_count()
+    api.simple_recon(ctx, dk, dS, ox)
+    assert ctx.launch_count() - n0 == counts[0]
+    assert rel_l2(ox.get(), R.simple_recon(_c128(k2), _c128(S))) < TOL
+    k3, S3 = _rand(rng, (1, 2, 40, 32)), _rand(rng, (2, 40, 32))
+    ox3 = ctx.empty((1, 40, 32), np.complex64)
+    api.simple_recon(ctx, ctx.to_device(k3), ctx.to_device(S3), ox3)
+    assert rel_l2(ox3.get(), R.simple_recon(_c128(k3), _c128(S3))) < TOL
+
+
 def test_fft2_in_place(ctx):
     rng = np.random.default_rng(0)
     k = _rand(rng, (3, 2, 48, 40))
