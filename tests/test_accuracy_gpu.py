@@ -31,3 +31,17 @@ def test_uneven_batch_members_within_gate(ctx):
         print(r)
     assert len(rows) >= 3
     assert all(r["fp32"] <= A.bar(r) and r["mixed"] <= A.bar(r) for r in rows)
+
+
+def test_stress_members_within_gate(ctx):
+    """Four members of the 256-reconstruction stress batch (largest coil
+    count, largest frame count, largest W*F*C, the first), one at a time."""
+    pytest.importorskip("torch")
+    shapes = A.batch_shapes(A.STRESS["n"], A.STRESS)
+    rows = []
+    for i in A.sample_members(shapes):
+        rows += A.solve(ctx, [shapes[i]])
+    for r in rows:
+        print(r)
+    assert len(rows) >= 3
+    assert all(r["fp32"] <= A.bar(r) and r["mixed"] <= A.bar(r) for r in rows)
