@@ -2,7 +2,11 @@
 // serialisation may start while its predecessor in the stream drains.  Such a
 // kernel reads nothing its predecessor writes before grid_dep_wait(), and
 // releases its own successor only after that wait, so no kernel's early part
-// runs before the kernel two launches back has completed.
+// runs before the kernel two launches back has completed.  One exception: the
+// motion-compensated row-local iteration (rowlocal.cuh) releases at its start
+// and waits only before its update; its successor (the fused tTV kernel of
+// the next iteration) waits before reading anything, and its own early part
+// reads only what the launch three back wrote.
 #pragma once
 
 #include <cuda_runtime.h>
