@@ -255,17 +255,30 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
 
   // S and IDFT_W(y) (in T since the setup) are inputs of the whole solve: they
   // are staged before the dependency wait
+  // this thread's 16-byte granules of an S tile: rows srow + i*RSTEP, columns
+  // 2*spart, 2*spart + 1 (the granule pattern repeats every RSTEP rows)
+  constexpr int GPR = kWB / 2, RSTEP = kColNT / GPR;
+  const int srow = t / GPR, spart = t % GPR;
+  const float2* const s_src0 = a.S + size_t(srow) * W + w0 + 2 * spart;
+  const float2* const t_src0 = a.T + size_t(rowbase) * C * W + w0;
   auto issue_S = [&](int c, int buf) {
-    const float2* src = a.S + size_t(c) * N + w0;
     float2* dst = Sb + (L::SB == 2 ? buf : 0) * H * kWB;
-    for (int q = t; q < H * (kWB / 2); q += kColNT) {
-      const int row = q / (kWB / 2), part = q % (kWB / 2);
-      cp_async16(dst + row * kWB + 2 * part, src + size_t(row) * W + 2 * part);
+    if constexpr (H % RSTEP == 0) {
+      const float2* src = s_src0 + size_t(c) * N;
+      float2* d0 = dst + srow * kWB + 2 * spart;
+#pragma unroll
+      for (int i = 0; i < H / RSTEP; ++i) cp_async16(d0 + i * RSTEP * kWB, src + size_t(i) * RSTEP * W);
+    } else {
+      const float2* src = a.S + size_t(c) * N + w0;
+      for (int q = t; q < H * GPR; q += kColNT) {
+        const int row = q / GPR, part = q % GPR;
+        cp_async16(dst + row * kWB + 2 * part, src + size_t(row) * W + 2 * part);
+      }
     }
   };
   auto issue_Y = [&](int c, int buf) {
     if (staged) {
-      const float2* src = a.T + (size_t(rowbase) * C + c) * W + w0;
+      const float2* src = t_src0 + size_t(c) * W;
       float2* dst = Yb + buf * RCAP * kWB;
       for (int q = t; q < nrows * (kWB / 2); q += kColNT) {
         const int j = q / (kWB / 2), part = q % (kWB / 2);
