@@ -493,7 +493,7 @@ __global__ void __maxnreg__(224)
     a.part_tv[2 * blk + 1] = t2;
   }
   if (rowlocal_last_cta(bm.ctl, inst, gridDim.x * unsigned(F)))
-    rowlocal_finish<kRtNT>(a, st, bm.ctl, inst, it, apk, a.ntv, sred, fm);
+    rowlocal_finish<kRtNT>(a, st, bm.ctl, inst, it, apk, a.ntv, a.ntv, sred, fm);
 }
 
 // ---------------------------------------------------------------------------

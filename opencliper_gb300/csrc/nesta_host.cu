@@ -650,7 +650,8 @@ int run_prepare(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm) {
   const int nblk_ne = (N + kNeNT - 1) / kNeNT;
   int rc;
   if ((rc = grow(P->fmean, P->fmean_cap, std::max<int>(1, int(prm->miniter)))) != GBN_OK) return rc;
-  if ((rc = grow(P->part_tv, P->part_tv_cap, 2 * F * (W / kWB))) != GBN_OK) return rc;
+  // one (|u|^2, Re<u,d>) pair per (frame, 8-column tile) and coil half (row-local iteration)
+  if ((rc = grow(P->part_tv, P->part_tv_cap, 4 * F * (W / kWB))) != GBN_OK) return rc;
   if ((rc = grow(P->part_r, P->part_r_cap, std::max(int(steps_max) * kRowWarps, 2 * F * (W / kWB)))) != GBN_OK)
     return rc;
   if ((rc = grow(P->part_ne, P->part_ne_cap, nblk_ne * kNeMaxSlots * 2)) != GBN_OK) return rc;

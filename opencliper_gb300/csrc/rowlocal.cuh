@@ -69,14 +69,13 @@ __device__ __forceinline__ bool rowlocal_last_cta(ClassCtl* ctl, int inst, unsig
 // and the next launch recomputes this iteration's update.  All NT threads call it.
 template <int NT>
 __device__ void rowlocal_finish(const FusedArgs& a, NestaDevState* st, ClassCtl* ctl, int inst, int it, float apk_used,
-                                int npr, double* sred, float* fm) {
+                                int ntv, int npr, double* sred, float* fm) {
   const int t = threadIdx.x;
   __threadfence();
   if (t < kFmeanCopy && t < st->miniter) fm[t] = __ldcg(a.fmean + t);
   constexpr int U = 8;
   double s1 = 0.0, s2 = 0.0, s3 = 0.0;
   const double2* ptv = reinterpret_cast<const double2*>(a.part_tv);
-  const int ntv = a.ntv;
   for (int i0 = 0; i0 < ntv; i0 += U * NT) {
     double2 vv[U];
 #pragma unroll
@@ -539,10 +538,12 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
     if (t < 32) tc::tmem_dealloc(tslot, TCOLS);
   }
 
-  // tTV objective partial sums over the tile (first half only; not in fixup mode)
+  // tTV objective partial sums over the tile, each CTA of the pair over half
+  // of its rows (n1 < A/2 for the first); not in fixup mode
   float su2 = 0.f, sud = 0.f;
-  if (half == 0 && !fix && !motion) {  // the motion-compensated form has them from k_mc_tv
+  if (!fix && !motion) {  // the motion-compensated form has them from k_mc_tv
     const float2* __restrict__ xm = xk + size_t((f + F - 1) % F) * N;
+    constexpr int NH = A / 2;
 #pragma unroll
     for (int ii = 0; ii < NI1; ++ii) {
       const int i = t + ii * kColNT;
@@ -550,6 +551,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
         const int w = i % kWB, s = i / kWB;
 #pragma unroll
         for (int n1 = 0; n1 < A; ++n1) {
+          if ((n1 < NH) != (half == 0)) continue;
           const float2 d = csub(xv[ii][n1], xm[size_t(B * n1 + s) * W + w0 + w]);
           const float2 u = tv_normalize(d, inv_mu);
           su2 = fmaf(u.x, u.x, fmaf(u.y, u.y, su2));
@@ -648,17 +650,18 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   // fixed-slot partial sums: ||rho||^2 of this CTA, the tTV terms of the tile
   const int blk = f * gridDim.x + blockIdx.x;
   const double pr = block_sum<kColNT>(double(racc), sred);
-  if (half == 0 && !motion) {  // the motion-compensated form's come from k_mc_tv, in the same buffer
+  if (!motion) {  // the motion-compensated form's come from k_mc_tv, in the same buffer
     const double t1 = block_sum<kColNT>(double(su2), sred);
     const double t2 = block_sum<kColNT>(double(sud), sred);
     if (t == 0) {
-      a.part_tv[2 * blk] = t1;
-      a.part_tv[2 * blk + 1] = t2;
+      a.part_tv[2 * (2 * blk + half)] = t1;
+      a.part_tv[2 * (2 * blk + half) + 1] = t2;
     }
   }
   if (t == 0) a.part_r[2 * blk + half] = pr;
   if (rowlocal_last_cta(bm.ctl, inst, 2u * gridDim.x * unsigned(F)))
-    rowlocal_finish<kColNT>(a, st, bm.ctl, inst, it, apk, 2 * F * int(gridDim.x), sred, fm);
+    rowlocal_finish<kColNT>(a, st, bm.ctl, inst, it, apk, motion ? a.ntv : 2 * F * int(gridDim.x),
+                            2 * F * int(gridDim.x), sred, fm);
 }
 
 }  // namespace gbn
