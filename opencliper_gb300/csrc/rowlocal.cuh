@@ -592,7 +592,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   const float apk = fix ? st->apk : 0.5f * (float(itx) + 1.0f);  // nesta_scalar_step's weights for k = itx
   const float tauk = fix ? st->tauk : 2.0f / (float(itx) + 3.0f);
   const float omt = 1.0f - tauk;
-  constexpr int BATCH = 4;
+  constexpr int BATCH = A <= 16 ? 8 : 4;  // one round of loads for a CTA's 8 rows at A = 16
 #pragma unroll
   for (int ii = 0; ii < NI3; ++ii) {
     const int i = t + ii * kColNT;
