@@ -67,10 +67,10 @@ struct Launchers {
       static bool ok0 = false, ok1 = false;
       if (motion) {
         allow_smem(k_iter_cols<L, true>, IterColsSmem<L>::BYTES, ok1);
-        launch_pdl(k_iter_cols<L, true>, grid, kColNT, IterColsSmem<L>::BYTES, s, tab, bm, it);
+        launch_pdl(k_iter_cols<L, true>, grid, IterColsSmem<L>::NT, IterColsSmem<L>::BYTES, s, tab, bm, it);
       } else {
         allow_smem(k_iter_cols<L, false>, IterColsSmem<L>::BYTES, ok0);
-        launch_pdl(k_iter_cols<L, false>, grid, kColNT, IterColsSmem<L>::BYTES, s, tab, bm, it);
+        launch_pdl(k_iter_cols<L, false>, grid, IterColsSmem<L>::NT, IterColsSmem<L>::BYTES, s, tab, bm, it);
       }
     }
   }

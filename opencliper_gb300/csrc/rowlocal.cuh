@@ -158,17 +158,32 @@ __device__ __forceinline__ void tmem_st_n(uint32_t taddr, const float* v) {
 }
 constexpr int iter_cols_sbufs(int L) { return iter_cols_tmem(L) ? 1 : 2; }
 
+// Threads per CTA: 128, or for the tensor-memory lengths one per pass-2 item
+// (kWB * A of them, rounded up to whole warps) where three such CTAs still fit
+// at 128 registers a thread (H = 288, 320: 160 threads).  With 128 threads
+// those items fall twice to some threads and the pass waits for them; more
+// threads at fewer CTAs per SM measured slower (H = 384: 288 us per iteration
+// with 192 threads at two CTAs, against 280 us).  The pass-1 and pass-3 items
+// (kWB * B = 128) stay on warps 0-3, whose tensor-memory lanes hold their state.
+constexpr int iter_cols_threads(int L) {
+  return (iter_cols_tmem(L) && (kWB * split_a(L) + 31) / 32 * 32 * 3 * 128 <= 65536) ? (kWB * split_a(L) + 31) / 32 * 32
+                                                                                     : kColNT;
+}
+
 // Shared-memory bytes of k_iter_cols<L> (the layout of IterColsSmem<L>).
 constexpr int iter_cols_bytes(int L) {
   const int a = split_a(L), b = split_b(L);
   const int ex = (a * col_ks(b) > b * col_ks(a)) ? a * col_ks(b) : b * col_ks(a);
   return (iter_cols_sbufs(L) * L * kWB + 2 * iter_cols_rcap(L) * kWB + ex + b * (a + 2) + a * (b + 2)) * 8 + L * 4 +
-         (kColNT / 32) * 8 + kFmeanCopy * 4 + 16;
+         (iter_cols_threads(L) / 32) * 8 + kFmeanCopy * 4 + 16;
 }
 
 template <int H>
 struct IterColsSmem {
   static constexpr int A = Split<H>::A, B = Split<H>::B;
+  static constexpr int NT = iter_cols_threads(H);   // threads per CTA
+  static constexpr int NI3 = cdiv(kWB * B, NT);     // inverse pass-2 items per thread
+  static constexpr int XST = NI3 == 1 ? kWB * B : NT;  // stride of the accumulator exchange
   static constexpr int KSF = col_ks(B);  // forward exchange: slot (k1, s*kWB + w), k1 < A
   static constexpr int KSI = col_ks(A);  // inverse exchange: slot (k1', s'*kWB + w), k1' < B
   static constexpr int EXN = (A * KSF > B * KSI) ? A * KSF : B * KSI;
@@ -184,22 +199,28 @@ struct IterColsSmem {
   static constexpr int TW_OFF = EX_OFF + EXN;
   static constexpr int TWI_OFF = B * TWF;                // inverse rows, from TW_OFF
   static constexpr int F2_END = TW_OFF + TWI_OFF + A * TWI;
-  static constexpr int BYTES = F2_END * 8 + H * 4 + (kColNT / 32) * 8 + kFmeanCopy * 4 + 16;
-  static_assert(cdiv(kWB * B, kColNT) * A * kColNT <= SB * H * kWB, "accumulator exchange must fit the S buffers");
+  static constexpr int BYTES = F2_END * 8 + H * 4 + (NT / 32) * 8 + kFmeanCopy * 4 + 16;
+  static_assert(NI3 * A * XST <= SB * H * kWB, "accumulator exchange must fit the S buffers");
   static_assert(BYTES == iter_cols_bytes(H), "layout and byte count agree");
   static_assert(TW_OFF % 2 == 0, "twiddle rows start on 16-byte boundaries");
 };
 
 
 // CTAs per SM the launch bounds ask for.  With x and the accumulators in
-// tensor memory, as many as shared memory allows (at most three); otherwise a
+// tensor memory, as many as shared memory allows and keep 128 registers a
+// thread (at most three); otherwise a
 // first factor A <= 16 keeps the per-thread state (x at the pass-1 items, the
 // accumulators, one pass-2 item) within 168 registers at three CTAs per SM,
 // and longer first factors hold more per thread at the two CTAs per SM (one
 // past 448) their shared memory allows, with up to 255 registers a thread.
 constexpr int iter_cols_min_blocks(int H) {
-  return iter_cols_tmem(H) ? ((228 * 1024) / (iter_cols_bytes(H) + 1024) < 3 ? (228 * 1024) / (iter_cols_bytes(H) + 1024) : 3)
-         : split_a(H) <= 16 ? 3 : (iter_cols_bytes(H) + 1024 <= 114 * 1024 ? 2 : 1);
+  if (iter_cols_tmem(H)) {
+    const int by_smem = (228 * 1024) / (iter_cols_bytes(H) + 1024);
+    const int by_regs = 65536 / (iter_cols_threads(H) * 128);  // at least 128 registers a thread
+    const int m = by_smem < by_regs ? by_smem : by_regs;
+    return m < 3 ? m : 3;
+  }
+  return split_a(H) <= 16 ? 3 : (iter_cols_bytes(H) + 1024 <= 114 * 1024 ? 2 : 1);
 }
 
 // Lengths that run the row-local iteration; the others (whose per-thread
@@ -212,19 +233,20 @@ constexpr bool iter_cols_ok(int H) {
 // MOTION: the motion-compensated form (tTV gradient M^T(tTVadj u) and the
 // tTV sums from the motion kernels launched before it).
 template <int H, bool MOTION>
-__global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_min_blocks(H))
+__global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(iter_cols_threads(H), iter_cols_min_blocks(H))
     k_iter_cols(const FusedArgs* __restrict__ tab, const __grid_constant__ BatchMap bm, int it) {
   using L = IterColsSmem<H>;
-  constexpr int A = L::A, B = L::B, KSF = L::KSF, KSI = L::KSI, RCAP = L::RCAP;
+  constexpr int A = L::A, B = L::B, KSF = L::KSF, KSI = L::KSI, RCAP = L::RCAP, NT = L::NT;
   constexpr int N1 = kWB * B;  // forward pass-1 items (w, s), s < B: rows B*n1 + s
   constexpr int N2 = kWB * A;  // forward pass-2 = inverse pass-1 items (w, k1), k1 < A: rows k1 + A*k2
   constexpr int N3 = kWB * B;  // inverse pass-2 items (w, k1'), k1' < B: rows k1' + B*k2
-  constexpr int NI1 = cdiv(N1, kColNT), NI2 = cdiv(N2, kColNT), NI3 = cdiv(N3, kColNT);
+  constexpr int NI1 = cdiv(N1, NT), NI2 = cdiv(N2, NT), NI3 = cdiv(N3, NT);
   // tensor memory: columns [0, 2A) x at the pass-1 item, [ACC0, ACC0 + 2A) the accumulators
   constexpr bool TM = iter_cols_tmem(H);
   constexpr int ACC0 = (2 * A + 15) / 16 * 16;
   constexpr uint32_t TCOLS = (ACC0 + 2 * A <= 32) ? 32u : (ACC0 + 2 * A <= 64) ? 64u : 128u;
-  static_assert(!TM || (N1 == kColNT && N3 == kColNT && ACC0 + 2 * A <= 128), "one whole item per thread");
+  static_assert(!TM || (N1 == kColNT && N3 == kColNT && NI1 == 1 && NI3 == 1 && ACC0 + 2 * A <= 128),
+                "one pass-1 and one pass-3 item on each thread of warps 0-3");
   __shared__ uint32_t tslot;
   extern __shared__ float4 smem4[];
   float2* Sb = reinterpret_cast<float2*>(smem4) + L::S_OFF;
@@ -233,7 +255,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   float2* tws = reinterpret_cast<float2*>(smem4) + L::TW_OFF;
   int* rcode = reinterpret_cast<int*>(reinterpret_cast<float2*>(smem4) + L::F2_END);
   double* sred = reinterpret_cast<double*>(rcode + H);
-  float* fm = reinterpret_cast<float*>(sred + kColNT / 32);
+  float* fm = reinterpret_cast<float*>(sred + NT / 32);
   namespace cgr = cooperative_groups;
   cgr::cluster_group cluster = cgr::this_cluster();
 
@@ -256,7 +278,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   // are staged before the dependency wait
   // this thread's 16-byte granules of an S tile: rows srow + i*RSTEP, columns
   // 2*spart, 2*spart + 1 (the granule pattern repeats every RSTEP rows)
-  constexpr int GPR = kWB / 2, RSTEP = kColNT / GPR;
+  constexpr int GPR = kWB / 2, RSTEP = NT / GPR;
   const int srow = t / GPR, spart = t % GPR;
   const float2* const s_src0 = a.S + size_t(srow) * W + w0 + 2 * spart;
   const float2* const t_src0 = a.T + size_t(rowbase) * C * W + w0;
@@ -269,7 +291,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
       for (int i = 0; i < H / RSTEP; ++i) cp_async16(d0 + i * RSTEP * kWB, src + size_t(i) * RSTEP * W);
     } else {
       const float2* src = a.S + size_t(c) * N + w0;
-      for (int q = t; q < H * GPR; q += kColNT) {
+      for (int q = t; q < H * GPR; q += NT) {
         const int row = q / GPR, part = q % GPR;
         cp_async16(dst + row * kWB + 2 * part, src + size_t(row) * W + 2 * part);
       }
@@ -279,7 +301,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
     if (staged) {
       const float2* src = t_src0 + size_t(c) * W;
       float2* dst = Yb + buf * RCAP * kWB;
-      for (int q = t; q < nrows * (kWB / 2); q += kColNT) {
+      for (int q = t; q < nrows * (kWB / 2); q += NT) {
         const int j = q / (kWB / 2), part = q % (kWB / 2);
         cp_async16(dst + j * kWB + 2 * part, src + size_t(j) * C * W + 2 * part);
       }
@@ -292,7 +314,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   cp_async_commit();
   // row codes: j >= 0 fully sampled kept row j; -2 - j kept row j without
   // samples (data only); -1 not kept
-  for (int i = t; i < H; i += kColNT) {
+  for (int i = t; i < H; i += NT) {
     const int j = a.rowmap[f * H + i];
     rcode[i] = (j < 0) ? -1 : (a.row_full[rowbase + j] ? j : -2 - j);
   }
@@ -300,7 +322,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   // pairs: row s, entry k1 = w_H^(s*k1) (forward first pass) and row k1,
   // entry k1' = w_H^(k1*k1') (inverse first pass); the global table holds them
   // as [k1*B + s] and [H + k1'*A + k1]
-  for (int d = t; d < L::TWI_OFF + A * L::TWI; d += kColNT) {
+  for (int d = t; d < L::TWI_OFF + A * L::TWI; d += NT) {
     if (d < L::TWI_OFF) {
       const int s = d / L::TWF, k1 = d % L::TWF;
       if (k1 < A) tws[d] = __ldg(a.twH + k1 * B + s);
@@ -359,7 +381,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   float2 xv[NI1][A];
 #pragma unroll
   for (int ii = 0; ii < NI1; ++ii) {
-    const int i = t + ii * kColNT;
+    const int i = t + ii * NT;
     if (i < N1) {
       const int w = i % kWB, s = i / kWB;
 #pragma unroll
@@ -373,7 +395,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
 #pragma unroll
     for (int k2 = 0; k2 < A; ++k2) acc[ii][k2] = make_float2(0.f, 0.f);
   if constexpr (TM) {  // x and the zeroed accumulators move to tensor memory for the coil loop
-    tmem_pieces<2 * A>([&](auto oc, auto nc) {
+    if (t < N1) tmem_pieces<2 * A>([&](auto oc, auto nc) {
       constexpr int o = decltype(oc)::value, n = decltype(nc)::value;
       float xf[n], zf[n];
 #pragma unroll
@@ -385,7 +407,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
       tmem_st_n<n>(tl + o, xf);
       tmem_st_n<n>(tl + ACC0 + o, zf);
     });
-    tc::tmem_wait_st();
+    if (t < N1) tc::tmem_wait_st();
   }
   const float s_row = a.s_row;
   float racc = 0.f;
@@ -395,8 +417,8 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
 #pragma unroll
   for (int ii = 0; ii < NI2; ++ii) {
     kept[ii] = 0u;
-    const int k1 = (t + ii * kColNT) / kWB;
-    if (t + ii * kColNT < N2) {
+    const int k1 = (t + ii * NT) / kWB;
+    if (t + ii * NT < N2) {
 #pragma unroll
       for (int k2 = 0; k2 < B; ++k2) kept[ii] |= (rcode[k1 + A * k2] != -1 ? 1u : 0u) << k2;
     }
@@ -416,7 +438,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
     // forward pass 1: S_c x_f, DFT_A, twiddles
 #pragma unroll
     for (int ii = 0; ii < NI1; ++ii) {
-      const int i = t + ii * kColNT;
+      const int i = t + ii * NT;
       if (i < N1) {
         const int w = i % kWB, s = i / kWB;
         float2 v[A];
@@ -443,7 +465,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
     float2 r[NI2][B];
 #pragma unroll
     for (int ii = 0; ii < NI2; ++ii) {
-      const int i = t + ii * kColNT;
+      const int i = t + ii * NT;
       if (i < N2) {
         const int w = i % kWB, k1 = i / kWB;
 #pragma unroll
@@ -467,7 +489,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
     // inverse pass 1 on the same items: DFT_B over rows A*n1 + k1, twiddles
 #pragma unroll
     for (int ii = 0; ii < NI2; ++ii) {
-      const int i = t + ii * kColNT;
+      const int i = t + ii * NT;
       if (i < N2) {
         const int w = i % kWB, k1 = i / kWB;
         dft<B>(r[ii]);
@@ -480,7 +502,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
     // inverse pass 2 (DFT_A: row k1' + B*k2) and conj(S_c) accumulation
 #pragma unroll
     for (int ii = 0; ii < NI3; ++ii) {
-      const int i = t + ii * kColNT;
+      const int i = t + ii * NT;
       if (i < N3) {
         const int w = i % kWB, k1p = i / kWB;
         float2 v[A];
@@ -521,8 +543,8 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
     }
   }
   if constexpr (TM) {  // x and the accumulators back to registers; the tensor memory is released
-    tc::tmem_wait_st();
-    tmem_pieces<2 * A>([&](auto oc, auto nc) {
+    if (t < N1) tc::tmem_wait_st();
+    if (t < N1) tmem_pieces<2 * A>([&](auto oc, auto nc) {
       constexpr int o = decltype(oc)::value, n = decltype(nc)::value;
       float xf[n], af[n];
       tmem_ld_n<n>(tl + o, xf);
@@ -539,19 +561,17 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   }
 
   // tTV objective partial sums over the tile, each CTA of the pair over half
-  // of its rows (n1 < A/2 for the first); not in fixup mode
+  // of its pass-1 items (s < B/2 for the first, whole warps); not in fixup mode
   float su2 = 0.f, sud = 0.f;
   if (!fix && !motion) {  // the motion-compensated form has them from k_mc_tv
     const float2* __restrict__ xm = xk + size_t((f + F - 1) % F) * N;
-    constexpr int NH = A / 2;
 #pragma unroll
     for (int ii = 0; ii < NI1; ++ii) {
-      const int i = t + ii * kColNT;
-      if (i < N1) {
+      const int i = t + ii * NT;
+      if (i < N1 && ((i / kWB < B / 2) == (half == 0))) {
         const int w = i % kWB, s = i / kWB;
 #pragma unroll
         for (int n1 = 0; n1 < A; ++n1) {
-          if ((n1 < NH) != (half == 0)) continue;
           const float2 d = csub(xv[ii][n1], xm[size_t(B * n1 + s) * W + w0 + w]);
           const float2 u = tv_normalize(d, inv_mu);
           su2 = fmaf(u.x, u.x, fmaf(u.y, u.y, su2));
@@ -569,7 +589,8 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
 #pragma unroll
   for (int ii = 0; ii < NI3; ++ii)
 #pragma unroll
-    for (int k2 = 0; k2 < A; ++k2) mine[(ii * A + k2) * kColNT + t] = acc[ii][k2];
+    for (int k2 = 0; k2 < A; ++k2)
+      if (t + ii * NT < N3) mine[(ii * A + k2) * L::XST + t] = acc[ii][k2];
   cluster.sync();
   const float2* other = cluster.map_shared_rank(mine, half ^ 1);
   constexpr int KH = A / 2;
@@ -578,8 +599,8 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   for (int ii = 0; ii < NI3; ++ii)
 #pragma unroll
     for (int k2 = 0; k2 < A; ++k2)
-      if (k2 >= kb && k2 < ke) {
-        const float2 o = other[(ii * A + k2) * kColNT + t];
+      if (k2 >= kb && k2 < ke && t + ii * NT < N3) {
+        const float2 o = other[(ii * A + k2) * L::XST + t];
         acc[ii][k2] = half ? cadd(o, acc[ii][k2]) : cadd(acc[ii][k2], o);
       }
   cluster.sync();
@@ -595,7 +616,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   constexpr int BATCH = A <= 16 ? 8 : 4;  // one round of loads for a CTA's 8 rows at A = 16
 #pragma unroll
   for (int ii = 0; ii < NI3; ++ii) {
-    const int i = t + ii * kColNT;
+    const int i = t + ii * NT;
     if (i < N3) {
       const int w = i % kWB, k1p = i / kWB;
 #pragma unroll
@@ -649,10 +670,10 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
 
   // fixed-slot partial sums: ||rho||^2 of this CTA, the tTV terms of the tile
   const int blk = f * gridDim.x + blockIdx.x;
-  const double pr = block_sum<kColNT>(double(racc), sred);
+  const double pr = block_sum<NT>(double(racc), sred);
   if (!motion) {  // the motion-compensated form's come from k_mc_tv, in the same buffer
-    const double t1 = block_sum<kColNT>(double(su2), sred);
-    const double t2 = block_sum<kColNT>(double(sud), sred);
+    const double t1 = block_sum<NT>(double(su2), sred);
+    const double t2 = block_sum<NT>(double(sud), sred);
     if (t == 0) {
       a.part_tv[2 * (2 * blk + half)] = t1;
       a.part_tv[2 * (2 * blk + half) + 1] = t2;
@@ -660,7 +681,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(kColNT, iter_cols_mi
   }
   if (t == 0) a.part_r[2 * blk + half] = pr;
   if (rowlocal_last_cta(bm.ctl, inst, 2u * gridDim.x * unsigned(F)))
-    rowlocal_finish<kColNT>(a, st, bm.ctl, inst, it, apk, motion ? a.ntv : 2 * F * int(gridDim.x),
+    rowlocal_finish<NT>(a, st, bm.ctl, inst, it, apk, motion ? a.ntv : 2 * F * int(gridDim.x),
                             2 * F * int(gridDim.x), sred, fm);
 }
 
