@@ -581,8 +581,33 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(iter_cols_threads(H)
     }
   }
 
-  // Sum the two halves' accumulators through distributed shared memory; each
-  // CTA finishes half of the tile's rows (k2 < A/2 for the first).
+  // This CTA finishes half of the tile's rows (k2 < A/2 for the first).  With
+  // first factors up to 16 the update's operands at those rows (x_k and its
+  // neighbouring frames, w_k, x_ref: independent of the accumulators) are
+  // loaded now, so that they arrive during the cluster exchange below.
+  constexpr int KH = A / 2, KM = A - KH;
+  const int kb = half ? KH : 0, ke = half ? A : KH;
+  const size_t offm = size_t((f + F - 1) % F) * N, off0 = size_t(f) * N, offp = size_t((f + 1) % F) * N;
+  constexpr bool PRE = !MOTION && NI3 == 1 && A <= 16;
+  float2 pxa[PRE ? KM : 1], pxm[PRE ? KM : 1], pxp[PRE ? KM : 1], pwo[PRE ? KM : 1], pxr[PRE ? KM : 1];
+  if constexpr (PRE) {
+    if (t < N3) {
+      const int w = t % kWB, k1p = t / kWB;
+#pragma unroll
+      for (int k = 0; k < KM; ++k) {
+        if (kb + k < ke) {
+          const size_t p = size_t(k1p + B * (kb + k)) * W + w0 + w;
+          pxa[k] = xk[off0 + p];
+          pxm[k] = xk[offm + p];
+          pxp[k] = xk[offp + p];
+          pwo[k] = wk[off0 + p];
+          pxr[k] = a.xref[off0 + p];
+        }
+      }
+    }
+  }
+
+  // Sum the two halves' accumulators through distributed shared memory.
   cp_async_wait<0>();
   __syncthreads();
   float2* mine = Sb;
@@ -593,8 +618,6 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(iter_cols_threads(H)
       if (t + ii * NT < N3) mine[(ii * A + k2) * L::XST + t] = acc[ii][k2];
   cluster.sync();
   const float2* other = cluster.map_shared_rank(mine, half ^ 1);
-  constexpr int KH = A / 2;
-  const int kb = half ? KH : 0, ke = half ? A : KH;
 #pragma unroll
   for (int ii = 0; ii < NI3; ++ii)
 #pragma unroll
@@ -608,14 +631,51 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(iter_cols_threads(H)
   // tTV gradient and Nesterov update of this CTA's rows
   if constexpr (motion) grid_dep_wait();  // M^T(tTVadj u) of x_k
   const float s_adj = a.s_adj;
-  const size_t offm = size_t((f + F - 1) % F) * N, off0 = size_t(f) * N, offp = size_t((f + 1) % F) * N;
   const float lambda = st->lambda, nLmu1 = -st->Lmu1;
   const float apk = fix ? st->apk : 0.5f * (float(itx) + 1.0f);  // nesta_scalar_step's weights for k = itx
   const float tauk = fix ? st->tauk : 2.0f / (float(itx) + 3.0f);
   const float omt = 1.0f - tauk;
+  // the update of one pixel: x_k, its neighbours in time (or M^T(tTVadj u)),
+  // w_k, x_ref and the accumulated A^H r
+  auto update = [&](size_t p, float2 xa, float2 xm, float2 xp, float2 wo, float2 xr, float2 accv) {
+    // operator_tTVadj gives u_{f+1} - u_f of the normalised temporal
+    // differences; NestaUp negates it, scales by lambda, adds A^H r
+    float2 adj;
+    if constexpr (motion) {
+      adj = xm;
+    } else {
+      const float2 u0 = tv_normalize(csub(xa, xm), inv_mu);
+      const float2 u1 = tv_normalize(csub(xp, xa), inv_mu);
+      adj = csub(u1, u0);
+    }
+    const float2 ares = cscale(accv, s_adj);
+    const float2 df = make_float2(__fadd_rn(__fmul_rn(-adj.x, lambda), ares.x),
+                                  __fadd_rn(__fmul_rn(-adj.y, lambda), ares.y));
+    const float2 yk = make_float2(fmaf(nLmu1, df.x, xa.x), fmaf(nLmu1, df.y, xa.y));
+    const float2 wnv = make_float2(fmaf(apk, df.x, wo.x), fmaf(apk, df.y, wo.y));
+    const float2 zk = make_float2(fmaf(nLmu1, wnv.x, xr.x), fmaf(nLmu1, wnv.y, xr.y));
+    wn[off0 + p] = wnv;
+    xn[off0 + p] = make_float2(fmaf(omt, yk.x, tauk * zk.x), fmaf(omt, yk.y, tauk * zk.y));
+  };
+  if constexpr (PRE) {
+    if (t < N3) {
+      float2 af[KM];  // the accumulators of this CTA's rows
+      if (half == 0) {
+#pragma unroll
+        for (int k = 0; k < KH; ++k) af[k] = acc[0][k];
+      } else {
+#pragma unroll
+        for (int k = 0; k < KM; ++k) af[k] = acc[0][KH + k];
+      }
+      const int w = t % kWB, k1p = t / kWB;
+#pragma unroll
+      for (int k = 0; k < KM; ++k)
+        if (kb + k < ke) update(size_t(k1p + B * (kb + k)) * W + w0 + w, pxa[k], pxm[k], pxp[k], pwo[k], pxr[k], af[k]);
+    }
+  }
   constexpr int BATCH = A <= 16 ? 8 : 4;  // one round of loads for a CTA's 8 rows at A = 16
 #pragma unroll
-  for (int ii = 0; ii < NI3; ++ii) {
+  for (int ii = 0; ii < (PRE ? 0 : NI3); ++ii) {
     const int i = t + ii * NT;
     if (i < N3) {
       const int w = i % kWB, k1p = i / kWB;
@@ -641,27 +701,8 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(iter_cols_threads(H)
 #pragma unroll
         for (int b = 0; b < BATCH; ++b) {
           const int k2 = k0 + b;
-          if (k2 < A && k2 >= kb && k2 < ke) {
-            const size_t p = size_t(k1p + B * k2) * W + w0 + w;
-            // operator_tTVadj gives u_{f+1} - u_f of the normalised temporal
-            // differences; NestaUp negates it, scales by lambda, adds A^H r
-            float2 adj;
-            if constexpr (motion) {
-              adj = xm[b];
-            } else {
-              const float2 u0 = tv_normalize(csub(xa[b], xm[b]), inv_mu);
-              const float2 u1 = tv_normalize(csub(xp[b], xa[b]), inv_mu);
-              adj = csub(u1, u0);
-            }
-            const float2 ares = cscale(acc[ii][k2], s_adj);
-            const float2 df = make_float2(__fadd_rn(__fmul_rn(-adj.x, lambda), ares.x),
-                                          __fadd_rn(__fmul_rn(-adj.y, lambda), ares.y));
-            const float2 yk = make_float2(fmaf(nLmu1, df.x, xa[b].x), fmaf(nLmu1, df.y, xa[b].y));
-            const float2 wnv = make_float2(fmaf(apk, df.x, wo[b].x), fmaf(apk, df.y, wo[b].y));
-            const float2 zk = make_float2(fmaf(nLmu1, wnv.x, xr[b].x), fmaf(nLmu1, wnv.y, xr[b].y));
-            wn[off0 + p] = wnv;
-            xn[off0 + p] = make_float2(fmaf(omt, yk.x, tauk * zk.x), fmaf(omt, yk.y, tauk * zk.y));
-          }
+          if (k2 < A && k2 >= kb && k2 < ke)
+            update(size_t(k1p + B * k2) * W + w0 + w, xa[b], xm[b], xp[b], wo[b], xr[b], acc[ii][k2]);
         }
       }
     }
