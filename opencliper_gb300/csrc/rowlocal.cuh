@@ -588,7 +588,11 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(iter_cols_threads(H)
   constexpr int KH = A / 2, KM = A - KH;
   const int kb = half ? KH : 0, ke = half ? A : KH;
   const size_t offm = size_t((f + F - 1) % F) * N, off0 = size_t(f) * N, offp = size_t((f + 1) % F) * N;
-  constexpr bool PRE = !MOTION && NI3 == 1 && A <= 16;
+  // (x_k, w_k and x_ref for every form with one pass-3 item per thread and
+  // A <= 24 at 168 registers a thread; the neighbouring frames too for the
+  // plain form at A <= 16; the rest after the exchange)
+  constexpr bool PRE = NI3 == 1 && (A <= 16 || (A <= 24 && NT == kColNT));
+  constexpr bool PRE_T = PRE && !MOTION && A <= 16;
   float2 pxa[PRE ? KM : 1], pxm[PRE ? KM : 1], pxp[PRE ? KM : 1], pwo[PRE ? KM : 1], pxr[PRE ? KM : 1];
   if constexpr (PRE) {
     if (t < N3) {
@@ -598,8 +602,10 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(iter_cols_threads(H)
         if (kb + k < ke) {
           const size_t p = size_t(k1p + B * (kb + k)) * W + w0 + w;
           pxa[k] = xk[off0 + p];
-          pxm[k] = xk[offm + p];
-          pxp[k] = xk[offp + p];
+          if constexpr (PRE_T) {
+            pxm[k] = xk[offm + p];
+            pxp[k] = xk[offp + p];
+          }
           pwo[k] = wk[off0 + p];
           pxr[k] = a.xref[off0 + p];
         }
@@ -668,6 +674,20 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(iter_cols_threads(H)
         for (int k = 0; k < KM; ++k) af[k] = acc[0][KH + k];
       }
       const int w = t % kWB, k1p = t / kWB;
+      if constexpr (!PRE_T) {
+#pragma unroll
+        for (int k = 0; k < KM; ++k) {
+          if (kb + k < ke) {
+            const size_t p = size_t(k1p + B * (kb + k)) * W + w0 + w;
+            if constexpr (motion) {
+              pxm[k] = a.grad_ext[off0 + p];  // M^T (tTVadj u) of the motion-compensated form
+            } else {
+              pxm[k] = xk[offm + p];
+              pxp[k] = xk[offp + p];
+            }
+          }
+        }
+      }
 #pragma unroll
       for (int k = 0; k < KM; ++k)
         if (kb + k < ke) update(size_t(k1p + B * (kb + k)) * W + w0 + w, pxa[k], pxm[k], pxp[k], pwo[k], pxr[k], af[k]);
