@@ -45,6 +45,40 @@ namespace gbn {
 
 constexpr int kStatusRowStructure = 7;  // NestaDevState::status: a kept row is partly sampled (row-local path)
 
+// Block-wide sums of three doubles per thread, in thread 0: each summed as
+// block_sum sums one (same order), with one pair of barriers for the three.
+// sred holds 3 * NT/32 doubles.
+template <int NT>
+__device__ __forceinline__ void rowlocal_block_sum3(double a, double b, double c, double* sred, double* ra, double* rb,
+                                                    double* rc) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    a += __shfl_down_sync(0xffffffffu, a, o);
+    b += __shfl_down_sync(0xffffffffu, b, o);
+    c += __shfl_down_sync(0xffffffffu, c, o);
+  }
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  __syncthreads();
+  if (lane == 0) {
+    sred[wid] = a;
+    sred[NT / 32 + wid] = b;
+    sred[2 * (NT / 32) + wid] = c;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double ta = 0.0, tb = 0.0, tc = 0.0;
+#pragma unroll
+    for (int i = 0; i < NT / 32; ++i) {
+      ta += sred[i];
+      tb += sred[NT / 32 + i];
+      tc += sred[2 * (NT / 32) + i];
+    }
+    *ra = ta;
+    *rb = tb;
+    *rc = tc;
+  }
+}
+
 // Counts this CTA as finished for instance `inst` (after thread 0 stored its
 // partial sums) and tells every thread whether it was the instance's last of
 // `total` CTAs.  All threads call it.  Only thread 0's stores need to be
@@ -175,7 +209,7 @@ constexpr int iter_cols_bytes(int L) {
   const int a = split_a(L), b = split_b(L);
   const int ex = (a * col_ks(b) > b * col_ks(a)) ? a * col_ks(b) : b * col_ks(a);
   return (iter_cols_sbufs(L) * L * kWB + 2 * iter_cols_rcap(L) * kWB + ex + b * (a + 2) + a * (b + 2)) * 8 + L * 4 +
-         (iter_cols_threads(L) / 32) * 8 + kFmeanCopy * 4 + 16;
+         3 * (iter_cols_threads(L) / 32) * 8 + kFmeanCopy * 4 + 16;
 }
 
 template <int H>
@@ -199,7 +233,7 @@ struct IterColsSmem {
   static constexpr int TW_OFF = EX_OFF + EXN;
   static constexpr int TWI_OFF = B * TWF;                // inverse rows, from TW_OFF
   static constexpr int F2_END = TW_OFF + TWI_OFF + A * TWI;
-  static constexpr int BYTES = F2_END * 8 + H * 4 + (NT / 32) * 8 + kFmeanCopy * 4 + 16;
+  static constexpr int BYTES = F2_END * 8 + H * 4 + 3 * (NT / 32) * 8 + kFmeanCopy * 4 + 16;
   static_assert(NI3 * A * XST <= SB * H * kWB, "accumulator exchange must fit the S buffers");
   static_assert(BYTES == iter_cols_bytes(H), "layout and byte count agree");
   static_assert(TW_OFF % 2 == 0, "twiddle rows start on 16-byte boundaries");
@@ -255,7 +289,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(iter_cols_threads(H)
   float2* tws = reinterpret_cast<float2*>(smem4) + L::TW_OFF;
   int* rcode = reinterpret_cast<int*>(reinterpret_cast<float2*>(smem4) + L::F2_END);
   double* sred = reinterpret_cast<double*>(rcode + H);
-  float* fm = reinterpret_cast<float*>(sred + NT / 32);
+  float* fm = reinterpret_cast<float*>(sred + 3 * (NT / 32));
   namespace cgr = cooperative_groups;
   cgr::cluster_group cluster = cgr::this_cluster();
 
@@ -620,8 +654,8 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(iter_cols_threads(H)
 #pragma unroll
   for (int ii = 0; ii < NI3; ++ii)
 #pragma unroll
-    for (int k2 = 0; k2 < A; ++k2)
-      if (t + ii * NT < N3) mine[(ii * A + k2) * L::XST + t] = acc[ii][k2];
+    for (int k2 = 0; k2 < A; ++k2)  // the rows the other CTA finishes
+      if ((k2 < kb || k2 >= ke) && t + ii * NT < N3) mine[(ii * A + k2) * L::XST + t] = acc[ii][k2];
   cluster.sync();
   const float2* other = cluster.map_shared_rank(mine, half ^ 1);
 #pragma unroll
@@ -731,16 +765,15 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(iter_cols_threads(H)
 
   // fixed-slot partial sums: ||rho||^2 of this CTA, the tTV terms of the tile
   const int blk = f * gridDim.x + blockIdx.x;
-  const double pr = block_sum<NT>(double(racc), sred);
-  if (!motion) {  // the motion-compensated form's come from k_mc_tv, in the same buffer
-    const double t1 = block_sum<NT>(double(su2), sred);
-    const double t2 = block_sum<NT>(double(sud), sred);
-    if (t == 0) {
+  double pr, t1, t2;
+  rowlocal_block_sum3<NT>(double(racc), double(su2), double(sud), sred, &pr, &t1, &t2);
+  if (t == 0) {
+    if (!motion) {  // the motion-compensated form's come from k_mc_tv, in the same buffer
       a.part_tv[2 * (2 * blk + half)] = t1;
       a.part_tv[2 * (2 * blk + half) + 1] = t2;
     }
+    a.part_r[2 * blk + half] = pr;
   }
-  if (t == 0) a.part_r[2 * blk + half] = pr;
   if (rowlocal_last_cta(bm.ctl, inst, 2u * gridDim.x * unsigned(F)))
     rowlocal_finish<NT>(a, st, bm.ctl, inst, it, apk, motion ? a.ntv : 2 * F * int(gridDim.x),
                             2 * F * int(gridDim.x), sred, fm);
