@@ -666,7 +666,9 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(iter_cols_threads(H)
         const float2 o = other[(ii * A + k2) * L::XST + t];
         acc[ii][k2] = half ? cadd(o, acc[ii][k2]) : cadd(acc[ii][k2], o);
       }
-  cluster.sync();
+  // the partner may still be reading this CTA's rows: signal that this CTA's
+  // reads are done now, and wait for the partner's only before exiting
+  asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
 
   // tTV gradient and Nesterov update of this CTA's rows
   if constexpr (motion) grid_dep_wait();  // M^T(tTVadj u) of x_k
@@ -761,6 +763,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(iter_cols_threads(H)
       }
     }
   }
+  asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
   if (fix) return;
 
   // fixed-slot partial sums: ||rho||^2 of this CTA, the tTV terms of the tile
