@@ -17,8 +17,9 @@
 //   A^H r = (sqrt(N)/N) sum_c conj(S_c) IDFT_H(rho)
 // and the whole inner iteration runs in one kernel.
 //
-// k_iter_cols<H>: grid (W/kWB, 2, frames) in clusters of 2 along y; CTA =
-// (frame, 8 columns, half of the coils).  Per coil: forward column DFT of
+// k_iter_cols<H, MOTION>: grid (W/kWB, 2, frames) in clusters of 2 along y;
+// CTA = (frame, 8 columns, half of the coils), 128 threads (160 at H = 288,
+// 320).  Per coil: forward column DFT of
 // S_c x_f (dit2<A,B>), residual on the kept rows, inverse column DFT
 // (dit2<B,A> of the conjugate) and conj(S_c) accumulation.  The forward
 // pass-2 item (w, k1) holds rows k1 + A*k2, exactly the rows the inverse
@@ -26,9 +27,12 @@
 // coil halves are summed through distributed shared memory, then the tTV
 // gradient (temporalTV.cl:78-107 with NestaUp's negation, vectorNormalization.cl
 // :42-56) and the Nesterov update (NestaUp.cpp:758-875) finish each pixel.
-// The tTV objective terms (Scnrm2, Cdotc of NestaUp.cpp:686-691) and ||r||^2
-// are written as fixed-slot partial sums; the last CTA of an instance reduces
-// them in fixed order and runs the scalar recurrence (nesta_scalar_step).
+// The tTV objective terms (Scnrm2, Cdotc of NestaUp.cpp:686-691; each CTA of
+// the pair over half of the tile) and ||r||^2 are written as fixed-slot
+// partial sums; the last CTA of an instance reduces them in fixed order and
+// runs the scalar recurrence (nesta_scalar_step).  Register budgets per length
+// (x and the accumulators in registers or in tensor memory) are set by
+// iter_cols_tmem / iter_cols_threads / iter_cols_min_blocks below.
 //
 // The update of iteration k uses apk = (k+1)/2 and tauk = 2/(k+3), what the
 // scalar recurrence yields unless the stopping test fires for the second time
