@@ -203,9 +203,13 @@ constexpr int iter_cols_sbufs(int L) { return iter_cols_tmem(L) ? 1 : 2; }
 // threads at fewer CTAs per SM measured slower (H = 384: 288 us per iteration
 // with 192 threads at two CTAs, against 280 us).  The pass-1 and pass-3 items
 // (kWB * B = 128) stay on warps 0-3, whose tensor-memory lanes hold their state.
+// Short columns with at most 64 pass-2 items (A <= 8: H = 64, 96, 128 ...)
+// run 64 threads with two pass-1 and pass-3 items each, so no thread idles in
+// pass 2, at twice the CTAs per SM.
 constexpr int iter_cols_threads(int L) {
   return (iter_cols_tmem(L) && (kWB * split_a(L) + 31) / 32 * 32 * 3 * 128 <= 65536) ? (kWB * split_a(L) + 31) / 32 * 32
-                                                                                     : kColNT;
+         : (!iter_cols_tmem(L) && kWB * split_a(L) <= 64 && kWB * split_b(L) == kColNT) ? 64
+                                                                                        : kColNT;
 }
 
 // Shared-memory bytes of k_iter_cols<L> (the layout of IterColsSmem<L>).
@@ -258,6 +262,7 @@ constexpr int iter_cols_min_blocks(int H) {
     const int m = by_smem < by_regs ? by_smem : by_regs;
     return m < 3 ? m : 3;
   }
+  if (iter_cols_threads(H) == 64) return 6;
   return split_a(H) <= 16 ? 3 : (iter_cols_bytes(H) + 1024 <= 114 * 1024 ? 2 : 1);
 }
 
