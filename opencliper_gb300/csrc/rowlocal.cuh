@@ -676,8 +676,9 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(iter_cols_threads(H)
         acc[ii][k2] = half ? cadd(o, acc[ii][k2]) : cadd(acc[ii][k2], o);
       }
   // the partner may still be reading this CTA's rows: signal that this CTA's
-  // reads are done now, and wait for the partner's only before exiting
-  asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
+  // reads are done now (their values are already consumed above, so the
+  // arrive needs no release fence), and wait for the partner's before exiting
+  asm volatile("barrier.cluster.arrive.relaxed.aligned;\n" ::: "memory");
 
   // tTV gradient and Nesterov update of this CTA's rows
   if constexpr (motion) grid_dep_wait();  // M^T(tTVadj u) of x_k
