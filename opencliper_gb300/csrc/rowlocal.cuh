@@ -624,13 +624,27 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(iter_cols_threads(H)
     }
   }
 
-  // This CTA finishes half of the tile's rows (k2 < A/2 for the first).  With
-  // first factors up to 16 the update's operands at those rows (x_k and its
-  // neighbouring frames, w_k, x_ref: independent of the accumulators) are
-  // loaded now, so that they arrive during the cluster exchange below.
+  // This CTA finishes half of the tile's rows (k2 < A/2 for the first).  The
+  // update's operands at those rows (x_k and its neighbouring frames, w_k,
+  // x_ref: independent of the accumulators) are requested between the two
+  // halves of the cluster barrier below, so that they arrive during the
+  // exchange.
   constexpr int KH = A / 2, KM = A - KH;
   const int kb = half ? KH : 0, ke = half ? A : KH;
   const size_t offm = size_t((f + F - 1) % F) * N, off0 = size_t(f) * N, offp = size_t((f + 1) % F) * N;
+  // Sum the two halves' accumulators through distributed shared memory.
+  cp_async_wait<0>();
+  __syncthreads();
+  float2* mine = Sb;
+#pragma unroll
+  for (int ii = 0; ii < NI3; ++ii)
+#pragma unroll
+    for (int k2 = 0; k2 < A; ++k2)  // the rows the other CTA finishes
+      if ((k2 < kb || k2 >= ke) && t + ii * NT < N3) mine[(ii * A + k2) * L::XST + t] = acc[ii][k2];
+  // the cluster barrier in two halves: the arrive publishes this CTA's rows
+  // (release), the update's operands are requested while the partner gets
+  // there, and the wait makes the partner's rows visible (acquire)
+  asm volatile("barrier.cluster.arrive.release.aligned;\n" ::: "memory");
   // (x_k, w_k and x_ref for every form with one pass-3 item per thread and
   // A <= 24 at 168 registers a thread; the neighbouring frames too for the
   // plain form at A <= 16; the rest after the exchange)
@@ -656,16 +670,7 @@ __global__ void __cluster_dims__(1, 2, 1) __launch_bounds__(iter_cols_threads(H)
     }
   }
 
-  // Sum the two halves' accumulators through distributed shared memory.
-  cp_async_wait<0>();
-  __syncthreads();
-  float2* mine = Sb;
-#pragma unroll
-  for (int ii = 0; ii < NI3; ++ii)
-#pragma unroll
-    for (int k2 = 0; k2 < A; ++k2)  // the rows the other CTA finishes
-      if ((k2 < kb || k2 >= ke) && t + ii * NT < N3) mine[(ii * A + k2) * L::XST + t] = acc[ii][k2];
-  cluster.sync();
+  asm volatile("barrier.cluster.wait.acquire.aligned;\n" ::: "memory");
   const float2* other = cluster.map_shared_rank(mine, half ^ 1);
 #pragma unroll
   for (int ii = 0; ii < NI3; ++ii)
