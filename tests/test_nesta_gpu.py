@@ -134,6 +134,42 @@ def test_row_local_iteration_matches_three_pass(ctx, W, H, F, C, Rr, prm):
     assert err <= 1e-4
 
 
+# the library's FFT lengths (gbn_supported_lengths), and those whose first
+# factor exceeds every per-thread budget of the row-local kernel (200 = 25 x 8,
+# 216 = 27 x 8, 504 = 63 x 8): three-pass only
+LENGTHS = [8, 16, 24, 32, 40, 48, 56, 64, 72, 80, 96, 112, 120, 128, 144, 160, 168, 192, 200, 216, 224, 240, 256,
+           280, 288, 320, 336, 360, 384, 392, 400, 432, 448, 480, 504, 512]
+THREE_PASS_ONLY = {200, 216, 504}
+
+
+@pytest.mark.parametrize("H", LENGTHS)
+def test_row_local_every_column_length(ctx, H):
+    """Every supported column length H (8 ... 512, each with its own
+    instantiation of the row-local kernel: factors, threads per CTA, register
+    or tensor-memory state, several items per thread where the second factor
+    exceeds 16): the row-local iteration against the three-pass iteration on
+    the same problem, 10 iterations.  The three lengths without a row-local
+    form run the three-pass iteration with the knob on or off, bit for bit
+    alike."""
+    assert g.supported_lengths() == LENGTHS
+    p = synth.make_problem(64, H, 3, 3, 8, seed=H)
+    assert np.isfinite(p.S).all() and np.isfinite(p.y).all()
+    prm = {**FIXED, "maxIter": 10}
+    o1, st1, n1 = _run_counting_iter(ctx, p, prm, 1)
+    o0, st0, n0 = _run_counting_iter(ctx, p, prm, 0)
+    assert n0 == 0
+    assert (n1 > 0) == (H not in THREE_PASS_ONLY), (H, n1)
+    assert st1["status"] == 0 and st0["status"] == 0
+    assert st1["inner_iters"] == st0["inner_iters"] == 10
+    assert np.isfinite(o1).all()
+    if H in THREE_PASS_ONLY:
+        assert np.array_equal(o1, o0)
+    else:
+        err = R.nrmse(o1, o0)
+        print(f"H={H}: row-local vs three-pass NRMSE {err:.3e}")
+        assert err <= 1e-5  # measured 5.5e-8 ... 3.6e-7
+
+
 def _run_counting_iter(ctx, p, prm, row_local: int):
     """Runs with the tuning knob row_local set; returns the image, the stats
     and how many row-local iteration kernels ran (event profile)."""
