@@ -18,6 +18,7 @@ from oracle import drand48
 from oracle import motion as M
 from oracle import nesta_ref as R
 from tests.conftest import rel_l2
+from tests.test_nesta_gpu import LENGTHS, THREE_PASS_ONLY
 
 pytestmark = pytest.mark.gpu
 
@@ -115,3 +116,47 @@ def test_motion_row_local_matches_three_pass(ctx):
     err = R.nrmse(outs[0], outs[1])
     print(f"motion row-local vs three-pass: NRMSE {err:.3e}")
     assert 0 < err <= 1e-4
+
+
+@pytest.mark.parametrize("H", [h for h in LENGTHS if h >= 16 and h not in THREE_PASS_ONLY])
+def test_motion_row_local_every_column_length(ctx, H):
+    """The motion-compensated row-local kernel (k_iter_cols<H, true>: the
+    update reads M^T g instead of the neighbouring frames, in the operand
+    prefetch or the batched loads as the length's budget chooses) at every
+    column length that has a row-local form (from 16: the motion rectangle
+    needs room inside the margins), against the three-pass iteration, 10
+    iterations from the same starting image."""
+    W, F, C = 64, 3, 3
+    p = synth.make_problem(W, H, F, C, 8, seed=H + 1)
+    xn, xm, bb = synth.make_motion(W, H, F, seed=H)
+    dy, dS, dm = ctx.to_device(p.y), ctx.to_device(p.S), ctx.to_device(p.mask)
+    prob = g.Problem(ctx, dy, dS, dm)
+    x = ctx.empty((F, H, W), np.complex64)
+    try:
+        prob.run(g.nesta_params(**{**FIXED_MC, "maxIter": 10}), x)
+        x0 = x.get()
+        prob.set_motion(ctx.to_device(xn), ctx.to_device(xm), bb)
+        prm = g.nesta_params(**{**FIXED_MC, "maxIter": 10})
+        s0 = ctx.rand48()
+        outs, sts, iters = [], [], []
+        for rl in (1, 0):
+            ctx.set_tuning("row_local", rl)
+            ctx.seed48(s0)
+            x.set(x0)
+            ctx.profile(True)
+            ctx.profile_reset()
+            sts.append(prob.run(prm, x))
+            iters.append(ctx.profile_read().get("iter", (0, 0.0))[0])
+            ctx.profile(False)
+            outs.append(x.get())
+    finally:
+        ctx.profile(False)
+        ctx.set_tuning("row_local", 1)
+        prob.close()
+    assert iters[0] == 10 and iters[1] == 0
+    assert sts[0]["status"] == 0 and sts[1]["status"] == 0
+    assert sts[0]["inner_iters"] == sts[1]["inner_iters"] == 10
+    assert np.isfinite(outs[0]).all()
+    err = R.nrmse(outs[0], outs[1])
+    print(f"H={H}: motion row-local vs three-pass NRMSE {err:.3e}")
+    assert err <= 1e-5  # measured 4.6e-8 ... 6.4e-8
