@@ -74,16 +74,29 @@ def phantom_series(W: int, H: int, F: int, rng: np.random.Generator) -> np.ndarr
 
 
 def coil_maps(W: int, H: int, C: int) -> np.ndarray:
+    """C Gaussian coil sensitivities around the field of view, normalised to
+    sum |S_c|^2 = 1 at every pixel.  Far from every coil (images much longer
+    than wide) the Gaussians underflow; those pixels are normalised from
+    exponents shifted by their largest, which leaves the others unchanged."""
     fov = float(min(W, H))
     yy, xx = np.mgrid[0:H, 0:W].astype(np.float64)
-    S = np.empty((C, H, W), np.complex128)
+    expo = np.empty((C, H, W), np.float64)
+    ph = np.empty(C, np.complex128)
     for c in range(C):
         ang = 2 * np.pi * c / C
         px = W / 2 + 0.5 * fov * np.cos(ang)
         py = H / 2 + 0.5 * fov * np.sin(ang)
         sig = 0.4 * fov
-        S[c] = np.exp(-((xx - px) ** 2 + (yy - py) ** 2) / (2 * sig * sig)) * np.exp(1j * ang)
-    S /= np.sqrt(np.sum(np.abs(S) ** 2, axis=0, keepdims=True))
+        expo[c] = -((xx - px) ** 2 + (yy - py) ** 2) / (2 * sig * sig)
+        ph[c] = np.exp(1j * ang)
+    S = np.exp(expo) * ph[:, None, None]
+    nrm = np.sqrt(np.sum(np.abs(S) ** 2, axis=0, keepdims=True))
+    far = nrm[0] < 1e-150
+    if far.any():
+        Sf = np.exp(expo[:, far] - expo[:, far].max(axis=0)) * ph[:, None]
+        S[:, far] = Sf
+        nrm[0][far] = np.sqrt(np.sum(np.abs(Sf) ** 2, axis=0))
+    S /= nrm
     return S.astype(np.complex64)
 
 

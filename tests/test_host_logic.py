@@ -25,6 +25,14 @@ def test_synthetic_problem_properties():
     assert np.array_equal(p.mask, np.repeat((p.rowmask * 255).astype(np.uint8)[:, :, None], W, axis=2))
 
 
+@pytest.mark.parametrize("W,H,C", [(16, 512, 3), (512, 8, 4), (256, 256, 12)])
+def test_coil_maps_normalised_at_every_aspect_ratio(W, H, C):
+    """Pixels far from every coil (16 x 512) stay finite and normalised."""
+    S = synth.coil_maps(W, H, C)
+    assert S.shape == (C, H, W) and np.isfinite(S).all()
+    assert np.allclose(np.sum(np.abs(S.astype(np.complex128)) ** 2, axis=0), 1.0, atol=1e-6)
+
+
 def test_synthetic_problem_is_seeded():
     a = synth.make_problem(32, 32, 3, 2, 4, seed=9)
     b = synth.make_problem(32, 32, 3, 2, 4, seed=9)
