@@ -112,3 +112,35 @@ def test_gpus_flag_launches_one_rank_per_gpu(tmp_path, capfd):
     assert len(lines) == 1
     out = json.loads(lines[0])
     assert out["n_gpus"] == 2 and out["max"] == 2.0
+
+
+def test_reference_arm_line(monkeypatch):
+    """bench.py --impl reference: the line's contract (the reference's metric,
+    unit and config, the measured steps within the wall-clock budget, the
+    e2e object with no host-device copies, the cpu_baseline describing the
+    run).  The whole-reconstruction timing is stubbed: one reconstruction of
+    the headline workload takes ~17 s of CPU."""
+    import argparse
+
+    import bench
+    calls, clock = [], [0.0]
+
+    def fake_recon():
+        calls.append(1)
+        clock[0] += 0.25
+        return 0.25
+
+    monkeypatch.setattr(bench.time, "perf_counter", lambda: clock[0])
+    monkeypatch.setattr(bench, "cpu_port_recon", fake_recon)
+    monkeypatch.setattr(bench, "_ref_problem", lambda: None)
+    monkeypatch.setattr(bench, "REF_BUDGET_S", 0.6)
+    monkeypatch.delenv("WORLD_SIZE", raising=False)
+    out = bench.run_reference(argparse.Namespace(steps=5), bench.Dist())
+    assert out["impl"] == "reference" and out["metric"] == bench.METRIC and out["unit"] == bench.UNIT
+    assert out["config"] == bench.workload_config()
+    # one warm-up, then steps while the next one still fits the budget
+    assert out["steps_requested"] == 5 and out["steps"] == 2 and len(calls) == 3
+    assert out["value"] == 4.0 and out["ms_per_step"] == 250.0 and out["higher_is_better"] is True
+    assert out["e2e"] == {"value": 4.0, "unit": bench.UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}
+    cb = out["cpu_baseline"]
+    assert cb["kind"] == "port" and cb["value"] == 4.0 and cb["cores"] >= 1 and cb["sample"]
