@@ -39,6 +39,8 @@ def test_version_and_lengths(built_lib):
     assert g.lib().gbn_version() == 1
     lens = g.supported_lengths()
     assert lens[0] == 8 and lens[-1] == 512 and len(lens) == 36
+    from tests.test_nesta_gpu import LENGTHS
+    assert lens == LENGTHS  # the list the every-length GPU tests walk
     for L in lens:
         n = L
         for p in (2, 3, 5, 7):
