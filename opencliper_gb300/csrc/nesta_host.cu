@@ -921,7 +921,12 @@ int simple_recon(gbn_ctx* ctx, const float2* y, const float2* S, float2* x, int 
   void* scr = nullptr;
   const bool mine = ctx->scratch_user == kScratchSimple;
   const int rc = ctx_scratch(ctx, simple_recon_bytes(W, H, F, C), &scr, kScratchSimple);
-  if (rc != GBN_OK) return rc;
+  if (rc != GBN_OK) {
+    // a failed allocation freed the old scratch: a later one at the same
+    // address holds no tables
+    ctx->simple_key = gbn_ctx::SimpleKey{};
+    return rc;
+  }
   gbn_ctx::SimpleKey& k = ctx->simple_key;
   const bool same = mine && k.y == y && k.S == S && k.x == x && k.ws == scr && k.W == W && k.H == H && k.F == F &&
                     k.C == C;
