@@ -370,8 +370,8 @@ GBN_API int gbn_batch_stats(gbn_batch* b, int i, gbn_nesta_stats* stats);
 GBN_API int gbn_batch_groups(gbn_batch* b, int* groups, int* tensor_core_groups);
 /* Group g (0 <= g < groups) of a batch: its W, H, member count, the members'
  * batch indices (member_idx: room for 64, or NULL) and the inner iteration it
- * runs (path: one of GBN_PATH_*).  No reference counterpart (batches are the
- * the benchmark spec's form). */
+ * runs (path: one of GBN_PATH_*).  No reference counterpart (the reference
+ * solves one reconstruction per NestaUp::launch). */
 #define GBN_PATH_THREE_PASS 0       /* forward column, row and adjoint column passes, FP32 */
 #define GBN_PATH_THREE_PASS_TC 1    /* the same with the forward column pass on the tensor cores */
 #define GBN_PATH_ROW_LOCAL 2        /* one fused kernel per iteration (row masks), FP32 */

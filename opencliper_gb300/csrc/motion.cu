@@ -964,7 +964,7 @@ int nesta_run_mc(gbn_ctx* ctx, gbn_problem* P, const gbn_nesta_params* prm, floa
   const BatchMap bm = single_map(F, P->ctl);
   int rc;
   // the row-local iteration (rowlocal.cuh) takes problems whose kept rows are
-  // fully sampled or unsampled; the row analysis's verdict comes back to
+  // fully sampled or unsampled; the row analysis's result comes back to
   // pinned host memory while the setup is queued
   const bool check_rows = ctx->row_local && kh->iter_cols;
   if (check_rows && (rc = partial_flag_ready(ctx)) != GBN_OK) return rc;

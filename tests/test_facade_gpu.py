@@ -52,7 +52,7 @@ def test_facade_matches_c_abi(ctx, driver, tmp_path):
     normU_mc, iters_mc, status_mc = lines[1].split()
     assert lines[2] == "refused bound_box"
 
-    # the same through the C ABI (fresh drand48 state, like the driver's new context)
+    # the same through the C ABI (fresh drand48 state, like the facade program's new context)
     ctx.seed48(drand48.state_to_seed16v(drand48.DEFAULT_STATE))
     prm = g.nesta_params(lambda_i=1e-2, mu_f=3e-4, La=1.0, maxIntIter=4, maxIter=30, stoptest=1, miniter=7, tolVar=3e-4)
     x_c, st = g.nesta_run_host(ctx, p.y, p.S, p.mask, prm)
