@@ -49,7 +49,7 @@ extern "C" {
 enum {
   GBN_OK = 0,
   GBN_ERR_INVALID = -1,     /* bad argument (reference: std::invalid_argument) */
-  GBN_ERR_UNSUPPORTED = -2, /* size/shape outside what this build implements */
+  GBN_ERR_UNSUPPORTED = -2, /* size/shape outside what this library implements */
   GBN_ERR_CUDA = -3,        /* CUDA runtime failure (reference: CLError) */
   GBN_ERR_NOMEM = -4        /* device allocation failed */
 };
@@ -281,7 +281,7 @@ GBN_API int gbn_problem_set_motion(gbn_problem* p, const float* d_xn, const int*
  * GroupwiseRegistration::InitParameters (GroupwiseRegistration.hpp:145-158);
  * the reference's defaults are tests/MRIRecon.cpp:121-129: W 1, flagW 1,
  * radius 40, E 3, Dp {4, 4}, nmax 100, et 0.01, eh 0.005,
- * lambda {0, 0.005, 0, 0.5}.  This build implements spline orders E = 1 to 3,
+ * lambda {0, 0.005, 0, 0.5}.  This library implements spline orders E = 1 to 3,
  * equal control spacing, and the circular region of interest (radius > 0);
  * the reference's whole-box mode (radius 0) stores a one-pixel bounding box
  * (GroupwiseRegistration.cpp:113-121) and is refused. */

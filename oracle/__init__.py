@@ -3,7 +3,7 @@
 This package restates OpenCLIPER's algorithm on the CPU (numpy/scipy) so that
 the CUDA library can be checked against it.  Only tests/, the smoke() check of
 __graft_entry__.py and the cpu_baseline leg of bench.py may import it, and only
-as the checker or the timed CPU baseline -- never as a product code path.
+to check results or as the timed CPU baseline -- never as a product code path.
 
 Parity status: the reference's OpenCL path cannot be built or run here (no
 OpenCL headers/ICD, no clFFT/CLBlast/matio), and the reference ships no golden
